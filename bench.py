@@ -1,0 +1,421 @@
+"""Throughput of the GB300 2D TE path on the 2000² Si-strip workload (one JSON line).
+
+A bench step is one complete run of the workload: 2024 × 2024 cells (2000² region +
+12-layer CPML per face), float32, Si strip (ε 12.11, 0.5 µm) in oxide (ε 2.085) at
+dl 0.02 µm, one Hz Gaussian point source in the core, three point DFT monitors at 16
+wavelengths each, 10 000 time steps from zero fields. The metric is Etalon's
+cell-updates/s = nx·ny·time steps / time (etalon/validation/throughput.py:4-5,68).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``value`` is device time (CUDA events on the simulation's stream) with the inputs
+resident in HBM; L2 is flushed (a 512 MB write) before every timed step. ``e2e``
+repeats the step through the C ABI from pinned host buffers: coefficient and table
+uploads, the run, and the read-back of fields and DFT accumulators are all timed.
+``--impl reference`` times the reference's CPU algorithm (the NumPy oracle, in row
+bands on every host core) on a bounded prefix of the same workload. With N > 1 (one
+process per GPU under torchrun) every rank runs its own replica: the workload is a
+single grid, so ranks share nothing ("replicas only").
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-updates/s (2000^2 fp32, bit-exact)"
+UNIT = "cell-updates/s"
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+
+
+# ----------------------------------------------------------------------------- helpers
+
+
+def workload(precision: str, time_steps: int):
+    from tests import cases
+
+    return cases.config2(precision, n_steps=time_steps)
+
+
+def algorithmic_bytes_per_step(p) -> int:
+    """Ex, Ey, Hz read+write, cb_ex, cb_ey read; ψ read+write in the strips; DFT acc read+write."""
+    s = np.dtype(p.real).itemsize
+    nx, ny, L = p.grid.nx, p.grid.ny, p.grid.pml_layers
+    dft = sum(sm.flat_index.size * sm.wavelengths.size for sm in p.samplings)
+    return s * (8 * nx * ny + 8 * L * (nx + ny)) + 4 * s * dft
+
+
+def hbm_peak() -> tuple[float, str]:
+    try:
+        return float(json.loads(PEAKS.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(kernel_tag: str):
+    """Per-launch DRAM bytes of the dominant kernel from its committed ncu summary, if any."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for line in f.read_text().splitlines():
+            if line.startswith(f"traffic_bytes_per_launch[{kernel_tag}]:"):
+                return float(line.split(":", 1)[1].split()[0]), f.name
+    return None, None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")  # fmt: skip
+    REASONS = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device, self.proc, self.lines = device, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)  # fmt: skip
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, v in zip(self.REASONS, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}  # fmt: skip
+
+
+def cpu_oracle_rate(precision: str, min_seconds: float, threads: int, time_steps: int = 10000):
+    """The oracle (NumPy restatement of Etalon's backend) on a bounded prefix of the workload."""
+    from etalon_gb300 import physics as ph
+    from oracle.te_numpy import OracleMonitor, OracleSource, OracleTE
+
+    p = workload(precision, time_steps)
+    o = OracleTE(
+        p.grid.nx, p.grid.ny, p.grid.dt, vars(ph.cast_coefficients(p)), p.real,
+        [OracleSource(i.component, i.i, i.j, i.coefficient,
+                      (i.pulse.wavelength, i.pulse.bandwidth, i.pulse.amplitude)) for i in p.injections],
+        [OracleMonitor(s.component, s.flat_index, s.frequencies) for s in p.samplings],
+    )  # fmt: skip
+    with ThreadPoolExecutor(threads) as pool:
+        kw = {"pool": pool, "bands": threads} if threads > 1 else {}
+        o.run(2, **kw)  # warm-up
+        t0, steps = time.perf_counter(), 0
+        while time.perf_counter() - t0 < min_seconds and steps < time_steps:
+            o.step(**kw)
+            steps += 1
+        wall = time.perf_counter() - t0
+    return p.grid.n_cells * steps / wall, steps, wall, p
+
+
+# ----------------------------------------------------------------------------- arms
+
+
+def dist_setup(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if os.environ.get("ETG_BENCH_IMPL", "ours") == "ours" else "gloo"
+        if backend == "nccl":
+            import torch
+
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def reduce_max(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, world, rank) -> None:
+    """Reference arm: Etalon's CPU algorithm (the oracle port) on this host's cores."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    rates = []
+    for k in range(args.warmup + args.steps):
+        rate, steps, wall, p = cpu_oracle_rate(args.precision, args.cpu_seconds, threads)
+        if k >= args.warmup:
+            rates.append((rate, steps, wall))
+    total_cells = sum(p.grid.n_cells * s for _, s, _ in rates)
+    total_wall = sum(w for _, _, w in rates)
+    value = total_cells / total_wall
+    sample = (f"{p.grid.nx}x{p.grid.ny} grid of the workload, {sum(s for _, s, _ in rates)} time steps "
+              f"over {args.steps} steps of ~{args.cpu_seconds:.0f} s each, NumPy oracle in {threads} row bands")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_wall / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision == "single" else "f64", "data": "synthetic",
+        "config": config_dict(p, args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))  # fmt: skip
+
+
+def config_dict(p, args) -> dict:
+    return {
+        "workload": "2000^2 region + 12-layer CPML (2024x2024 cells), Si strip waveguide in oxide, "
+                    "dl 0.02 um, Hz Gaussian point source, 3 point DFT monitors x 16 wavelengths",
+        "grid": [p.grid.nx, p.grid.ny], "time_steps_per_step": p.n_steps, "precision": args.precision,
+        "l2": "flushed before each timed step (512 MB write)",
+        "parallelism": f"replicas x{int(os.environ.get('WORLD_SIZE', '1'))}",
+    }  # fmt: skip
+
+
+def run_ours(args, world, rank, local) -> None:
+    import torch
+
+    from etalon_gb300 import _lib
+    from etalon_gb300 import physics as ph
+    from etalon_gb300.engine import TEEngine
+
+    _lib.call("etg_set_device", local)
+    p = workload(args.precision, args.time_steps)
+    e = TEEngine(p, kernel=args.kernel)
+    e.set_option(_lib.OPT_TIMING, 1)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def one(timed: bool):
+        e.reset()
+        flush.zero_()
+        torch.cuda.synchronize()
+        e.advance(p.n_steps)
+        ms, launches = e.last_timing()
+        return ms, launches
+
+    for _ in range(args.warmup):
+        one(False)
+    barrier(world)
+    torch.cuda.synchronize()
+    _lib.call("etg_synchronize")
+    total_ms, launches, wall0 = 0.0, 0, time.perf_counter()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            ms, n_launch = one(True)
+            total_ms += ms
+            launches += n_launch
+    _lib.call("etg_synchronize")
+    torch.cuda.synchronize()
+    barrier(world)
+    wall = time.perf_counter() - wall0
+    e.synchronize()
+    total_ms = reduce_max(world, total_ms)
+    cells = p.grid.n_cells * p.n_steps
+    value = world * cells * args.steps / (total_ms / 1e3)
+
+    # e2e through the C ABI: pinned host inputs in, fields and accumulators out, all timed
+    c = ph.cast_coefficients(p)
+    names = ("cb_ex", "cb_ey", "bx_e", "cx_e", "ikx_e", "bx_h", "cx_h", "ikx_h",
+             "by_e", "cy_e", "iky_e", "by_h", "cy_h", "iky_h")  # fmt: skip
+    pinned = {}
+    for k in names:
+        a = getattr(c, k)
+        pinned[k] = _lib.pinned_empty(a.shape, a.dtype)
+        pinned[k][...] = a
+    pc = type("Pinned", (), {**pinned, "db": c.db, "inv_dx": c.inv_dx, "inv_dy": c.inv_dy})
+    src_tables = [_lib.pinned_empty((p.n_steps, i.i.size), p.real) for i in p.injections]
+    for t, inj in zip(src_tables, p.injections):
+        t[...] = inj.delta_table(0, p.n_steps, p.grid.dt, p.real)
+    mon_tables = [_lib.pinned_empty((p.n_steps, s.wavelengths.size), p.complex) for s in p.samplings]
+    for t, s in zip(mon_tables, p.samplings):
+        t[...] = ph.phasor_table(s, 0, p.n_steps, p.grid.dt, p.complex)
+    out_fields = {f: _lib.pinned_empty(e.field_shape(f), p.real) for f in ("ex", "ey", "hz")}
+    h2d = sum(a.nbytes for a in pinned.values()) + sum(t.nbytes for t in src_tables + mon_tables)
+    d2h = sum(a.nbytes for a in out_fields.values()) + sum(
+        2 * s.wavelengths.size * s.flat_index.size * np.dtype(p.real).itemsize for s in p.samplings)
+
+    def e2e_step():
+        e.set_coefficients(pc)
+        for k, t in enumerate(src_tables):
+            e.set_source_table(k, 0, t)
+        for k, t in enumerate(mon_tables):
+            e.set_phasor_table(k, 0, t)
+        e.reset()
+        e.advance(p.n_steps)
+        for f, out in out_fields.items():
+            _lib.call("etg_sim_get_field", e._h, _lib.FIELD_IDS[f], out.ctypes.data)
+        return [e.dft(k) for k in range(len(e.monitors))]
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = reduce_max(world, time.perf_counter() - t0)
+    e2e_value = world * cells * args.steps / e2e_s
+
+    # roofline of the dominant kernel (algorithmic bytes / average launch duration)
+    peak, peak_kind = hbm_peak()
+    b_step = algorithmic_bytes_per_step(p)
+    kernel = kernel_name(e)
+    steps_per_launch = launch_depth(e)
+    launch_ms = total_ms / args.steps / (p.n_steps / steps_per_launch)
+    achieved = b_step * steps_per_launch / (launch_ms / 1e3) / 1e9
+    traffic, traffic_src = ncu_traffic(kernel)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision == "single" else "f64", "data": "synthetic",
+        "config": config_dict(p, args),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": b_step * steps_per_launch,
+                     "steps_per_launch": steps_per_launch,
+                     "traffic": traffic, "traffic_source": traffic_src},
+        "clocks": clocks.summary(),
+        "wall_ms_per_step": 1e3 * wall / args.steps,
+    }  # fmt: skip
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, steps, cwall, _ = cpu_oracle_rate(args.precision, args.cpu_seconds, threads)
+        out["cpu_baseline"] = {
+            "value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{p.grid.nx}x{p.grid.ny} workload grid, {steps} time steps in {cwall:.1f} s, "
+                      f"NumPy oracle in {threads} row bands",
+        }  # fmt: skip
+    if args.fp64:
+        out["fp64"] = fp64_line(args, local)
+    if rank == 0:
+        print(json.dumps(out))
+    e.close()
+
+
+def kernel_name(e) -> str:
+    from etalon_gb300 import _lib
+    import ctypes as C
+
+    v = C.c_int64()
+    _lib.call("etg_sim_get_option", e._h, _lib.OPT_KERNEL, C.byref(v))
+    return "k_tb_step" if v.value == 2 else "k_fused_h+k_fused_e"
+
+
+def launch_depth(e) -> int:
+    """Time steps per launch of the dominant kernel (one for the one-step kernels)."""
+    import ctypes as C
+
+    from etalon_gb300 import _lib
+
+    kind, depth = C.c_int64(), C.c_int64()
+    _lib.call("etg_sim_get_option", e._h, _lib.OPT_KERNEL, C.byref(kind))
+    _lib.call("etg_sim_get_option", e._h, _lib.OPT_TB_DEPTH, C.byref(depth))
+    return int(depth.value) if kind.value == 2 else 1
+
+
+def fp64_line(args, local) -> dict:
+    """The same workload in float64, fewer steps (GB300's FP64 rate bounds it, not HBM)."""
+    import torch
+
+    from etalon_gb300 import _lib
+    from etalon_gb300.engine import TEEngine
+
+    p = workload("double", args.time_steps)
+    e = TEEngine(p)
+    e.set_option(_lib.OPT_TIMING, 1)
+    e.advance(p.n_steps)
+    ms = []
+    for _ in range(2):
+        e.reset()
+        torch.cuda.synchronize()
+        e.advance(p.n_steps)
+        ms.append(e.last_timing()[0])
+    e.close()
+    t = sum(ms) / len(ms)
+    return {"value": p.grid.n_cells * p.n_steps / (t / 1e3), "unit": UNIT, "ms_per_step": t}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="single", choices=["single", "double"])
+    ap.add_argument("--time-steps", type=int, default=10000)
+    ap.add_argument("--kernel", default="auto", choices=["auto", "plain", "tb"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fp64", action="store_true", help="add a float64 line of the same workload")
+    args = ap.parse_args()
+    os.environ["ETG_BENCH_IMPL"] = args.impl
+    world, rank, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,227 @@
+"""Etalon's per-step backend protocol on the GB300 kernels.
+
+``Gb300Backend`` has the methods and attributes of Etalon's backends
+(etalon/fdtd/backends/__init__.py:1-53, cupy_backend.py:30-98): ``to_device``,
+``to_host``, ``synchronize``, ``update_h_te``, ``update_e_te``, ``accumulate_dft``,
+``name``, ``device`` and ``xp``. Etalon's unchanged ``FDTDSolver`` steps on it, one
+C-ABI call per method. Device arrays are ``DeviceArray``: HBM buffers owned through
+the C-ABI allocator (no CuPy, no PyTorch), supporting exactly what the solver does to
+them — row views of phasor tables and ``field[i, j] -= delta`` for injection
+(etalon/fdtd/solver.py:83-110).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from collections import defaultdict
+from typing import Any
+
+import numpy as np
+
+from . import _lib
+from ._lib import call
+
+
+class _Pool:
+    """Caches freed device buffers by size, so per-step temporaries do not cudaMalloc."""
+
+    def __init__(self) -> None:
+        self.free: dict[int, list[int]] = defaultdict(list)
+        self.lock = threading.Lock()
+
+    def get(self, nbytes: int) -> int:
+        key = max(256, (nbytes + 255) // 256 * 256)
+        with self.lock:
+            if self.free[key]:
+                return self.free[key].pop()
+        p = C.c_void_p()
+        call("etg_malloc", C.byref(p), key)
+        return p.value
+
+    def put(self, nbytes: int, ptr: int) -> None:
+        key = max(256, (nbytes + 255) // 256 * 256)
+        with self.lock:
+            self.free[key].append(ptr)
+
+    def release(self) -> None:
+        with self.lock:
+            for ptrs in self.free.values():
+                for p in ptrs:
+                    _lib.lib().etg_free(p)
+            self.free.clear()
+
+
+POOL = _Pool()
+
+
+class DeviceArray:
+    """A C-contiguous array in device memory."""
+
+    __array_priority__ = 1000
+
+    def __init__(self, shape, dtype, ptr: int | None = None, base: "DeviceArray | None" = None):
+        self.shape = tuple(int(s) for s in shape)
+        self.dtype = np.dtype(dtype)
+        self.size = int(np.prod(self.shape, dtype=np.int64))
+        self.nbytes = self.size * self.dtype.itemsize
+        self.base = base
+        self._owner = ptr is None
+        self.ptr = POOL.get(self.nbytes) if ptr is None else int(ptr)
+
+    @property
+    def ndim(self) -> int:
+        return len(self.shape)
+
+    @classmethod
+    def from_host(cls, a: np.ndarray) -> "DeviceArray":
+        a = np.ascontiguousarray(a)
+        out = cls(a.shape, a.dtype)
+        call("etg_memcpy_h2d", out.ptr, a.ctypes.data, a.nbytes)
+        return out
+
+    def get(self) -> np.ndarray:
+        out = np.empty(self.shape, self.dtype)
+        call("etg_memcpy_d2h", out.ctypes.data, self.ptr, self.nbytes)
+        return out
+
+    def __array__(self, dtype=None, copy=None):
+        a = self.get()
+        return a if dtype is None else a.astype(dtype)
+
+    def copy(self) -> "DeviceArray":
+        out = DeviceArray(self.shape, self.dtype)
+        call("etg_memcpy_d2d", out.ptr, self.ptr, self.nbytes)
+        return out
+
+    def __len__(self) -> int:
+        return self.shape[0]
+
+    def __getitem__(self, key):
+        if isinstance(key, (int, np.integer)) and self.ndim >= 1:
+            k = int(key) + (self.shape[0] if key < 0 else 0)
+            if not 0 <= k < self.shape[0]:
+                raise IndexError(f"index {key} out of range for axis 0 of size {self.shape[0]}")
+            row = self.nbytes // self.shape[0]
+            return DeviceArray(self.shape[1:], self.dtype, self.ptr + k * row, base=self)
+        if isinstance(key, tuple) and len(key) == 2 and all(isinstance(k, DeviceArray) for k in key):
+            return _Indexed(self, key[0], key[1])
+        raise TypeError(f"DeviceArray supports a row index or two index arrays, not {key!r}")
+
+    def __setitem__(self, key, value) -> None:
+        if isinstance(value, _Indexed) and value.target is self and value.applied:
+            return  # the in-place update already ran (field[i, j] -= delta)
+        raise TypeError("DeviceArray only supports in-place updates through field[i, j] -= delta")
+
+    def __repr__(self) -> str:
+        return f"DeviceArray(shape={self.shape}, dtype={self.dtype})"
+
+    def __del__(self) -> None:
+        if self._owner and self.ptr:
+            try:
+                POOL.put(self.nbytes, self.ptr)
+            except Exception:
+                pass
+            self.ptr = 0
+
+
+class _Indexed:
+    """``field[i, j]`` of a DeviceArray, for ``field[i, j] -= delta`` (solver.py:89)."""
+
+    def __init__(self, target: DeviceArray, i: DeviceArray, j: DeviceArray):
+        if target.ndim != 2 or i.shape != j.shape:
+            raise ValueError("field[i, j] needs a 2D field and index arrays of one shape")
+        self.target, self.i, self.j = target, i, j
+        self.applied = False
+
+    def __isub__(self, delta: DeviceArray) -> "_Indexed":
+        t = self.target
+        if not isinstance(delta, DeviceArray) or delta.dtype != t.dtype or delta.size != self.i.size:
+            raise TypeError("field[i, j] -= delta needs a device delta of the field's dtype and size")
+        if self.i.dtype != np.int64 or self.j.dtype != np.int64:
+            raise TypeError("injection indices must be int64")
+        call("etg_scatter_sub", _lib.dtype_code(t.dtype), t.shape[1], self.i.size, t.ptr,
+             self.i.ptr, self.j.ptr, delta.ptr)  # fmt: skip
+        self.applied = True
+        return self
+
+
+class _ArrayModule:
+    """The ``xp`` of this backend: array creation and host conversion."""
+
+    float32, float64, complex64, complex128 = np.float32, np.float64, np.complex64, np.complex128
+
+    @staticmethod
+    def asarray(a, dtype=None) -> DeviceArray:
+        if isinstance(a, DeviceArray) and (dtype is None or np.dtype(dtype) == a.dtype):
+            return a
+        return DeviceArray.from_host(np.asarray(a, dtype=dtype))
+
+    @staticmethod
+    def zeros(shape, dtype=np.float64) -> DeviceArray:
+        out = DeviceArray(np.atleast_1d(shape) if np.isscalar(shape) else shape, dtype)
+        call("etg_memset", out.ptr, 0, out.nbytes)
+        return out
+
+    @staticmethod
+    def asnumpy(a) -> np.ndarray:
+        return a.get() if isinstance(a, DeviceArray) else np.asarray(a)
+
+
+xp = _ArrayModule()
+
+
+class Gb300Backend:
+    """One GB300 GPU through libetalon_gb300; a drop-in for Etalon's "cuda" backend."""
+
+    name = "cuda"
+    xp = xp
+
+    def __init__(self, precision: str = "single") -> None:
+        if precision not in ("single", "double"):
+            raise ValueError(f"precision must be 'single' or 'double', not {precision!r}")
+        try:
+            dev, gpu, _ = _lib.device_info()
+        except _lib.BackendUnavailable as error:
+            raise RuntimeError(f"backend='cuda' (GB300) is unavailable: {error}") from error
+        except _lib.EtgError as error:
+            raise RuntimeError(f"backend='cuda' found no usable CUDA device ({error})") from error
+        self.precision = precision
+        self.device = f"cuda:{dev} {gpu}"
+
+    def to_device(self, a: np.ndarray) -> DeviceArray:
+        return DeviceArray.from_host(np.asarray(a))
+
+    def to_host(self, a: Any) -> np.ndarray:
+        return a.get() if isinstance(a, DeviceArray) else np.asarray(a)
+
+    def synchronize(self) -> None:
+        call("etg_synchronize")
+
+    @staticmethod
+    def _p(a: DeviceArray) -> int:
+        if not isinstance(a, DeviceArray):
+            raise TypeError(f"expected a device array, got {type(a).__name__}")
+        return a.ptr
+
+    def update_h_te(self, s) -> None:
+        """Hz^(n−½) → Hz^(n+½) (etalon/fdtd/backends/numpy_backend.py:41-49)."""
+        p = self._p
+        call("etg_update_h_te", _lib.dtype_code(s.hz.dtype), s.nx, s.ny, p(s.hz), p(s.ex), p(s.ey),
+             p(s.psi_hz_x), p(s.psi_hz_y), p(s.bx_h), p(s.cx_h), p(s.ikx_h), p(s.by_h), p(s.cy_h),
+             p(s.iky_h), float(s.db), float(s.inv_dx), float(s.inv_dy))  # fmt: skip
+
+    def update_e_te(self, s) -> None:
+        """Ex^n, Ey^n → n+1 (etalon/fdtd/backends/numpy_backend.py:51-61)."""
+        p = self._p
+        call("etg_update_e_te", _lib.dtype_code(s.ex.dtype), s.nx, s.ny, p(s.ex), p(s.ey), p(s.hz),
+             p(s.psi_ex_y), p(s.psi_ey_x), p(s.cb_ex), p(s.cb_ey), p(s.bx_e), p(s.cx_e), p(s.ikx_e),
+             p(s.by_e), p(s.cy_e), p(s.iky_e), float(s.inv_dx), float(s.inv_dy))  # fmt: skip
+
+    def accumulate_dft(self, acc, field, index, phasors) -> None:
+        """acc[f, k] += field.flat[index[k]] · phasors[f] (numpy_backend.py:63-67)."""
+        n_f, n_nodes = acc.shape
+        if index.dtype != np.int64:
+            raise TypeError("DFT node indices must be int64")
+        call("etg_accumulate_dft", _lib.dtype_code(field.dtype), n_f, n_nodes, self._p(acc),
+             self._p(field), self._p(index), self._p(phasors))  # fmt: skip

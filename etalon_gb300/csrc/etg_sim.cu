@@ -1,0 +1,633 @@
+// The resident simulation handle (etg_sim): HBM layout, tables, step loop, CUDA graphs.
+//
+// One handle is one Etalon FDTDSolver run (etalon/fdtd/solver.py:49-160) kept on the
+// device: the per-step host work of the reference — computing the source delta and
+// copying it to the device, building phasor rows — is replaced by tables uploaded
+// once, and a block of steps is one graph launch.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "etg_sim.h"
+#include "etg_tb.h"
+
+namespace etg {
+
+struct Source {
+  int comp;
+  std::vector<int64_t> i, j;
+  void* table = nullptr;  // (rows, n_nodes) dtype
+  int64_t n0 = 0, rows = 0;
+};
+
+struct Monitor {
+  int comp, ix0, nxm, jy0, nym, n_f;
+  void* acc = nullptr;    // (n_f, nxm*nym) complex
+  void* table = nullptr;  // (rows, n_f) complex
+  int64_t n0 = 0, rows = 0;
+};
+
+}  // namespace etg
+
+using namespace etg;
+
+struct etg_sim {
+  int dtype = ETG_F32;
+  int nx = 0, ny = 0;
+  int64_t P = 0, rows = 0;
+  void* field[7] = {};  // ETG_EX .. ETG_PSI_HZ_Y, pitched
+  void* cb[2] = {};     // cb_ex, cb_ey, pitched
+  void* c1d[12] = {};   // bx_e cx_e ikx_e bx_h cx_h ikx_h by_e cy_e iky_e by_h cy_h iky_h
+  double db = 0, inv_dx = 0, inv_dy = 0;
+  bool have_coeffs = false;
+  // rows / columns whose psi may be non-zero (from c != 0, b outside (0, inf) or uploaded psi)
+  std::vector<char> live_x, live_y, psi_live_x, psi_live_y;
+  int xs_lo = 0, xs_hi = 0, ys_lo = 0, ys_hi = 0;
+  std::vector<Source> sources;
+  std::vector<Monitor> monitors;
+  int64_t* d_step = nullptr;
+  int* d_flag = nullptr;
+  int64_t h_step = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0;
+  int64_t last_launches = 0;
+  int64_t opt[8] = {0, 4, 32, 0, 0, 0, 0, 0};
+  std::map<int64_t, cudaGraphExec_t> graphs;  // keyed by steps per graph
+  TBState* tb = nullptr;                      // temporally blocked kernel state
+
+  size_t esize() const { return (size_t)dtype; }
+  int64_t field_rows(int f) const { return (f == ETG_EY || f == ETG_PSI_EY_X) ? nx + 1 : nx; }
+  int64_t field_cols(int f) const { return (f == ETG_EX || f == ETG_PSI_EX_Y) ? ny + 1 : ny; }
+};
+
+namespace {
+
+// Longest run of indices not marked live: [lo, hi). Everything outside is a CPML strip.
+void strip_bounds(const std::vector<char>& live, int* lo, int* hi) {
+  const int n = (int)live.size();
+  int best_lo = 0, best_len = -1, run_lo = 0;
+  for (int k = 0; k <= n; ++k) {
+    if (k == n || live[k]) {
+      if (k - run_lo > best_len) {
+        best_len = k - run_lo;
+        best_lo = run_lo;
+      }
+      run_lo = k + 1;
+    }
+  }
+  *lo = best_lo;
+  *hi = best_lo + std::max(best_len, 0);
+}
+
+template <typename T>
+bool coefficient_live(T b, T c) {
+  // psi' = b psi + c dF stays exactly +0 from +0 when c == 0 and b is positive and finite.
+  return !(c == T(0)) || !(b > T(0)) || !std::isfinite((double)b);
+}
+
+void invalidate_graphs(etg_sim* s) {
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  s->graphs.clear();
+}
+
+void update_strips(etg_sim* s) {
+  std::vector<char> lx(s->nx + 1, 0), ly(s->ny + 1, 0);
+  for (int k = 0; k <= s->nx; ++k) lx[k] = s->live_x[k] || s->psi_live_x[k];
+  for (int k = 0; k <= s->ny; ++k) ly[k] = s->live_y[k] || s->psi_live_y[k];
+  const int old[4] = {s->xs_lo, s->xs_hi, s->ys_lo, s->ys_hi};
+  strip_bounds(lx, &s->xs_lo, &s->xs_hi);
+  strip_bounds(ly, &s->ys_lo, &s->ys_hi);
+  if (old[0] != s->xs_lo || old[1] != s->xs_hi || old[2] != s->ys_lo || old[3] != s->ys_hi) {
+    invalidate_graphs(s);  // the strip bounds are captured kernel parameters
+    if (s->tb) tb_invalidate(s->tb);
+  }
+}
+
+template <typename T>
+SimArgs<T> sim_args(etg_sim* s) {
+  SimArgs<T> a;
+  a.nx = s->nx;
+  a.ny = s->ny;
+  a.P = s->P;
+  a.ex = (T*)s->field[ETG_EX];
+  a.ey = (T*)s->field[ETG_EY];
+  a.hz = (T*)s->field[ETG_HZ];
+  a.psi_ex_y = (T*)s->field[ETG_PSI_EX_Y];
+  a.psi_ey_x = (T*)s->field[ETG_PSI_EY_X];
+  a.psi_hz_x = (T*)s->field[ETG_PSI_HZ_X];
+  a.psi_hz_y = (T*)s->field[ETG_PSI_HZ_Y];
+  a.cb_ex = (const T*)s->cb[0];
+  a.cb_ey = (const T*)s->cb[1];
+  const T** c[12] = {&a.bx_e, &a.cx_e, &a.ikx_e, &a.bx_h, &a.cx_h, &a.ikx_h,
+                     &a.by_e, &a.cy_e, &a.iky_e, &a.by_h, &a.cy_h, &a.iky_h};
+  for (int k = 0; k < 12; ++k) *c[k] = (const T*)s->c1d[k];
+  a.db = (T)s->db;
+  a.inv_dx = (T)s->inv_dx;
+  a.inv_dy = (T)s->inv_dy;
+  a.xs_lo = s->xs_lo;
+  a.xs_hi = s->xs_hi;
+  a.ys_lo = s->ys_lo;
+  a.ys_hi = s->ys_hi;
+  a.step = s->d_step;
+  a.flag = s->d_flag;
+  return a;
+}
+
+template <typename T>
+int build_plans(etg_sim* s, PhasePlan<T>* ph, PhasePlan<T>* pe) {
+  memset(ph, 0, sizeof *ph);
+  memset(pe, 0, sizeof *pe);
+  for (const Source& src : s->sources) {
+    PhasePlan<T>* p = src.comp == ETG_HZ ? ph : pe;
+    for (size_t k = 0; k < src.i.size(); ++k) {
+      ETG_REQUIRE(p->n_src < MAX_SRC_NODES, ETG_ERR_ARGUMENT,
+                  "more than %d source nodes in one half step", MAX_SRC_NODES);
+      SrcDesc<T>& d = p->src[p->n_src++];
+      d.table = (const T*)src.table + k;
+      d.n0 = src.n0;
+      d.rows = src.rows;
+      d.i = (int)src.i[k];
+      d.j = (int)src.j[k];
+      d.stride = (int)src.i.size();
+      d.comp = src.comp;
+    }
+  }
+  for (const Monitor& m : s->monitors) {
+    PhasePlan<T>* p = m.comp == ETG_HZ ? ph : pe;
+    ETG_REQUIRE(p->n_mon < MAX_MONITORS, ETG_ERR_ARGUMENT,
+                "more than %d monitor components in one half step", MAX_MONITORS);
+    MonDesc<T>& d = p->mon[p->n_mon++];
+    d.acc = (T*)m.acc;
+    d.table = (const T*)m.table;
+    d.n0 = m.n0;
+    d.rows = m.rows;
+    d.ix0 = m.ix0;
+    d.nxm = m.nxm;
+    d.jy0 = m.jy0;
+    d.nym = m.nym;
+    d.n_f = m.n_f;
+    d.comp = m.comp;
+  }
+  return ETG_OK;
+}
+
+int check_tables(etg_sim* s, int64_t n_steps) {
+  const int64_t a = s->h_step, b = s->h_step + n_steps;
+  for (size_t k = 0; k < s->sources.size(); ++k) {
+    const Source& src = s->sources[k];
+    ETG_REQUIRE(src.n0 <= a && b <= src.n0 + src.rows, ETG_ERR_STATE,
+                "source %zu has deltas for steps [%lld, %lld) but the run needs [%lld, %lld)", k,
+                (long long)src.n0, (long long)(src.n0 + src.rows), (long long)a, (long long)b);
+  }
+  for (size_t k = 0; k < s->monitors.size(); ++k) {
+    const Monitor& m = s->monitors[k];
+    ETG_REQUIRE(m.n0 <= a && b <= m.n0 + m.rows, ETG_ERR_STATE,
+                "monitor %zu has phasors for steps [%lld, %lld) but the run needs [%lld, %lld)", k,
+                (long long)m.n0, (long long)(m.n0 + m.rows), (long long)a, (long long)b);
+  }
+  return ETG_OK;
+}
+
+template <typename T>
+int advance_plain(etg_sim* s, int64_t n_steps) {
+  PhasePlan<T> ph, pe;
+  int rc = build_plans<T>(s, &ph, &pe);
+  if (rc) return rc;
+  SimArgs<T> a = sim_args<T>(s);
+  const int64_t g = s->opt[ETG_OPT_GRAPH_STEPS];
+  int64_t done = 0;
+  if (g > 0 && n_steps >= g) {
+    auto it = s->graphs.find(g);
+    if (it == s->graphs.end()) {
+      cudaGraph_t graph;
+      ETG_TRY_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < g; ++k) launch_step_plain<T>(a, ph, pe, k, s->stream);
+      launch_step_add<T>(a, g, s->stream);
+      cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+      ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+      cudaGraphExec_t exec;
+      e = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+      it = s->graphs.emplace(g, exec).first;
+    }
+    for (; done + g <= n_steps; done += g) {
+      ETG_TRY_CUDA(cudaGraphLaunch(it->second, s->stream));
+      g_launches += 2 * g + 1;
+    }
+  }
+  const int64_t rem = n_steps - done;
+  for (int k = 0; k < rem; ++k) launch_step_plain<T>(a, ph, pe, k, s->stream);
+  if (rem) launch_step_add<T>(a, rem, s->stream);
+  ETG_LAUNCH_CHECK();
+  return ETG_OK;
+}
+
+template <typename T>
+int advance_dispatch(etg_sim* s, int64_t n_steps) {
+  const int64_t kernel = s->opt[ETG_OPT_KERNEL];
+  if (kernel == 2 || (kernel == 0 && tb_supported<T>(s->nx, s->ny))) {
+    PhasePlan<T> ph, pe;
+    int rc = build_plans<T>(s, &ph, &pe);
+    if (rc) return rc;
+    if (!s->tb) s->tb = tb_create();
+    return tb_advance<T>(s->tb, sim_args<T>(s), ph, pe, n_steps, s->opt, s->stream);
+  }
+  return advance_plain<T>(s, n_steps);
+}
+
+int copy_field_in(etg_sim* s, void* dst, const void* host, int64_t rows, int64_t cols) {
+  ETG_TRY_CUDA(cudaMemcpy2DAsync(dst, s->P * s->esize(), host, cols * s->esize(), cols * s->esize(),
+                                 rows, cudaMemcpyHostToDevice, s->stream));
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  return ETG_OK;
+}
+
+template <typename T>
+void mark_nonzero(const T* a, int64_t rows, int64_t cols, std::vector<char>& by_row,
+                  std::vector<char>& by_col) {
+  for (int64_t r = 0; r < rows; ++r)
+    for (int64_t c = 0; c < cols; ++c) {
+      const T v = a[r * cols + c];
+      if (!(v == T(0)) || std::signbit((double)v)) {
+        by_row[r] = 1;
+        by_col[c] = 1;
+      }
+    }
+}
+
+int zero_device(etg_sim* s) {
+  for (int f = 0; f < 7; ++f)
+    ETG_TRY_CUDA(cudaMemsetAsync(s->field[f], 0, s->rows * s->P * s->esize(), s->stream));
+  for (Monitor& m : s->monitors)
+    ETG_TRY_CUDA(cudaMemsetAsync(m.acc, 0, (size_t)2 * m.n_f * m.nxm * m.nym * s->esize(), s->stream));
+  ETG_TRY_CUDA(cudaMemsetAsync(s->d_step, 0, sizeof(int64_t), s->stream));
+  ETG_TRY_CUDA(cudaMemsetAsync(s->d_flag, 0, sizeof(int), s->stream));
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  s->h_step = 0;
+  return ETG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int etg_sim_create(etg_sim** out, int dtype, int nx, int ny) {
+  ETG_REQUIRE(out, ETG_ERR_ARGUMENT, "etg_sim_create: null output pointer");
+  ETG_REQUIRE(dtype_ok(dtype), ETG_ERR_ARGUMENT, "etg_sim_create: dtype must be 4 or 8, got %d", dtype);
+  ETG_REQUIRE(nx >= 2 && ny >= 2 && nx < (1 << 28) && ny < (1 << 28), ETG_ERR_ARGUMENT,
+              "etg_sim_create: grid %d x %d out of range", nx, ny);
+  if (fault_injected("etg_sim_create")) return ETG_ERR_INJECTED;
+  *out = nullptr;
+  etg_sim* s = new etg_sim;
+  s->dtype = dtype;
+  s->nx = nx;
+  s->ny = ny;
+  s->P = ((int64_t)ny + 1 + 31) / 32 * 32;
+  s->rows = (int64_t)nx + 2;
+  s->live_x.assign(nx + 1, 0);
+  s->live_y.assign(ny + 1, 0);
+  s->psi_live_x.assign(nx + 1, 0);
+  s->psi_live_y.assign(ny + 1, 0);
+  int rc = ETG_OK;
+  auto fail = [&](int code) {
+    etg_sim_destroy(s);
+    return code;
+  };
+  const size_t plane = (size_t)s->rows * s->P * s->esize();
+  for (int f = 0; f < 7 && rc == ETG_OK; ++f) rc = etg_malloc(&s->field[f], plane);
+  for (int k = 0; k < 2 && rc == ETG_OK; ++k) rc = etg_malloc(&s->cb[k], plane);
+  const int64_t len[12] = {nx + 1, nx + 1, nx + 1, nx, nx, nx, ny + 1, ny + 1, ny + 1, ny, ny, ny};
+  for (int k = 0; k < 12 && rc == ETG_OK; ++k) rc = etg_malloc(&s->c1d[k], (len[k] + 8) * s->esize());
+  if (rc == ETG_OK) rc = etg_malloc((void**)&s->d_step, sizeof(int64_t));
+  if (rc == ETG_OK) rc = etg_malloc((void**)&s->d_flag, sizeof(int));
+  if (rc) return fail(rc);
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess) {
+    set_error("etg_sim_create: stream/event creation failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return fail(ETG_ERR_CUDA);
+  }
+  for (int k = 0; k < 2; ++k)
+    if (cudaMemsetAsync(s->cb[k], 0, plane, s->stream) != cudaSuccess) return fail(ETG_ERR_CUDA);
+  for (int k = 0; k < 12; ++k)
+    if (cudaMemsetAsync(s->c1d[k], 0, (len[k] + 8) * s->esize(), s->stream) != cudaSuccess)
+      return fail(ETG_ERR_CUDA);
+  rc = zero_device(s);
+  if (rc) return fail(rc);
+  update_strips(s);
+  *out = s;
+  return ETG_OK;
+}
+
+int etg_sim_destroy(etg_sim* s) {
+  if (!s) return ETG_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  invalidate_graphs(s);
+  if (s->tb) tb_destroy(s->tb);
+  for (void* p : s->field) cudaFree(p);
+  for (void* p : s->cb) cudaFree(p);
+  for (void* p : s->c1d) cudaFree(p);
+  for (Source& src : s->sources) cudaFree(src.table);
+  for (Monitor& m : s->monitors) {
+    cudaFree(m.acc);
+    cudaFree(m.table);
+  }
+  cudaFree(s->d_step);
+  cudaFree(s->d_flag);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return ETG_OK;
+}
+
+int etg_sim_set_coefficients(etg_sim* s, const void* cb_ex, const void* cb_ey, const void* bx_e,
+                             const void* cx_e, const void* ikx_e, const void* bx_h,
+                             const void* cx_h, const void* ikx_h, const void* by_e,
+                             const void* cy_e, const void* iky_e, const void* by_h,
+                             const void* cy_h, const void* iky_h, double db, double inv_dx,
+                             double inv_dy) {
+  ETG_REQUIRE(s && cb_ex && cb_ey, ETG_ERR_ARGUMENT, "etg_sim_set_coefficients: null argument");
+  int rc = copy_field_in(s, s->cb[0], cb_ex, s->nx, s->ny + 1);
+  if (rc == ETG_OK) rc = copy_field_in(s, s->cb[1], cb_ey, s->nx + 1, s->ny);
+  if (rc) return rc;
+  const void* c[12] = {bx_e, cx_e, ikx_e, bx_h, cx_h, ikx_h, by_e, cy_e, iky_e, by_h, cy_h, iky_h};
+  const int64_t len[12] = {s->nx + 1, s->nx + 1, s->nx + 1, s->nx, s->nx, s->nx,
+                           s->ny + 1, s->ny + 1, s->ny + 1, s->ny, s->ny, s->ny};
+  for (int k = 0; k < 12; ++k) {
+    ETG_REQUIRE(c[k], ETG_ERR_ARGUMENT, "etg_sim_set_coefficients: null 1D array %d", k);
+    ETG_TRY_CUDA(cudaMemcpy(s->c1d[k], c[k], len[k] * s->esize(), cudaMemcpyHostToDevice));
+  }
+  // live CPML rows/columns: psi_hz_x (h, i < nx), psi_ey_x (e, 1 <= i <= nx-1), same for y
+  std::fill(s->live_x.begin(), s->live_x.end(), 0);
+  std::fill(s->live_y.begin(), s->live_y.end(), 0);
+  auto scan = [&](auto tag) {
+    using T = decltype(tag);
+    const T *bxe = (const T*)bx_e, *cxe = (const T*)cx_e, *bxh = (const T*)bx_h, *cxh = (const T*)cx_h;
+    const T *bye = (const T*)by_e, *cye = (const T*)cy_e, *byh = (const T*)by_h, *cyh = (const T*)cy_h;
+    for (int i = 0; i < s->nx; ++i) s->live_x[i] |= coefficient_live(bxh[i], cxh[i]);
+    for (int i = 1; i < s->nx; ++i) s->live_x[i] |= coefficient_live(bxe[i], cxe[i]);
+    for (int j = 0; j < s->ny; ++j) s->live_y[j] |= coefficient_live(byh[j], cyh[j]);
+    for (int j = 1; j < s->ny; ++j) s->live_y[j] |= coefficient_live(bye[j], cye[j]);
+  };
+  if (s->dtype == ETG_F32) scan(float{}); else scan(double{});
+  if (s->db != db || s->inv_dx != inv_dx || s->inv_dy != inv_dy) {
+    invalidate_graphs(s);  // captured kernel parameters
+    if (s->tb) tb_invalidate(s->tb);
+  }
+  s->db = db;
+  s->inv_dx = inv_dx;
+  s->inv_dy = inv_dy;
+  s->have_coeffs = true;
+  update_strips(s);
+  return ETG_OK;
+}
+
+int etg_sim_add_source(etg_sim* s, int component, int n_nodes, const int64_t* i, const int64_t* j,
+                       int64_t n0, int64_t rows, const void* table) {
+  ETG_REQUIRE(s && i && j && table && n_nodes > 0 && rows >= 0, ETG_ERR_ARGUMENT,
+              "etg_sim_add_source: bad arguments");
+  ETG_REQUIRE(component == ETG_EX || component == ETG_EY || component == ETG_HZ, ETG_ERR_ARGUMENT,
+              "etg_sim_add_source: component must be ETG_EX, ETG_EY or ETG_HZ");
+  const int64_t nr = component == ETG_EY ? s->nx + 1 : s->nx;
+  const int64_t nc = component == ETG_EX ? s->ny + 1 : s->ny;
+  for (int k = 0; k < n_nodes; ++k)
+    ETG_REQUIRE(i[k] >= 0 && i[k] < nr && j[k] >= 0 && j[k] < nc, ETG_ERR_ARGUMENT,
+                "etg_sim_add_source: node (%lld, %lld) outside the %lld x %lld array",
+                (long long)i[k], (long long)j[k], (long long)nr, (long long)nc);
+  if (s->tb) tb_invalidate(s->tb);
+  Source src;
+  src.comp = component;
+  src.i.assign(i, i + n_nodes);
+  src.j.assign(j, j + n_nodes);
+  src.n0 = n0;
+  src.rows = rows;
+  const size_t bytes = (size_t)std::max<int64_t>(rows, 1) * n_nodes * s->esize();
+  int rc = etg_malloc(&src.table, bytes);
+  if (rc) return rc;
+  if (rows) ETG_TRY_CUDA(cudaMemcpy(src.table, table, rows * n_nodes * s->esize(), cudaMemcpyHostToDevice));
+  s->sources.push_back(src);
+  invalidate_graphs(s);
+  return ETG_OK;
+}
+
+int etg_sim_set_deltas(etg_sim* s, int source, int64_t n0, int64_t rows, const void* table) {
+  ETG_REQUIRE(s && source >= 0 && source < (int)s->sources.size() && rows >= 0 && table,
+              ETG_ERR_ARGUMENT, "etg_sim_set_deltas: bad source %d", source);
+  Source& src = s->sources[source];
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  const bool same = rows == src.rows && n0 == src.n0;  // captured graphs stay valid
+  if (rows > src.rows) {
+    cudaFree(src.table);
+    src.table = nullptr;
+    int rc = etg_malloc(&src.table, rows * src.i.size() * s->esize());
+    if (rc) return rc;
+  }
+  ETG_TRY_CUDA(cudaMemcpy(src.table, table, rows * src.i.size() * s->esize(), cudaMemcpyHostToDevice));
+  src.n0 = n0;
+  src.rows = rows;
+  if (!same) {
+    invalidate_graphs(s);
+    if (s->tb) tb_invalidate(s->tb);
+  }
+  return ETG_OK;
+}
+
+int etg_sim_add_monitor(etg_sim* s, int component, int ix0, int nxm, int jy0, int nym, int n_f,
+                        int64_t n0, int64_t rows, const void* table, int* monitor) {
+  ETG_REQUIRE(s && table && monitor && n_f > 0 && nxm > 0 && nym > 0 && rows >= 0,
+              ETG_ERR_ARGUMENT, "etg_sim_add_monitor: bad arguments");
+  ETG_REQUIRE(component == ETG_EX || component == ETG_EY || component == ETG_HZ, ETG_ERR_ARGUMENT,
+              "etg_sim_add_monitor: component must be ETG_EX, ETG_EY or ETG_HZ");
+  const int64_t nr = component == ETG_EY ? s->nx + 1 : s->nx;
+  const int64_t nc = component == ETG_EX ? s->ny + 1 : s->ny;
+  ETG_REQUIRE(ix0 >= 0 && jy0 >= 0 && ix0 + nxm <= nr && jy0 + nym <= nc, ETG_ERR_ARGUMENT,
+              "etg_sim_add_monitor: rectangle [%d,%d)x[%d,%d) outside the %lld x %lld array", ix0,
+              ix0 + nxm, jy0, jy0 + nym, (long long)nr, (long long)nc);
+  if (s->tb) tb_invalidate(s->tb);
+  Monitor m{component, ix0, nxm, jy0, nym, n_f};
+  m.n0 = n0;
+  m.rows = rows;
+  const size_t acc_bytes = (size_t)2 * n_f * nxm * nym * s->esize();
+  int rc = etg_malloc(&m.acc, acc_bytes);
+  if (rc == ETG_OK) rc = etg_malloc(&m.table, (size_t)2 * std::max<int64_t>(rows, 1) * n_f * s->esize());
+  if (rc) {
+    cudaFree(m.acc);
+    return rc;
+  }
+  ETG_TRY_CUDA(cudaMemset(m.acc, 0, acc_bytes));
+  if (rows) ETG_TRY_CUDA(cudaMemcpy(m.table, table, 2 * rows * n_f * s->esize(), cudaMemcpyHostToDevice));
+  *monitor = (int)s->monitors.size();
+  s->monitors.push_back(m);
+  invalidate_graphs(s);
+  return ETG_OK;
+}
+
+int etg_sim_set_phasors(etg_sim* s, int monitor, int64_t n0, int64_t rows, const void* table) {
+  ETG_REQUIRE(s && monitor >= 0 && monitor < (int)s->monitors.size() && rows >= 0 && table,
+              ETG_ERR_ARGUMENT, "etg_sim_set_phasors: bad monitor %d", monitor);
+  Monitor& m = s->monitors[monitor];
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  const bool same = rows == m.rows && n0 == m.n0;  // captured graphs stay valid
+  if (rows > m.rows) {
+    cudaFree(m.table);
+    m.table = nullptr;
+    int rc = etg_malloc(&m.table, (size_t)2 * rows * m.n_f * s->esize());
+    if (rc) return rc;
+  }
+  ETG_TRY_CUDA(cudaMemcpy(m.table, table, 2 * rows * m.n_f * s->esize(), cudaMemcpyHostToDevice));
+  m.n0 = n0;
+  m.rows = rows;
+  if (!same) {
+    invalidate_graphs(s);
+    if (s->tb) tb_invalidate(s->tb);
+  }
+  return ETG_OK;
+}
+
+int etg_sim_set_field(etg_sim* s, int f, const void* host) {
+  ETG_REQUIRE(s && host && f >= 0 && f < 7, ETG_ERR_ARGUMENT, "etg_sim_set_field: bad field %d", f);
+  const int64_t r = s->field_rows(f), c = s->field_cols(f);
+  int rc = copy_field_in(s, s->field[f], host, r, c);
+  if (rc) return rc;
+  if (f >= ETG_PSI_EX_Y) {  // uploaded psi widens the strips to wherever it is non-zero
+    std::vector<char> rows_nz(r, 0), cols_nz(c, 0);
+    if (s->dtype == ETG_F32) mark_nonzero((const float*)host, r, c, rows_nz, cols_nz);
+    else mark_nonzero((const double*)host, r, c, rows_nz, cols_nz);
+    if (f == ETG_PSI_HZ_X || f == ETG_PSI_EY_X)
+      for (int64_t k = 0; k < r; ++k) s->psi_live_x[k] |= rows_nz[k];
+    else
+      for (int64_t k = 0; k < c; ++k) s->psi_live_y[k] |= cols_nz[k];
+    update_strips(s);
+  }
+  return ETG_OK;
+}
+
+int etg_sim_get_field(etg_sim* s, int f, void* host) {
+  ETG_REQUIRE(s && host && f >= 0 && f < 7, ETG_ERR_ARGUMENT, "etg_sim_get_field: bad field %d", f);
+  const int64_t r = s->field_rows(f), c = s->field_cols(f);
+  ETG_TRY_CUDA(cudaMemcpy2DAsync(host, c * s->esize(), s->field[f], s->P * s->esize(), c * s->esize(),
+                                 r, cudaMemcpyDeviceToHost, s->stream));
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  return ETG_OK;
+}
+
+int etg_sim_get_dft(etg_sim* s, int monitor, void* host) {
+  ETG_REQUIRE(s && host && monitor >= 0 && monitor < (int)s->monitors.size(), ETG_ERR_ARGUMENT,
+              "etg_sim_get_dft: bad monitor %d", monitor);
+  const Monitor& m = s->monitors[monitor];
+  ETG_TRY_CUDA(cudaMemcpyAsync(host, m.acc, (size_t)2 * m.n_f * m.nxm * m.nym * s->esize(),
+                               cudaMemcpyDeviceToHost, s->stream));
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  return ETG_OK;
+}
+
+int etg_sim_set_dft(etg_sim* s, int monitor, const void* host) {
+  ETG_REQUIRE(s && host && monitor >= 0 && monitor < (int)s->monitors.size(), ETG_ERR_ARGUMENT,
+              "etg_sim_set_dft: bad monitor %d", monitor);
+  const Monitor& m = s->monitors[monitor];
+  ETG_TRY_CUDA(cudaMemcpyAsync(m.acc, host, (size_t)2 * m.n_f * m.nxm * m.nym * s->esize(),
+                               cudaMemcpyHostToDevice, s->stream));
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  return ETG_OK;
+}
+
+int etg_sim_reset(etg_sim* s) {
+  ETG_REQUIRE(s, ETG_ERR_ARGUMENT, "etg_sim_reset: null handle");
+  std::fill(s->psi_live_x.begin(), s->psi_live_x.end(), 0);
+  std::fill(s->psi_live_y.begin(), s->psi_live_y.end(), 0);
+  update_strips(s);
+  return zero_device(s);
+}
+
+int etg_sim_advance(etg_sim* s, int64_t n_steps) {
+  ETG_REQUIRE(s && n_steps >= 0, ETG_ERR_ARGUMENT, "etg_sim_advance: bad arguments");
+  ETG_REQUIRE(s->have_coeffs, ETG_ERR_STATE, "etg_sim_advance: coefficients not set");
+  if (fault_injected("etg_sim_advance")) return ETG_ERR_INJECTED;
+  if (n_steps == 0) return ETG_OK;
+  int rc = check_tables(s, n_steps);
+  if (rc) return rc;
+  const bool timing = s->opt[ETG_OPT_TIMING] != 0;
+  const int64_t launches0 = g_launches;
+  if (timing) ETG_TRY_CUDA(cudaEventRecord(s->ev0, s->stream));
+  rc = s->dtype == ETG_F32 ? advance_dispatch<float>(s, n_steps) : advance_dispatch<double>(s, n_steps);
+  if (rc) return rc;
+  if (s->opt[ETG_OPT_CHECK_FINITE]) {
+    if (s->dtype == ETG_F32) launch_check_finite<float>(sim_args<float>(s), s->stream);
+    else launch_check_finite<double>(sim_args<double>(s), s->stream);
+    ETG_LAUNCH_CHECK();
+  }
+  if (timing) {
+    ETG_TRY_CUDA(cudaEventRecord(s->ev1, s->stream));
+    ETG_TRY_CUDA(cudaEventSynchronize(s->ev1));
+    float ms = 0;
+    ETG_TRY_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    s->last_ms = ms;
+  }
+  s->last_launches = g_launches - launches0;
+  s->h_step += n_steps;
+  return ETG_OK;
+}
+
+int etg_sim_step_index(etg_sim* s, int64_t* n) {
+  ETG_REQUIRE(s && n, ETG_ERR_ARGUMENT, "etg_sim_step_index: null argument");
+  *n = s->h_step;
+  return ETG_OK;
+}
+
+int etg_sim_set_step_index(etg_sim* s, int64_t n) {
+  ETG_REQUIRE(s && n >= 0, ETG_ERR_ARGUMENT, "etg_sim_set_step_index: bad arguments");
+  ETG_TRY_CUDA(cudaMemcpyAsync(s->d_step, &n, sizeof n, cudaMemcpyHostToDevice, s->stream));
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  s->h_step = n;
+  return ETG_OK;
+}
+
+int etg_sim_synchronize(etg_sim* s) {
+  ETG_REQUIRE(s, ETG_ERR_ARGUMENT, "etg_sim_synchronize: null handle");
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  int flag = 0;
+  ETG_TRY_CUDA(cudaMemcpy(&flag, s->d_flag, sizeof flag, cudaMemcpyDeviceToHost));
+  if (flag) {
+    ETG_TRY_CUDA(cudaMemset(s->d_flag, 0, sizeof(int)));
+    if (flag & ERRBIT_TIMEOUT) {
+      set_error("a bounded device-side wait gave up (flags 0x%x)", flag);
+      return ETG_ERR_TIMEOUT;
+    }
+    if (flag & ERRBIT_TABLE) {
+      set_error("a source or phasor table did not cover a step (flags 0x%x)", flag);
+      return ETG_ERR_STATE;
+    }
+    if (flag & ERRBIT_NONFINITE) {
+      set_error("a field became NaN or Inf (flags 0x%x)", flag);
+      return ETG_ERR_NONFINITE;
+    }
+  }
+  return ETG_OK;
+}
+
+int etg_sim_set_option(etg_sim* s, int option, int64_t value) {
+  ETG_REQUIRE(s && option >= 0 && option < 8, ETG_ERR_ARGUMENT, "etg_sim_set_option: bad option %d", option);
+  ETG_REQUIRE(value >= 0, ETG_ERR_ARGUMENT, "etg_sim_set_option: negative value");
+  s->opt[option] = value;
+  invalidate_graphs(s);
+  if (s->tb) tb_invalidate(s->tb);
+  return ETG_OK;
+}
+
+int etg_sim_get_option(etg_sim* s, int option, int64_t* value) {
+  ETG_REQUIRE(s && value && option >= 0 && option < 8, ETG_ERR_ARGUMENT, "etg_sim_get_option: bad option");
+  *value = s->opt[option];
+  return ETG_OK;
+}
+
+int etg_sim_last_timing(etg_sim* s, double* ms, int64_t* launches) {
+  ETG_REQUIRE(s, ETG_ERR_ARGUMENT, "etg_sim_last_timing: null handle");
+  if (ms) *ms = s->last_ms;
+  if (launches) *launches = s->last_launches;
+  return ETG_OK;
+}
+
+}  // extern "C"

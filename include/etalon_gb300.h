@@ -1,0 +1,163 @@
+/* etalon_gb300 — C ABI of the GB300 (sm_103a) 2D TE FDTD backend for Etalon.
+ *
+ * Plain C types only: pointers, sizes, int status. Every entry point returns ETG_OK (0)
+ * or an ETG_ERR_* code and leaves a message for etg_last_error() on the calling thread.
+ * Arrays are C-ordered with y fastest, in the shapes of Etalon's TEState
+ * (etalon/fdtd/state.py:15-49): Hz (nx, ny), Ex (nx, ny+1), Ey (nx+1, ny).
+ * `dtype` is ETG_F32 or ETG_F64; complex arrays are interleaved (re, im) pairs.
+ *
+ * Paths in the comments are files of the Etalon project that each entry point
+ * replaces or mirrors.
+ */
+#ifndef ETALON_GB300_H
+#define ETALON_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define ETG_OK 0
+#define ETG_ERR_ARGUMENT 1   /* bad size, pointer, id or dtype */
+#define ETG_ERR_CUDA 2       /* a CUDA runtime call failed */
+#define ETG_ERR_ALLOC 3      /* device or pinned allocation failed */
+#define ETG_ERR_STATE 4      /* call not valid now (e.g. a table does not cover the steps) */
+#define ETG_ERR_INJECTED 5   /* failure injected on the host (ETG_FAULT, tests only) */
+#define ETG_ERR_NONFINITE 6  /* a field became NaN or Inf */
+#define ETG_ERR_TIMEOUT 7    /* a bounded device-side wait gave up */
+
+#define ETG_F32 4
+#define ETG_F64 8
+
+/* field ids (etalon/fdtd/state.py:15-49) */
+#define ETG_EX 0
+#define ETG_EY 1
+#define ETG_HZ 2
+#define ETG_PSI_EX_Y 3
+#define ETG_PSI_EY_X 4
+#define ETG_PSI_HZ_X 5
+#define ETG_PSI_HZ_Y 6
+
+/* ---------------------------------------------------------------- library */
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* etg_last_error(void);
+/* ABI version: (major << 16) | minor. */
+int etg_version(void);
+/* Current device ordinal, its name and SM count (replaces the device probe of
+ * etalon/fdtd/backends/cupy_backend.py:36-59). */
+int etg_device_info(int* device, char* name, int name_len, int* sm_count);
+/* Wait for all work this library queued on the device. (cupy_backend.py:67-68) */
+int etg_synchronize(void);
+/* Make `device` current for this library on the calling thread (the library links its own
+ * CUDA runtime, so the caller's current device does not carry over; cupy.cuda.Device). */
+int etg_set_device(int device);
+
+/* ---------------------------------------------------------------- device memory
+ * Backing store of the per-step backend's device arrays
+ * (replaces cupy.asarray / cupy.asnumpy in cupy_backend.py:61-65). */
+int etg_malloc(void** ptr, size_t bytes);
+int etg_free(void* ptr);
+int etg_memcpy_h2d(void* dst, const void* src, size_t bytes);
+int etg_memcpy_d2h(void* dst, const void* src, size_t bytes);
+int etg_memcpy_d2d(void* dst, const void* src, size_t bytes);
+int etg_memset(void* dst, int value, size_t bytes);
+/* Page-locked host memory, for host<->device copies at full link speed. */
+int etg_host_alloc(void** ptr, size_t bytes);
+int etg_host_free(void* ptr);
+
+/* ---------------------------------------------------------------- per-step protocol
+ * One call = one backend method of Etalon's backend protocol
+ * (etalon/fdtd/backends/__init__.py:1-53), on contiguous device arrays in TEState
+ * layout. Results are bit-identical to NumpyBackend (IEEE order, no contraction). */
+
+/* Hz^(n-1/2) -> Hz^(n+1/2) with CPML psi_hz_x/psi_hz_y.
+ * Replaces update_te.cu:14-39 / numpy_backend.py:41-49. */
+int etg_update_h_te(int dtype, int nx, int ny, void* hz, const void* ex, const void* ey,
+                    void* psi_hz_x, void* psi_hz_y, const void* bx_h, const void* cx_h,
+                    const void* ikx_h, const void* by_h, const void* cy_h, const void* iky_h,
+                    double db, double inv_dx, double inv_dy);
+/* Ex, Ey -> n+1 with CPML psi_ex_y/psi_ey_x; outer tangential E stays 0 (PEC).
+ * Replaces update_te.cu:41-75 / numpy_backend.py:51-61. */
+int etg_update_e_te(int dtype, int nx, int ny, void* ex, void* ey, const void* hz,
+                    void* psi_ex_y, void* psi_ey_x, const void* cb_ex, const void* cb_ey,
+                    const void* bx_e, const void* cx_e, const void* ikx_e, const void* by_e,
+                    const void* cy_e, const void* iky_e, double inv_dx, double inv_dy);
+/* acc[f, k] += field.flat[index[k]] * phasors[f]; acc (n_f, n_nodes) complex.
+ * Replaces dft.cu:8-23 / numpy_backend.py:63-67. */
+int etg_accumulate_dft(int dtype, int n_f, int n_nodes, void* acc, const void* field,
+                       const int64_t* index, const void* phasors);
+/* field[i[k], j[k]] -= delta[k] for k < n, field 2D with n_cols columns; NumPy
+ * fancy-index semantics (all reads before writes, last duplicate wins).
+ * Replaces the source injection of etalon/fdtd/solver.py:83-89. */
+int etg_scatter_sub(int dtype, int64_t n_cols, int n, void* field, const int64_t* i,
+                    const int64_t* j, const void* delta);
+
+/* ---------------------------------------------------------------- fused simulation
+ * A resident 2D TE run: fields, CPML strips, coefficients, per-step source deltas
+ * and phasor tables all in HBM; etg_sim_advance runs whole steps (H, inject M,
+ * DFT H, E, inject J, DFT E — etalon/fdtd/solver.py:120-128) with no host
+ * round trip. Replaces FDTDSolver.step/run (solver.py:120-160). */
+typedef struct etg_sim etg_sim;
+
+int etg_sim_create(etg_sim** out, int dtype, int nx, int ny);
+int etg_sim_destroy(etg_sim* sim);
+/* Coefficients already cast to dtype (etalon/fdtd/state.py:75-97): cb_ex (nx, ny+1),
+ * cb_ey (nx+1, ny), *_e of x (nx+1), *_h of x (nx), *_e of y (ny+1), *_h of y (ny). */
+int etg_sim_set_coefficients(etg_sim* sim, const void* cb_ex, const void* cb_ey,
+                             const void* bx_e, const void* cx_e, const void* ikx_e,
+                             const void* bx_h, const void* cx_h, const void* ikx_h,
+                             const void* by_e, const void* cy_e, const void* iky_e,
+                             const void* by_h, const void* cy_h, const void* iky_h,
+                             double db, double inv_dx, double inv_dy);
+/* A point source on `component` (ETG_EX/EY/HZ) over n_nodes nodes (i, j) with its
+ * per-step deltas for steps n0 .. n0+rows-1: table (rows, n_nodes) in dtype, the
+ * values subtracted (etalon/fdtd/sources.py:54-56 cast to dtype). Sources apply in
+ * the order they are added. */
+int etg_sim_add_source(etg_sim* sim, int component, int n_nodes, const int64_t* i,
+                       const int64_t* j, int64_t n0, int64_t rows, const void* table);
+/* A DFT monitor component over the node rectangle [ix0, ix0+nxm) x [jy0, jy0+nym)
+ * (x-major, etalon/fdtd/dft.py:92-107) at n_f frequencies, with phasor rows for steps
+ * n0 .. n0+rows-1: table (rows, n_f) complex. Writes its id to *monitor. */
+int etg_sim_add_monitor(etg_sim* sim, int component, int ix0, int nxm, int jy0, int nym,
+                        int n_f, int64_t n0, int64_t rows, const void* table, int* monitor);
+/* Replace the phasor rows of a monitor (next chunk of a long run). */
+int etg_sim_set_phasors(etg_sim* sim, int monitor, int64_t n0, int64_t rows, const void* table);
+/* Replace the delta rows of source number `source` (in order of addition). */
+int etg_sim_set_deltas(etg_sim* sim, int source, int64_t n0, int64_t rows, const void* table);
+/* Host <-> device copies of one field in TEState shape. */
+int etg_sim_set_field(etg_sim* sim, int field, const void* host);
+int etg_sim_get_field(etg_sim* sim, int field, void* host);
+/* Accumulator of a monitor: (n_f, nxm*nym) complex. */
+int etg_sim_get_dft(etg_sim* sim, int monitor, void* host);
+int etg_sim_set_dft(etg_sim* sim, int monitor, const void* host);
+/* Zero fields, psi and accumulators; step index back to 0. */
+int etg_sim_reset(etg_sim* sim);
+/* Run n_steps whole steps from the current step index. */
+int etg_sim_advance(etg_sim* sim, int64_t n_steps);
+int etg_sim_step_index(etg_sim* sim, int64_t* n);
+int etg_sim_set_step_index(etg_sim* sim, int64_t n);
+/* Block until the simulation's stream is idle; reports device-side errors. */
+int etg_sim_synchronize(etg_sim* sim);
+/* Tuning options (ETG_OPT_*), see below. */
+int etg_sim_set_option(etg_sim* sim, int option, int64_t value);
+int etg_sim_get_option(etg_sim* sim, int option, int64_t* value);
+/* Device-side timing of the last etg_sim_advance (CUDA events on its stream):
+ * total milliseconds and the number of kernel launches it made. */
+int etg_sim_last_timing(etg_sim* sim, double* ms, int64_t* launches);
+
+#define ETG_OPT_KERNEL 0        /* 0 = auto, 1 = one step per launch, 2 = temporal blocking */
+#define ETG_OPT_TB_DEPTH 1      /* steps per launch of the temporally blocked kernel */
+#define ETG_OPT_GRAPH_STEPS 2   /* steps captured per CUDA graph (0 = no graphs) */
+#define ETG_OPT_TILE_ROWS 3     /* tile rows of the temporally blocked kernel */
+#define ETG_OPT_TILE_COLS 4     /* tile columns of the temporally blocked kernel */
+#define ETG_OPT_CHECK_FINITE 5  /* 1 = flag NaN/Inf after each advance */
+#define ETG_OPT_TIMING 6        /* 1 = record CUDA-event timing of each advance */
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ETALON_GB300_H */

@@ -1,0 +1,362 @@
+"""CUDA path vs Etalon's NumPy reference: bit-for-bit parity through the C ABI (needs a GPU).
+
+Two oracles are used. The fixtures of tests/golden/ hold Etalon's own inputs and
+output hashes, so a match there is a match with the reference itself. The NumPy
+oracle (oracle/te_numpy.py, pinned to the same fixtures on CPU) is run live on the
+same inputs, for cases without a fixture and at the headline size.
+
+Contract (as Etalon's tests/gpu/test_cupy_equality.py, tightened): every field, every
+CPML ψ and every DFT accumulator is bitwise identical, in float32 and float64.
+"""
+
+from __future__ import annotations
+
+import os
+from concurrent.futures import ThreadPoolExecutor
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+
+from etalon_gb300 import _lib
+from etalon_gb300 import physics as ph
+from etalon_gb300.engine import TEEngine
+from tests import cases
+from tests.golden_io import COEFFS, FIELDS, GOLDEN, compare_outputs, count, load, oracle_from_golden, sha
+
+pytestmark = pytest.mark.gpu
+PRECISIONS = ["single", "double"]
+
+
+def _dtype(precision):
+    return np.float32 if precision == "single" else np.float64
+
+
+def golden_coeffs(g):
+    c = SimpleNamespace(**{k: g[f"in_{k}"] for k in COEFFS if f"in_{k}" in g})
+    c.db, c.inv_dx, c.inv_dy = g["in_scalars"]
+    return c
+
+
+def engine_with_reference_inputs(name, precision, g, **kw):
+    """An engine on the case's problem, fed Etalon's own cast coefficients and host tables."""
+    n = int(g["n_steps"])
+    p = cases.CASES[name](precision=precision, n_steps=n)
+    e = TEEngine(p, **kw)
+    e.set_coefficients(golden_coeffs(g))
+    for k in range(count(g, "src")):
+        e.set_source_table(k, 0, g[f"src{k}_table"])
+    for k in range(count(g, "mon")):
+        e.set_phasor_table(k, 0, g[f"mon{k}_table"])
+    return e, n
+
+
+def engine_outputs(e):
+    return {f: e.field(f) for f in FIELDS}, [e.dft(k) for k in range(len(e.monitors))]
+
+
+# ----------------------------------------------------------------- per-step protocol
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("update", ["update_h_te", "update_e_te"])
+def test_g1_g2_protocol_kernels_random_state(gpu, precision, update):
+    """Etalon's random 67×53 state, CPML live on every node (its G1/G2)."""
+    from etalon_gb300.backend import Gb300Backend
+    from oracle import te_numpy
+
+    dtype = _dtype(precision)
+    g = load("kernels", precision)
+    grid, c, fields = cases.random_state_inputs(dtype)
+    backend = Gb300Backend(precision)
+    s = SimpleNamespace(nx=grid.nx, ny=grid.ny, db=c.db, inv_dx=c.inv_dx, inv_dy=c.inv_dy)
+    for k in COEFFS:
+        setattr(s, k, backend.to_device(getattr(c, k)))
+    for k, v in fields.items():
+        setattr(s, k, backend.to_device(v))
+    getattr(backend, update)(s)
+    ref = SimpleNamespace(nx=grid.nx, ny=grid.ny, **vars(c), **{k: v.copy() for k, v in fields.items()})
+    {"update_h_te": te_numpy.update_h, "update_e_te": te_numpy.update_e}[update](ref)
+    for f in FIELDS:
+        out = backend.to_host(getattr(s, f))
+        np.testing.assert_array_equal(out, getattr(ref, f), err_msg=f)
+        if sha(fields[f]) == str(g[f"{update}_in_{f}_sha"]):
+            assert sha(out) == str(g[f"{update}_out_{f}_sha"]), f
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_g3_protocol_dft_kernel(gpu, precision):
+    from etalon_gb300.backend import Gb300Backend
+
+    dtype = _dtype(precision)
+    g = load("kernels", precision)
+    field, index, phasors, acc = cases.dft_inputs(dtype)
+    backend = Gb300Backend(precision)
+    acc_d = backend.to_device(acc)
+    backend.accumulate_dft(acc_d, backend.to_device(field), backend.to_device(index), backend.to_device(phasors))
+    expect = acc + field.ravel()[index][None, :] * phasors[:, None]
+    np.testing.assert_array_equal(backend.to_host(acc_d), expect)
+    assert sha(backend.to_host(acc_d)) == str(g["dft_out_acc_sha"])
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("name", ["g4_full", "small"])
+def test_protocol_full_run_matches_reference(gpu, name, precision):
+    """Etalon's step loop over the per-step backend reproduces Etalon's run bit for bit (its G4)."""
+    from etalon_gb300.backend import Gb300Backend
+    from tests.protocol_loop import ProtocolRun
+
+    g = load(name, precision)
+    run = ProtocolRun(Gb300Backend(precision), g, precision)
+    for _ in range(int(g["n_steps"])):
+        run.step()
+    assert compare_outputs(g, run.fields(), run.accs()) == []
+
+
+# ----------------------------------------------------------------- fused engine
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("name", ["config1", "g4_full", "small"])
+@pytest.mark.parametrize("kernel", ["plain", "auto"])
+def test_engine_full_run_matches_reference(gpu, name, precision, kernel):
+    g = load(name, precision)
+    e, n = engine_with_reference_inputs(name, precision, g, kernel=kernel)
+    e.advance(n)
+    e.synchronize()
+    fields, accs = engine_outputs(e)
+    assert np.abs(fields["hz"]).max() > 0
+    assert compare_outputs(g, fields, accs) == []
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("name", ["g4_full", "small"])
+def test_engine_own_setup_matches_live_oracle(gpu, name, precision):
+    """The engine's own host setup and tables vs the oracle run here on the same problem."""
+    from oracle.te_numpy import OracleMonitor, OracleSource, OracleTE
+
+    p = cases.CASES[name](precision=precision)
+    n = p.n_steps or 300
+    p.n_steps = n
+    e = TEEngine(p)
+    e.advance(n)
+    c = vars(ph.cast_coefficients(p))
+    o = OracleTE(p.grid.nx, p.grid.ny, p.grid.dt, c, p.real,
+                 [OracleSource(i.component, i.i, i.j, i.coefficient,
+                               (i.pulse.wavelength, i.pulse.bandwidth, i.pulse.amplitude))
+                  for i in p.injections],
+                 [OracleMonitor(s.component, s.flat_index, s.frequencies) for s in p.samplings])  # fmt: skip
+    o.run(n)
+    for f in FIELDS:
+        np.testing.assert_array_equal(e.field(f), getattr(o, f), err_msg=f)
+    for k, acc in enumerate(o.acc):
+        np.testing.assert_array_equal(e.dft(k), acc)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_engine_block_boundaries_do_not_change_bits(gpu, precision):
+    """Advancing in uneven blocks (graph blocks, remainders, single steps) is bitwise neutral."""
+    g = load("g4_full", precision)
+    a, n = engine_with_reference_inputs("g4_full", precision, g)
+    a.advance(n)
+    b, _ = engine_with_reference_inputs("g4_full", precision, g, graph_steps=8)
+    done = 0
+    for k in (1, 2, 7, 8, 9, 31, 32, 33, 100):
+        b.advance(k)
+        done += k
+    b.advance(n - done)
+    fa, aa = engine_outputs(a)
+    fb, ab = engine_outputs(b)
+    for f in FIELDS:
+        np.testing.assert_array_equal(fa[f], fb[f], err_msg=f)
+    for x, y in zip(aa, ab):
+        np.testing.assert_array_equal(x, y)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("steps", [1, 2, 5])
+def test_engine_random_state_live_psi(gpu, precision, steps):
+    """Random fields and ψ with random CPML on every node (ψ strips cover the whole grid)."""
+    from oracle import te_numpy
+
+    dtype = _dtype(precision)
+    grid, c, fields = cases.random_state_inputs(dtype)
+    p = ph.TEProblem(grid, {}, None, None, [], [], precision, n_steps=steps)
+    e = TEEngine.__new__(TEEngine)
+    _init_bare_engine(e, p, c)
+    for f, v in fields.items():
+        e.set_field(f, v)
+    e.advance(steps)
+    ref = SimpleNamespace(nx=grid.nx, ny=grid.ny, **vars(c), **{k: v.copy() for k, v in fields.items()})
+    for _ in range(steps):
+        te_numpy.update_h(ref)
+        te_numpy.update_e(ref)
+    for f in FIELDS:
+        np.testing.assert_array_equal(e.field(f), getattr(ref, f), err_msg=f)
+
+
+def _init_bare_engine(e, p, c):
+    """A TEEngine on explicit cast coefficients (no sources, no monitors)."""
+    import ctypes as C
+
+    g = p.grid
+    e.problem, e.nx, e.ny, e.dt = p, g.nx, g.ny, g.dt
+    e.real, e.complex, e.n_steps = p.real, p.complex, p.n_steps
+    e._lib = _lib.lib()
+    h = C.c_void_p()
+    _lib.call("etg_sim_create", C.byref(h), _lib.dtype_code(p.real), g.nx, g.ny)
+    e._h = h
+    e.sources, e.monitors = [], []
+    e.set_coefficients(c)
+
+
+@pytest.mark.parametrize("precision", ["double", "single"])
+def test_engine_centred_source_is_exactly_symmetric(gpu, precision):
+    """Mirror x, mirror y and x↔y swap hold bit for bit (Etalon test_numpy_backend.py:61-85)."""
+    p = cases.centred(precision)
+    assert p.injections[0].weights.size == 1
+    e = TEEngine(p)
+    e.advance(p.n_steps)
+    f = e.fields()
+    hz, ex, ey = f["Hz"], f["Ex"], f["Ey"]
+    assert np.abs(hz).max() > 0
+    np.testing.assert_array_equal(hz, hz[::-1, :])
+    np.testing.assert_array_equal(hz, hz[:, ::-1])
+    np.testing.assert_array_equal(hz, hz.T)
+    np.testing.assert_array_equal(ex, ex[::-1, :])
+    np.testing.assert_array_equal(ex, -ex[:, ::-1])
+    np.testing.assert_array_equal(ey, -ey[::-1, :])
+    np.testing.assert_array_equal(ey, -ex.T)
+
+
+def test_engine_discrete_energy_is_conserved(gpu):
+    """W = ½Σε(Eⁿ)² + ½Σμ H^(n−½)H^(n+½) is invariant in a PEC cavity (Etalon test_numpy_backend.py:21-58).
+
+    Anisotropic cells and a dielectric block, so a swapped axis or a wrong sign breaks it.
+    """
+    nx, ny, dx, dy = 40, 30, 0.05, 0.04
+    grid = ph.YeeGrid2D(nx=nx, ny=ny, dx=dx, dy=dy, dt=ph.courant_time_step(0.99, dx, dy),
+                        pml_layers=0, x_min=0.0, y_min=0.0)  # fmt: skip
+    eps = {c: np.ones(grid.shape(c)) for c in ("Ex", "Ey")}
+    eps["Ex"][10:25, 8:20] = 4.0
+    eps["Ey"][10:25, 8:20] = 4.0
+
+    def no_pml(n):
+        return ph.CPMLAxis(np.ones(n + 1), np.zeros(n + 1), np.ones(n + 1), np.ones(n), np.zeros(n), np.ones(n))
+
+    p = ph.TEProblem(grid, eps, no_pml(nx), no_pml(ny), [], [], "double", n_steps=2000)
+    e = TEEngine(p)
+    x, y = grid.coords("Hz")
+    e.set_field("hz", np.exp(-((x[:, None] - 0.8) ** 2 + (y[None, :] - 0.5) ** 2) / 0.02))
+    h_prev = e.field("hz")
+    ex_prev, ey_prev = e.field("ex"), e.field("ey")
+    energies = []
+    for _ in range(2000):
+        e.advance(1)  # E^n, H^(n−½) → E^(n+1), H^(n+½)
+        hz = e.field("hz")
+        w = 0.5 * ph.EPSILON_0 * ((eps["Ex"] * ex_prev**2).sum() + (eps["Ey"] * ey_prev**2).sum())
+        energies.append(w + 0.5 * ph.MU_0 * (h_prev * hz).sum())
+        h_prev, ex_prev, ey_prev = hz, e.field("ex"), e.field("ey")
+    assert np.abs(ex_prev).max() > 0
+    energies = np.array(energies)
+    np.testing.assert_allclose(energies, energies[0], rtol=1e-11)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_reset_replays_bit_for_bit(gpu, precision):
+    g = load("small", precision)
+    e, n = engine_with_reference_inputs("small", precision, g)
+    e.advance(n)
+    first = engine_outputs(e)
+    e.reset()
+    assert e.n == 0
+    e.advance(n)
+    second = engine_outputs(e)
+    for f in FIELDS:
+        np.testing.assert_array_equal(first[0][f], second[0][f])
+    assert compare_outputs(g, *second) == []
+
+
+def test_missing_table_rows_are_an_error_not_garbage(gpu):
+    p = cases.small("single")
+    e = TEEngine(p)
+    e.set_source_table(0, 0, p.injections[0].delta_table(0, 10, p.grid.dt, p.real))
+    with pytest.raises(_lib.EtgError, match="deltas for steps"):
+        _lib.call("etg_sim_advance", e._h, 20)
+
+
+def test_nonfinite_field_is_reported(gpu):
+    p = cases.small("single")
+    e = TEEngine(p)
+    e.set_option(_lib.OPT_CHECK_FINITE, 1)
+    hz = np.zeros(e.field_shape("hz"), np.float32)
+    hz[5, 5] = np.inf
+    e.set_field("hz", hz)
+    e.advance(3)
+    with pytest.raises(_lib.NonFiniteField):
+        e.synchronize()
+
+
+# ----------------------------------------------------------------- headline size
+
+
+def _config2_fixture_usable(g, p):
+    """Whether this machine's host tables are Etalon's (the fixture stores their hashes)."""
+    n = int(g["n_steps"])
+    for k, inj in enumerate(p.injections):
+        if sha(inj.delta_table(0, n, p.grid.dt, p.real)) != str(g[f"src{k}_table_sha"]):
+            return False
+    for k, s in enumerate(p.samplings):
+        if sha(ph.phasor_table(s, 0, n, p.grid.dt, p.complex)) != str(g[f"mon{k}_table_sha"]):
+            return False
+    return True
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_config2_full_length_matches_reference(gpu, precision):
+    """2024² (2000² + 12-layer CPML) Si strip: 10 000 steps fp32 / 1 000 steps fp64 vs Etalon."""
+    if not (GOLDEN / f"config2_{precision}.npz").exists():
+        pytest.skip("config2 fixture not generated")
+    g = load("config2", precision)
+    n = int(g["n_steps"])
+    p = cases.config2(precision, n_steps=n)
+    if not _config2_fixture_usable(g, p):
+        pytest.skip("this platform's float64 libm gives other host tables than the fixture's; "
+                    "parity at this size is then pinned by test_config2_prefix_vs_live_oracle")
+    c = ph.cast_coefficients(p)
+    assert sha(c.cb_ex) == str(g["in_cb_ex_sha"]) and sha(c.cb_ey) == str(g["in_cb_ey_sha"])
+    for k in COEFFS[2:]:
+        setattr(c, k, g[f"in_{k}"])
+    e = TEEngine(p)
+    e.set_coefficients(c)
+    e.advance(n)
+    e.synchronize()
+    assert compare_outputs(g, *engine_outputs(e)) == []
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_config2_prefix_vs_live_oracle(gpu, precision):
+    """The headline grid for 120 steps against the oracle run on this host's cores."""
+    n = 120
+    p = cases.config2(precision, n_steps=n)
+    e = TEEngine(p)
+    e.advance(n)
+    o = _oracle_for(p)
+    workers = min(16, os.cpu_count() or 1)
+    with ThreadPoolExecutor(workers) as pool:
+        o.run(n, pool=pool, bands=workers)
+    for f in FIELDS:
+        np.testing.assert_array_equal(e.field(f), getattr(o, f), err_msg=f)
+    for k, acc in enumerate(o.acc):
+        np.testing.assert_array_equal(e.dft(k), acc)
+
+
+def _oracle_for(p):
+    from oracle.te_numpy import OracleMonitor, OracleSource, OracleTE
+
+    return OracleTE(
+        p.grid.nx, p.grid.ny, p.grid.dt, vars(ph.cast_coefficients(p)), p.real,
+        [OracleSource(i.component, i.i, i.j, i.coefficient,
+                      (i.pulse.wavelength, i.pulse.bandwidth, i.pulse.amplitude)) for i in p.injections],
+        [OracleMonitor(s.component, s.flat_index, s.frequencies) for s in p.samplings],
+    )  # fmt: skip

@@ -43,7 +43,9 @@ struct etg_sim {
   bool have_coeffs = false;
   // rows / columns whose psi may be non-zero (from c != 0, b outside (0, inf) or uploaded psi)
   std::vector<char> live_x, live_y, psi_live_x, psi_live_y;
+  std::vector<char> nonunit_x, nonunit_y;  // rows / columns whose CPML terms are not "+ 0"
   int xs_lo = 0, xs_hi = 0, ys_lo = 0, ys_hi = 0;
+  int ux_lo = 0, ux_hi = 0, uy_lo = 0, uy_hi = 0;
   std::vector<Source> sources;
   std::vector<Monitor> monitors;
   int64_t* d_step = nullptr;
@@ -96,10 +98,15 @@ void update_strips(etg_sim* s) {
   std::vector<char> lx(s->nx + 1, 0), ly(s->ny + 1, 0);
   for (int k = 0; k <= s->nx; ++k) lx[k] = s->live_x[k] || s->psi_live_x[k];
   for (int k = 0; k <= s->ny; ++k) ly[k] = s->live_y[k] || s->psi_live_y[k];
-  const int old[4] = {s->xs_lo, s->xs_hi, s->ys_lo, s->ys_hi};
+  const int old[8] = {s->xs_lo, s->xs_hi, s->ys_lo, s->ys_hi, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi};
   strip_bounds(lx, &s->xs_lo, &s->xs_hi);
   strip_bounds(ly, &s->ys_lo, &s->ys_hi);
-  if (old[0] != s->xs_lo || old[1] != s->xs_hi || old[2] != s->ys_lo || old[3] != s->ys_hi) {
+  for (int k = 0; k <= s->nx; ++k) lx[k] = lx[k] || s->nonunit_x[k];
+  for (int k = 0; k <= s->ny; ++k) ly[k] = ly[k] || s->nonunit_y[k];
+  strip_bounds(lx, &s->ux_lo, &s->ux_hi);
+  strip_bounds(ly, &s->uy_lo, &s->uy_hi);
+  const int now[8] = {s->xs_lo, s->xs_hi, s->ys_lo, s->ys_hi, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi};
+  if (memcmp(old, now, sizeof old) != 0) {
     invalidate_graphs(s);  // the strip bounds are captured kernel parameters
     if (s->tb) tb_invalidate(s->tb);
   }
@@ -130,6 +137,10 @@ SimArgs<T> sim_args(etg_sim* s) {
   a.xs_hi = s->xs_hi;
   a.ys_lo = s->ys_lo;
   a.ys_hi = s->ys_hi;
+  a.ux_lo = s->ux_lo;
+  a.ux_hi = s->ux_hi;
+  a.uy_lo = s->uy_lo;
+  a.uy_hi = s->uy_hi;
   a.step = s->d_step;
   a.flag = s->d_flag;
   return a;
@@ -291,6 +302,8 @@ int etg_sim_create(etg_sim** out, int dtype, int nx, int ny) {
   s->live_y.assign(ny + 1, 0);
   s->psi_live_x.assign(nx + 1, 0);
   s->psi_live_y.assign(ny + 1, 0);
+  s->nonunit_x.assign(nx + 1, 1);
+  s->nonunit_y.assign(ny + 1, 1);
   int rc = ETG_OK;
   auto fail = [&](int code) {
     etg_sim_destroy(s);
@@ -363,14 +376,29 @@ int etg_sim_set_coefficients(etg_sim* s, const void* cb_ex, const void* cb_ey, c
   // live CPML rows/columns: psi_hz_x (h, i < nx), psi_ey_x (e, 1 <= i <= nx-1), same for y
   std::fill(s->live_x.begin(), s->live_x.end(), 0);
   std::fill(s->live_y.begin(), s->live_y.end(), 0);
+  std::fill(s->nonunit_x.begin(), s->nonunit_x.end(), 0);
+  std::fill(s->nonunit_y.begin(), s->nonunit_y.end(), 0);
   auto scan = [&](auto tag) {
     using T = decltype(tag);
     const T *bxe = (const T*)bx_e, *cxe = (const T*)cx_e, *bxh = (const T*)bx_h, *cxh = (const T*)cx_h;
     const T *bye = (const T*)by_e, *cye = (const T*)cy_e, *byh = (const T*)by_h, *cyh = (const T*)cy_h;
-    for (int i = 0; i < s->nx; ++i) s->live_x[i] |= coefficient_live(bxh[i], cxh[i]);
-    for (int i = 1; i < s->nx; ++i) s->live_x[i] |= coefficient_live(bxe[i], cxe[i]);
-    for (int j = 0; j < s->ny; ++j) s->live_y[j] |= coefficient_live(byh[j], cyh[j]);
-    for (int j = 1; j < s->ny; ++j) s->live_y[j] |= coefficient_live(bye[j], cye[j]);
+    const T *kxe = (const T*)ikx_e, *kxh = (const T*)ikx_h, *kye = (const T*)iky_e, *kyh = (const T*)iky_h;
+    for (int i = 0; i < s->nx; ++i) {
+      s->live_x[i] |= coefficient_live(bxh[i], cxh[i]);
+      s->nonunit_x[i] |= !(kxh[i] == T(1));
+    }
+    for (int i = 1; i < s->nx; ++i) {
+      s->live_x[i] |= coefficient_live(bxe[i], cxe[i]);
+      s->nonunit_x[i] |= !(kxe[i] == T(1));
+    }
+    for (int j = 0; j < s->ny; ++j) {
+      s->live_y[j] |= coefficient_live(byh[j], cyh[j]);
+      s->nonunit_y[j] |= !(kyh[j] == T(1));
+    }
+    for (int j = 1; j < s->ny; ++j) {
+      s->live_y[j] |= coefficient_live(bye[j], cye[j]);
+      s->nonunit_y[j] |= !(kye[j] == T(1));
+    }
   };
   if (s->dtype == ETG_F32) scan(float{}); else scan(double{});
   if (s->db != db || s->inv_dx != inv_dx || s->inv_dy != inv_dy) {

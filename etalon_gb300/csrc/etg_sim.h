@@ -49,6 +49,9 @@ struct SimArgs {
   // CPML strips: rows i < xs_lo or i >= xs_hi, columns j < ys_lo or j >= ys_hi carry psi;
   // everywhere else psi is exactly +0 and is neither read nor written.
   int xs_lo, xs_hi, ys_lo, ys_hi;
+  // Unit rectangle: rows [ux_lo, ux_hi) x columns [uy_lo, uy_hi) have c = 0, b > 0 and
+  // 1/kappa = 1 exactly and no psi, so the CPML terms of their update reduce to "+ 0".
+  int ux_lo, ux_hi, uy_lo, uy_hi;
   int64_t* step;  // device step counter n of the first step of a launch block
   int* flag;      // device error bits (ERRBIT_*)
 };

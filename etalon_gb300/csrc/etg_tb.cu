@@ -1,22 +1,577 @@
-// Temporally blocked kernels: not enabled yet; the one-step kernels run every advance.
+// Temporally blocked 2D TE kernels: K whole time steps per launch, one HBM pass.
+//
+// The grid of cells (i, j) in [0, nx] x [0, ny] — each cell holding Hz(i, j), Ex(i, j),
+// Ey(i, j) on the shared pitched index i * P + j — is cut into output tiles of OR x OC
+// cells. A CTA loads its tile plus a halo of K cells on every side (one step of the
+// leapfrog reads at most one neighbour in each direction, so K steps need K cells),
+// advances the extended tile K steps on chip, and writes the output tile to the other
+// buffer of a ping-pong pair. Halo cells are recomputed by every tile that needs them,
+// from the same inputs with the same operations, so they are bit-identical to the
+// owner's values; point sources are injected wherever a tile holds the node, and DFT
+// monitors accumulate only in the owning tile, in step order.
+//
+// Threads own fixed cells: lane -> column lane + 32u (u < U), warp row -> row ty + 8v
+// (v < V), so a CTA of 32 x 8 threads covers ER = 8V rows and EC = 32U columns. A thread
+// keeps its own Ex, Ey, Hz in registers; neighbours are read from shared memory, which
+// each half step refreshes behind a barrier (H reads Ex, Ey; E reads Hz).
+//
+// Interior tiles (whose extended region lies in the unit rectangle, where c = 0 and
+// 1/kappa = 1 exactly) take the lean update: the CPML terms there are b*0 + 0*d = +0 and
+// d * 1 = d, so Etalon's expression reduces exactly to "d + 0" for finite d. CPML tiles
+// run Etalon's full expression with psi held in shared memory.
+#include <algorithm>
+#include <vector>
+
 #include "etg_tb.h"
 
 namespace etg {
 
-struct TBState {};
+constexpr int TB_THREADS = 256;
+
+template <typename T>
+struct TBDst {
+  T *ex, *ey, *hz, *psi_ex_y, *psi_ey_x, *psi_hz_x, *psi_hz_y;
+};
+
+template <typename T, int V, int U, int K, bool PML>
+struct TBShape {
+  static constexpr int ER = 8 * V, EC = 32 * U, OR = ER - 2 * K, OC = EC - 2 * K;
+  static constexpr int PLANES = PML ? 7 : 3;
+  static constexpr size_t SMEM = (size_t)PLANES * ER * EC * sizeof(T);
+  static_assert(V * U <= 32, "cell masks are 32 bits");
+  static_assert(OR > 0 && OC > 0, "halo larger than the tile");
+};
+
+template <typename T>
+__device__ __forceinline__ T zero() { return T(0); }
+
+template <typename T, int V, int U, int K, bool PML>
+__global__ void __launch_bounds__(TB_THREADS, 1)
+k_tb_step(SimArgs<T> a, TBDst<T> dst, const int2* __restrict__ tiles, PhasePlan<T> ph,
+          PhasePlan<T> pe, int step_off) {
+  using S = TBShape<T, V, U, K, PML>;
+  constexpr int ER = S::ER, EC = S::EC, PL = ER * EC;
+  extern __shared__ __align__(16) unsigned char tb_smem[];
+  T* sEx = reinterpret_cast<T*>(tb_smem);
+  T* sEy = sEx + PL;
+  T* sHz = sEy + PL;
+  T* sPsi = sHz + PL;  // PML only: psi_hz_x, psi_hz_y, psi_ex_y, psi_ey_x planes
+  __shared__ uint32_t s_rel[4];  // relevant plan entries: H sources, E sources, H monitors, E monitors
+
+  const int lane = threadIdx.x, ty = threadIdx.y;
+  const int2 tile = tiles[blockIdx.x];
+  const int R0 = tile.x - K, C0 = tile.y - K;  // global cell of local (0, 0)
+  const int nx = a.nx, ny = a.ny;
+  const int64_t P = a.P;
+
+  // which plan entries touch this tile (sources: extended region; monitors: output region)
+  if (ty == 0) {
+    auto src_hits = [&](const PhasePlan<T>& p) {
+      bool hit = false;
+      if (lane < p.n_src) {
+        const SrcDesc<T>& d = p.src[lane];
+        hit = d.i >= R0 && d.i < R0 + ER && d.j >= C0 && d.j < C0 + EC;
+      }
+      return __ballot_sync(0xffffffffu, hit);
+    };
+    auto mon_hits = [&](const PhasePlan<T>& p) {
+      bool hit = false;
+      if (lane < p.n_mon) {
+        const MonDesc<T>& d = p.mon[lane];
+        hit = d.ix0 < tile.x + S::OR && d.ix0 + d.nxm > tile.x && d.jy0 < tile.y + S::OC &&
+              d.jy0 + d.nym > tile.y;
+      }
+      return __ballot_sync(0xffffffffu, hit);
+    };
+    const uint32_t r0 = src_hits(ph), r1 = src_hits(pe), r2 = mon_hits(ph), r3 = mon_hits(pe);
+    if (lane == 0) {
+      s_rel[0] = r0;
+      s_rel[1] = r1;
+      s_rel[2] = r2;
+      s_rel[3] = r3;
+    }
+  }
+
+  T ex[V][U], ey[V][U], hz[V][U];
+  uint32_t mH = 0, mEx = 0, mEy = 0, mOut = 0;  // per-cell masks, bit c = v * U + u
+#pragma unroll
+  for (int v = 0; v < V; ++v)
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int li = ty + 8 * v, lj = lane + 32 * u, i = R0 + li, j = C0 + lj, c = v * U + u;
+      const bool in = (unsigned)i <= (unsigned)nx && (unsigned)j <= (unsigned)ny;
+      const int64_t g = (int64_t)i * P + j;
+      ex[v][u] = in ? a.ex[g] : zero<T>();
+      ey[v][u] = in ? a.ey[g] : zero<T>();
+      hz[v][u] = in ? a.hz[g] : zero<T>();
+      sEx[li * EC + lj] = ex[v][u];
+      sEy[li * EC + lj] = ey[v][u];
+      if (i >= 0 && i < nx && j >= 0 && j < ny && li < ER - 1 && lj < EC - 1) mH |= 1u << c;
+      if (i >= 0 && i < nx && j >= 1 && j <= ny - 1 && lj >= 1) mEx |= 1u << c;
+      if (i >= 1 && i <= nx - 1 && j >= 0 && j < ny && li >= 1) mEy |= 1u << c;
+      if (in && li >= K && li < K + S::OR && lj >= K && lj < K + S::OC) mOut |= 1u << c;
+      if (PML) {
+        const bool sx = i < a.xs_lo || i >= a.xs_hi, sy = j < a.ys_lo || j >= a.ys_hi;
+        sPsi[0 * PL + li * EC + lj] = (in && sx) ? a.psi_hz_x[g] : zero<T>();
+        sPsi[1 * PL + li * EC + lj] = (in && sy) ? a.psi_hz_y[g] : zero<T>();
+        sPsi[2 * PL + li * EC + lj] = (in && sy) ? a.psi_ex_y[g] : zero<T>();
+        sPsi[3 * PL + li * EC + lj] = (in && sx) ? a.psi_ey_x[g] : zero<T>();
+      }
+    }
+  __syncthreads();
+  const uint32_t relSrcH = s_rel[0], relSrcE = s_rel[1], relMonH = s_rel[2], relMonE = s_rel[3];
+  const int64_t n_base = *a.step + step_off;
+
+  for (int s = 0; s < K; ++s) {
+    const int64_t n = n_base + s;
+    // ---------------------------------------------------------------- H half step
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int c = v * U + u;
+        if (!(mH >> c & 1u)) continue;
+        const int li = ty + 8 * v, lj = lane + 32 * u;
+        const T exn = sEx[li * EC + lj + 1];
+        const T eyn = sEy[(li + 1) * EC + lj];
+        const T dex_dy = mul(sub(exn, ex[v][u]), a.inv_dy);
+        const T dey_dx = mul(sub(eyn, ey[v][u]), a.inv_dx);
+        if (!PML) {
+          hz[v][u] = add(hz[v][u], mul(a.db, sub(add(dex_dy, zero<T>()), add(dey_dx, zero<T>()))));
+        } else {
+          const int i = R0 + li, j = C0 + lj;
+          const bool sx = i < a.xs_lo || i >= a.xs_hi, sy = j < a.ys_lo || j >= a.ys_hi;
+          T* px_p = sPsi + 0 * PL + li * EC + lj;
+          T* py_p = sPsi + 1 * PL + li * EC + lj;
+          const T py = add(mul(a.by_h[j], *py_p), mul(a.cy_h[j], dex_dy));
+          const T px = add(mul(a.bx_h[i], *px_p), mul(a.cx_h[i], dey_dx));
+          if (sy) *py_p = py;
+          if (sx) *px_p = px;
+          hz[v][u] = add(hz[v][u], mul(a.db, sub(add(mul(dex_dy, a.iky_h[j]), py),
+                                                 add(mul(dey_dx, a.ikx_h[i]), px))));
+        }
+      }
+    if (relSrcH) {  // magnetic sources at n dt, after the update (solver.py:120-123)
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = R0 + ty + 8 * v, j = C0 + lane + 32 * u;
+          for (uint32_t m = relSrcH; m; m &= m - 1) {
+            const SrcDesc<T>& d = ph.src[__ffs(m) - 1];
+            if (d.i != i || d.j != j) continue;
+            const int64_t r = n - d.n0;
+            if (r < 0 || r >= d.rows) atomicOr(a.flag, ERRBIT_TABLE);
+            else hz[v][u] = sub(hz[v][u], d.table[r * d.stride]);
+          }
+        }
+    }
+    if (relMonH) {  // DFT of H at (n + 1/2) dt, owned nodes only
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (!(mOut >> (v * U + u) & 1u)) continue;
+          const int i = R0 + ty + 8 * v, j = C0 + lane + 32 * u;
+          for (uint32_t m = relMonH; m; m &= m - 1) {
+            const MonDesc<T>& d = ph.mon[__ffs(m) - 1];
+            const unsigned di = (unsigned)(i - d.ix0), dj = (unsigned)(j - d.jy0);
+            if (di >= (unsigned)d.nxm || dj >= (unsigned)d.nym) continue;
+            const int64_t r = n - d.n0;
+            if (r < 0 || r >= d.rows) {
+              atomicOr(a.flag, ERRBIT_TABLE);
+              continue;
+            }
+            const int64_t nodes = (int64_t)d.nxm * d.nym, k = (int64_t)di * d.nym + dj;
+            const T* phr = d.table + 2 * r * d.n_f;
+            for (int f = 0; f < d.n_f; ++f) {
+              T* acc = d.acc + 2 * (f * nodes + k);
+              acc[0] = add(acc[0], mul(hz[v][u], phr[2 * f]));
+              acc[1] = add(acc[1], mul(hz[v][u], phr[2 * f + 1]));
+            }
+          }
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+#pragma unroll
+      for (int u = 0; u < U; ++u) sHz[(ty + 8 * v) * EC + lane + 32 * u] = hz[v][u];
+    __syncthreads();
+    // ---------------------------------------------------------------- E half step
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int c = v * U + u;
+        const int li = ty + 8 * v, lj = lane + 32 * u;
+        const int i = R0 + li, j = C0 + lj;
+        const int64_t g = (int64_t)i * P + j;
+        if (mEx >> c & 1u) {
+          const T d = mul(sub(hz[v][u], sHz[li * EC + lj - 1]), a.inv_dy);
+          const T cb = a.cb_ex[g];
+          if (!PML) {
+            ex[v][u] = add(ex[v][u], mul(cb, add(d, zero<T>())));
+          } else {
+            T* pp = sPsi + 2 * PL + li * EC + lj;
+            const T p = add(mul(a.by_e[j], *pp), mul(a.cy_e[j], d));
+            if (j < a.ys_lo || j >= a.ys_hi) *pp = p;
+            ex[v][u] = add(ex[v][u], mul(cb, add(mul(d, a.iky_e[j]), p)));
+          }
+        }
+        if (mEy >> c & 1u) {
+          const T d = mul(sub(hz[v][u], sHz[(li - 1) * EC + lj]), a.inv_dx);
+          const T cb = a.cb_ey[g];
+          if (!PML) {
+            ey[v][u] = sub(ey[v][u], mul(cb, add(d, zero<T>())));
+          } else {
+            T* pp = sPsi + 3 * PL + li * EC + lj;
+            const T p = add(mul(a.bx_e[i], *pp), mul(a.cx_e[i], d));
+            if (i < a.xs_lo || i >= a.xs_hi) *pp = p;
+            ey[v][u] = sub(ey[v][u], mul(cb, add(mul(d, a.ikx_e[i]), p)));
+          }
+        }
+      }
+    if (relSrcE) {  // electric sources at (n + 1/2) dt (solver.py:124-125)
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = R0 + ty + 8 * v, j = C0 + lane + 32 * u;
+          for (uint32_t m = relSrcE; m; m &= m - 1) {
+            const SrcDesc<T>& d = pe.src[__ffs(m) - 1];
+            if (d.i != i || d.j != j) continue;
+            const int64_t r = n - d.n0;
+            if (r < 0 || r >= d.rows) {
+              atomicOr(a.flag, ERRBIT_TABLE);
+              continue;
+            }
+            if (d.comp == ETG_EX) ex[v][u] = sub(ex[v][u], d.table[r * d.stride]);
+            else ey[v][u] = sub(ey[v][u], d.table[r * d.stride]);
+          }
+        }
+    }
+    if (relMonE) {  // DFT of E at (n + 1) dt
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (!(mOut >> (v * U + u) & 1u)) continue;
+          const int i = R0 + ty + 8 * v, j = C0 + lane + 32 * u;
+          for (uint32_t m = relMonE; m; m &= m - 1) {
+            const MonDesc<T>& d = pe.mon[__ffs(m) - 1];
+            const unsigned di = (unsigned)(i - d.ix0), dj = (unsigned)(j - d.jy0);
+            if (di >= (unsigned)d.nxm || dj >= (unsigned)d.nym) continue;
+            const int64_t r = n - d.n0;
+            if (r < 0 || r >= d.rows) {
+              atomicOr(a.flag, ERRBIT_TABLE);
+              continue;
+            }
+            const T val = d.comp == ETG_EX ? ex[v][u] : ey[v][u];
+            const int64_t nodes = (int64_t)d.nxm * d.nym, k = (int64_t)di * d.nym + dj;
+            const T* phr = d.table + 2 * r * d.n_f;
+            for (int f = 0; f < d.n_f; ++f) {
+              T* acc = d.acc + 2 * (f * nodes + k);
+              acc[0] = add(acc[0], mul(val, phr[2 * f]));
+              acc[1] = add(acc[1], mul(val, phr[2 * f + 1]));
+            }
+          }
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int o = (ty + 8 * v) * EC + lane + 32 * u;
+        sEx[o] = ex[v][u];
+        sEy[o] = ey[v][u];
+      }
+    __syncthreads();
+  }
+
+  // write the output tile to the other buffer
+#pragma unroll
+  for (int v = 0; v < V; ++v)
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (!(mOut >> (v * U + u) & 1u)) continue;
+      const int li = ty + 8 * v, lj = lane + 32 * u, i = R0 + li, j = C0 + lj;
+      const int64_t g = (int64_t)i * P + j;
+      dst.ex[g] = ex[v][u];
+      dst.ey[g] = ey[v][u];
+      dst.hz[g] = hz[v][u];
+      if (PML) {
+        const bool sx = i < a.xs_lo || i >= a.xs_hi, sy = j < a.ys_lo || j >= a.ys_hi;
+        if (sx) {
+          dst.psi_hz_x[g] = sPsi[0 * PL + li * EC + lj];
+          dst.psi_ey_x[g] = sPsi[3 * PL + li * EC + lj];
+        }
+        if (sy) {
+          dst.psi_hz_y[g] = sPsi[1 * PL + li * EC + lj];
+          dst.psi_ex_y[g] = sPsi[2 * PL + li * EC + lj];
+        }
+      }
+    }
+}
+
+// ------------------------------------------------------------------------ host side
+
+struct TBConfig {
+  int dtype, V, U, K;
+};
+
+// Compiled tile shapes: (rows = 8V, columns = 32U, steps K).
+static const TBConfig kConfigs[] = {
+    {ETG_F32, 6, 4, 4}, {ETG_F32, 6, 4, 3}, {ETG_F32, 6, 4, 2}, {ETG_F32, 8, 4, 4},
+    {ETG_F32, 8, 4, 6}, {ETG_F32, 4, 4, 2}, {ETG_F32, 8, 2, 4},
+    {ETG_F64, 4, 4, 2}, {ETG_F64, 4, 4, 3}, {ETG_F64, 6, 2, 2},
+};
+static const TBConfig kDefault32 = {ETG_F32, 6, 4, 4};
+static const TBConfig kDefault64 = {ETG_F64, 4, 4, 2};
+
+struct TBState {
+  void* alt[7] = {};  // second buffer of each field / psi plane, same pitch
+  size_t alt_bytes = 0;
+  int2* tiles = nullptr;  // interior tiles first, then CPML tiles
+  int n_inner = 0, n_pml = 0;
+  TBConfig cfg = {0, 0, 0, 0};
+  int nx = -1, ny = -1;
+  bool tiles_valid = false;
+  std::map<int64_t, cudaGraphExec_t> graphs;
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
 
 TBState* tb_create() { return new TBState; }
-void tb_destroy(TBState* tb) { delete tb; }
-void tb_invalidate(TBState*) {}
+
+static void tb_drop_graphs(TBState* tb) {
+  for (auto& kv : tb->graphs) cudaGraphExecDestroy(kv.second);
+  tb->graphs.clear();
+}
+
+void tb_destroy(TBState* tb) {
+  if (!tb) return;
+  tb_drop_graphs(tb);
+  for (void* p : tb->alt) cudaFree(p);
+  cudaFree(tb->tiles);
+  if (tb->side) cudaStreamDestroy(tb->side);
+  if (tb->fork) cudaEventDestroy(tb->fork);
+  if (tb->join) cudaEventDestroy(tb->join);
+  delete tb;
+}
+
+void tb_invalidate(TBState* tb) {
+  if (!tb) return;
+  tb_drop_graphs(tb);
+  tb->tiles_valid = false;
+}
+
+// Chosen by "auto": float32 grids of at least 64 x 64 cells. In float64, GB300's FP64 rate
+// rather than HBM bounds the step, and the halo recomputation would cost more than it saves.
+template <typename T>
+bool tb_supported(int nx, int ny) {
+  return sizeof(T) == 4 && nx >= 64 && ny >= 64;
+}
+
+template <typename T, int V, int U, int K, bool PML>
+static cudaError_t tb_launch_one(const SimArgs<T>& a, const TBDst<T>& d, const int2* tiles, int n,
+                                 const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
+                                 cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  using S = TBShape<T, V, U, K, PML>;
+  k_tb_step<T, V, U, K, PML><<<n, dim3(32, 8), S::SMEM, s>>>(a, d, tiles, ph, pe, step_off);
+  g_launches += 1;
+  return cudaGetLastError();
+}
+
+template <typename T, int V, int U, int K>
+static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<T>& d,
+                                  const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
+                                  cudaStream_t s) {
+  // interior tiles on the main stream, CPML tiles on a side branch (parallel graph nodes)
+  cudaError_t e = cudaEventRecord(tb->fork, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(tb->side, tb->fork, 0);
+  if (e == cudaSuccess)
+    e = tb_launch_one<T, V, U, K, true>(a, d, tb->tiles + tb->n_inner, tb->n_pml, ph, pe, step_off, tb->side);
+  if (e == cudaSuccess) e = tb_launch_one<T, V, U, K, false>(a, d, tb->tiles, tb->n_inner, ph, pe, step_off, s);
+  if (e == cudaSuccess) e = cudaEventRecord(tb->join, tb->side);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, tb->join, 0);
+  return e;
+}
 
 template <typename T>
-bool tb_supported(int, int) { return false; }
+static SimArgs<T> swap_args(const SimArgs<T>& a, TBState* tb) {
+  SimArgs<T> b = a;
+  b.ex = (T*)tb->alt[ETG_EX];
+  b.ey = (T*)tb->alt[ETG_EY];
+  b.hz = (T*)tb->alt[ETG_HZ];
+  b.psi_ex_y = (T*)tb->alt[ETG_PSI_EX_Y];
+  b.psi_ey_x = (T*)tb->alt[ETG_PSI_EY_X];
+  b.psi_hz_x = (T*)tb->alt[ETG_PSI_HZ_X];
+  b.psi_hz_y = (T*)tb->alt[ETG_PSI_HZ_Y];
+  return b;
+}
 
 template <typename T>
-int tb_advance(TBState*, const SimArgs<T>&, const PhasePlan<T>&, const PhasePlan<T>&, int64_t,
-               const int64_t*, cudaStream_t) {
-  set_error("temporally blocked kernel not available in this build");
-  return ETG_ERR_STATE;
+static TBDst<T> as_dst(const SimArgs<T>& a) {
+  return TBDst<T>{a.ex, a.ey, a.hz, a.psi_ex_y, a.psi_ey_x, a.psi_hz_x, a.psi_hz_y};
+}
+
+// Two launches A -> B -> A covering 2K steps from step_off.
+template <typename T, int V, int U, int K>
+static cudaError_t tb_two(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& ph,
+                          const PhasePlan<T>& pe, int step_off, cudaStream_t s) {
+  const SimArgs<T> b = swap_args(a, tb);
+  cudaError_t e = tb_launch_pair<T, V, U, K>(tb, a, as_dst(b), ph, pe, step_off, s);
+  if (e == cudaSuccess) e = tb_launch_pair<T, V, U, K>(tb, b, as_dst(a), ph, pe, step_off + K, s);
+  return e;
+}
+
+// Dynamic shared memory above 48 KB must be allowed per kernel, before any launch or capture.
+template <typename T, int V, int U, int K>
+static cudaError_t tb_attrs() {
+  cudaError_t e = cudaFuncSetAttribute(k_tb_step<T, V, U, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)TBShape<T, V, U, K, false>::SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_tb_step<T, V, U, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TBShape<T, V, U, K, true>::SMEM);
+  return e;
+}
+
+template <typename T>
+struct TBFns {
+  cudaError_t (*two)(TBState*, const SimArgs<T>&, const PhasePlan<T>&, const PhasePlan<T>&, int, cudaStream_t);
+  cudaError_t (*attrs)();
+};
+
+template <typename T>
+static TBFns<T> pick(const TBConfig& c) {
+#define ETG_TB_CASE(DT, VV, UU, KK) \
+  if (c.dtype == DT && c.V == VV && c.U == UU && c.K == KK) return {&tb_two<T, VV, UU, KK>, &tb_attrs<T, VV, UU, KK>};
+  if constexpr (sizeof(T) == 4) {
+    ETG_TB_CASE(ETG_F32, 6, 4, 4)
+    ETG_TB_CASE(ETG_F32, 6, 4, 3)
+    ETG_TB_CASE(ETG_F32, 6, 4, 2)
+    ETG_TB_CASE(ETG_F32, 8, 4, 4)
+    ETG_TB_CASE(ETG_F32, 8, 4, 6)
+    ETG_TB_CASE(ETG_F32, 4, 4, 2)
+    ETG_TB_CASE(ETG_F32, 8, 2, 4)
+  } else {
+    ETG_TB_CASE(ETG_F64, 4, 4, 2)
+    ETG_TB_CASE(ETG_F64, 4, 4, 3)
+    ETG_TB_CASE(ETG_F64, 6, 2, 2)
+  }
+#undef ETG_TB_CASE
+  return {nullptr, nullptr};
+}
+
+template <typename T>
+static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt) {
+  const int dt = (int)sizeof(T);
+  TBConfig want = dt == 4 ? kDefault32 : kDefault64;
+  if (opt[ETG_OPT_TB_DEPTH] > 0) want.K = (int)opt[ETG_OPT_TB_DEPTH];
+  if (opt[ETG_OPT_TILE_ROWS] > 0) want.V = (int)(opt[ETG_OPT_TILE_ROWS] / 8);
+  if (opt[ETG_OPT_TILE_COLS] > 0) want.U = (int)(opt[ETG_OPT_TILE_COLS] / 32);
+  if (!pick<T>(want).two) {
+    std::string have;
+    for (const TBConfig& c : kConfigs)
+      if (c.dtype == dt) have += " " + std::to_string(8 * c.V) + "x" + std::to_string(32 * c.U) + "/K" + std::to_string(c.K);
+    set_error("no compiled temporally blocked kernel with tile %dx%d and depth %d (have:%s)",
+              8 * want.V, 32 * want.U, want.K, have.c_str());
+    return ETG_ERR_ARGUMENT;
+  }
+  if (want.V != tb->cfg.V || want.U != tb->cfg.U || want.K != tb->cfg.K || want.dtype != tb->cfg.dtype) {
+    tb_invalidate(tb);
+    tb->cfg = want;
+    ETG_TRY_CUDA(pick<T>(want).attrs());
+  }
+  const size_t bytes = (size_t)(a.nx + 2) * a.P * sizeof(T);
+  if (tb->alt_bytes != bytes) {
+    tb_invalidate(tb);
+    for (void*& p : tb->alt) {
+      cudaFree(p);
+      p = nullptr;
+    }
+    for (void*& p : tb->alt) {
+      if (cudaMalloc(&p, bytes) != cudaSuccess || cudaMemset(p, 0, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("temporal blocking: cannot allocate %zu bytes for the second field buffer", bytes);
+        return ETG_ERR_ALLOC;
+      }
+    }
+    tb->alt_bytes = bytes;
+  }
+  if (!tb->side) {
+    ETG_TRY_CUDA(cudaStreamCreateWithFlags(&tb->side, cudaStreamNonBlocking));
+    ETG_TRY_CUDA(cudaEventCreateWithFlags(&tb->fork, cudaEventDisableTiming));
+    ETG_TRY_CUDA(cudaEventCreateWithFlags(&tb->join, cudaEventDisableTiming));
+  }
+  if (!tb->tiles_valid || tb->nx != a.nx || tb->ny != a.ny) {
+    const int ER = 8 * tb->cfg.V, EC = 32 * tb->cfg.U, K = tb->cfg.K;
+    const int OR = ER - 2 * K, OC = EC - 2 * K;
+    std::vector<int2> inner, pml;
+    for (int r0 = 0; r0 <= a.nx; r0 += OR)
+      for (int c0 = 0; c0 <= a.ny; c0 += OC) {
+        const bool unit = r0 - K >= a.ux_lo && r0 + OR + K <= a.ux_hi && c0 - K >= a.uy_lo &&
+                          c0 + OC + K <= a.uy_hi;
+        (unit ? inner : pml).push_back(make_int2(r0, c0));
+      }
+    tb->n_inner = (int)inner.size();
+    tb->n_pml = (int)pml.size();
+    inner.insert(inner.end(), pml.begin(), pml.end());
+    cudaFree(tb->tiles);
+    tb->tiles = nullptr;
+    ETG_TRY_CUDA(cudaMalloc(&tb->tiles, inner.size() * sizeof(int2)));
+    ETG_TRY_CUDA(cudaMemcpy(tb->tiles, inner.data(), inner.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    tb->nx = a.nx;
+    tb->ny = a.ny;
+    tb->tiles_valid = true;
+    tb_drop_graphs(tb);
+  }
+  return ETG_OK;
+}
+
+template <typename T>
+int tb_advance(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& ph, const PhasePlan<T>& pe,
+               int64_t n_steps, const int64_t* opt, cudaStream_t s) {
+  int rc = tb_prepare<T>(tb, a, opt);
+  if (rc) return rc;
+  const auto two = pick<T>(tb->cfg).two;
+  const int K = tb->cfg.K;
+  const int64_t pairs = n_steps / (2 * K);
+  const int64_t per_graph = std::max<int64_t>(1, opt[ETG_OPT_GRAPH_STEPS] / (2 * K));
+  int64_t done = 0;  // pairs launched
+  if (opt[ETG_OPT_GRAPH_STEPS] > 0 && pairs >= per_graph) {
+    auto it = tb->graphs.find(per_graph);
+    if (it == tb->graphs.end()) {
+      cudaGraph_t graph;
+      ETG_TRY_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = cudaSuccess;
+      for (int64_t p = 0; p < per_graph && e == cudaSuccess; ++p) e = two(tb, a, ph, pe, (int)(2 * K * p), s);
+      if (e == cudaSuccess) launch_step_add<T>(a, 2 * K * per_graph, s);
+      cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+      ETG_REQUIRE(e == cudaSuccess && e2 == cudaSuccess, ETG_ERR_CUDA, "temporal-blocking graph capture failed: %s",
+                  cudaGetErrorString(e != cudaSuccess ? e : e2));
+      cudaGraphExec_t exec;
+      e = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+      it = tb->graphs.emplace(per_graph, exec).first;
+    }
+    for (; done + per_graph <= pairs; done += per_graph) {
+      ETG_TRY_CUDA(cudaGraphLaunch(it->second, s));
+      g_launches += 4 * per_graph + 1;
+    }
+  }
+  if (done < pairs) {
+    for (int64_t p = 0; done + p < pairs; ++p) ETG_TRY_CUDA(two(tb, a, ph, pe, (int)(2 * K * p), s));
+    launch_step_add<T>(a, 2 * K * (pairs - done), s);
+  }
+  // the remainder (< 2K steps) with the one-step kernels, in place on the primary buffer
+  const int64_t rem = n_steps - 2 * K * pairs;
+  for (int64_t k = 0; k < rem; ++k) launch_step_plain<T>(a, ph, pe, (int)k, s);
+  if (rem) launch_step_add<T>(a, rem, s);
+  ETG_LAUNCH_CHECK();
+  return ETG_OK;
 }
 
 template bool tb_supported<float>(int, int);

@@ -360,3 +360,94 @@ def _oracle_for(p):
                       (i.pulse.wavelength, i.pulse.bandwidth, i.pulse.amplitude)) for i in p.injections],
         [OracleMonitor(s.component, s.flat_index, s.frequencies) for s in p.samplings],
     )  # fmt: skip
+
+
+# ----------------------------------------------------------------- temporal blocking
+
+TB_SHAPES_F32 = [(48, 128, 4), (48, 128, 3), (48, 128, 2), (64, 128, 4), (64, 128, 6), (32, 128, 2), (64, 64, 4)]
+TB_SHAPES_F64 = [(32, 128, 2), (32, 128, 3), (48, 64, 2)]
+
+
+def _tb_engine(name, precision, g, shape, **kw):
+    e, n = engine_with_reference_inputs(name, precision, g, kernel="tb", **kw)
+    rows, cols, k = shape
+    e.set_option(_lib.OPT_TILE_ROWS, rows)
+    e.set_option(_lib.OPT_TILE_COLS, cols)
+    e.set_option(_lib.OPT_TB_DEPTH, k)
+    return e, n
+
+
+@pytest.mark.parametrize("name", ["config1", "g4_full"])
+@pytest.mark.parametrize(("precision", "shape"), [("single", s) for s in TB_SHAPES_F32] +
+                         [("double", s) for s in TB_SHAPES_F64])  # fmt: skip
+def test_tb_matches_reference(gpu, name, precision, shape):
+    """Every compiled tile shape and depth reproduces Etalon's run bit for bit."""
+    g = load(name, precision)
+    e, n = _tb_engine(name, precision, g, shape)
+    e.advance(n)
+    e.synchronize()
+    assert compare_outputs(g, *engine_outputs(e)) == []
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_tb_seams_and_remainders(gpu, precision):
+    """Blocks of 1, 2K−1, 2K, 2K+1 … steps (TB pairs, graph replays, one-step remainders) agree."""
+    g = load("g4_full", precision)
+    shape = (48, 128, 4) if precision == "single" else (32, 128, 2)
+    a, n = _tb_engine("g4_full", precision, g, shape)
+    a.advance(n)
+    b, _ = _tb_engine("g4_full", precision, g, shape, graph_steps=16)
+    k = shape[2]
+    done = 0
+    for step in (1, 2 * k - 1, 2 * k, 2 * k + 1, 3, 16, 17, 33, 64, 65):
+        b.advance(step)
+        done += step
+    b.advance(n - done)
+    fa, aa = engine_outputs(a)
+    fb, ab = engine_outputs(b)
+    for f in FIELDS:
+        np.testing.assert_array_equal(fa[f], fb[f], err_msg=f)
+    for x, y in zip(aa, ab):
+        np.testing.assert_array_equal(x, y)
+    assert compare_outputs(g, fb, ab) == []
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("steps", [4, 9])
+def test_tb_random_state_live_psi(gpu, precision, steps):
+    """Random fields, ψ and CPML on every node: every tile takes the full CPML path."""
+    from oracle import te_numpy
+
+    dtype = _dtype(precision)
+    grid, c, fields = cases.random_state_inputs(dtype)
+    p = ph.TEProblem(grid, {}, None, None, [], [], precision, n_steps=steps)
+    e = TEEngine.__new__(TEEngine)
+    _init_bare_engine(e, p, c)
+    e.set_kernel("tb")
+    e.set_option(_lib.OPT_TB_DEPTH, 2)
+    e.set_option(_lib.OPT_TILE_ROWS, 32)
+    e.set_option(_lib.OPT_TILE_COLS, 128)
+    for f, v in fields.items():
+        e.set_field(f, v)
+    e.advance(steps)
+    ref = SimpleNamespace(nx=grid.nx, ny=grid.ny, **vars(c), **{k: v.copy() for k, v in fields.items()})
+    for _ in range(steps):
+        te_numpy.update_h(ref)
+        te_numpy.update_e(ref)
+    for f in FIELDS:
+        np.testing.assert_array_equal(e.field(f), getattr(ref, f), err_msg=f)
+
+
+@pytest.mark.parametrize("region", [137, 211])
+def test_tb_odd_grids_vs_live_oracle(gpu, region):
+    """Odd and prime region sizes put tile edges across the CPML and the monitors."""
+    n = 40
+    p = cases.config2("single", n_steps=n, region=region)
+    e = TEEngine(p, kernel="tb")
+    e.advance(n)
+    o = _oracle_for(p)
+    o.run(n)
+    for f in FIELDS:
+        np.testing.assert_array_equal(e.field(f), getattr(o, f), err_msg=f)
+    for k, acc in enumerate(o.acc):
+        np.testing.assert_array_equal(e.dft(k), acc)

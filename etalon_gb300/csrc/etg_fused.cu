@@ -62,6 +62,25 @@ __device__ __forceinline__ void accumulate(const PhasePlan<T>& p, int comp, int 
   }
 }
 
+// Record Hz^(n+1/2) of the thread's nodes that lie in the trace window (adjoint support).
+template <typename T>
+__device__ __forceinline__ void write_trace(const TraceDesc<T>& t, int i, int j0, int64_t n,
+                                            const T* val, int* flag) {
+  if (!t.buf) return;
+  const unsigned di = (unsigned)(i - t.ti0);
+  if (di >= (unsigned)t.tnx || j0 + 3 < t.tj0 || j0 >= t.tj0 + t.tny) return;
+  const int64_t r = n - t.n0;
+  if (r < 0 || r >= t.rows) {
+    atomicOr(flag, ERRBIT_TABLE);
+    return;
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const unsigned dj = (unsigned)(j0 + u - t.tj0);
+    if (dj < (unsigned)t.tny) t.buf[(r * t.tnx + di) * t.tny + dj] = val[u];
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) k_fused_h(SimArgs<T> a, PhasePlan<T> plan, int step_off) {
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
@@ -96,6 +115,7 @@ __global__ void __launch_bounds__(128) k_fused_h(SimArgs<T> a, PhasePlan<T> plan
   apply_sources(plan, ETG_HZ, i, j0, n, hz.v, a.flag);
   hz.store(a.hz + row + j0);
   accumulate(plan, ETG_HZ, i, j0, n, hz.v, a.flag);
+  write_trace(plan.trace, i, j0, n, hz.v, a.flag);
 }
 
 template <typename T>

@@ -12,57 +12,7 @@
 #include "etg_sim.h"
 #include "etg_tb.h"
 
-namespace etg {
-
-struct Source {
-  int comp;
-  std::vector<int64_t> i, j;
-  void* table = nullptr;  // (rows, n_nodes) dtype
-  int64_t n0 = 0, rows = 0;
-};
-
-struct Monitor {
-  int comp, ix0, nxm, jy0, nym, n_f;
-  void* acc = nullptr;    // (n_f, nxm*nym) complex
-  void* table = nullptr;  // (rows, n_f) complex
-  int64_t n0 = 0, rows = 0;
-};
-
-}  // namespace etg
-
 using namespace etg;
-
-struct etg_sim {
-  int dtype = ETG_F32;
-  int nx = 0, ny = 0;
-  int64_t P = 0, rows = 0;
-  void* field[7] = {};  // ETG_EX .. ETG_PSI_HZ_Y, pitched
-  void* cb[2] = {};     // cb_ex, cb_ey, pitched
-  void* c1d[12] = {};   // bx_e cx_e ikx_e bx_h cx_h ikx_h by_e cy_e iky_e by_h cy_h iky_h
-  double db = 0, inv_dx = 0, inv_dy = 0;
-  bool have_coeffs = false;
-  // rows / columns whose psi may be non-zero (from c != 0, b outside (0, inf) or uploaded psi)
-  std::vector<char> live_x, live_y, psi_live_x, psi_live_y;
-  std::vector<char> nonunit_x, nonunit_y;  // rows / columns whose CPML terms are not "+ 0"
-  int xs_lo = 0, xs_hi = 0, ys_lo = 0, ys_hi = 0;
-  int ux_lo = 0, ux_hi = 0, uy_lo = 0, uy_hi = 0;
-  std::vector<Source> sources;
-  std::vector<Monitor> monitors;
-  int64_t* d_step = nullptr;
-  int* d_flag = nullptr;
-  int64_t h_step = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  double last_ms = 0;
-  int64_t last_launches = 0;
-  int64_t opt[8] = {0, 4, 32, 0, 0, 0, 0, 0};
-  std::map<int64_t, cudaGraphExec_t> graphs;  // keyed by steps per graph
-  TBState* tb = nullptr;                      // temporally blocked kernel state
-
-  size_t esize() const { return (size_t)dtype; }
-  int64_t field_rows(int f) const { return (f == ETG_EY || f == ETG_PSI_EY_X) ? nx + 1 : nx; }
-  int64_t field_cols(int f) const { return (f == ETG_EX || f == ETG_PSI_EX_Y) ? ny + 1 : ny; }
-};
 
 namespace {
 
@@ -165,7 +115,17 @@ int build_plans(etg_sim* s, PhasePlan<T>* ph, PhasePlan<T>* pe) {
       d.comp = src.comp;
     }
   }
+  if (s->trace_buf) {
+    ph->trace.buf = (T*)s->trace_buf;
+    ph->trace.n0 = s->trace_n0;
+    ph->trace.rows = s->trace_rows;
+    ph->trace.ti0 = s->trace_ti0;
+    ph->trace.tnx = s->trace_tnx;
+    ph->trace.tj0 = s->trace_tj0;
+    ph->trace.tny = s->trace_tny;
+  }
   for (const Monitor& m : s->monitors) {
+    if (!s->monitors_on) break;
     PhasePlan<T>* p = m.comp == ETG_HZ ? ph : pe;
     ETG_REQUIRE(p->n_mon < MAX_MONITORS, ETG_ERR_ARGUMENT,
                 "more than %d monitor components in one half step", MAX_MONITORS);
@@ -282,6 +242,25 @@ int zero_device(etg_sim* s) {
 }
 
 }  // namespace
+
+namespace etg {
+
+int sim_advance_internal(etg_sim* s, int64_t n_steps) {
+  if (n_steps == 0) return ETG_OK;
+  int rc = check_tables(s, n_steps);
+  if (rc) return rc;
+  rc = s->dtype == ETG_F32 ? advance_dispatch<float>(s, n_steps) : advance_dispatch<double>(s, n_steps);
+  if (rc) return rc;
+  s->h_step += n_steps;
+  return ETG_OK;
+}
+
+void sim_invalidate(etg_sim* s) {
+  invalidate_graphs(s);
+  if (s->tb) tb_invalidate(s->tb);
+}
+
+}  // namespace etg
 
 extern "C" {
 

@@ -28,12 +28,22 @@ struct MonDesc {
   int ix0, nxm, jy0, nym, n_f, comp;
 };
 
+// Trace of Hz^(n+1/2) over a window of cells, written at every H half step by the owner of
+// each cell: buf[(n - n0) * tnx * tny + (i - ti0) * tny + (j - tj0)]. Used by the adjoint.
+template <typename T>
+struct TraceDesc {
+  T* buf;  // nullptr: no trace
+  int64_t n0, rows;
+  int ti0, tnx, tj0, tny;
+};
+
 // Sources and monitors of one half step (H or E), passed by value as a kernel parameter.
 template <typename T>
 struct PhasePlan {
   int n_src, n_mon;
   SrcDesc<T> src[MAX_SRC_NODES];
   MonDesc<T> mon[MAX_MONITORS];
+  TraceDesc<T> trace;  // H plan only
 };
 
 // Fields and coefficients in HBM. Every 2D array has rows of pitch P elements (P a
@@ -69,4 +79,72 @@ void launch_step_add(const SimArgs<T>& a, int64_t k, cudaStream_t s);
 template <typename T>
 void launch_check_finite(const SimArgs<T>& a, cudaStream_t s);
 
+struct TBState;
+
+}  // namespace etg
+
+namespace etg {
+
+struct Source {
+  int comp;
+  std::vector<int64_t> i, j;
+  void* table = nullptr;  // (rows, n_nodes) dtype
+  int64_t n0 = 0, rows = 0;
+};
+
+struct Monitor {
+  int comp, ix0, nxm, jy0, nym, n_f;
+  void* acc = nullptr;    // (n_f, nxm*nym) complex
+  void* table = nullptr;  // (rows, n_f) complex
+  int64_t n0 = 0, rows = 0;
+};
+
+}  // namespace etg
+
+// The resident simulation behind the etg_sim_* entry points (internal layout).
+struct etg_sim {
+  using Source = etg::Source;
+  using Monitor = etg::Monitor;
+  using TBState = etg::TBState;
+  int dtype = ETG_F32;
+  int nx = 0, ny = 0;
+  int64_t P = 0, rows = 0;
+  void* field[7] = {};  // ETG_EX .. ETG_PSI_HZ_Y, pitched
+  void* cb[2] = {};     // cb_ex, cb_ey, pitched
+  void* c1d[12] = {};   // bx_e cx_e ikx_e bx_h cx_h ikx_h by_e cy_e iky_e by_h cy_h iky_h
+  double db = 0, inv_dx = 0, inv_dy = 0;
+  bool have_coeffs = false;
+  // rows / columns whose psi may be non-zero (from c != 0, b outside (0, inf) or uploaded psi)
+  std::vector<char> live_x, live_y, psi_live_x, psi_live_y;
+  std::vector<char> nonunit_x, nonunit_y;  // rows / columns whose CPML terms are not "+ 0"
+  int xs_lo = 0, xs_hi = 0, ys_lo = 0, ys_hi = 0;
+  int ux_lo = 0, ux_hi = 0, uy_lo = 0, uy_hi = 0;
+  std::vector<Source> sources;
+  std::vector<Monitor> monitors;
+  int64_t* d_step = nullptr;
+  int* d_flag = nullptr;
+  int64_t h_step = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0;
+  int64_t last_launches = 0;
+  int64_t opt[8] = {0, 4, 32, 0, 0, 0, 0, 0};
+  std::map<int64_t, cudaGraphExec_t> graphs;  // keyed by steps per graph
+  TBState* tb = nullptr;                      // temporally blocked kernel state
+  // adjoint support: Hz trace window and whether monitors accumulate (off while recomputing)
+  void* trace_buf = nullptr;
+  int64_t trace_n0 = 0, trace_rows = 0;
+  int trace_ti0 = 0, trace_tnx = 0, trace_tj0 = 0, trace_tny = 0;
+  bool monitors_on = true;
+
+  size_t esize() const { return (size_t)dtype; }
+  int64_t field_rows(int f) const { return (f == ETG_EY || f == ETG_PSI_EY_X) ? nx + 1 : nx; }
+  int64_t field_cols(int f) const { return (f == ETG_EX || f == ETG_PSI_EX_Y) ? ny + 1 : ny; }
+};
+
+
+namespace etg {
+// Internal entry points of etg_sim.cu used by the adjoint (etg_adjoint.cu).
+int sim_advance_internal(etg_sim* s, int64_t n_steps);  // advance without timing or fault injection
+void sim_invalidate(etg_sim* s);                        // drop graphs after a change of plans
 }  // namespace etg

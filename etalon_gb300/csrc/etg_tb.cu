@@ -2,24 +2,28 @@
 //
 // The grid of cells (i, j) in [0, nx] x [0, ny] — each cell holding Hz(i, j), Ex(i, j),
 // Ey(i, j) on the shared pitched index i * P + j — is cut into output tiles of OR x OC
-// cells. A CTA loads its tile plus a halo of K cells on every side (one step of the
-// leapfrog reads at most one neighbour in each direction, so K steps need K cells),
-// advances the extended tile K steps on chip, and writes the output tile to the other
-// buffer of a ping-pong pair. Halo cells are recomputed by every tile that needs them,
-// from the same inputs with the same operations, so they are bit-identical to the
-// owner's values; point sources are injected wherever a tile holds the node, and DFT
-// monitors accumulate only in the owning tile, in step order.
+// cells. A CTA loads its tile plus a halo of K cells on every side (one leapfrog step reads
+// at most one neighbour in each direction, so K steps need K cells), advances the extended
+// tile K steps in shared memory, and writes the output tile to the other buffer of a
+// ping-pong pair. Halo cells are recomputed by every tile that needs them, from the same
+// inputs with the same operations, so they are bit-identical to the owner's values; point
+// sources are injected wherever a tile holds the node, and DFT monitors accumulate only in
+// the owning tile, in step order. After step s only cells at least s from the tile edge are
+// valid; the edge cells read zero padding and are never used for an output cell.
 //
-// Threads own fixed cells: lane -> column lane + 32u (u < U), warp row -> row ty + 8v
-// (v < V), so a CTA of 32 x 8 threads covers ER = 8V rows and EC = 32U columns. A thread
-// keeps its own Ex, Ey, Hz in registers; neighbours are read from shared memory, which
-// each half step refreshes behind a barrier (H reads Ex, Ey; E reads Hz).
+// Layout on chip: Ex, Ey, Hz planes of (ER + 2) x (EC + 2W) elements (a zero pad row above
+// and below, W pad columns left and right). A warp owns one row at a time, each lane W
+// consecutive columns (one 128-bit access per plane); the column neighbours of a lane come
+// from the adjacent lane by shuffle, row neighbours from the planes, which each half step
+// refreshes behind a barrier (H reads Ex, Ey; E reads Hz). cb stays in registers.
 //
-// Interior tiles (whose extended region lies in the unit rectangle, where c = 0 and
-// 1/kappa = 1 exactly) take the lean update: the CPML terms there are b*0 + 0*d = +0 and
-// d * 1 = d, so Etalon's expression reduces exactly to "d + 0" for finite d. CPML tiles
-// run Etalon's full expression with psi held in shared memory.
+// Interior tiles — extended region inside [1, nx) x [1, ny) and inside the unit rectangle,
+// where c = 0 and 1/kappa = 1 exactly — take the lean update: Etalon's CPML terms are
+// b*0 + 0*d = +0 and d * 1 = d there, so its expression reduces exactly to "d + 0" for finite
+// d, and no cell of such a tile is a PEC edge. CPML tiles run Etalon's full expression with
+// per-cell domain checks and psi in four more planes.
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "etg_tb.h"
@@ -33,39 +37,136 @@ struct TBDst {
   T *ex, *ey, *hz, *psi_ex_y, *psi_ey_x, *psi_hz_x, *psi_hz_y;
 };
 
-template <typename T, int V, int U, int K, bool PML>
+template <typename T>
+struct TBVec;  // W elements per lane, one 16-byte access
+template <>
+struct TBVec<float> {
+  static constexpr int W = 4;
+  float v[4];
+  __device__ __forceinline__ void ld(const float* p) {
+    const float4 a = *reinterpret_cast<const float4*>(p);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  }
+  __device__ __forceinline__ void st(float* p) const {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+  __device__ __forceinline__ void zero() { v[0] = v[1] = v[2] = v[3] = 0.f; }
+};
+template <>
+struct TBVec<double> {
+  static constexpr int W = 2;
+  double v[2];
+  __device__ __forceinline__ void ld(const double* p) {
+    const double2 a = *reinterpret_cast<const double2*>(p);
+    v[0] = a.x; v[1] = a.y;
+  }
+  __device__ __forceinline__ void st(double* p) const {
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+  }
+  __device__ __forceinline__ void zero() { v[0] = v[1] = 0.0; }
+};
+
+template <typename T, int RPT, int K, bool PML>
 struct TBShape {
-  static constexpr int ER = 8 * V, EC = 32 * U, OR = ER - 2 * K, OC = EC - 2 * K;
+  static constexpr int W = TBVec<T>::W;
+  static constexpr int ER = 8 * RPT, EC = 32 * W, OR = ER - 2 * K, OC = EC - 2 * K;
+  static constexpr int SW = EC + 2 * W, PL = (ER + 2) * SW;
   static constexpr int PLANES = PML ? 7 : 3;
-  static constexpr size_t SMEM = (size_t)PLANES * ER * EC * sizeof(T);
-  static_assert(V * U <= 32, "cell masks are 32 bits");
+  static constexpr size_t SMEM = (size_t)PLANES * PL * sizeof(T);
+  static_assert(K % W == 0, "the halo must keep vectors aligned");
   static_assert(OR > 0 && OC > 0, "halo larger than the tile");
 };
 
 template <typename T>
 __device__ __forceinline__ T zero() { return T(0); }
 
-template <typename T, int V, int U, int K, bool PML>
-__global__ void __launch_bounds__(TB_THREADS, 1)
+// DFT of the owned output cells of one half step (H: Hz from sA; E: Ex from sA, Ey from sB).
+template <typename T, int RPT, int K, int W, int ER, int EC, int SW>
+__device__ __forceinline__ void tb_accumulate(const PhasePlan<T>& p, uint32_t rel, const T* sA,
+                                              const T* sB, int R0, int C0, int ty, int lane,
+                                              int64_t n, int* flag) {
+  for (uint32_t m = rel; m; m &= m - 1) {
+    const MonDesc<T>& d = p.mon[__ffs(m) - 1];
+    const int64_t r = n - d.n0;
+    if (r < 0 || r >= d.rows) {
+      atomicOr(flag, ERRBIT_TABLE);
+      continue;
+    }
+    const T* plane = (d.comp == ETG_EY) ? sB : sA;
+    const int64_t nodes = (int64_t)d.nxm * d.nym;
+    const T* phr = d.table + 2 * r * d.n_f;
+#pragma unroll
+    for (int t = 0; t < RPT; ++t) {
+      const int li = ty + 8 * t;
+      if (li < K || li >= ER - K) continue;
+      const unsigned di = (unsigned)(R0 + li - d.ix0);
+      if (di >= (unsigned)d.nxm) continue;
+#pragma unroll
+      for (int e = 0; e < W; ++e) {
+        const int lj = W * lane + e;
+        if (lj < K || lj >= EC - K) continue;
+        const unsigned dj = (unsigned)(C0 + lj - d.jy0);
+        if (dj >= (unsigned)d.nym) continue;
+        const T val = plane[(li + 1) * SW + W + lj];
+        const int64_t k = (int64_t)di * d.nym + dj;
+        for (int f = 0; f < d.n_f; ++f) {
+          T* acc = d.acc + 2 * (f * nodes + k);
+          acc[0] = add(acc[0], mul(val, phr[2 * f]));
+          acc[1] = add(acc[1], mul(val, phr[2 * f + 1]));
+        }
+      }
+    }
+  }
+}
+
+// Hz^(n+1/2) of the owned output cells inside the trace window (adjoint support).
+template <typename T, int RPT, int K, int W, int ER, int EC, int SW>
+__device__ __forceinline__ void tb_trace(const TraceDesc<T>& t, const T* sHz, int R0, int C0, int ty,
+                                         int lane, int64_t n, int* flag) {
+  const int64_t r = n - t.n0;
+  if (r < 0 || r >= t.rows) {
+    atomicOr(flag, ERRBIT_TABLE);
+    return;
+  }
+#pragma unroll
+  for (int q = 0; q < RPT; ++q) {
+    const int li = ty + 8 * q;
+    if (li < K || li >= ER - K) continue;
+    const unsigned di = (unsigned)(R0 + li - t.ti0);
+    if (di >= (unsigned)t.tnx) continue;
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      const int lj = W * lane + e;
+      if (lj < K || lj >= EC - K) continue;
+      const unsigned dj = (unsigned)(C0 + lj - t.tj0);
+      if (dj < (unsigned)t.tny) t.buf[(r * t.tnx + di) * t.tny + dj] = sHz[(li + 1) * SW + W + lj];
+    }
+  }
+}
+
+template <typename T, int RPT, int K, bool PML>
+__global__ void __launch_bounds__(TB_THREADS, PML ? 1 : 2)
 k_tb_step(SimArgs<T> a, TBDst<T> dst, const int2* __restrict__ tiles, PhasePlan<T> ph,
           PhasePlan<T> pe, int step_off) {
-  using S = TBShape<T, V, U, K, PML>;
-  constexpr int ER = S::ER, EC = S::EC, PL = ER * EC;
+  using S = TBShape<T, RPT, K, PML>;
+  using Vw = TBVec<T>;
+  constexpr int W = S::W, ER = S::ER, EC = S::EC, SW = S::SW, PL = S::PL;
   extern __shared__ __align__(16) unsigned char tb_smem[];
-  T* sEx = reinterpret_cast<T*>(tb_smem);
-  T* sEy = sEx + PL;
-  T* sHz = sEy + PL;
-  T* sPsi = sHz + PL;  // PML only: psi_hz_x, psi_hz_y, psi_ex_y, psi_ey_x planes
+  T* const sEx = reinterpret_cast<T*>(tb_smem);
+  T* const sEy = sEx + PL;
+  T* const sHz = sEy + PL;
+  T* const sPsi = sHz + PL;  // PML only: psi_hz_x, psi_hz_y, psi_ex_y, psi_ey_x planes
   __shared__ uint32_t s_rel[4];  // relevant plan entries: H sources, E sources, H monitors, E monitors
 
   const int lane = threadIdx.x, ty = threadIdx.y;
   const int2 tile = tiles[blockIdx.x];
-  const int R0 = tile.x - K, C0 = tile.y - K;  // global cell of local (0, 0)
+  const int R0 = tile.x - K, C0 = tile.y - K;  // global cell of local (0, 0); C0 % W == 0
   const int nx = a.nx, ny = a.ny;
   const int64_t P = a.P;
+  const int lj0 = W * lane, j0 = C0 + lj0;  // this lane's first column, local and global
+  const bool lane_in = j0 >= 0 && j0 + W <= P;
 
-  // which plan entries touch this tile (sources: extended region; monitors: output region)
-  if (ty == 0) {
+  if (ty == 0) {  // which plan entries touch this tile (sources: extended region; monitors: output)
     auto src_hits = [&](const PhasePlan<T>& p) {
       bool hit = false;
       if (lane < p.n_src) {
@@ -91,249 +192,235 @@ k_tb_step(SimArgs<T> a, TBDst<T> dst, const int2* __restrict__ tiles, PhasePlan<
       s_rel[3] = r3;
     }
   }
+  // zero padding: rows -1 and ER of every plane, W columns on each side
+  for (int k = threadIdx.x + 32 * ty; k < S::PLANES * 2 * SW; k += TB_THREADS) {
+    const int plane = k / (2 * SW), r = (k / SW) % 2, c = k % SW;
+    reinterpret_cast<T*>(tb_smem)[plane * PL + (r ? ER + 1 : 0) * SW + c] = zero<T>();
+  }
+  for (int k = threadIdx.x + 32 * ty; k < S::PLANES * ER * 2 * W; k += TB_THREADS) {
+    const int plane = k / (ER * 2 * W), r = (k / (2 * W)) % ER, c = k % (2 * W);
+    reinterpret_cast<T*>(tb_smem)[plane * PL + (r + 1) * SW + (c < W ? c : EC + c)] = zero<T>();
+  }
 
-  T ex[V][U], ey[V][U], hz[V][U];
-  uint32_t mH = 0, mEx = 0, mEy = 0, mOut = 0;  // per-cell masks, bit c = v * U + u
+  // load the extended tile; cb stays in registers for the E updates
+  T cbx[RPT][W], cby[RPT][W];
 #pragma unroll
-  for (int v = 0; v < V; ++v)
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int li = ty + 8 * v, lj = lane + 32 * u, i = R0 + li, j = C0 + lj, c = v * U + u;
-      const bool in = (unsigned)i <= (unsigned)nx && (unsigned)j <= (unsigned)ny;
-      const int64_t g = (int64_t)i * P + j;
-      ex[v][u] = in ? a.ex[g] : zero<T>();
-      ey[v][u] = in ? a.ey[g] : zero<T>();
-      hz[v][u] = in ? a.hz[g] : zero<T>();
-      sEx[li * EC + lj] = ex[v][u];
-      sEy[li * EC + lj] = ey[v][u];
-      if (i >= 0 && i < nx && j >= 0 && j < ny && li < ER - 1 && lj < EC - 1) mH |= 1u << c;
-      if (i >= 0 && i < nx && j >= 1 && j <= ny - 1 && lj >= 1) mEx |= 1u << c;
-      if (i >= 1 && i <= nx - 1 && j >= 0 && j < ny && li >= 1) mEy |= 1u << c;
-      if (in && li >= K && li < K + S::OR && lj >= K && lj < K + S::OC) mOut |= 1u << c;
-      if (PML) {
-        const bool sx = i < a.xs_lo || i >= a.xs_hi, sy = j < a.ys_lo || j >= a.ys_hi;
-        sPsi[0 * PL + li * EC + lj] = (in && sx) ? a.psi_hz_x[g] : zero<T>();
-        sPsi[1 * PL + li * EC + lj] = (in && sy) ? a.psi_hz_y[g] : zero<T>();
-        sPsi[2 * PL + li * EC + lj] = (in && sy) ? a.psi_ex_y[g] : zero<T>();
-        sPsi[3 * PL + li * EC + lj] = (in && sx) ? a.psi_ey_x[g] : zero<T>();
-      }
+  for (int t = 0; t < RPT; ++t) {
+    const int li = ty + 8 * t, i = R0 + li;
+    const bool in = lane_in && (unsigned)i <= (unsigned)nx;
+    const int64_t g = (int64_t)i * P + j0;
+    const int o = (li + 1) * SW + W + lj0;
+    Vw ex, ey, hz, cx, cy;
+    if (in) {
+      ex.ld(a.ex + g);
+      ey.ld(a.ey + g);
+      hz.ld(a.hz + g);
+      cx.ld(a.cb_ex + g);
+      cy.ld(a.cb_ey + g);
+    } else {
+      ex.zero();
+      ey.zero();
+      hz.zero();
+      cx.zero();
+      cy.zero();
     }
+    ex.st(sEx + o);
+    ey.st(sEy + o);
+    hz.st(sHz + o);
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      cbx[t][e] = cx.v[e];
+      cby[t][e] = cy.v[e];
+    }
+    if (PML) {
+      Vw p0, p1, p2, p3;
+      if (in) {
+        p0.ld(a.psi_hz_x + g);
+        p1.ld(a.psi_hz_y + g);
+        p2.ld(a.psi_ex_y + g);
+        p3.ld(a.psi_ey_x + g);
+      } else {
+        p0.zero();
+        p1.zero();
+        p2.zero();
+        p3.zero();
+      }
+      p0.st(sPsi + 0 * PL + o);
+      p1.st(sPsi + 1 * PL + o);
+      p2.st(sPsi + 2 * PL + o);
+      p3.st(sPsi + 3 * PL + o);
+    }
+  }
+  // CPML tiles: this lane's y profiles (per column) in registers
+  T byh[W], cyh[W], kyh[W], bye[W], cye[W], kye[W];
+  if (PML) {
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      const int j = min(max(j0 + e, 0), ny - 1);
+      const int je = min(max(j0 + e, 0), ny);
+      byh[e] = a.by_h[j];
+      cyh[e] = a.cy_h[j];
+      kyh[e] = a.iky_h[j];
+      bye[e] = a.by_e[je];
+      cye[e] = a.cy_e[je];
+      kye[e] = a.iky_e[je];
+    }
+  }
   __syncthreads();
   const uint32_t relSrcH = s_rel[0], relSrcE = s_rel[1], relMonH = s_rel[2], relMonE = s_rel[3];
   const int64_t n_base = *a.step + step_off;
+  const T db = a.db, idx = a.inv_dx, idy = a.inv_dy;
+  const bool traced = ph.trace.buf && ph.trace.ti0 < tile.x + S::OR && ph.trace.ti0 + ph.trace.tnx > tile.x &&
+                      ph.trace.tj0 < tile.y + S::OC && ph.trace.tj0 + ph.trace.tny > tile.y;
 
   for (int s = 0; s < K; ++s) {
     const int64_t n = n_base + s;
     // ---------------------------------------------------------------- H half step
 #pragma unroll
-    for (int v = 0; v < V; ++v)
+    for (int t = 0; t < RPT; ++t) {
+      const int li = ty + 8 * t;
+      const int o = (li + 1) * SW + W + lj0;
+      Vw ex, ey, eyn, hz;
+      ex.ld(sEx + o);
+      ey.ld(sEy + o);
+      eyn.ld(sEy + o + SW);
+      hz.ld(sHz + o);
+      T exr = __shfl_down_sync(0xffffffffu, ex.v[0], 1);
+      if (lane == 31) exr = sEx[o + W];
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int c = v * U + u;
-        if (!(mH >> c & 1u)) continue;
-        const int li = ty + 8 * v, lj = lane + 32 * u;
-        const T exn = sEx[li * EC + lj + 1];
-        const T eyn = sEy[(li + 1) * EC + lj];
-        const T dex_dy = mul(sub(exn, ex[v][u]), a.inv_dy);
-        const T dey_dx = mul(sub(eyn, ey[v][u]), a.inv_dx);
+      for (int e = 0; e < W; ++e) {
+        const T exn = e < W - 1 ? ex.v[e + 1] : exr;
+        const T dex_dy = mul(sub(exn, ex.v[e]), idy);
+        const T dey_dx = mul(sub(eyn.v[e], ey.v[e]), idx);
         if (!PML) {
-          hz[v][u] = add(hz[v][u], mul(a.db, sub(add(dex_dy, zero<T>()), add(dey_dx, zero<T>()))));
+          hz.v[e] = add(hz.v[e], mul(db, sub(add(dex_dy, zero<T>()), add(dey_dx, zero<T>()))));
         } else {
-          const int i = R0 + li, j = C0 + lj;
-          const bool sx = i < a.xs_lo || i >= a.xs_hi, sy = j < a.ys_lo || j >= a.ys_hi;
-          T* px_p = sPsi + 0 * PL + li * EC + lj;
-          T* py_p = sPsi + 1 * PL + li * EC + lj;
-          const T py = add(mul(a.by_h[j], *py_p), mul(a.cy_h[j], dex_dy));
-          const T px = add(mul(a.bx_h[i], *px_p), mul(a.cx_h[i], dey_dx));
-          if (sy) *py_p = py;
-          if (sx) *px_p = px;
-          hz[v][u] = add(hz[v][u], mul(a.db, sub(add(mul(dex_dy, a.iky_h[j]), py),
-                                                 add(mul(dey_dx, a.ikx_h[i]), px))));
+          const int i = R0 + li, j = j0 + e;
+          if (i >= 0 && i < nx && j >= 0 && j < ny) {
+            T* pxp = sPsi + 0 * PL + o + e;
+            T* pyp = sPsi + 1 * PL + o + e;
+            const T py = add(mul(byh[e], *pyp), mul(cyh[e], dex_dy));
+            const T px = add(mul(a.bx_h[i], *pxp), mul(a.cx_h[i], dey_dx));
+            if (j < a.ys_lo || j >= a.ys_hi) *pyp = py;
+            if (i < a.xs_lo || i >= a.xs_hi) *pxp = px;
+            hz.v[e] = add(hz.v[e], mul(db, sub(add(mul(dex_dy, kyh[e]), py), add(mul(dey_dx, a.ikx_h[i]), px))));
+          }
         }
       }
+      hz.st(sHz + o);
+    }
     if (relSrcH) {  // magnetic sources at n dt, after the update (solver.py:120-123)
-#pragma unroll
-      for (int v = 0; v < V; ++v)
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int i = R0 + ty + 8 * v, j = C0 + lane + 32 * u;
-          for (uint32_t m = relSrcH; m; m &= m - 1) {
-            const SrcDesc<T>& d = ph.src[__ffs(m) - 1];
-            if (d.i != i || d.j != j) continue;
-            const int64_t r = n - d.n0;
-            if (r < 0 || r >= d.rows) atomicOr(a.flag, ERRBIT_TABLE);
-            else hz[v][u] = sub(hz[v][u], d.table[r * d.stride]);
-          }
-        }
+      for (uint32_t m = relSrcH; m; m &= m - 1) {
+        const SrcDesc<T>& d = ph.src[__ffs(m) - 1];
+        const int li = d.i - R0, lj = d.j - C0;
+        if ((li & 7) != ty || lj / W != lane) continue;
+        const int64_t r = n - d.n0;
+        T* cell = sHz + (li + 1) * SW + W + lj;
+        if (r < 0 || r >= d.rows) atomicOr(a.flag, ERRBIT_TABLE);
+        else *cell = sub(*cell, d.table[r * d.stride]);
+      }
     }
-    if (relMonH) {  // DFT of H at (n + 1/2) dt, owned nodes only
-#pragma unroll
-      for (int v = 0; v < V; ++v)
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          if (!(mOut >> (v * U + u) & 1u)) continue;
-          const int i = R0 + ty + 8 * v, j = C0 + lane + 32 * u;
-          for (uint32_t m = relMonH; m; m &= m - 1) {
-            const MonDesc<T>& d = ph.mon[__ffs(m) - 1];
-            const unsigned di = (unsigned)(i - d.ix0), dj = (unsigned)(j - d.jy0);
-            if (di >= (unsigned)d.nxm || dj >= (unsigned)d.nym) continue;
-            const int64_t r = n - d.n0;
-            if (r < 0 || r >= d.rows) {
-              atomicOr(a.flag, ERRBIT_TABLE);
-              continue;
-            }
-            const int64_t nodes = (int64_t)d.nxm * d.nym, k = (int64_t)di * d.nym + dj;
-            const T* phr = d.table + 2 * r * d.n_f;
-            for (int f = 0; f < d.n_f; ++f) {
-              T* acc = d.acc + 2 * (f * nodes + k);
-              acc[0] = add(acc[0], mul(hz[v][u], phr[2 * f]));
-              acc[1] = add(acc[1], mul(hz[v][u], phr[2 * f + 1]));
-            }
-          }
-        }
-    }
-#pragma unroll
-    for (int v = 0; v < V; ++v)
-#pragma unroll
-      for (int u = 0; u < U; ++u) sHz[(ty + 8 * v) * EC + lane + 32 * u] = hz[v][u];
+    if (relMonH) tb_accumulate<T, RPT, K, W, ER, EC, SW>(ph, relMonH, sHz, nullptr, R0, C0, ty, lane, n, a.flag);
+    if (traced) tb_trace<T, RPT, K, W, ER, EC, SW>(ph.trace, sHz, R0, C0, ty, lane, n, a.flag);
     __syncthreads();
     // ---------------------------------------------------------------- E half step
 #pragma unroll
-    for (int v = 0; v < V; ++v)
+    for (int t = 0; t < RPT; ++t) {
+      const int li = ty + 8 * t;
+      const int o = (li + 1) * SW + W + lj0;
+      Vw hz, hzu, ex, ey;
+      hz.ld(sHz + o);
+      hzu.ld(sHz + o - SW);
+      ex.ld(sEx + o);
+      ey.ld(sEy + o);
+      T hzl = __shfl_up_sync(0xffffffffu, hz.v[W - 1], 1);
+      if (lane == 0) hzl = sHz[o - 1];
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int c = v * U + u;
-        const int li = ty + 8 * v, lj = lane + 32 * u;
-        const int i = R0 + li, j = C0 + lj;
-        const int64_t g = (int64_t)i * P + j;
-        if (mEx >> c & 1u) {
-          const T d = mul(sub(hz[v][u], sHz[li * EC + lj - 1]), a.inv_dy);
-          const T cb = a.cb_ex[g];
-          if (!PML) {
-            ex[v][u] = add(ex[v][u], mul(cb, add(d, zero<T>())));
-          } else {
-            T* pp = sPsi + 2 * PL + li * EC + lj;
-            const T p = add(mul(a.by_e[j], *pp), mul(a.cy_e[j], d));
+      for (int e = 0; e < W; ++e) {
+        const T hzp = e > 0 ? hz.v[e - 1] : hzl;
+        const T dy = mul(sub(hz.v[e], hzp), idy);
+        const T dx = mul(sub(hz.v[e], hzu.v[e]), idx);
+        if (!PML) {
+          ex.v[e] = add(ex.v[e], mul(cbx[t][e], add(dy, zero<T>())));
+          ey.v[e] = sub(ey.v[e], mul(cby[t][e], add(dx, zero<T>())));
+        } else {
+          const int i = R0 + li, j = j0 + e;
+          if (i >= 0 && i < nx && j >= 1 && j <= ny - 1) {
+            T* pp = sPsi + 2 * PL + o + e;
+            const T p = add(mul(bye[e], *pp), mul(cye[e], dy));
             if (j < a.ys_lo || j >= a.ys_hi) *pp = p;
-            ex[v][u] = add(ex[v][u], mul(cb, add(mul(d, a.iky_e[j]), p)));
+            ex.v[e] = add(ex.v[e], mul(cbx[t][e], add(mul(dy, kye[e]), p)));
           }
-        }
-        if (mEy >> c & 1u) {
-          const T d = mul(sub(hz[v][u], sHz[(li - 1) * EC + lj]), a.inv_dx);
-          const T cb = a.cb_ey[g];
-          if (!PML) {
-            ey[v][u] = sub(ey[v][u], mul(cb, add(d, zero<T>())));
-          } else {
-            T* pp = sPsi + 3 * PL + li * EC + lj;
-            const T p = add(mul(a.bx_e[i], *pp), mul(a.cx_e[i], d));
+          if (i >= 1 && i <= nx - 1 && j >= 0 && j < ny) {
+            T* pp = sPsi + 3 * PL + o + e;
+            const T p = add(mul(a.bx_e[i], *pp), mul(a.cx_e[i], dx));
             if (i < a.xs_lo || i >= a.xs_hi) *pp = p;
-            ey[v][u] = sub(ey[v][u], mul(cb, add(mul(d, a.ikx_e[i]), p)));
+            ey.v[e] = sub(ey.v[e], mul(cby[t][e], add(mul(dx, a.ikx_e[i]), p)));
           }
         }
       }
+      ex.st(sEx + o);
+      ey.st(sEy + o);
+    }
     if (relSrcE) {  // electric sources at (n + 1/2) dt (solver.py:124-125)
-#pragma unroll
-      for (int v = 0; v < V; ++v)
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int i = R0 + ty + 8 * v, j = C0 + lane + 32 * u;
-          for (uint32_t m = relSrcE; m; m &= m - 1) {
-            const SrcDesc<T>& d = pe.src[__ffs(m) - 1];
-            if (d.i != i || d.j != j) continue;
-            const int64_t r = n - d.n0;
-            if (r < 0 || r >= d.rows) {
-              atomicOr(a.flag, ERRBIT_TABLE);
-              continue;
-            }
-            if (d.comp == ETG_EX) ex[v][u] = sub(ex[v][u], d.table[r * d.stride]);
-            else ey[v][u] = sub(ey[v][u], d.table[r * d.stride]);
-          }
-        }
-    }
-    if (relMonE) {  // DFT of E at (n + 1) dt
-#pragma unroll
-      for (int v = 0; v < V; ++v)
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          if (!(mOut >> (v * U + u) & 1u)) continue;
-          const int i = R0 + ty + 8 * v, j = C0 + lane + 32 * u;
-          for (uint32_t m = relMonE; m; m &= m - 1) {
-            const MonDesc<T>& d = pe.mon[__ffs(m) - 1];
-            const unsigned di = (unsigned)(i - d.ix0), dj = (unsigned)(j - d.jy0);
-            if (di >= (unsigned)d.nxm || dj >= (unsigned)d.nym) continue;
-            const int64_t r = n - d.n0;
-            if (r < 0 || r >= d.rows) {
-              atomicOr(a.flag, ERRBIT_TABLE);
-              continue;
-            }
-            const T val = d.comp == ETG_EX ? ex[v][u] : ey[v][u];
-            const int64_t nodes = (int64_t)d.nxm * d.nym, k = (int64_t)di * d.nym + dj;
-            const T* phr = d.table + 2 * r * d.n_f;
-            for (int f = 0; f < d.n_f; ++f) {
-              T* acc = d.acc + 2 * (f * nodes + k);
-              acc[0] = add(acc[0], mul(val, phr[2 * f]));
-              acc[1] = add(acc[1], mul(val, phr[2 * f + 1]));
-            }
-          }
-        }
-    }
-#pragma unroll
-    for (int v = 0; v < V; ++v)
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int o = (ty + 8 * v) * EC + lane + 32 * u;
-        sEx[o] = ex[v][u];
-        sEy[o] = ey[v][u];
+      for (uint32_t m = relSrcE; m; m &= m - 1) {
+        const SrcDesc<T>& d = pe.src[__ffs(m) - 1];
+        const int li = d.i - R0, lj = d.j - C0;
+        if ((li & 7) != ty || lj / W != lane) continue;
+        const int64_t r = n - d.n0;
+        T* cell = (d.comp == ETG_EX ? sEx : sEy) + (li + 1) * SW + W + lj;
+        if (r < 0 || r >= d.rows) atomicOr(a.flag, ERRBIT_TABLE);
+        else *cell = sub(*cell, d.table[r * d.stride]);
       }
+    }
+    if (relMonE) tb_accumulate<T, RPT, K, W, ER, EC, SW>(pe, relMonE, sEx, sEy, R0, C0, ty, lane, n, a.flag);
     __syncthreads();
   }
 
-  // write the output tile to the other buffer
+  // write the output tile (vectors lie wholly inside or outside it, since K and OC are
+  // multiples of W)
+  if (lj0 < K || lj0 >= K + S::OC || !lane_in) return;
 #pragma unroll
-  for (int v = 0; v < V; ++v)
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      if (!(mOut >> (v * U + u) & 1u)) continue;
-      const int li = ty + 8 * v, lj = lane + 32 * u, i = R0 + li, j = C0 + lj;
-      const int64_t g = (int64_t)i * P + j;
-      dst.ex[g] = ex[v][u];
-      dst.ey[g] = ey[v][u];
-      dst.hz[g] = hz[v][u];
-      if (PML) {
-        const bool sx = i < a.xs_lo || i >= a.xs_hi, sy = j < a.ys_lo || j >= a.ys_hi;
-        if (sx) {
-          dst.psi_hz_x[g] = sPsi[0 * PL + li * EC + lj];
-          dst.psi_ey_x[g] = sPsi[3 * PL + li * EC + lj];
-        }
-        if (sy) {
-          dst.psi_hz_y[g] = sPsi[1 * PL + li * EC + lj];
-          dst.psi_ex_y[g] = sPsi[2 * PL + li * EC + lj];
-        }
-      }
+  for (int t = 0; t < RPT; ++t) {
+    const int li = ty + 8 * t, i = R0 + li;
+    if (li < K || li >= K + S::OR || (unsigned)i > (unsigned)nx) continue;
+    const int64_t g = (int64_t)i * P + j0;
+    const int o = (li + 1) * SW + W + lj0;
+    Vw v;
+    v.ld(sEx + o);
+    v.st(dst.ex + g);
+    v.ld(sEy + o);
+    v.st(dst.ey + g);
+    v.ld(sHz + o);
+    v.st(dst.hz + g);
+    if (PML) {  // psi stays +0 outside its strips in both buffers, so whole vectors are copied
+      v.ld(sPsi + 0 * PL + o);
+      v.st(dst.psi_hz_x + g);
+      v.ld(sPsi + 1 * PL + o);
+      v.st(dst.psi_hz_y + g);
+      v.ld(sPsi + 2 * PL + o);
+      v.st(dst.psi_ex_y + g);
+      v.ld(sPsi + 3 * PL + o);
+      v.st(dst.psi_ey_x + g);
     }
+  }
 }
 
 // ------------------------------------------------------------------------ host side
 
 struct TBConfig {
-  int dtype, V, U, K;
+  int dtype, RPT, K;  // tile rows 8 * RPT, columns 32 * W (128 for f32, 64 for f64), depth K
 };
 
-// Compiled tile shapes: (rows = 8V, columns = 32U, steps K).
-static const TBConfig kConfigs[] = {
-    {ETG_F32, 6, 4, 4}, {ETG_F32, 6, 4, 3}, {ETG_F32, 6, 4, 2}, {ETG_F32, 8, 4, 4},
-    {ETG_F32, 8, 4, 6}, {ETG_F32, 4, 4, 2}, {ETG_F32, 8, 2, 4},
-    {ETG_F64, 4, 4, 2}, {ETG_F64, 4, 4, 3}, {ETG_F64, 6, 2, 2},
-};
-static const TBConfig kDefault32 = {ETG_F32, 6, 4, 4};
-static const TBConfig kDefault64 = {ETG_F64, 4, 4, 2};
+static constexpr TBConfig kDefault32 = {ETG_F32, 5, 4};
+static constexpr TBConfig kDefault64 = {ETG_F64, 5, 2};
 
 struct TBState {
   void* alt[7] = {};  // second buffer of each field / psi plane, same pitch
   size_t alt_bytes = 0;
   int2* tiles = nullptr;  // interior tiles first, then CPML tiles
   int n_inner = 0, n_pml = 0;
-  TBConfig cfg = {0, 0, 0, 0};
+  TBConfig cfg = {0, 0, 0};
   int nx = -1, ny = -1;
   bool tiles_valid = false;
   std::map<int64_t, cudaGraphExec_t> graphs;
@@ -372,18 +459,18 @@ bool tb_supported(int nx, int ny) {
   return sizeof(T) == 4 && nx >= 64 && ny >= 64;
 }
 
-template <typename T, int V, int U, int K, bool PML>
+template <typename T, int RPT, int K, bool PML>
 static cudaError_t tb_launch_one(const SimArgs<T>& a, const TBDst<T>& d, const int2* tiles, int n,
                                  const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                  cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  using S = TBShape<T, V, U, K, PML>;
-  k_tb_step<T, V, U, K, PML><<<n, dim3(32, 8), S::SMEM, s>>>(a, d, tiles, ph, pe, step_off);
+  using S = TBShape<T, RPT, K, PML>;
+  k_tb_step<T, RPT, K, PML><<<n, dim3(32, 8), S::SMEM, s>>>(a, d, tiles, ph, pe, step_off);
   g_launches += 1;
   return cudaGetLastError();
 }
 
-template <typename T, int V, int U, int K>
+template <typename T, int RPT, int K>
 static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<T>& d,
                                   const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                   cudaStream_t s) {
@@ -391,8 +478,8 @@ static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<
   cudaError_t e = cudaEventRecord(tb->fork, s);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(tb->side, tb->fork, 0);
   if (e == cudaSuccess)
-    e = tb_launch_one<T, V, U, K, true>(a, d, tb->tiles + tb->n_inner, tb->n_pml, ph, pe, step_off, tb->side);
-  if (e == cudaSuccess) e = tb_launch_one<T, V, U, K, false>(a, d, tb->tiles, tb->n_inner, ph, pe, step_off, s);
+    e = tb_launch_one<T, RPT, K, true>(a, d, tb->tiles + tb->n_inner, tb->n_pml, ph, pe, step_off, tb->side);
+  if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false>(a, d, tb->tiles, tb->n_inner, ph, pe, step_off, s);
   if (e == cudaSuccess) e = cudaEventRecord(tb->join, tb->side);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(s, tb->join, 0);
   return e;
@@ -417,23 +504,23 @@ static TBDst<T> as_dst(const SimArgs<T>& a) {
 }
 
 // Two launches A -> B -> A covering 2K steps from step_off.
-template <typename T, int V, int U, int K>
+template <typename T, int RPT, int K>
 static cudaError_t tb_two(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& ph,
                           const PhasePlan<T>& pe, int step_off, cudaStream_t s) {
   const SimArgs<T> b = swap_args(a, tb);
-  cudaError_t e = tb_launch_pair<T, V, U, K>(tb, a, as_dst(b), ph, pe, step_off, s);
-  if (e == cudaSuccess) e = tb_launch_pair<T, V, U, K>(tb, b, as_dst(a), ph, pe, step_off + K, s);
+  cudaError_t e = tb_launch_pair<T, RPT, K>(tb, a, as_dst(b), ph, pe, step_off, s);
+  if (e == cudaSuccess) e = tb_launch_pair<T, RPT, K>(tb, b, as_dst(a), ph, pe, step_off + K, s);
   return e;
 }
 
 // Dynamic shared memory above 48 KB must be allowed per kernel, before any launch or capture.
-template <typename T, int V, int U, int K>
+template <typename T, int RPT, int K>
 static cudaError_t tb_attrs() {
-  cudaError_t e = cudaFuncSetAttribute(k_tb_step<T, V, U, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)TBShape<T, V, U, K, false>::SMEM);
+  cudaError_t e = cudaFuncSetAttribute(k_tb_step<T, RPT, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)TBShape<T, RPT, K, false>::SMEM);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_tb_step<T, V, U, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)TBShape<T, V, U, K, true>::SMEM);
+    e = cudaFuncSetAttribute(k_tb_step<T, RPT, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TBShape<T, RPT, K, true>::SMEM);
   return e;
 }
 
@@ -443,43 +530,65 @@ struct TBFns {
   cudaError_t (*attrs)();
 };
 
+// Compiled shapes (rows = 8 * RPT, depth K); the CPML variant's seven planes must fit 227 KB.
+#define ETG_TB_SHAPES_F32(X) X(ETG_F32, 4, 4) X(ETG_F32, 5, 4) X(ETG_F32, 6, 4) X(ETG_F32, 7, 4) X(ETG_F32, 7, 8)
+#define ETG_TB_SHAPES_F64(X) X(ETG_F64, 4, 2) X(ETG_F64, 5, 2) X(ETG_F64, 6, 2) X(ETG_F64, 5, 4)
+
 template <typename T>
 static TBFns<T> pick(const TBConfig& c) {
-#define ETG_TB_CASE(DT, VV, UU, KK) \
-  if (c.dtype == DT && c.V == VV && c.U == UU && c.K == KK) return {&tb_two<T, VV, UU, KK>, &tb_attrs<T, VV, UU, KK>};
+#define ETG_TB_CASE(DT, R, KK) \
+  if (c.dtype == DT && c.RPT == R && c.K == KK) return {&tb_two<T, R, KK>, &tb_attrs<T, R, KK>};
   if constexpr (sizeof(T) == 4) {
-    ETG_TB_CASE(ETG_F32, 6, 4, 4)
-    ETG_TB_CASE(ETG_F32, 6, 4, 3)
-    ETG_TB_CASE(ETG_F32, 6, 4, 2)
-    ETG_TB_CASE(ETG_F32, 8, 4, 4)
-    ETG_TB_CASE(ETG_F32, 8, 4, 6)
-    ETG_TB_CASE(ETG_F32, 4, 4, 2)
-    ETG_TB_CASE(ETG_F32, 8, 2, 4)
+    ETG_TB_SHAPES_F32(ETG_TB_CASE)
   } else {
-    ETG_TB_CASE(ETG_F64, 4, 4, 2)
-    ETG_TB_CASE(ETG_F64, 4, 4, 3)
-    ETG_TB_CASE(ETG_F64, 6, 2, 2)
+    ETG_TB_SHAPES_F64(ETG_TB_CASE)
   }
 #undef ETG_TB_CASE
   return {nullptr, nullptr};
 }
 
+static std::string shapes_text(int dtype) {
+  std::string out;
+#define ETG_TB_NAME(DT, R, KK) \
+  if (DT == dtype) out += " " + std::to_string(8 * R) + "x" + std::to_string(DT == ETG_F32 ? 128 : 64) + "/K" + std::to_string(KK);
+  ETG_TB_SHAPES_F32(ETG_TB_NAME)
+  ETG_TB_SHAPES_F64(ETG_TB_NAME)
+#undef ETG_TB_NAME
+  return out;
+}
+
+// Interior tiles need their whole extended region in the unit rectangle and off the outer
+// (PEC) edges.
+static void split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_hi, int ER, int EC,
+                        int K, std::vector<int2>* tiles, int* n_inner) {
+  const int OR = ER - 2 * K, OC = EC - 2 * K;
+  const int rlo = std::max(ux_lo, 1), rhi = std::min(ux_hi, nx), clo = std::max(uy_lo, 1), chi = std::min(uy_hi, ny);
+  std::vector<int2> inner, pml;
+  for (int r0 = 0; r0 <= nx; r0 += OR)
+    for (int c0 = 0; c0 <= ny; c0 += OC) {
+      const bool unit = r0 - K >= rlo && r0 + OR + K <= rhi && c0 - K >= clo && c0 + OC + K <= chi;
+      (unit ? inner : pml).push_back(make_int2(r0, c0));
+    }
+  *n_inner = (int)inner.size();
+  inner.insert(inner.end(), pml.begin(), pml.end());
+  *tiles = inner;
+}
+
 template <typename T>
 static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt) {
   const int dt = (int)sizeof(T);
+  const int EC = 32 * TBVec<T>::W;
   TBConfig want = dt == 4 ? kDefault32 : kDefault64;
   if (opt[ETG_OPT_TB_DEPTH] > 0) want.K = (int)opt[ETG_OPT_TB_DEPTH];
-  if (opt[ETG_OPT_TILE_ROWS] > 0) want.V = (int)(opt[ETG_OPT_TILE_ROWS] / 8);
-  if (opt[ETG_OPT_TILE_COLS] > 0) want.U = (int)(opt[ETG_OPT_TILE_COLS] / 32);
-  if (!pick<T>(want).two) {
-    std::string have;
-    for (const TBConfig& c : kConfigs)
-      if (c.dtype == dt) have += " " + std::to_string(8 * c.V) + "x" + std::to_string(32 * c.U) + "/K" + std::to_string(c.K);
-    set_error("no compiled temporally blocked kernel with tile %dx%d and depth %d (have:%s)",
-              8 * want.V, 32 * want.U, want.K, have.c_str());
+  if (opt[ETG_OPT_TILE_ROWS] > 0) want.RPT = (int)(opt[ETG_OPT_TILE_ROWS] / 8);
+  const bool cols_ok = opt[ETG_OPT_TILE_COLS] == 0 || opt[ETG_OPT_TILE_COLS] == EC;
+  if (!cols_ok || opt[ETG_OPT_TILE_ROWS] % 8 != 0 || !pick<T>(want).two) {
+    set_error("no compiled temporally blocked kernel with tile %lldx%lld and depth %d (have:%s)",
+              (long long)(opt[ETG_OPT_TILE_ROWS] ? opt[ETG_OPT_TILE_ROWS] : 8 * want.RPT),
+              (long long)(opt[ETG_OPT_TILE_COLS] ? opt[ETG_OPT_TILE_COLS] : EC), want.K, shapes_text(dt).c_str());
     return ETG_ERR_ARGUMENT;
   }
-  if (want.V != tb->cfg.V || want.U != tb->cfg.U || want.K != tb->cfg.K || want.dtype != tb->cfg.dtype) {
+  if (want.RPT != tb->cfg.RPT || want.K != tb->cfg.K || want.dtype != tb->cfg.dtype) {
     tb_invalidate(tb);
     tb->cfg = want;
     ETG_TRY_CUDA(pick<T>(want).attrs());
@@ -506,18 +615,10 @@ static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt) {
     ETG_TRY_CUDA(cudaEventCreateWithFlags(&tb->join, cudaEventDisableTiming));
   }
   if (!tb->tiles_valid || tb->nx != a.nx || tb->ny != a.ny) {
-    const int ER = 8 * tb->cfg.V, EC = 32 * tb->cfg.U, K = tb->cfg.K;
-    const int OR = ER - 2 * K, OC = EC - 2 * K;
-    std::vector<int2> inner, pml;
-    for (int r0 = 0; r0 <= a.nx; r0 += OR)
-      for (int c0 = 0; c0 <= a.ny; c0 += OC) {
-        const bool unit = r0 - K >= a.ux_lo && r0 + OR + K <= a.ux_hi && c0 - K >= a.uy_lo &&
-                          c0 + OC + K <= a.uy_hi;
-        (unit ? inner : pml).push_back(make_int2(r0, c0));
-      }
-    tb->n_inner = (int)inner.size();
-    tb->n_pml = (int)pml.size();
-    inner.insert(inner.end(), pml.begin(), pml.end());
+    std::vector<int2> inner;
+    split_tiles(a.nx, a.ny, a.ux_lo, a.ux_hi, a.uy_lo, a.uy_hi, 8 * tb->cfg.RPT, EC, tb->cfg.K, &inner,
+                &tb->n_inner);
+    tb->n_pml = (int)inner.size() - tb->n_inner;
     cudaFree(tb->tiles);
     tb->tiles = nullptr;
     ETG_TRY_CUDA(cudaMalloc(&tb->tiles, inner.size() * sizeof(int2)));
@@ -580,5 +681,45 @@ template int tb_advance<float>(TBState*, const SimArgs<float>&, const PhasePlan<
                                const PhasePlan<float>&, int64_t, const int64_t*, cudaStream_t);
 template int tb_advance<double>(TBState*, const SimArgs<double>&, const PhasePlan<double>&,
                                 const PhasePlan<double>&, int64_t, const int64_t*, cudaStream_t);
+
+}  // namespace etg
+
+// ------------------------------------------------------------------------ default-shape helpers
+
+namespace etg {
+
+void tb_default_shape(int dtype, int* ER, int* EC, int* K) {
+  const TBConfig& c = dtype == ETG_F64 ? kDefault64 : kDefault32;
+  *ER = 8 * c.RPT;
+  *EC = dtype == ETG_F64 ? 64 : 128;
+  *K = c.K;
+}
+
+void tb_tiles(int dtype, int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_hi,
+              std::vector<int2>* tiles, int* n_inner) {
+  int ER, EC, K;
+  tb_default_shape(dtype, &ER, &EC, &K);
+  split_tiles(nx, ny, ux_lo, ux_hi, uy_lo, uy_hi, ER, EC, K, tiles, n_inner);
+}
+
+template <typename T>
+cudaError_t tb_default_launch(const SimArgs<T>& src, const SimArgs<T>& dst, const int2* tiles,
+                              int n_inner, int n_pml, int step_off, cudaStream_t s) {
+  constexpr TBConfig c = sizeof(T) == 4 ? kDefault32 : kDefault64;
+  constexpr int RPT = c.RPT, K = c.K;
+  PhasePlan<T> none;
+  memset(&none, 0, sizeof none);
+  cudaError_t e = tb_attrs<T, RPT, K>();
+  if (e == cudaSuccess)
+    e = tb_launch_one<T, RPT, K, false>(src, as_dst(dst), tiles, n_inner, none, none, step_off, s);
+  if (e == cudaSuccess)
+    e = tb_launch_one<T, RPT, K, true>(src, as_dst(dst), tiles + n_inner, n_pml, none, none, step_off, s);
+  return e;
+}
+
+template cudaError_t tb_default_launch<float>(const SimArgs<float>&, const SimArgs<float>&, const int2*,
+                                              int, int, int, cudaStream_t);
+template cudaError_t tb_default_launch<double>(const SimArgs<double>&, const SimArgs<double>&,
+                                               const int2*, int, int, int, cudaStream_t);
 
 }  // namespace etg

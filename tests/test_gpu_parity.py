@@ -364,8 +364,8 @@ def _oracle_for(p):
 
 # ----------------------------------------------------------------- temporal blocking
 
-TB_SHAPES_F32 = [(48, 128, 4), (48, 128, 3), (48, 128, 2), (64, 128, 4), (64, 128, 6), (32, 128, 2), (64, 64, 4)]
-TB_SHAPES_F64 = [(32, 128, 2), (32, 128, 3), (48, 64, 2)]
+TB_SHAPES_F32 = [(32, 128, 4), (40, 128, 4), (48, 128, 4), (56, 128, 4), (56, 128, 8)]
+TB_SHAPES_F64 = [(32, 64, 2), (40, 64, 2), (48, 64, 2), (40, 64, 4)]
 
 
 def _tb_engine(name, precision, g, shape, **kw):
@@ -393,7 +393,7 @@ def test_tb_matches_reference(gpu, name, precision, shape):
 def test_tb_seams_and_remainders(gpu, precision):
     """Blocks of 1, 2K−1, 2K, 2K+1 … steps (TB pairs, graph replays, one-step remainders) agree."""
     g = load("g4_full", precision)
-    shape = (48, 128, 4) if precision == "single" else (32, 128, 2)
+    shape = (40, 128, 4) if precision == "single" else (40, 64, 2)
     a, n = _tb_engine("g4_full", precision, g, shape)
     a.advance(n)
     b, _ = _tb_engine("g4_full", precision, g, shape, graph_steps=16)
@@ -424,9 +424,8 @@ def test_tb_random_state_live_psi(gpu, precision, steps):
     e = TEEngine.__new__(TEEngine)
     _init_bare_engine(e, p, c)
     e.set_kernel("tb")
-    e.set_option(_lib.OPT_TB_DEPTH, 2)
+    e.set_option(_lib.OPT_TB_DEPTH, 4 if precision == "single" else 2)
     e.set_option(_lib.OPT_TILE_ROWS, 32)
-    e.set_option(_lib.OPT_TILE_COLS, 128)
     for f, v in fields.items():
         e.set_field(f, v)
     e.advance(steps)

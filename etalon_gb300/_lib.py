@@ -60,6 +60,7 @@ SIGNATURES: dict[str, list] = {
     "etg_sim_set_option": [vp, i32, i64],
     "etg_sim_get_option": [vp, i32, pi64],
     "etg_sim_last_timing": [vp, C.POINTER(f64), pi64],
+    "etg_tb_advance_static": [i32, i32, i32, i64] + [vp] * 21 + [f64, f64, f64, i64],
 }
 
 

@@ -149,6 +149,39 @@ int etg_sim_get_option(etg_sim* sim, int option, int64_t* value);
  * total milliseconds and the number of kernel launches it made. */
 int etg_sim_last_timing(etg_sim* sim, double* ms, int64_t* launches);
 
+/* ---------------------------------------------------------------- no-allocation advance
+ * Has no counterpart in Etalon. For callers that cannot allocate device memory when they
+ * step fields: an application that owns all device memory through its own fixed arena, a
+ * process under a hard device-memory budget, or a loop that cannot afford the device-wide
+ * synchronisation of cudaMalloc/cudaFree. It advances fields the
+ * caller owns by n_steps steps (no sources, no monitors) with the temporally blocked
+ * kernel, and keeps its second buffer, tile list and step counter in one static device
+ * array of ETG_STATIC_SCRATCH_BYTES, held by every GPU that loads the library until the
+ * process exits. It calls no cudaMalloc, cudaFree or allocating library routine.
+ *
+ * Layout: every field, psi and cb array has nx + 2 rows of `pitch` elements (pitch a
+ * multiple of 32 and >= ny + 1), element (i, j) at i * pitch + j, the TEState array in the
+ * top-left corner and zeros elsewhere; pointers are 16-byte aligned. psi must be +0 wherever
+ * the CPML c coefficient of its axis is 0 (true of any run started from zero fields).
+ * 1D coefficients are contiguous as for etg_sim_set_coefficients.
+ *
+ * A grid needs 7 * (nx + 2) * pitch * dtype bytes plus its tile list; larger grids are
+ * rejected with ETG_ERR_ARGUMENT. The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress, with that device current); make that first call before any
+ * stream capture on that device.
+ * Work runs on the default stream and the call returns when it is done. All calls share
+ * the array and it keeps the last call's contents: calls that overlap on the GPU (from
+ * several host threads) race. */
+#define ETG_STATIC_SCRATCH_BYTES (16 << 20)
+int etg_tb_advance_static(int dtype, int nx, int ny, int64_t pitch, void* ex, void* ey, void* hz,
+                          void* psi_ex_y, void* psi_ey_x, void* psi_hz_x, void* psi_hz_y,
+                          const void* cb_ex, const void* cb_ey, const void* bx_e,
+                          const void* cx_e, const void* ikx_e, const void* bx_h, const void* cx_h,
+                          const void* ikx_h, const void* by_e, const void* cy_e,
+                          const void* iky_e, const void* by_h, const void* cy_h,
+                          const void* iky_h, double db, double inv_dx, double inv_dy,
+                          int64_t n_steps);
+
 #define ETG_OPT_KERNEL 0        /* 0 = auto, 1 = one step per launch, 2 = temporal blocking */
 #define ETG_OPT_TB_DEPTH 1      /* steps per launch of the temporally blocked kernel */
 #define ETG_OPT_GRAPH_STEPS 2   /* steps captured per CUDA graph (0 = no graphs) */

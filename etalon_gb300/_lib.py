@@ -45,6 +45,7 @@ SIGNATURES: dict[str, list] = {
     "etg_sim_destroy": [vp],
     "etg_sim_set_coefficients": [vp] + [vp] * 14 + [f64, f64, f64],
     "etg_sim_add_source": [vp, i32, i32, vp, vp, i64, i64, vp],
+    "etg_sim_set_cb_window": [vp, i32, i32, i32, i32, i32, vp],
     "etg_sim_add_monitor": [vp, i32, i32, i32, i32, i32, i32, i64, i64, vp, C.POINTER(i32)],
     "etg_sim_set_phasors": [vp, i32, i64, i64, vp],
     "etg_sim_set_deltas": [vp, i32, i64, i64, vp],
@@ -60,6 +61,10 @@ SIGNATURES: dict[str, list] = {
     "etg_sim_set_option": [vp, i32, i64],
     "etg_sim_get_option": [vp, i32, pi64],
     "etg_sim_last_timing": [vp, C.POINTER(f64), pi64],
+    "etg_adj_create": [C.POINTER(vp), vp, i32, i32, i32, i32],
+    "etg_adj_destroy": [vp],
+    "etg_adj_forward": [vp, i64, i64],
+    "etg_adj_backward": [vp, C.POINTER(vp), C.POINTER(C.c_double), C.POINTER(C.c_double)],
     "etg_tb_advance_static": [i32, i32, i32, i64] + [vp] * 21 + [f64, f64, f64, i64],
 }
 

@@ -1,0 +1,518 @@
+// Discrete adjoint of the 2D TE leapfrog (no counterpart in Etalon): dJ/dcb over a design
+// window, for an objective J of the DFT monitor accumulators.
+//
+// Forward step n (etalon/fdtd/solver.py:120-128, numpy_backend.py:41-67):
+//   H:  A_y = dEx/dy·iky_h + psi_hz_y',  A_x = dEy/dx·ikx_h + psi_hz_x',  Hz' = Hz + db (A_y - A_x)
+//   E:  Ex' = Ex + cb_ex (dHz/dy·iky_e + psi_ex_y'),  Ey' = Ey - cb_ey (dHz/dx·ikx_e + psi_ey_x')
+//   with psi' = b psi + c d and d the scaled differences; then sources and DFTs.
+// The reverse sweep runs n = N-1 … 0 with lambda = dJ/d(state) and two kernels per step:
+//   RE(n): lambda_Hz(n+1/2) += transpose(E update) + DFT-H source, lambda_psi_e updated,
+//          dJ/dcb += lambda_E(n+1) · C^n on the design window, C^n from the recorded Hz trace;
+//   RH(n): lambda_E(n) += transpose(H update) + DFT-E source of step n-1, lambda_psi_h updated.
+// The adjoint of a DFT term acc += v·ph is dJ/dv = Re(G)·Re(ph) + Im(G)·Im(ph), G = dJ/dacc.
+// Every scaled difference of the forward appears once in each transposed gather, so each
+// thread recomputes the neighbour's term; lambda_psi is double-buffered for that.
+//
+// What the gradient needs from the forward is Hz^(n+1/2) on the design window plus one cell
+// of halo at every step. The forward either records it for all steps ("trace" mode) or keeps
+// full-state checkpoints every S ~ sqrt(N) steps and re-records it segment by segment in the
+// reverse sweep ("checkpoint" mode); both give the same bits.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "etg_sim.h"
+
+namespace etg {
+
+// One DFT monitor with its objective gradient G = dJ/dacc (n_f, nodes) complex.
+template <typename T>
+struct AdjMon {
+  const T* table;  // phasor rows (rows, n_f) complex
+  const T* g;      // (n_f, nxm*nym) complex
+  int64_t n0, rows;
+  int ix0, nxm, jy0, nym, n_f, comp;
+};
+
+template <typename T>
+struct AdjPlan {
+  int n_mon;
+  AdjMon<T> mon[MAX_MONITORS];
+};
+
+template <typename T>
+struct AdjArgs {
+  SimArgs<T> s;                      // geometry, coefficients, strips of the simulation
+  T *lex, *ley, *lhz;                // adjoint fields, pitched like the fields
+  const T *lpsi_in[4];               // psi_hz_x, psi_hz_y, psi_ex_y, psi_ey_x (this sweep's input)
+  T* lpsi_out[4];
+  const T* trace;                    // Hz^(n+1/2) on [ti0, ti0+tnx) x [tj0, tj0+tny) per step
+  int64_t trace_n0;
+  int ti0, tnx, tj0, tny;
+  int i0, nxd, j0, nyd;              // design cells
+  double *gx, *gy;                   // dJ/dcb_ex (nxd, nyd+1), dJ/dcb_ey (nxd+1, nyd)
+};
+
+// Sum_f Re(G)·Re(ph) + Im(G)·Im(ph) for node (i, j) of component comp, if monitored.
+template <typename T>
+__device__ __forceinline__ T adj_source(const AdjPlan<T>& p, int comp, int i, int j, int64_t n) {
+  T acc = T(0);
+  for (int m = 0; m < p.n_mon; ++m) {
+    const AdjMon<T>& d = p.mon[m];
+    if (d.comp != comp) continue;
+    const unsigned di = (unsigned)(i - d.ix0), dj = (unsigned)(j - d.jy0);
+    if (di >= (unsigned)d.nxm || dj >= (unsigned)d.nym) continue;
+    const int64_t r = n - d.n0;
+    if (r < 0 || r >= d.rows) continue;  // the host checks table coverage before the sweep
+    const int64_t nodes = (int64_t)d.nxm * d.nym, k = (int64_t)di * d.nym + dj;
+    const T* ph = d.table + 2 * r * d.n_f;
+    for (int f = 0; f < d.n_f; ++f) {
+      const T* g = d.g + 2 * (f * nodes + k);
+      acc = acc + g[0] * ph[2 * f] + g[1] * ph[2 * f + 1];
+    }
+  }
+  return acc;
+}
+
+// Transposed E update of the Ex node (i, j): returns dJ/d(dHz/dy) and updates lambda_psi_ex_y.
+template <typename T>
+__device__ __forceinline__ T gx_at(const AdjArgs<T>& a, int i, int j, bool own) {
+  const SimArgs<T>& s = a.s;
+  if (j < 1 || j > s.ny - 1 || i < 0 || i >= s.nx) return T(0);
+  const int64_t g = (int64_t)i * s.P + j;
+  const T lc = s.cb_ex[g] * a.lex[g];
+  if (j < s.ys_lo || j >= s.ys_hi) {
+    const T lpt = a.lpsi_in[2][g] + lc;
+    if (own) a.lpsi_out[2][g] = s.by_e[j] * lpt;
+    return s.iky_e[j] * lc + s.cy_e[j] * lpt;
+  }
+  return s.iky_e[j] * lc;
+}
+
+// Transposed E update of the Ey node (i, j): returns dJ/d(dHz/dx) and updates lambda_psi_ey_x.
+template <typename T>
+__device__ __forceinline__ T gy_at(const AdjArgs<T>& a, int i, int j, bool own) {
+  const SimArgs<T>& s = a.s;
+  if (i < 1 || i > s.nx - 1 || j < 0 || j >= s.ny) return T(0);
+  const int64_t g = (int64_t)i * s.P + j;
+  const T lc = -(s.cb_ey[g] * a.ley[g]);
+  if (i < s.xs_lo || i >= s.xs_hi) {
+    const T lpt = a.lpsi_in[3][g] + lc;
+    if (own) a.lpsi_out[3][g] = s.bx_e[i] * lpt;
+    return s.ikx_e[i] * lc + s.cx_e[i] * lpt;
+  }
+  return s.ikx_e[i] * lc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_adj_re(AdjArgs<T> a, AdjPlan<T> ph, int64_t n) {
+  const SimArgs<T>& s = a.s;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.nx || j >= s.ny) return;
+  const int64_t g = (int64_t)i * s.P + j;
+  const T gx0 = gx_at(a, i, j, true), gx1 = gx_at(a, i, j + 1, false);
+  const T gy0 = gy_at(a, i, j, true), gy1 = gy_at(a, i + 1, j, false);
+  a.lhz[g] = a.lhz[g] + s.inv_dy * (gx0 - gx1) + s.inv_dx * (gy0 - gy1) + adj_source(ph, ETG_HZ, i, j, n);
+  // dJ/dcb on the design window: Ex' = Ex + cb·C, Ey' = Ey - cb·C, C as the forward rounds it
+  const int64_t r = n - a.trace_n0;
+  const int ri = i - a.ti0, rj = j - a.tj0;
+  const T* tr = a.trace + r * a.tnx * a.tny;
+  if (i >= a.i0 && i < a.i0 + a.nxd && j >= a.j0 && j <= a.j0 + a.nyd) {
+    const T c = add(mul(sub(tr[ri * a.tny + rj], tr[ri * a.tny + rj - 1]), s.inv_dy), T(0));
+    a.gx[(int64_t)(i - a.i0) * (a.nyd + 1) + (j - a.j0)] += (double)a.lex[g] * (double)c;
+  }
+  if (i >= a.i0 && i <= a.i0 + a.nxd && j >= a.j0 && j < a.j0 + a.nyd) {
+    const T c = add(mul(sub(tr[ri * a.tny + rj], tr[(ri - 1) * a.tny + rj]), s.inv_dx), T(0));
+    a.gy[(int64_t)(i - a.i0) * a.nyd + (j - a.j0)] -= (double)a.ley[g] * (double)c;
+  }
+}
+
+// Transposed H update of the Hz cell (i, j): dJ/d(dEx/dy), dJ/d(dEy/dx); updates lambda_psi_h.
+template <typename T>
+__device__ __forceinline__ void h_at(const AdjArgs<T>& a, int i, int j, bool own, T* hx, T* hy) {
+  const SimArgs<T>& s = a.s;
+  if (i < 0 || i >= s.nx || j < 0 || j >= s.ny) {
+    *hx = *hy = T(0);
+    return;
+  }
+  const int64_t g = (int64_t)i * s.P + j;
+  const T la = s.db * a.lhz[g];
+  if (j < s.ys_lo || j >= s.ys_hi) {
+    const T lpt = a.lpsi_in[1][g] + la;
+    if (own) a.lpsi_out[1][g] = s.by_h[j] * lpt;
+    *hx = s.iky_h[j] * la + s.cy_h[j] * lpt;
+  } else {
+    *hx = s.iky_h[j] * la;
+  }
+  if (i < s.xs_lo || i >= s.xs_hi) {
+    const T lpt = a.lpsi_in[0][g] - la;
+    if (own) a.lpsi_out[0][g] = s.bx_h[i] * lpt;
+    *hy = -(s.ikx_h[i] * la) + s.cx_h[i] * lpt;
+  } else {
+    *hy = -(s.ikx_h[i] * la);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_adj_rh(AdjArgs<T> a, AdjPlan<T> pe, int64_t n_src) {
+  const SimArgs<T>& s = a.s;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;  // rows 0 .. nx
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;  // columns 0 .. ny
+  if (i > s.nx || j > s.ny) return;
+  const int64_t g = (int64_t)i * s.P + j;
+  T hx0, hy0, hxl, hyl, hxu, hyu;
+  h_at(a, i, j, true, &hx0, &hy0);
+  h_at(a, i, j - 1, false, &hxl, &hyl);
+  h_at(a, i - 1, j, false, &hxu, &hyu);
+  if (i < s.nx) {  // Ex(i, j), j in [0, ny]
+    T v = a.lex[g] + s.inv_dy * (hxl - hx0);
+    if (n_src >= 0) v = v + adj_source(pe, ETG_EX, i, j, n_src);
+    a.lex[g] = v;
+  }
+  if (j < s.ny) {  // Ey(i, j), i in [0, nx]
+    T v = a.ley[g] + s.inv_dx * (hyu - hy0);
+    if (n_src >= 0) v = v + adj_source(pe, ETG_EY, i, j, n_src);
+    a.ley[g] = v;
+  }
+}
+
+// lambda_E += DFT-E source of step n (the last step, before the sweep starts).
+template <typename T>
+__global__ void k_adj_esrc(AdjArgs<T> a, AdjPlan<T> pe, int64_t n) {
+  const SimArgs<T>& s = a.s;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > s.nx || j > s.ny) return;
+  const int64_t g = (int64_t)i * s.P + j;
+  if (i < s.nx) a.lex[g] = a.lex[g] + adj_source(pe, ETG_EX, i, j, n);
+  if (j < s.ny) a.ley[g] = a.ley[g] + adj_source(pe, ETG_EY, i, j, n);
+}
+
+}  // namespace etg
+
+using namespace etg;
+
+struct etg_adj {
+  etg_sim* sim = nullptr;
+  int i0 = 0, nxd = 0, j0 = 0, nyd = 0;
+  int ti0 = 0, tnx = 0, tj0 = 0, tny = 0;
+  int64_t n_steps = 0, stride = 0;  // stride 0: trace of every step
+  void* trace = nullptr;
+  size_t trace_cap = 0;
+  std::vector<void*> ckpt;  // each 7 planes
+  void* lam[3] = {};        // lambda Ex, Ey, Hz
+  void* lpsi[2][4] = {};    // double-buffered lambda psi
+  double* grad = nullptr;   // gx then gy
+  std::vector<void*> gacc;  // per monitor, device G
+};
+
+namespace {
+
+size_t plane_bytes(const etg_sim* s) { return (size_t)s->rows * s->P * s->esize(); }
+
+int ensure(void** p, size_t bytes) {
+  if (*p) return ETG_OK;
+  return etg_malloc(p, bytes);
+}
+
+template <typename T>
+AdjArgs<T> adj_args(etg_adj* A, SimArgs<T> sa, int par_e, int par_h, int64_t trace_n0) {
+  AdjArgs<T> a;
+  memset(&a, 0, sizeof a);
+  a.s = sa;
+  a.lex = (T*)A->lam[0];
+  a.ley = (T*)A->lam[1];
+  a.lhz = (T*)A->lam[2];
+  for (int k = 0; k < 4; ++k) {
+    const int par = k < 2 ? par_h : par_e;
+    a.lpsi_in[k] = (const T*)A->lpsi[par][k];
+    a.lpsi_out[k] = (T*)A->lpsi[1 - par][k];
+  }
+  a.trace = (const T*)A->trace;
+  a.trace_n0 = trace_n0;
+  a.ti0 = A->ti0;
+  a.tnx = A->tnx;
+  a.tj0 = A->tj0;
+  a.tny = A->tny;
+  a.i0 = A->i0;
+  a.nxd = A->nxd;
+  a.j0 = A->j0;
+  a.nyd = A->nyd;
+  a.gx = A->grad;
+  a.gy = A->grad + (size_t)A->nxd * (A->nyd + 1);
+  return a;
+}
+
+template <typename T>
+SimArgs<T> sim_args_of(etg_sim* s) {
+  SimArgs<T> a;
+  memset(&a, 0, sizeof a);
+  a.nx = s->nx;
+  a.ny = s->ny;
+  a.P = s->P;
+  a.ex = (T*)s->field[ETG_EX];
+  a.ey = (T*)s->field[ETG_EY];
+  a.hz = (T*)s->field[ETG_HZ];
+  a.cb_ex = (const T*)s->cb[0];
+  a.cb_ey = (const T*)s->cb[1];
+  const T** c[12] = {&a.bx_e, &a.cx_e, &a.ikx_e, &a.bx_h, &a.cx_h, &a.ikx_h,
+                     &a.by_e, &a.cy_e, &a.iky_e, &a.by_h, &a.cy_h, &a.iky_h};
+  for (int k = 0; k < 12; ++k) *c[k] = (const T*)s->c1d[k];
+  a.db = (T)s->db;
+  a.inv_dx = (T)s->inv_dx;
+  a.inv_dy = (T)s->inv_dy;
+  a.xs_lo = s->xs_lo;
+  a.xs_hi = s->xs_hi;
+  a.ys_lo = s->ys_lo;
+  a.ys_hi = s->ys_hi;
+  a.step = s->d_step;
+  a.flag = s->d_flag;
+  return a;
+}
+
+void set_trace(etg_sim* s, void* buf, int64_t n0, int64_t rows, const etg_adj* A) {
+  s->trace_buf = buf;
+  s->trace_n0 = n0;
+  s->trace_rows = rows;
+  s->trace_ti0 = A->ti0;
+  s->trace_tnx = A->tnx;
+  s->trace_tj0 = A->tj0;
+  s->trace_tny = A->tny;
+  sim_invalidate(s);
+}
+
+void clear_trace(etg_sim* s) {
+  s->trace_buf = nullptr;
+  sim_invalidate(s);
+}
+
+int copy_state(etg_sim* s, void* const* to, void* const* from) {
+  for (int f = 0; f < 7; ++f)
+    ETG_TRY_CUDA(cudaMemcpyAsync(to[f], from[f], plane_bytes(s), cudaMemcpyDeviceToDevice, s->stream));
+  return ETG_OK;
+}
+
+// Reverse steps n_hi-1 … n_lo; the trace buffer holds steps from trace_n0.
+template <typename T>
+int backward_sweep(etg_adj* A, int64_t n_hi, int64_t n_lo, int64_t trace_n0, int* par_e, int* par_h,
+                   const AdjPlan<T>& ph, const AdjPlan<T>& pe) {
+  etg_sim* s = A->sim;
+  const SimArgs<T> sa = sim_args_of<T>(s);
+  const dim3 block(32, 4);
+  const dim3 gre((s->ny + 31) / 32, (s->nx + 3) / 4), grh((s->ny + 1 + 31) / 32, (s->nx + 1 + 3) / 4);
+  for (int64_t n = n_hi - 1; n >= n_lo; --n) {
+    AdjArgs<T> a = adj_args<T>(A, sa, *par_e, *par_h, trace_n0);
+    k_adj_re<T><<<gre, block, 0, s->stream>>>(a, ph, n);
+    *par_e ^= 1;
+    a = adj_args<T>(A, sa, *par_e, *par_h, trace_n0);
+    k_adj_rh<T><<<grh, block, 0, s->stream>>>(a, pe, n >= 1 ? n - 1 : -1);
+    *par_h ^= 1;
+    g_launches += 2;
+  }
+  ETG_LAUNCH_CHECK();
+  return ETG_OK;
+}
+
+template <typename T>
+int build_adj_plans(etg_adj* A, AdjPlan<T>* ph, AdjPlan<T>* pe) {
+  memset(ph, 0, sizeof *ph);
+  memset(pe, 0, sizeof *pe);
+  etg_sim* s = A->sim;
+  for (size_t k = 0; k < s->monitors.size(); ++k) {
+    if (!A->gacc[k]) continue;
+    const Monitor& m = s->monitors[k];
+    AdjPlan<T>* p = m.comp == ETG_HZ ? ph : pe;
+    ETG_REQUIRE(p->n_mon < MAX_MONITORS, ETG_ERR_ARGUMENT, "too many monitors in the objective");
+    ETG_REQUIRE(m.n0 <= 0 && A->n_steps <= m.n0 + m.rows, ETG_ERR_STATE,
+                "monitor %zu has phasors for steps [%lld, %lld), the adjoint needs [0, %lld)", k,
+                (long long)m.n0, (long long)(m.n0 + m.rows), (long long)A->n_steps);
+    AdjMon<T>& d = p->mon[p->n_mon++];
+    d.table = (const T*)m.table;
+    d.g = (const T*)A->gacc[k];
+    d.n0 = m.n0;
+    d.rows = m.rows;
+    d.ix0 = m.ix0;
+    d.nxm = m.nxm;
+    d.jy0 = m.jy0;
+    d.nym = m.nym;
+    d.n_f = m.n_f;
+    d.comp = m.comp;
+  }
+  return ETG_OK;
+}
+
+template <typename T>
+int adj_backward(etg_adj* A, const void* const* grad_acc, double* gx_host, double* gy_host) {
+  etg_sim* s = A->sim;
+  const size_t pb = plane_bytes(s);
+  for (int k = 0; k < 3; ++k) {
+    int rc = ensure(&A->lam[k], pb);
+    if (rc) return rc;
+    ETG_TRY_CUDA(cudaMemsetAsync(A->lam[k], 0, pb, s->stream));
+  }
+  for (int b = 0; b < 2; ++b)
+    for (int k = 0; k < 4; ++k) {
+      int rc = ensure(&A->lpsi[b][k], pb);
+      if (rc) return rc;
+      ETG_TRY_CUDA(cudaMemsetAsync(A->lpsi[b][k], 0, pb, s->stream));
+    }
+  const size_t gbytes = ((size_t)A->nxd * (A->nyd + 1) + (size_t)(A->nxd + 1) * A->nyd) * sizeof(double);
+  int rc = ensure((void**)&A->grad, gbytes);
+  if (rc) return rc;
+  ETG_TRY_CUDA(cudaMemsetAsync(A->grad, 0, gbytes, s->stream));
+  A->gacc.assign(s->monitors.size(), nullptr);
+  for (size_t k = 0; k < s->monitors.size(); ++k) {
+    if (!grad_acc || !grad_acc[k]) continue;
+    const Monitor& m = s->monitors[k];
+    const size_t bytes = (size_t)2 * m.n_f * m.nxm * m.nym * s->esize();
+    rc = etg_malloc(&A->gacc[k], bytes);
+    if (rc) return rc;
+    ETG_TRY_CUDA(cudaMemcpy(A->gacc[k], grad_acc[k], bytes, cudaMemcpyHostToDevice));
+  }
+  AdjPlan<T> ph, pe;
+  rc = build_adj_plans<T>(A, &ph, &pe);
+  if (rc == ETG_OK) {
+    const SimArgs<T> sa = sim_args_of<T>(s);
+    int par_e = 0, par_h = 0;
+    AdjArgs<T> a0 = adj_args<T>(A, sa, par_e, par_h, 0);
+    const dim3 block(32, 4), grh((s->ny + 1 + 31) / 32, (s->nx + 1 + 3) / 4);
+    k_adj_esrc<T><<<grh, block, 0, s->stream>>>(a0, pe, A->n_steps - 1);
+    g_launches += 1;
+    if (A->stride == 0) {
+      rc = backward_sweep<T>(A, A->n_steps, 0, 0, &par_e, &par_h, ph, pe);
+    } else {
+      const int64_t S = A->stride;
+      const int64_t nseg = (A->n_steps + S - 1) / S;
+      s->monitors_on = false;
+      sim_invalidate(s);
+      for (int64_t k = nseg - 1; k >= 0 && rc == ETG_OK; --k) {
+        const int64_t lo = k * S, hi = std::min(A->n_steps, lo + S);
+        void* from[7];
+        for (int f = 0; f < 7; ++f) from[f] = (char*)A->ckpt[k] + f * plane_bytes(s);
+        rc = copy_state(s, s->field, from);
+        if (rc) break;
+        ETG_TRY_CUDA(cudaMemcpyAsync(s->d_step, &lo, sizeof lo, cudaMemcpyHostToDevice, s->stream));
+        ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+        s->h_step = lo;
+        set_trace(s, A->trace, lo, hi - lo, A);
+        rc = sim_advance_internal(s, hi - lo);
+        clear_trace(s);
+        if (rc == ETG_OK) rc = backward_sweep<T>(A, hi, lo, lo, &par_e, &par_h, ph, pe);
+      }
+      s->monitors_on = true;
+      sim_invalidate(s);
+    }
+  }
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  for (void*& p : A->gacc) {
+    cudaFree(p);
+    p = nullptr;
+  }
+  if (rc) return rc;
+  ETG_TRY_CUDA(cudaMemcpy(gx_host, A->grad, (size_t)A->nxd * (A->nyd + 1) * sizeof(double), cudaMemcpyDeviceToHost));
+  ETG_TRY_CUDA(cudaMemcpy(gy_host, A->grad + (size_t)A->nxd * (A->nyd + 1),
+                          (size_t)(A->nxd + 1) * A->nyd * sizeof(double), cudaMemcpyDeviceToHost));
+  return ETG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int etg_adj_create(etg_adj** out, etg_sim* sim, int i0, int nxd, int j0, int nyd) {
+  ETG_REQUIRE(out && sim, ETG_ERR_ARGUMENT, "etg_adj_create: null argument");
+  ETG_REQUIRE(nxd > 0 && nyd > 0, ETG_ERR_ARGUMENT, "etg_adj_create: empty design window");
+  // the window with one cell of halo must lie in the unit rectangle, off the PEC edges
+  const int rlo = std::max(sim->ux_lo, 1), rhi = std::min(sim->ux_hi, sim->nx);
+  const int clo = std::max(sim->uy_lo, 1), chi = std::min(sim->uy_hi, sim->ny);
+  ETG_REQUIRE(i0 - 1 >= rlo && i0 + nxd + 1 <= rhi && j0 - 1 >= clo && j0 + nyd + 1 <= chi,
+              ETG_ERR_ARGUMENT,
+              "etg_adj_create: design window [%d,%d)x[%d,%d) must lie, with one cell of margin, inside "
+              "the region where the CPML terms vanish ([%d,%d)x[%d,%d))",
+              i0, i0 + nxd, j0, j0 + nyd, rlo, rhi, clo, chi);
+  for (const Source& src : sim->sources)
+    for (size_t k = 0; k < src.i.size(); ++k)
+      ETG_REQUIRE(src.comp == ETG_HZ || !(src.i[k] >= i0 - 1 && src.i[k] <= i0 + nxd && src.j[k] >= j0 - 1 &&
+                                          src.j[k] <= j0 + nyd),
+                  ETG_ERR_ARGUMENT, "etg_adj_create: an electric source lies on the design window");
+  etg_adj* A = new etg_adj;
+  A->sim = sim;
+  A->i0 = i0;
+  A->nxd = nxd;
+  A->j0 = j0;
+  A->nyd = nyd;
+  A->ti0 = i0 - 1;
+  A->tnx = nxd + 2;
+  A->tj0 = j0 - 1;
+  A->tny = nyd + 2;
+  *out = A;
+  return ETG_OK;
+}
+
+int etg_adj_destroy(etg_adj* A) {
+  if (!A) return ETG_OK;
+  if (A->sim && A->sim->trace_buf == A->trace) clear_trace(A->sim);
+  cudaFree(A->trace);
+  for (void* p : A->ckpt) cudaFree(p);
+  for (void* p : A->lam) cudaFree(p);
+  for (auto& b : A->lpsi)
+    for (void* p : b) cudaFree(p);
+  cudaFree(A->grad);
+  for (void* p : A->gacc) cudaFree(p);
+  delete A;
+  return ETG_OK;
+}
+
+int etg_adj_forward(etg_adj* A, int64_t n_steps, int64_t stride) {
+  ETG_REQUIRE(A && n_steps > 0 && stride >= 0, ETG_ERR_ARGUMENT, "etg_adj_forward: bad arguments");
+  etg_sim* s = A->sim;
+  int rc = etg_sim_reset(s);
+  if (rc) return rc;
+  A->n_steps = n_steps;
+  A->stride = stride;
+  const size_t cell_bytes = (size_t)A->tnx * A->tny * s->esize();
+  const int64_t rows = stride == 0 ? n_steps : std::min(stride, n_steps);
+  if (A->trace_cap < rows * cell_bytes) {
+    cudaFree(A->trace);
+    A->trace = nullptr;
+    A->trace_cap = 0;
+    rc = etg_malloc(&A->trace, rows * cell_bytes);
+    if (rc) return rc;
+    A->trace_cap = rows * cell_bytes;
+  }
+  if (stride == 0) {
+    set_trace(s, A->trace, 0, n_steps, A);
+    rc = sim_advance_internal(s, n_steps);
+    clear_trace(s);
+    if (rc) return rc;
+  } else {
+    const int64_t nseg = (n_steps + stride - 1) / stride;
+    for (void* p : A->ckpt) cudaFree(p);
+    A->ckpt.assign(nseg, nullptr);
+    const size_t pb = plane_bytes(s);
+    for (int64_t k = 0; k < nseg; ++k) {
+      rc = etg_malloc(&A->ckpt[k], 7 * pb);
+      if (rc) return rc;
+      void* to[7];
+      for (int f = 0; f < 7; ++f) to[f] = (char*)A->ckpt[k] + f * pb;
+      rc = copy_state(s, to, s->field);
+      if (rc) return rc;
+      rc = sim_advance_internal(s, std::min(stride, n_steps - k * stride));
+      if (rc) return rc;
+    }
+  }
+  return etg_sim_synchronize(s);
+}
+
+int etg_adj_backward(etg_adj* A, const void* const* grad_acc, double* grad_cb_ex, double* grad_cb_ey) {
+  ETG_REQUIRE(A && grad_cb_ex && grad_cb_ey, ETG_ERR_ARGUMENT, "etg_adj_backward: null argument");
+  ETG_REQUIRE(A->n_steps > 0, ETG_ERR_STATE, "etg_adj_backward: run etg_adj_forward first");
+  int rc = A->sim->dtype == ETG_F32 ? adj_backward<float>(A, grad_acc, grad_cb_ex, grad_cb_ey)
+                                    : adj_backward<double>(A, grad_acc, grad_cb_ex, grad_cb_ey);
+  if (rc) return rc;
+  return etg_sim_synchronize(A->sim);
+}
+
+}  // extern "C"

@@ -392,6 +392,20 @@ int etg_sim_set_coefficients(etg_sim* s, const void* cb_ex, const void* cb_ey, c
   return ETG_OK;
 }
 
+int etg_sim_set_cb_window(etg_sim* s, int which, int i0, int rows, int j0, int cols, const void* host) {
+  ETG_REQUIRE(s && host && (which == 0 || which == 1) && rows > 0 && cols > 0, ETG_ERR_ARGUMENT,
+              "etg_sim_set_cb_window: bad arguments");
+  const int64_t nr = which == 1 ? s->nx + 1 : s->nx, nc = which == 0 ? s->ny + 1 : s->ny;
+  ETG_REQUIRE(i0 >= 0 && j0 >= 0 && i0 + rows <= nr && j0 + cols <= nc, ETG_ERR_ARGUMENT,
+              "etg_sim_set_cb_window: window [%d,%d)x[%d,%d) outside the %lld x %lld array", i0, i0 + rows,
+              j0, j0 + cols, (long long)nr, (long long)nc);
+  char* dst = (char*)s->cb[which] + ((int64_t)i0 * s->P + j0) * s->esize();
+  ETG_TRY_CUDA(cudaMemcpy2DAsync(dst, s->P * s->esize(), host, cols * s->esize(), cols * s->esize(), rows,
+                                 cudaMemcpyHostToDevice, s->stream));
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  return ETG_OK;
+}
+
 int etg_sim_add_source(etg_sim* s, int component, int n_nodes, const int64_t* i, const int64_t* j,
                        int64_t n0, int64_t rows, const void* table) {
   ETG_REQUIRE(s && i && j && table && n_nodes > 0 && rows >= 0, ETG_ERR_ARGUMENT,
@@ -627,6 +641,11 @@ int etg_sim_set_option(etg_sim* s, int option, int64_t value) {
 int etg_sim_get_option(etg_sim* s, int option, int64_t* value) {
   ETG_REQUIRE(s && value && option >= 0 && option < 8, ETG_ERR_ARGUMENT, "etg_sim_get_option: bad option");
   *value = s->opt[option];
+  if (*value == 0 && (option == ETG_OPT_TB_DEPTH || option == ETG_OPT_TILE_ROWS || option == ETG_OPT_TILE_COLS)) {
+    int er, ec, k;  // the default tile shape of this dtype
+    tb_default_shape(s->dtype, &er, &ec, &k);
+    *value = option == ETG_OPT_TB_DEPTH ? k : option == ETG_OPT_TILE_ROWS ? er : ec;
+  }
   return ETG_OK;
 }
 

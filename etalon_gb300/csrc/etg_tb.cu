@@ -4,24 +4,26 @@
 // Ey(i, j) on the shared pitched index i * P + j — is cut into output tiles of OR x OC
 // cells. A CTA loads its tile plus a halo of K cells on every side (one leapfrog step reads
 // at most one neighbour in each direction, so K steps need K cells), advances the extended
-// tile K steps in shared memory, and writes the output tile to the other buffer of a
-// ping-pong pair. Halo cells are recomputed by every tile that needs them, from the same
-// inputs with the same operations, so they are bit-identical to the owner's values; point
-// sources are injected wherever a tile holds the node, and DFT monitors accumulate only in
-// the owning tile, in step order. After step s only cells at least s from the tile edge are
-// valid; the edge cells read zero padding and are never used for an output cell.
+// tile K steps on chip, and writes the output tile to the other buffer of a ping-pong pair.
+// Halo cells are recomputed by every tile that needs them, from the same inputs with the
+// same operations, so they are bit-identical to the owner's values; point sources are
+// injected wherever a tile holds the node, and DFT monitors accumulate only in the owning
+// tile, in step order. After step s only cells at least s from the tile edge are valid; the
+// edge cells see zeros beyond the tile and are never used for an output cell.
 //
-// Layout on chip: Ex, Ey, Hz planes of (ER + 2) x (EC + 2W) elements (a zero pad row above
-// and below, W pad columns left and right). A warp owns one row at a time, each lane W
-// consecutive columns (one 128-bit access per plane); the column neighbours of a lane come
-// from the adjacent lane by shuffle, row neighbours from the planes, which each half step
-// refreshes behind a barrier (H reads Ex, Ey; E reads Hz). cb stays in registers.
+// Mapping: warp ty owns the RPT consecutive rows [ty*RPT, (ty+1)*RPT) of the extended tile
+// (ER = 8 RPT rows), lane l the W columns [W l, W l + W) (EC = 32 W, one 16-byte access per
+// row). Each thread keeps Ex, Ey, Hz of its RPT x W cells in registers for all K steps:
+// column neighbours come from the adjacent lane by shuffle, row neighbours from its own
+// registers, and only a warp's first row of Ey and last row of Hz cross to the warps above
+// and below, through shared memory, behind the two barriers of each step. cb (and psi in
+// CPML tiles) sit in shared memory, read only by the owning thread.
 //
 // Interior tiles — extended region inside [1, nx) x [1, ny) and inside the unit rectangle,
 // where c = 0 and 1/kappa = 1 exactly — take the lean update: Etalon's CPML terms are
 // b*0 + 0*d = +0 and d * 1 = d there, so its expression reduces exactly to "d + 0" for finite
 // d, and no cell of such a tile is a PEC edge. CPML tiles run Etalon's full expression with
-// per-cell domain checks and psi in four more planes.
+// per-cell domain checks.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -70,9 +72,11 @@ template <typename T, int RPT, int K, bool PML>
 struct TBShape {
   static constexpr int W = TBVec<T>::W;
   static constexpr int ER = 8 * RPT, EC = 32 * W, OR = ER - 2 * K, OC = EC - 2 * K;
-  static constexpr int SW = EC + 2 * W, PL = (ER + 2) * SW;
-  static constexpr int PLANES = PML ? 7 : 3;
-  static constexpr size_t SMEM = (size_t)PLANES * PL * sizeof(T);
+  static constexpr int PL = ER * EC;                    // one plane: cb or psi
+  static constexpr int PLANES = PML ? 6 : 2;            // cb_ex, cb_ey (+ 4 psi)
+  static constexpr int XCH = 9 * EC;                    // one exchange buffer: 8 warps + a zero row
+  static constexpr size_t SMEM = ((size_t)PLANES * PL + 2 * XCH) * sizeof(T);
+  static constexpr int MIN_BLOCKS = PML ? 1 : (RPT <= 5 ? 2 : 1);
   static_assert(K % W == 0, "the halo must keep vectors aligned");
   static_assert(OR > 0 && OC > 0, "halo larger than the tile");
 };
@@ -80,82 +84,72 @@ struct TBShape {
 template <typename T>
 __device__ __forceinline__ T zero() { return T(0); }
 
-// DFT of the owned output cells of one half step (H: Hz from sA; E: Ex from sA, Ey from sB).
-template <typename T, int RPT, int K, int W, int ER, int EC, int SW>
-__device__ __forceinline__ void tb_accumulate(const PhasePlan<T>& p, uint32_t rel, const T* sA,
-                                              const T* sB, int R0, int C0, int ty, int lane,
-                                              int64_t n, int* flag) {
-  for (uint32_t m = rel; m; m &= m - 1) {
-    const MonDesc<T>& d = p.mon[__ffs(m) - 1];
-    const int64_t r = n - d.n0;
-    if (r < 0 || r >= d.rows) {
-      atomicOr(flag, ERRBIT_TABLE);
-      continue;
-    }
-    const T* plane = (d.comp == ETG_EY) ? sB : sA;
-    const int64_t nodes = (int64_t)d.nxm * d.nym;
-    const T* phr = d.table + 2 * r * d.n_f;
+// acc[f, k] += value * phasor[n, f] for the owned output cells of this thread inside monitor d.
+template <typename T, int RPT, int W>
+__device__ __forceinline__ void tb_dft(const MonDesc<T>& d, const TBVec<T> (&val)[RPT], int i0, int j0,
+                                       int t_lo, int t_hi, int e_lo, int e_hi, int64_t r) {
+  const int64_t nodes = (int64_t)d.nxm * d.nym;
+  const T* phr = d.table + 2 * r * d.n_f;
 #pragma unroll
-    for (int t = 0; t < RPT; ++t) {
-      const int li = ty + 8 * t;
-      if (li < K || li >= ER - K) continue;
-      const unsigned di = (unsigned)(R0 + li - d.ix0);
-      if (di >= (unsigned)d.nxm) continue;
+  for (int t = 0; t < RPT; ++t) {
+    if (t < t_lo || t >= t_hi) continue;
+    const unsigned di = (unsigned)(i0 + t - d.ix0);
+    if (di >= (unsigned)d.nxm) continue;
 #pragma unroll
-      for (int e = 0; e < W; ++e) {
-        const int lj = W * lane + e;
-        if (lj < K || lj >= EC - K) continue;
-        const unsigned dj = (unsigned)(C0 + lj - d.jy0);
-        if (dj >= (unsigned)d.nym) continue;
-        const T val = plane[(li + 1) * SW + W + lj];
-        const int64_t k = (int64_t)di * d.nym + dj;
-        for (int f = 0; f < d.n_f; ++f) {
-          T* acc = d.acc + 2 * (f * nodes + k);
-          acc[0] = add(acc[0], mul(val, phr[2 * f]));
-          acc[1] = add(acc[1], mul(val, phr[2 * f + 1]));
-        }
+    for (int e = 0; e < W; ++e) {
+      if (e < e_lo || e >= e_hi) continue;
+      const unsigned dj = (unsigned)(j0 + e - d.jy0);
+      if (dj >= (unsigned)d.nym) continue;
+      const int64_t k = (int64_t)di * d.nym + dj;
+      for (int f = 0; f < d.n_f; ++f) {
+        T* acc = d.acc + 2 * (f * nodes + k);
+        acc[0] = add(acc[0], mul(val[t].v[e], phr[2 * f]));
+        acc[1] = add(acc[1], mul(val[t].v[e], phr[2 * f + 1]));
       }
     }
   }
 }
 
-// Hz^(n+1/2) of the owned output cells inside the trace window (adjoint support).
-template <typename T, int RPT, int K, int W, int ER, int EC, int SW>
-__device__ __forceinline__ void tb_trace(const TraceDesc<T>& t, const T* sHz, int R0, int C0, int ty,
-                                         int lane, int64_t n, int* flag) {
-  const int64_t r = n - t.n0;
-  if (r < 0 || r >= t.rows) {
-    atomicOr(flag, ERRBIT_TABLE);
-    return;
-  }
-#pragma unroll
-  for (int q = 0; q < RPT; ++q) {
-    const int li = ty + 8 * q;
-    if (li < K || li >= ER - K) continue;
-    const unsigned di = (unsigned)(R0 + li - t.ti0);
-    if (di >= (unsigned)t.tnx) continue;
-#pragma unroll
-    for (int e = 0; e < W; ++e) {
-      const int lj = W * lane + e;
-      if (lj < K || lj >= EC - K) continue;
-      const unsigned dj = (unsigned)(C0 + lj - t.tj0);
-      if (dj < (unsigned)t.tny) t.buf[(r * t.tnx + di) * t.tny + dj] = sHz[(li + 1) * SW + W + lj];
+// Subtract the deltas of step n of the sources whose node this thread holds.
+template <typename T, int RPT, int W>
+__device__ __forceinline__ void tb_inject(const PhasePlan<T>& p, uint32_t rel, TBVec<T> (&ex)[RPT],
+                                          TBVec<T> (&ey)[RPT], TBVec<T> (&hz)[RPT], int i0, int j0,
+                                          int64_t n, int* flag) {
+  for (uint32_t m = rel; m; m &= m - 1) {
+    const SrcDesc<T>& d = p.src[__ffs(m) - 1];
+    const int t_o = d.i - i0, e_o = d.j - j0;
+    if ((unsigned)t_o >= (unsigned)RPT || (unsigned)e_o >= (unsigned)W) continue;
+    const int64_t r = n - d.n0;
+    if (r < 0 || r >= d.rows) {
+      atomicOr(flag, ERRBIT_TABLE);
+      continue;
     }
+    const T delta = d.table[r * d.stride];
+#pragma unroll
+    for (int t = 0; t < RPT; ++t)
+#pragma unroll
+      for (int e = 0; e < W; ++e)
+        if (t == t_o && e == e_o) {
+          if (d.comp == ETG_HZ) hz[t].v[e] = sub(hz[t].v[e], delta);
+          else if (d.comp == ETG_EX) ex[t].v[e] = sub(ex[t].v[e], delta);
+          else ey[t].v[e] = sub(ey[t].v[e], delta);
+        }
   }
 }
 
 template <typename T, int RPT, int K, bool PML>
-__global__ void __launch_bounds__(TB_THREADS, PML ? 1 : 2)
+__global__ void __launch_bounds__(TB_THREADS, TBShape<T, RPT, K, PML>::MIN_BLOCKS)
 k_tb_step(SimArgs<T> a, TBDst<T> dst, const int2* __restrict__ tiles, PhasePlan<T> ph,
           PhasePlan<T> pe, int step_off) {
   using S = TBShape<T, RPT, K, PML>;
   using Vw = TBVec<T>;
-  constexpr int W = S::W, ER = S::ER, EC = S::EC, SW = S::SW, PL = S::PL;
+  constexpr int W = S::W, ER = S::ER, EC = S::EC, PL = S::PL;
   extern __shared__ __align__(16) unsigned char tb_smem[];
-  T* const sEx = reinterpret_cast<T*>(tb_smem);
-  T* const sEy = sEx + PL;
-  T* const sHz = sEy + PL;
-  T* const sPsi = sHz + PL;  // PML only: psi_hz_x, psi_hz_y, psi_ex_y, psi_ey_x planes
+  T* const sCbx = reinterpret_cast<T*>(tb_smem);
+  T* const sCby = sCbx + PL;
+  T* const sPsi = sCby + PL;                     // CPML tiles: psi_hz_x, psi_hz_y, psi_ex_y, psi_ey_x
+  T* const sHzX = sCbx + S::PLANES * PL;         // [k = ty + 1]: last-row Hz of warp ty; [0] = zeros
+  T* const sEyX = sHzX + S::XCH;                 // [k = ty]: first-row Ey of warp ty; [8] = zeros
   __shared__ uint32_t s_rel[4];  // relevant plan entries: H sources, E sources, H monitors, E monitors
 
   const int lane = threadIdx.x, ty = threadIdx.y;
@@ -163,7 +157,8 @@ k_tb_step(SimArgs<T> a, TBDst<T> dst, const int2* __restrict__ tiles, PhasePlan<
   const int R0 = tile.x - K, C0 = tile.y - K;  // global cell of local (0, 0); C0 % W == 0
   const int nx = a.nx, ny = a.ny;
   const int64_t P = a.P;
-  const int lj0 = W * lane, j0 = C0 + lj0;  // this lane's first column, local and global
+  const int lj0 = W * lane, j0 = C0 + lj0;     // this lane's first column, local and global
+  const int lr0 = RPT * ty, i0 = R0 + lr0;     // this warp's first row, local and global
   const bool lane_in = j0 >= 0 && j0 + W <= P;
 
   if (ty == 0) {  // which plan entries touch this tile (sources: extended region; monitors: output)
@@ -191,47 +186,40 @@ k_tb_step(SimArgs<T> a, TBDst<T> dst, const int2* __restrict__ tiles, PhasePlan<
       s_rel[2] = r2;
       s_rel[3] = r3;
     }
+    Vw z;
+    z.zero();
+    z.st(sHzX + lj0);  // the row above the tile
   }
-  // zero padding: rows -1 and ER of every plane, W columns on each side
-  for (int k = threadIdx.x + 32 * ty; k < S::PLANES * 2 * SW; k += TB_THREADS) {
-    const int plane = k / (2 * SW), r = (k / SW) % 2, c = k % SW;
-    reinterpret_cast<T*>(tb_smem)[plane * PL + (r ? ER + 1 : 0) * SW + c] = zero<T>();
-  }
-  for (int k = threadIdx.x + 32 * ty; k < S::PLANES * ER * 2 * W; k += TB_THREADS) {
-    const int plane = k / (ER * 2 * W), r = (k / (2 * W)) % ER, c = k % (2 * W);
-    reinterpret_cast<T*>(tb_smem)[plane * PL + (r + 1) * SW + (c < W ? c : EC + c)] = zero<T>();
+  if (ty == 7) {
+    Vw z;
+    z.zero();
+    z.st(sEyX + 8 * EC + lj0);  // the row below the tile
   }
 
-  // load the extended tile; cb stays in registers for the E updates
-  T cbx[RPT][W], cby[RPT][W];
+  // load the extended tile: fields to registers, cb (and psi) to shared memory
+  Vw ex[RPT], ey[RPT], hz[RPT];
 #pragma unroll
   for (int t = 0; t < RPT; ++t) {
-    const int li = ty + 8 * t, i = R0 + li;
+    const int li = lr0 + t, i = i0 + t;
     const bool in = lane_in && (unsigned)i <= (unsigned)nx;
     const int64_t g = (int64_t)i * P + j0;
-    const int o = (li + 1) * SW + W + lj0;
-    Vw ex, ey, hz, cx, cy;
+    const int o = li * EC + lj0;
+    Vw cx, cy;
     if (in) {
-      ex.ld(a.ex + g);
-      ey.ld(a.ey + g);
-      hz.ld(a.hz + g);
+      ex[t].ld(a.ex + g);
+      ey[t].ld(a.ey + g);
+      hz[t].ld(a.hz + g);
       cx.ld(a.cb_ex + g);
       cy.ld(a.cb_ey + g);
     } else {
-      ex.zero();
-      ey.zero();
-      hz.zero();
+      ex[t].zero();
+      ey[t].zero();
+      hz[t].zero();
       cx.zero();
       cy.zero();
     }
-    ex.st(sEx + o);
-    ey.st(sEy + o);
-    hz.st(sHz + o);
-#pragma unroll
-    for (int e = 0; e < W; ++e) {
-      cbx[t][e] = cx.v[e];
-      cby[t][e] = cy.v[e];
-    }
+    cx.st(sCbx + o);
+    cy.st(sCby + o);
     if (PML) {
       Vw p0, p1, p2, p3;
       if (in) {
@@ -251,13 +239,14 @@ k_tb_step(SimArgs<T> a, TBDst<T> dst, const int2* __restrict__ tiles, PhasePlan<
       p3.st(sPsi + 3 * PL + o);
     }
   }
-  // CPML tiles: this lane's y profiles (per column) in registers
+  ey[0].st(sEyX + ty * EC + lj0);
+  // CPML tiles: this thread's profiles in registers (columns per lane, rows per warp)
   T byh[W], cyh[W], kyh[W], bye[W], cye[W], kye[W];
+  T bxh[RPT], cxh[RPT], kxh[RPT], bxe[RPT], cxe[RPT], kxe[RPT];
   if (PML) {
 #pragma unroll
     for (int e = 0; e < W; ++e) {
-      const int j = min(max(j0 + e, 0), ny - 1);
-      const int je = min(max(j0 + e, 0), ny);
+      const int j = min(max(j0 + e, 0), ny - 1), je = min(max(j0 + e, 0), ny);
       byh[e] = a.by_h[j];
       cyh[e] = a.cy_h[j];
       kyh[e] = a.iky_h[j];
@@ -265,135 +254,154 @@ k_tb_step(SimArgs<T> a, TBDst<T> dst, const int2* __restrict__ tiles, PhasePlan<
       cye[e] = a.cy_e[je];
       kye[e] = a.iky_e[je];
     }
+#pragma unroll
+    for (int t = 0; t < RPT; ++t) {
+      const int i = min(max(i0 + t, 0), nx - 1), ie = min(max(i0 + t, 0), nx);
+      bxh[t] = a.bx_h[i];
+      cxh[t] = a.cx_h[i];
+      kxh[t] = a.ikx_h[i];
+      bxe[t] = a.bx_e[ie];
+      cxe[t] = a.cx_e[ie];
+      kxe[t] = a.ikx_e[ie];
+    }
   }
   __syncthreads();
   const uint32_t relSrcH = s_rel[0], relSrcE = s_rel[1], relMonH = s_rel[2], relMonE = s_rel[3];
   const int64_t n_base = *a.step + step_off;
   const T db = a.db, idx = a.inv_dx, idy = a.inv_dy;
+  // owned output cells of this thread: rows t in [t_lo, t_hi), columns e in [e_lo, e_hi)
+  const int t_lo = max(0, K - lr0), t_hi = min(RPT, ER - K - lr0);
+  const int e_lo = lj0 >= K ? 0 : W, e_hi = lj0 + W <= EC - K ? W : 0;
   const bool traced = ph.trace.buf && ph.trace.ti0 < tile.x + S::OR && ph.trace.ti0 + ph.trace.tnx > tile.x &&
                       ph.trace.tj0 < tile.y + S::OC && ph.trace.tj0 + ph.trace.tny > tile.y;
 
   for (int s = 0; s < K; ++s) {
     const int64_t n = n_base + s;
     // ---------------------------------------------------------------- H half step
+    {
+      Vw eyb;
+      eyb.ld(sEyX + (ty + 1) * EC + lj0);  // Ey of the row below this warp
 #pragma unroll
-    for (int t = 0; t < RPT; ++t) {
-      const int li = ty + 8 * t;
-      const int o = (li + 1) * SW + W + lj0;
-      Vw ex, ey, eyn, hz;
-      ex.ld(sEx + o);
-      ey.ld(sEy + o);
-      eyn.ld(sEy + o + SW);
-      hz.ld(sHz + o);
-      T exr = __shfl_down_sync(0xffffffffu, ex.v[0], 1);
-      if (lane == 31) exr = sEx[o + W];
+      for (int t = 0; t < RPT; ++t) {
+        T exr = __shfl_down_sync(0xffffffffu, ex[t].v[0], 1);
+        if (lane == 31) exr = zero<T>();
 #pragma unroll
-      for (int e = 0; e < W; ++e) {
-        const T exn = e < W - 1 ? ex.v[e + 1] : exr;
-        const T dex_dy = mul(sub(exn, ex.v[e]), idy);
-        const T dey_dx = mul(sub(eyn.v[e], ey.v[e]), idx);
-        if (!PML) {
-          hz.v[e] = add(hz.v[e], mul(db, sub(add(dex_dy, zero<T>()), add(dey_dx, zero<T>()))));
-        } else {
-          const int i = R0 + li, j = j0 + e;
-          if (i >= 0 && i < nx && j >= 0 && j < ny) {
-            T* pxp = sPsi + 0 * PL + o + e;
-            T* pyp = sPsi + 1 * PL + o + e;
-            const T py = add(mul(byh[e], *pyp), mul(cyh[e], dex_dy));
-            const T px = add(mul(a.bx_h[i], *pxp), mul(a.cx_h[i], dey_dx));
-            if (j < a.ys_lo || j >= a.ys_hi) *pyp = py;
-            if (i < a.xs_lo || i >= a.xs_hi) *pxp = px;
-            hz.v[e] = add(hz.v[e], mul(db, sub(add(mul(dex_dy, kyh[e]), py), add(mul(dey_dx, a.ikx_h[i]), px))));
+        for (int e = 0; e < W; ++e) {
+          const T exn = e < W - 1 ? ex[t].v[e + 1] : exr;
+          const T eyn = t < RPT - 1 ? ey[t + 1].v[e] : eyb.v[e];
+          const T dex_dy = mul(sub(exn, ex[t].v[e]), idy);
+          const T dey_dx = mul(sub(eyn, ey[t].v[e]), idx);
+          if (!PML) {
+            hz[t].v[e] = add(hz[t].v[e], mul(db, sub(add(dex_dy, zero<T>()), add(dey_dx, zero<T>()))));
+          } else {
+            const int i = i0 + t, j = j0 + e;
+            if (i >= 0 && i < nx && j >= 0 && j < ny) {
+              T* pxp = sPsi + 0 * PL + (lr0 + t) * EC + lj0 + e;
+              T* pyp = sPsi + 1 * PL + (lr0 + t) * EC + lj0 + e;
+              const T py = add(mul(byh[e], *pyp), mul(cyh[e], dex_dy));
+              const T px = add(mul(bxh[t], *pxp), mul(cxh[t], dey_dx));
+              if (j < a.ys_lo || j >= a.ys_hi) *pyp = py;
+              if (i < a.xs_lo || i >= a.xs_hi) *pxp = px;
+              hz[t].v[e] = add(hz[t].v[e], mul(db, sub(add(mul(dex_dy, kyh[e]), py), add(mul(dey_dx, kxh[t]), px))));
+            }
           }
         }
       }
-      hz.st(sHz + o);
     }
-    if (relSrcH) {  // magnetic sources at n dt, after the update (solver.py:120-123)
-      for (uint32_t m = relSrcH; m; m &= m - 1) {
-        const SrcDesc<T>& d = ph.src[__ffs(m) - 1];
-        const int li = d.i - R0, lj = d.j - C0;
-        if ((li & 7) != ty || lj / W != lane) continue;
+    if (relSrcH) tb_inject<T, RPT, W>(ph, relSrcH, ex, ey, hz, i0, j0, n, a.flag);
+    if (relMonH) {  // DFT of H at (n + 1/2) dt, owned nodes only
+      for (uint32_t m = relMonH; m; m &= m - 1) {
+        const MonDesc<T>& d = ph.mon[__ffs(m) - 1];
         const int64_t r = n - d.n0;
-        T* cell = sHz + (li + 1) * SW + W + lj;
         if (r < 0 || r >= d.rows) atomicOr(a.flag, ERRBIT_TABLE);
-        else *cell = sub(*cell, d.table[r * d.stride]);
+        else tb_dft<T, RPT, W>(d, hz, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
       }
     }
-    if (relMonH) tb_accumulate<T, RPT, K, W, ER, EC, SW>(ph, relMonH, sHz, nullptr, R0, C0, ty, lane, n, a.flag);
-    if (traced) tb_trace<T, RPT, K, W, ER, EC, SW>(ph.trace, sHz, R0, C0, ty, lane, n, a.flag);
+    if (traced) {
+      const TraceDesc<T>& tr = ph.trace;
+      const int64_t r = n - tr.n0;
+      if (r < 0 || r >= tr.rows) {
+        atomicOr(a.flag, ERRBIT_TABLE);
+      } else {
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+          const unsigned di = (unsigned)(i0 + t - tr.ti0);
+          if (t < t_lo || t >= t_hi || di >= (unsigned)tr.tnx) continue;
+#pragma unroll
+          for (int e = 0; e < W; ++e) {
+            const unsigned dj = (unsigned)(j0 + e - tr.tj0);
+            if (e >= e_lo && e < e_hi && dj < (unsigned)tr.tny) tr.buf[(r * tr.tnx + di) * tr.tny + dj] = hz[t].v[e];
+          }
+        }
+      }
+    }
+    hz[RPT - 1].st(sHzX + (ty + 1) * EC + lj0);
     __syncthreads();
     // ---------------------------------------------------------------- E half step
+    {
+      Vw hza;
+      hza.ld(sHzX + ty * EC + lj0);  // Hz of the row above this warp
 #pragma unroll
-    for (int t = 0; t < RPT; ++t) {
-      const int li = ty + 8 * t;
-      const int o = (li + 1) * SW + W + lj0;
-      Vw hz, hzu, ex, ey;
-      hz.ld(sHz + o);
-      hzu.ld(sHz + o - SW);
-      ex.ld(sEx + o);
-      ey.ld(sEy + o);
-      T hzl = __shfl_up_sync(0xffffffffu, hz.v[W - 1], 1);
-      if (lane == 0) hzl = sHz[o - 1];
+      for (int t = 0; t < RPT; ++t) {
+        T hzl = __shfl_up_sync(0xffffffffu, hz[t].v[W - 1], 1);
+        if (lane == 0) hzl = zero<T>();
+        Vw cx, cy;
+        cx.ld(sCbx + (lr0 + t) * EC + lj0);
+        cy.ld(sCby + (lr0 + t) * EC + lj0);
 #pragma unroll
-      for (int e = 0; e < W; ++e) {
-        const T hzp = e > 0 ? hz.v[e - 1] : hzl;
-        const T dy = mul(sub(hz.v[e], hzp), idy);
-        const T dx = mul(sub(hz.v[e], hzu.v[e]), idx);
-        if (!PML) {
-          ex.v[e] = add(ex.v[e], mul(cbx[t][e], add(dy, zero<T>())));
-          ey.v[e] = sub(ey.v[e], mul(cby[t][e], add(dx, zero<T>())));
-        } else {
-          const int i = R0 + li, j = j0 + e;
-          if (i >= 0 && i < nx && j >= 1 && j <= ny - 1) {
-            T* pp = sPsi + 2 * PL + o + e;
-            const T p = add(mul(bye[e], *pp), mul(cye[e], dy));
-            if (j < a.ys_lo || j >= a.ys_hi) *pp = p;
-            ex.v[e] = add(ex.v[e], mul(cbx[t][e], add(mul(dy, kye[e]), p)));
-          }
-          if (i >= 1 && i <= nx - 1 && j >= 0 && j < ny) {
-            T* pp = sPsi + 3 * PL + o + e;
-            const T p = add(mul(a.bx_e[i], *pp), mul(a.cx_e[i], dx));
-            if (i < a.xs_lo || i >= a.xs_hi) *pp = p;
-            ey.v[e] = sub(ey.v[e], mul(cby[t][e], add(mul(dx, a.ikx_e[i]), p)));
+        for (int e = 0; e < W; ++e) {
+          const T hzp = e > 0 ? hz[t].v[e - 1] : hzl;
+          const T hzu = t > 0 ? hz[t - 1].v[e] : hza.v[e];
+          const T dy = mul(sub(hz[t].v[e], hzp), idy);
+          const T dx = mul(sub(hz[t].v[e], hzu), idx);
+          if (!PML) {
+            ex[t].v[e] = add(ex[t].v[e], mul(cx.v[e], add(dy, zero<T>())));
+            ey[t].v[e] = sub(ey[t].v[e], mul(cy.v[e], add(dx, zero<T>())));
+          } else {
+            const int i = i0 + t, j = j0 + e;
+            if (i >= 0 && i < nx && j >= 1 && j <= ny - 1) {
+              T* pp = sPsi + 2 * PL + (lr0 + t) * EC + lj0 + e;
+              const T p = add(mul(bye[e], *pp), mul(cye[e], dy));
+              if (j < a.ys_lo || j >= a.ys_hi) *pp = p;
+              ex[t].v[e] = add(ex[t].v[e], mul(cx.v[e], add(mul(dy, kye[e]), p)));
+            }
+            if (i >= 1 && i <= nx - 1 && j >= 0 && j < ny) {
+              T* pp = sPsi + 3 * PL + (lr0 + t) * EC + lj0 + e;
+              const T p = add(mul(bxe[t], *pp), mul(cxe[t], dx));
+              if (i < a.xs_lo || i >= a.xs_hi) *pp = p;
+              ey[t].v[e] = sub(ey[t].v[e], mul(cy.v[e], add(mul(dx, kxe[t]), p)));
+            }
           }
         }
       }
-      ex.st(sEx + o);
-      ey.st(sEy + o);
     }
-    if (relSrcE) {  // electric sources at (n + 1/2) dt (solver.py:124-125)
-      for (uint32_t m = relSrcE; m; m &= m - 1) {
-        const SrcDesc<T>& d = pe.src[__ffs(m) - 1];
-        const int li = d.i - R0, lj = d.j - C0;
-        if ((li & 7) != ty || lj / W != lane) continue;
+    if (relSrcE) tb_inject<T, RPT, W>(pe, relSrcE, ex, ey, hz, i0, j0, n, a.flag);
+    if (relMonE) {  // DFT of E at (n + 1) dt
+      for (uint32_t m = relMonE; m; m &= m - 1) {
+        const MonDesc<T>& d = pe.mon[__ffs(m) - 1];
         const int64_t r = n - d.n0;
-        T* cell = (d.comp == ETG_EX ? sEx : sEy) + (li + 1) * SW + W + lj;
         if (r < 0 || r >= d.rows) atomicOr(a.flag, ERRBIT_TABLE);
-        else *cell = sub(*cell, d.table[r * d.stride]);
+        else if (d.comp == ETG_EX) tb_dft<T, RPT, W>(d, ex, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
+        else tb_dft<T, RPT, W>(d, ey, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
       }
     }
-    if (relMonE) tb_accumulate<T, RPT, K, W, ER, EC, SW>(pe, relMonE, sEx, sEy, R0, C0, ty, lane, n, a.flag);
+    ey[0].st(sEyX + ty * EC + lj0);
     __syncthreads();
   }
 
-  // write the output tile (vectors lie wholly inside or outside it, since K and OC are
-  // multiples of W)
-  if (lj0 < K || lj0 >= K + S::OC || !lane_in) return;
+  // write the output tile (vectors lie wholly inside or outside it: K, OC are multiples of W)
+  if (e_lo != 0 || e_hi != W || !lane_in) return;
 #pragma unroll
   for (int t = 0; t < RPT; ++t) {
-    const int li = ty + 8 * t, i = R0 + li;
-    if (li < K || li >= K + S::OR || (unsigned)i > (unsigned)nx) continue;
+    const int i = i0 + t;
+    if (t < t_lo || t >= t_hi || (unsigned)i > (unsigned)nx) continue;
     const int64_t g = (int64_t)i * P + j0;
-    const int o = (li + 1) * SW + W + lj0;
-    Vw v;
-    v.ld(sEx + o);
-    v.st(dst.ex + g);
-    v.ld(sEy + o);
-    v.st(dst.ey + g);
-    v.ld(sHz + o);
-    v.st(dst.hz + g);
+    ex[t].st(dst.ex + g);
+    ey[t].st(dst.ey + g);
+    hz[t].st(dst.hz + g);
     if (PML) {  // psi stays +0 outside its strips in both buffers, so whole vectors are copied
+      const int o = (lr0 + t) * EC + lj0;
+      Vw v;
       v.ld(sPsi + 0 * PL + o);
       v.st(dst.psi_hz_x + g);
       v.ld(sPsi + 1 * PL + o);
@@ -530,9 +538,9 @@ struct TBFns {
   cudaError_t (*attrs)();
 };
 
-// Compiled shapes (rows = 8 * RPT, depth K); the CPML variant's seven planes must fit 227 KB.
-#define ETG_TB_SHAPES_F32(X) X(ETG_F32, 4, 4) X(ETG_F32, 5, 4) X(ETG_F32, 6, 4) X(ETG_F32, 7, 4) X(ETG_F32, 7, 8)
-#define ETG_TB_SHAPES_F64(X) X(ETG_F64, 4, 2) X(ETG_F64, 5, 2) X(ETG_F64, 6, 2) X(ETG_F64, 5, 4)
+// Compiled shapes (rows = 8 * RPT, depth K); the CPML variant's six planes must fit 227 KB.
+#define ETG_TB_SHAPES_F32(X) X(ETG_F32, 4, 4) X(ETG_F32, 5, 4) X(ETG_F32, 6, 4) X(ETG_F32, 8, 4) X(ETG_F32, 8, 8)
+#define ETG_TB_SHAPES_F64(X) X(ETG_F64, 4, 2) X(ETG_F64, 5, 2) X(ETG_F64, 8, 2) X(ETG_F64, 8, 4)
 
 template <typename T>
 static TBFns<T> pick(const TBConfig& c) {

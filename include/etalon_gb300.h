@@ -113,6 +113,9 @@ int etg_sim_set_coefficients(etg_sim* sim, const void* cb_ex, const void* cb_ey,
                              const void* by_e, const void* cy_e, const void* iky_e,
                              const void* by_h, const void* cy_h, const void* iky_h,
                              double db, double inv_dx, double inv_dy);
+/* Replace a window of cb_ex (which = 0, array (nx, ny+1)) or cb_ey (which = 1, (nx+1, ny)):
+ * rows [i0, i0+rows) x columns [j0, j0+cols) from a host array (rows, cols) in dtype. */
+int etg_sim_set_cb_window(etg_sim* sim, int which, int i0, int rows, int j0, int cols, const void* host);
 /* A point source on `component` (ETG_EX/EY/HZ) over n_nodes nodes (i, j) with its
  * per-step deltas for steps n0 .. n0+rows-1: table (rows, n_nodes) in dtype, the
  * values subtracted (etalon/fdtd/sources.py:54-56 cast to dtype). Sources apply in
@@ -148,6 +151,24 @@ int etg_sim_get_option(etg_sim* sim, int option, int64_t* value);
 /* Device-side timing of the last etg_sim_advance (CUDA events on its stream):
  * total milliseconds and the number of kernel launches it made. */
 int etg_sim_last_timing(etg_sim* sim, double* ms, int64_t* launches);
+
+/* ---------------------------------------------------------------- adjoint
+ * No counterpart in Etalon. Gradient of an objective J(DFT accumulators) with respect to
+ * cb_ex and cb_ey on a design window of cells [i0, i0+nxd) x [j0, j0+nyd): the Ex nodes
+ * (i0..i0+nxd-1, j0..j0+nyd) and the Ey nodes (i0..i0+nxd, j0..j0+nyd-1). The window, with one
+ * cell of margin, must lie where the CPML terms vanish, and hold no electric source. */
+typedef struct etg_adj etg_adj;
+int etg_adj_create(etg_adj** out, etg_sim* sim, int i0, int nxd, int j0, int nyd);
+int etg_adj_destroy(etg_adj* adj);
+/* Forward run of n_steps from zero fields (monitors accumulate as in etg_sim_advance).
+ * stride 0 records Hz on the window at every step; stride S > 0 keeps full-state
+ * checkpoints every S steps instead and recomputes each segment in the backward pass. */
+int etg_adj_forward(etg_adj* adj, int64_t n_steps, int64_t stride);
+/* Reverse sweep: grad_acc[m] is dJ/d(accumulator m), (n_f, nodes) complex in dtype, or NULL
+ * for monitors J does not use (one entry per monitor, in order of addition). Writes
+ * dJ/dcb_ex (nxd, nyd+1) and dJ/dcb_ey (nxd+1, nyd) in float64. The simulation's fields are
+ * left in an unspecified state. */
+int etg_adj_backward(etg_adj* adj, const void* const* grad_acc, double* grad_cb_ex, double* grad_cb_ey);
 
 /* ---------------------------------------------------------------- no-allocation advance
  * Has no counterpart in Etalon. For callers that cannot allocate device memory when they

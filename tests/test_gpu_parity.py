@@ -364,8 +364,8 @@ def _oracle_for(p):
 
 # ----------------------------------------------------------------- temporal blocking
 
-TB_SHAPES_F32 = [(32, 128, 4), (40, 128, 4), (48, 128, 4), (56, 128, 4), (56, 128, 8)]
-TB_SHAPES_F64 = [(32, 64, 2), (40, 64, 2), (48, 64, 2), (40, 64, 4)]
+TB_SHAPES_F32 = [(32, 128, 4), (40, 128, 4), (48, 128, 4), (64, 128, 4), (64, 128, 8)]
+TB_SHAPES_F64 = [(32, 64, 2), (40, 64, 2), (64, 64, 2), (64, 64, 4)]
 
 
 def _tb_engine(name, precision, g, shape, **kw):

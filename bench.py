@@ -230,13 +230,14 @@ def config_dict(p, args) -> dict:
 def run_ours(args, world, rank, local) -> None:
     import torch
 
-    from etalon_gb300 import _lib
+    from etalon_gb300 import _lib, autotune
     from etalon_gb300 import physics as ph
     from etalon_gb300.engine import TEEngine
 
     _lib.call("etg_set_device", local)
     p = workload(args.precision, args.time_steps)
-    e = TEEngine(p, kernel=args.kernel)
+    e = TEEngine(p, kernel="auto" if args.kernel == "tuned" else args.kernel)
+    choice = list(autotune.tune(e)) if args.kernel == "tuned" else [args.kernel]
     e.set_option(_lib.OPT_TIMING, 1)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -310,14 +311,8 @@ def run_ours(args, world, rank, local) -> None:
     e2e_s = reduce_max(world, time.perf_counter() - t0)
     e2e_value = world * cells * args.steps / e2e_s
 
-    # roofline of the dominant kernel (algorithmic bytes / average launch duration)
-    peak, peak_kind = hbm_peak()
-    b_step = algorithmic_bytes_per_step(p)
-    kernel = kernel_name(e)
-    steps_per_launch = launch_depth(e)
-    launch_ms = total_ms / args.steps / (p.n_steps / steps_per_launch)
-    achieved = b_step * steps_per_launch / (launch_ms / 1e3) / 1e9
-    traffic, traffic_src = ncu_traffic(kernel)
+    # roofline of the dominant kernel: algorithmic bytes per launch / its average launch time
+    roofline = kernel_roofline(e, p)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -326,11 +321,8 @@ def run_ours(args, world, rank, local) -> None:
         "config": config_dict(p, args),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": b_step * steps_per_launch,
-                     "steps_per_launch": steps_per_launch,
-                     "traffic": traffic, "traffic_source": traffic_src},
+        "roofline": roofline,
+        "kernel_choice": choice,
         "clocks": clocks.summary(),
         "wall_ms_per_step": 1e3 * wall / args.steps,
     }  # fmt: skip
@@ -342,6 +334,8 @@ def run_ours(args, world, rank, local) -> None:
             "sample": f"{p.grid.nx}x{p.grid.ny} workload grid, {steps} time steps in {cwall:.1f} s, "
                       f"NumPy oracle in {threads} row bands",
         }  # fmt: skip
+    if not args.no_batched:
+        out["batched"] = batched_line(args, local)
     if args.fp64:
         out["fp64"] = fp64_line(args, local)
     if rank == 0:
@@ -349,25 +343,107 @@ def run_ours(args, world, rank, local) -> None:
     e.close()
 
 
-def kernel_name(e) -> str:
+def kernel_roofline(e, p) -> dict:
+    """Roofline of the dominant kernel, timed live with CUDA events on its launching stream.
+
+    Temporally blocked path: one more run of the workload with every interior-tile and
+    CPML-tile launch timed on its own (option TIMING = 2: the two kernels one after the
+    other, an event pair around each, no graphs). The interior kernel advances its output
+    cells K steps per launch; its algorithmic bytes are those of K single-pass steps over
+    them, 8 values per cell-step (Ex, Ey, Hz read and write, cb_ex and cb_ey read).
+    One-step path: the run's own time per step against the algorithmic bytes of a step.
+    """
     from etalon_gb300 import _lib
+
+    peak, peak_kind = hbm_peak()
+    s = np.dtype(p.real).itemsize
+    kind, rows, depth = (get_option(e, o) for o in (_lib.OPT_KERNEL, _lib.OPT_TILE_ROWS, _lib.OPT_TB_DEPTH))
+    e.set_option(_lib.OPT_TIMING, 2)
+    e.reset()
+    e.advance(p.n_steps)
+    e.synchronize()
+    kt = e.kernel_timing()
+    e.set_option(_lib.OPT_TIMING, 1)
+    ms, launches, cells = kt["interior"]
+    if launches:
+        dt = "float" if s == 4 else "double"
+        name = f"k_tb_step<{dt},{rows // 8},{depth},false>"
+        launch_ms = ms / launches
+        bytes_launch = 8 * s * cells * depth
+        cp_ms, cp_launches, cp_cells = kt["cpml"]
+        extra = {"kernel": name, "tile": [rows, 128 if s == 4 else 64], "steps_per_launch": depth,
+                 "output_cells_per_launch": cells, "launch_ms": launch_ms, "launches_timed": launches,
+                 "cpml_kernel": {"launch_ms": cp_ms / max(cp_launches, 1), "output_cells_per_launch": cp_cells},
+                 "timing": "CUDA events around each launch, one extra run of the workload, kernels serialised"}
+        tag = "k_tb_step_interior"
+    elif kind == 3:  # persistent TMA kernel: the run's device time over its launches
+        e.reset()
+        e.advance(p.n_steps)
+        total, _ = e.last_timing()
+        n_launch = 2 * (p.n_steps // (2 * depth))
+        launch_ms = total / max(n_launch, 1)
+        bytes_launch = algorithmic_bytes_per_step(p) * depth
+        extra = {"kernel": f"k_tb_tma<{rows // 8},{depth}>", "steps_per_launch": depth, "launch_ms": launch_ms,
+                 "timing": "CUDA events around the run, divided by its launches"}
+        tag = "k_tb_tma"
+    else:  # one-step kernels: the timed run's own device time
+        e.reset()
+        e.advance(p.n_steps)
+        total, _ = e.last_timing()
+        launch_ms = total / p.n_steps
+        bytes_launch = algorithmic_bytes_per_step(p)
+        extra = {"kernel": "k_fused_h+k_fused_e", "steps_per_launch": 1, "launch_ms": launch_ms,
+                 "timing": "CUDA events around the run, per step"}
+        tag = "k_fused"
+    achieved = bytes_launch / (launch_ms / 1e3) / 1e9
+    traffic, traffic_src = ncu_traffic(tag)
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": f"{peak_kind} (hbm_gbs)", "traffic": traffic, "traffic_source": traffic_src,
+            "algorithmic_bytes_per_launch": bytes_launch, **extra}  # fmt: skip
+
+
+def get_option(e, option: int) -> int:
     import ctypes as C
+
+    from etalon_gb300 import _lib
 
     v = C.c_int64()
-    _lib.call("etg_sim_get_option", e._h, _lib.OPT_KERNEL, C.byref(v))
-    return "k_tb_step" if v.value == 2 else "k_fused_h+k_fused_e"
+    _lib.call("etg_sim_get_option", e._h, option, C.byref(v))
+    return int(v.value)
 
 
-def launch_depth(e) -> int:
-    """Time steps per launch of the dominant kernel (one for the one-step kernels)."""
-    import ctypes as C
+def batched_line(args, local) -> dict:
+    """64 seeded synthetic devices (bends, rings, MMIs; interiors 256-1536 cells per axis,
+    12-layer CPML, one Hz source, 4 point monitors x 8 wavelengths), float32, 5000 time steps,
+    stepped together by one Batch: tiles of all 64 in each launch, CUDA graphs per step block."""
+    import torch
 
-    from etalon_gb300 import _lib
+    from etalon_gb300 import _lib, autotune
+    from etalon_gb300.batch import Batch
+    from tests import cases
 
-    kind, depth = C.c_int64(), C.c_int64()
-    _lib.call("etg_sim_get_option", e._h, _lib.OPT_KERNEL, C.byref(kind))
-    _lib.call("etg_sim_get_option", e._h, _lib.OPT_TB_DEPTH, C.byref(depth))
-    return int(depth.value) if kind.value == 2 else 1
+    problems = cases.synthetic_batch(64, n_steps=args.batch_time_steps)
+    b = Batch(problems)
+    choice = autotune.tune_batch(b)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    cells = sum(p.grid.n_cells for p in problems)
+    ms, launches = [], 0
+    for k in range(3):
+        b.reset()
+        flush.zero_()
+        torch.cuda.synchronize()
+        b.advance(args.batch_time_steps)
+        t, n = b.last_timing()
+        if k:  # the first run is the warm-up
+            ms.append(t)
+            launches += n
+    b.close()
+    t = sum(ms) / len(ms)
+    return {"metric": "cell-updates/s (64 synthetic devices 256^2-1536^2 + CPML, fp32, one batch)",
+            "value": cells * args.batch_time_steps / (t / 1e3), "unit": UNIT, "ms_per_run": t,
+            "sims": len(problems), "cells": cells, "time_steps": args.batch_time_steps,
+            "tile_rows_depth": list(choice), "gpu_launches_per_run": launches // len(ms),
+            "runs_timed": len(ms), "l2": "flushed before each run"}  # fmt: skip
 
 
 def fp64_line(args, local) -> dict:
@@ -400,9 +476,11 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="single", choices=["single", "double"])
     ap.add_argument("--time-steps", type=int, default=10000)
-    ap.add_argument("--kernel", default="auto", choices=["auto", "plain", "tb"])
+    ap.add_argument("--kernel", default="tuned", choices=["tuned", "auto", "plain", "tb"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-device batched line")
+    ap.add_argument("--batch-time-steps", type=int, default=5000)
     ap.add_argument("--fp64", action="store_true", help="add a float64 line of the same workload")
     args = ap.parse_args()
     os.environ["ETG_BENCH_IMPL"] = args.impl

@@ -61,6 +61,13 @@ SIGNATURES: dict[str, list] = {
     "etg_sim_set_option": [vp, i32, i64],
     "etg_sim_get_option": [vp, i32, pi64],
     "etg_sim_last_timing": [vp, C.POINTER(f64), pi64],
+    "etg_sim_kernel_timing": [vp, C.POINTER(f64), pi64, pi64],
+    "etg_batch_create": [C.POINTER(vp), i32, C.POINTER(vp)],
+    "etg_batch_destroy": [vp],
+    "etg_batch_advance": [vp, i64],
+    "etg_batch_synchronize": [vp],
+    "etg_batch_set_option": [vp, i32, i64],
+    "etg_batch_last_timing": [vp, C.POINTER(f64), pi64],
     "etg_adj_create": [C.POINTER(vp), vp, i32, i32, i32, i32],
     "etg_adj_destroy": [vp],
     "etg_adj_forward": [vp, i64, i64],

@@ -1,0 +1,296 @@
+// Batched stepping of many resident simulations (no counterpart in Etalon, which runs one
+// FDTDSolver per simulation): one launch pair per K steps advances every simulation of the
+// batch, whatever its size. Each tile names its simulation; per-simulation arguments, second
+// buffers and source/monitor plans live in device memory (BatchSim). Blocks of steps are CUDA
+// graphs, as for a single simulation, and every simulation's result is bit-identical to its
+// own run (the tiles compute exactly what the single-simulation kernels compute).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "etg_tb.h"
+
+using namespace etg;
+
+struct etg_batch {
+  std::vector<etg_sim*> sims;
+  int dtype = ETG_F32;
+  std::vector<void*> alt;          // per simulation: 7 planes of the second buffer
+  std::vector<size_t> alt_bytes;
+  void* d_sims = nullptr;          // BatchSim<T>[n]
+  std::vector<unsigned char> h_sims;
+  int4* d_tiles = nullptr;
+  int n_inner = 0, n_pml = 0, tiles_er = 0, tiles_k = 0;
+  int64_t** d_steps = nullptr;     // each simulation's step counter
+  cudaStream_t stream = nullptr, side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr, ev0 = nullptr, ev1 = nullptr, done = nullptr;
+  int64_t opt[8] = {0, 0, 32, 0, 0, 0, 0, 0};
+  std::map<int64_t, cudaGraphExec_t> graphs;
+  double last_ms = 0;
+  int64_t last_launches = 0;
+};
+
+namespace {
+
+__global__ void k_batch_step_add(int64_t* const* steps, int n, int64_t k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) *steps[i] += k;
+}
+
+void drop_graphs(etg_batch* b) {
+  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  b->graphs.clear();
+}
+
+template <typename T>
+int refresh(etg_batch* b, int ER, int K, bool* changed) {
+  const int n = (int)b->sims.size();
+  std::vector<unsigned char> host((size_t)n * sizeof(BatchSim<T>));
+  for (int k = 0; k < n; ++k) {
+    etg_sim* s = b->sims[k];
+    BatchSim<T> e;
+    memset(&e, 0, sizeof e);
+    const size_t bytes = (size_t)(s->nx + 2) * s->P * sizeof(T);
+    if (b->alt_bytes[k] != bytes) {
+      cudaFree(b->alt[k]);
+      b->alt[k] = nullptr;
+      int rc = etg_malloc(&b->alt[k], 7 * bytes);
+      if (rc) return rc;
+      ETG_TRY_CUDA(cudaMemset(b->alt[k], 0, 7 * bytes));
+      b->alt_bytes[k] = bytes;
+    }
+    const SimArgs<T> a = sim_args_export<T>(s);
+    SimArgs<T> bb = a;
+    T** bp[7] = {&bb.ex, &bb.ey, &bb.hz, &bb.psi_ex_y, &bb.psi_ey_x, &bb.psi_hz_x, &bb.psi_hz_y};
+    for (int f = 0; f < 7; ++f) *bp[f] = (T*)((char*)b->alt[k] + f * bytes);
+    e.src[0] = a;
+    e.src[1] = bb;
+    e.dst[0] = TBDst<T>{bb.ex, bb.ey, bb.hz, bb.psi_ex_y, bb.psi_ey_x, bb.psi_hz_x, bb.psi_hz_y};
+    e.dst[1] = TBDst<T>{a.ex, a.ey, a.hz, a.psi_ex_y, a.psi_ey_x, a.psi_hz_x, a.psi_hz_y};
+    int rc = sim_plans_export<T>(s, &e.ph, &e.pe);
+    if (rc) return rc;
+    memcpy(host.data() + (size_t)k * sizeof e, &e, sizeof e);
+  }
+  *changed = host != b->h_sims;
+  if (*changed) {
+    if (!b->d_sims) {
+      int rc = etg_malloc(&b->d_sims, host.size());
+      if (rc) return rc;
+    }
+    ETG_TRY_CUDA(cudaMemcpy(b->d_sims, host.data(), host.size(), cudaMemcpyHostToDevice));
+    b->h_sims.swap(host);
+  }
+  if (*changed || b->tiles_er != ER || b->tiles_k != K) {
+    std::vector<int4> inner, pml;
+    for (int k = 0; k < n; ++k) {
+      etg_sim* s = b->sims[k];
+      PhasePlan<T> ph, pe;
+      sim_plans_export<T>(s, &ph, &pe);
+      std::vector<int4> hot;
+      for (const PhasePlan<T>* p : {&ph, &pe}) {
+        for (int q = 0; q < p->n_src; ++q) hot.push_back(make_int4(p->src[q].i, p->src[q].j, p->src[q].i + 1, p->src[q].j + 1));
+        for (int q = 0; q < p->n_mon; ++q)
+          hot.push_back(make_int4(p->mon[q].ix0, p->mon[q].jy0, p->mon[q].ix0 + p->mon[q].nxm, p->mon[q].jy0 + p->mon[q].nym));
+      }
+      std::vector<int2> t;
+      int ni = 0;
+      tb_split_tiles(s->nx, s->ny, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi, ER, 32 * (sizeof(T) == 4 ? 4 : 2), K, hot, &t, &ni);
+      for (int q = 0; q < (int)t.size(); ++q) (q < ni ? inner : pml).push_back(make_int4(k, t[q].x, t[q].y, 0));
+    }
+    b->n_inner = (int)inner.size();
+    b->n_pml = (int)pml.size();
+    inner.insert(inner.end(), pml.begin(), pml.end());
+    cudaFree(b->d_tiles);
+    b->d_tiles = nullptr;
+    int rc = etg_malloc((void**)&b->d_tiles, std::max<size_t>(1, inner.size()) * sizeof(int4));
+    if (rc) return rc;
+    ETG_TRY_CUDA(cudaMemcpy(b->d_tiles, inner.data(), inner.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    b->tiles_er = ER;
+    b->tiles_k = K;
+    *changed = true;
+  }
+  return ETG_OK;
+}
+
+template <typename T>
+int batch_advance(etg_batch* b, int64_t n_steps) {
+  int ER, EC, K;
+  tb_default_shape((int)sizeof(T), &ER, &EC, &K);
+  if (b->opt[ETG_OPT_TILE_ROWS] > 0) ER = (int)b->opt[ETG_OPT_TILE_ROWS];
+  if (b->opt[ETG_OPT_TB_DEPTH] > 0) K = (int)b->opt[ETG_OPT_TB_DEPTH];
+  int rc = tb_batch_attrs<T>(ER, K);
+  if (rc) return rc;
+  bool changed = false;
+  rc = refresh<T>(b, ER, K, &changed);
+  if (rc) return rc;
+  if (changed) drop_graphs(b);
+  const int n = (int)b->sims.size();
+  const int64_t pairs = n_steps / (2 * K);
+  const int64_t per_graph = std::max<int64_t>(1, b->opt[ETG_OPT_GRAPH_STEPS] / (2 * K));
+  auto pair = [&](int64_t p) -> int {
+    int r = tb_batch_pair<T>(ER, K, b->d_sims, b->d_tiles, b->n_inner, b->n_pml, 0, (int)(2 * K * p), b->stream,
+                             b->side, b->fork, b->join);
+    if (r == ETG_OK)
+      r = tb_batch_pair<T>(ER, K, b->d_sims, b->d_tiles, b->n_inner, b->n_pml, 1, (int)(2 * K * p + K), b->stream,
+                           b->side, b->fork, b->join);
+    return r;
+  };
+  auto add_steps = [&](int64_t k) {
+    k_batch_step_add<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_steps, n, k);
+    g_launches += 1;
+  };
+  int64_t done = 0;
+  if (b->opt[ETG_OPT_GRAPH_STEPS] > 0 && pairs >= per_graph) {
+    auto it = b->graphs.find(per_graph);
+    if (it == b->graphs.end()) {
+      cudaGraph_t graph;
+      ETG_TRY_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      int r = ETG_OK;
+      for (int64_t p = 0; p < per_graph && r == ETG_OK; ++p) r = pair(p);
+      if (r == ETG_OK) add_steps(2 * K * per_graph);
+      cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+      if (r) return r;
+      ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "batch graph capture failed: %s", cudaGetErrorString(e));
+      cudaGraphExec_t exec;
+      e = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "batch graph instantiate failed: %s", cudaGetErrorString(e));
+      it = b->graphs.emplace(per_graph, exec).first;
+    }
+    for (; done + per_graph <= pairs; done += per_graph) {
+      ETG_TRY_CUDA(cudaGraphLaunch(it->second, b->stream));
+      g_launches += 4 * per_graph + 1;
+    }
+  }
+  if (done < pairs) {
+    for (int64_t p = 0; done + p < pairs; ++p) {
+      rc = pair(p);
+      if (rc) return rc;
+    }
+    add_steps(2 * K * (pairs - done));
+  }
+  const int64_t rem = n_steps - 2 * K * pairs;  // one-step kernels, simulation by simulation
+  if (rem) {
+    for (etg_sim* s : b->sims) {
+      PhasePlan<T> ph, pe;
+      rc = sim_plans_export<T>(s, &ph, &pe);
+      if (rc) return rc;
+      const SimArgs<T> a = sim_args_export<T>(s);
+      for (int64_t k = 0; k < rem; ++k) launch_step_plain<T>(a, ph, pe, (int)k, b->stream);
+    }
+    add_steps(rem);
+  }
+  ETG_LAUNCH_CHECK();
+  return ETG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int etg_batch_create(etg_batch** out, int n_sims, etg_sim* const* sims) {
+  ETG_REQUIRE(out && sims && n_sims > 0, ETG_ERR_ARGUMENT, "etg_batch_create: bad arguments");
+  for (int k = 0; k < n_sims; ++k) {
+    ETG_REQUIRE(sims[k], ETG_ERR_ARGUMENT, "etg_batch_create: simulation %d is null", k);
+    ETG_REQUIRE(sims[k]->dtype == sims[0]->dtype, ETG_ERR_ARGUMENT, "etg_batch_create: mixed precisions");
+    ETG_REQUIRE(sims[k]->have_coeffs, ETG_ERR_STATE, "etg_batch_create: simulation %d has no coefficients", k);
+  }
+  etg_batch* b = new etg_batch;
+  b->sims.assign(sims, sims + n_sims);
+  b->dtype = sims[0]->dtype;
+  b->alt.assign(n_sims, nullptr);
+  b->alt_bytes.assign(n_sims, 0);
+  std::vector<int64_t*> steps(n_sims);
+  for (int k = 0; k < n_sims; ++k) steps[k] = sims[k]->d_step;
+  int rc = etg_malloc((void**)&b->d_steps, n_sims * sizeof(int64_t*));
+  if (rc == ETG_OK &&
+      (cudaMemcpy(b->d_steps, steps.data(), n_sims * sizeof(int64_t*), cudaMemcpyHostToDevice) != cudaSuccess ||
+       cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)) {
+    set_error("etg_batch_create: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = ETG_ERR_CUDA;
+  }
+  if (rc) {
+    etg_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return ETG_OK;
+}
+
+int etg_batch_destroy(etg_batch* b) {
+  if (!b) return ETG_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  drop_graphs(b);
+  for (void* p : b->alt) cudaFree(p);
+  cudaFree(b->d_sims);
+  cudaFree(b->d_tiles);
+  cudaFree(b->d_steps);
+  for (cudaEvent_t e : {b->fork, b->join, b->ev0, b->ev1, b->done})
+    if (e) cudaEventDestroy(e);
+  if (b->side) cudaStreamDestroy(b->side);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return ETG_OK;
+}
+
+int etg_batch_advance(etg_batch* b, int64_t n_steps) {
+  ETG_REQUIRE(b && n_steps >= 0, ETG_ERR_ARGUMENT, "etg_batch_advance: bad arguments");
+  if (fault_injected("etg_batch_advance")) return ETG_ERR_INJECTED;
+  if (n_steps == 0) return ETG_OK;
+  for (etg_sim* s : b->sims) {
+    int rc = sim_check_tables(s, n_steps);
+    if (rc) return rc;
+    ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));  // uploads on a simulation's own stream are done
+  }
+  const bool timing = b->opt[ETG_OPT_TIMING] != 0;
+  const int64_t launches0 = g_launches;
+  if (timing) ETG_TRY_CUDA(cudaEventRecord(b->ev0, b->stream));
+  int rc = b->dtype == ETG_F32 ? batch_advance<float>(b, n_steps) : batch_advance<double>(b, n_steps);
+  if (rc) return rc;
+  if (timing) {
+    ETG_TRY_CUDA(cudaEventRecord(b->ev1, b->stream));
+    ETG_TRY_CUDA(cudaEventSynchronize(b->ev1));
+    float ms = 0;
+    ETG_TRY_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    b->last_ms = ms;
+  }
+  b->last_launches = g_launches - launches0;
+  // later work on a simulation's own stream (reads, uploads, single runs) waits for the batch
+  ETG_TRY_CUDA(cudaEventRecord(b->done, b->stream));
+  for (etg_sim* s : b->sims) {
+    ETG_TRY_CUDA(cudaStreamWaitEvent(s->stream, b->done, 0));
+    s->h_step += n_steps;
+  }
+  return ETG_OK;
+}
+
+int etg_batch_synchronize(etg_batch* b) {
+  ETG_REQUIRE(b, ETG_ERR_ARGUMENT, "etg_batch_synchronize: null handle");
+  ETG_TRY_CUDA(cudaStreamSynchronize(b->stream));
+  for (etg_sim* s : b->sims) {
+    int rc = etg_sim_synchronize(s);
+    if (rc) return rc;
+  }
+  return ETG_OK;
+}
+
+int etg_batch_set_option(etg_batch* b, int option, int64_t value) {
+  ETG_REQUIRE(b && option >= 0 && option < 8 && value >= 0, ETG_ERR_ARGUMENT, "etg_batch_set_option: bad option");
+  b->opt[option] = value;
+  drop_graphs(b);
+  return ETG_OK;
+}
+
+int etg_batch_last_timing(etg_batch* b, double* ms, int64_t* launches) {
+  ETG_REQUIRE(b, ETG_ERR_ARGUMENT, "etg_batch_last_timing: null handle");
+  if (ms) *ms = b->last_ms;
+  if (launches) *launches = b->last_launches;
+  return ETG_OK;
+}
+
+}  // extern "C"

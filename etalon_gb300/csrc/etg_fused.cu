@@ -52,12 +52,7 @@ __device__ __forceinline__ void accumulate(const PhasePlan<T>& p, int comp, int 
     for (int u = 0; u < 4; ++u) {
       const unsigned dj = (unsigned)(j0 + u - d.jy0);
       if (dj >= (unsigned)d.nym) continue;
-      const int64_t k = (int64_t)di * d.nym + dj;
-      for (int f = 0; f < d.n_f; ++f) {
-        T* a = d.acc + 2 * (f * nodes + k);
-        a[0] = add(a[0], mul(val[u], ph[2 * f]));
-        a[1] = add(a[1], mul(val[u], ph[2 * f + 1]));
-      }
+      dft_node(d.acc, nodes, (int64_t)di * d.nym + dj, ph, d.n_f, val[u]);
     }
   }
 }

@@ -199,7 +199,7 @@ int advance_plain(etg_sim* s, int64_t n_steps) {
 template <typename T>
 int advance_dispatch(etg_sim* s, int64_t n_steps) {
   const int64_t kernel = s->opt[ETG_OPT_KERNEL];
-  if (kernel == 2 || (kernel == 0 && tb_supported<T>(s->nx, s->ny))) {
+  if (kernel == 2 || kernel == 3 || (kernel == 0 && tb_supported<T>(s->nx, s->ny))) {
     PhasePlan<T> ph, pe;
     int rc = build_plans<T>(s, &ph, &pe);
     if (rc) return rc;
@@ -259,6 +259,23 @@ void sim_invalidate(etg_sim* s) {
   invalidate_graphs(s);
   if (s->tb) tb_invalidate(s->tb);
 }
+
+template <typename T>
+SimArgs<T> sim_args_export(etg_sim* s) {
+  return sim_args<T>(s);
+}
+
+template <typename T>
+int sim_plans_export(etg_sim* s, PhasePlan<T>* ph, PhasePlan<T>* pe) {
+  return build_plans<T>(s, ph, pe);
+}
+
+int sim_check_tables(etg_sim* s, int64_t n_steps) { return check_tables(s, n_steps); }
+
+template SimArgs<float> sim_args_export<float>(etg_sim*);
+template SimArgs<double> sim_args_export<double>(etg_sim*);
+template int sim_plans_export<float>(etg_sim*, PhasePlan<float>*, PhasePlan<float>*);
+template int sim_plans_export<double>(etg_sim*, PhasePlan<double>*, PhasePlan<double>*);
 
 }  // namespace etg
 
@@ -643,9 +660,15 @@ int etg_sim_get_option(etg_sim* s, int option, int64_t* value) {
   *value = s->opt[option];
   if (*value == 0 && (option == ETG_OPT_TB_DEPTH || option == ETG_OPT_TILE_ROWS || option == ETG_OPT_TILE_COLS)) {
     int er, ec, k;  // the default tile shape of this dtype
-    tb_default_shape(s->dtype, &er, &ec, &k);
+    tb_default_shape(s->dtype, &er, &ec, &k, (int)s->opt[ETG_OPT_KERNEL]);
     *value = option == ETG_OPT_TB_DEPTH ? k : option == ETG_OPT_TILE_ROWS ? er : ec;
   }
+  return ETG_OK;
+}
+
+int etg_sim_kernel_timing(etg_sim* s, double* ms, int64_t* launches, int64_t* cells) {
+  ETG_REQUIRE(s && ms && launches && cells, ETG_ERR_ARGUMENT, "etg_sim_kernel_timing: bad arguments");
+  tb_kernel_timing(s->tb, ms, launches, cells);
   return ETG_OK;
 }
 

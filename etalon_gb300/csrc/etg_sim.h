@@ -70,6 +70,34 @@ constexpr int ERRBIT_TABLE = 1;      // a source or phasor table did not cover a
 constexpr int ERRBIT_NONFINITE = 2;  // NaN/Inf seen by the finiteness check
 constexpr int ERRBIT_TIMEOUT = 4;    // a bounded wait gave up
 
+// acc[f, k] += v * ph[f] for f = 0 .. n_f-1 of one node: the adds of each accumulator keep
+// their order, but the loads of eight frequencies are issued before any store, so a node's
+// update costs a few memory round trips instead of one per frequency.
+template <typename T>
+__device__ __noinline__ void dft_node(T* __restrict__ acc, int64_t nodes, int64_t k,
+                                         const T* __restrict__ ph, int n_f, T v) {
+  for (int f0 = 0; f0 < n_f; f0 += 8) {
+    const int m = n_f - f0 < 8 ? n_f - f0 : 8;
+    T re[8], im[8], pr[8], pi[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (q < m) {
+        const T* a = acc + 2 * ((f0 + q) * nodes + k);
+        re[q] = a[0];
+        im[q] = a[1];
+        pr[q] = __ldg(ph + 2 * (f0 + q));
+        pi[q] = __ldg(ph + 2 * (f0 + q) + 1);
+      }
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (q < m) {
+        T* a = acc + 2 * ((f0 + q) * nodes + k);
+        a[0] = add(re[q], mul(v, pr[q]));
+        a[1] = add(im[q], mul(v, pi[q]));
+      }
+  }
+}
+
 // Launchers implemented per kernel family; stream-ordered, no synchronisation.
 template <typename T>
 void launch_step_plain(const SimArgs<T>& a, const PhasePlan<T>& ph, const PhasePlan<T>& pe,
@@ -147,4 +175,9 @@ namespace etg {
 // Internal entry points of etg_sim.cu used by the adjoint (etg_adjoint.cu).
 int sim_advance_internal(etg_sim* s, int64_t n_steps);  // advance without timing or fault injection
 void sim_invalidate(etg_sim* s);                        // drop graphs after a change of plans
+template <typename T>
+SimArgs<T> sim_args_export(etg_sim* s);                 // kernel arguments of the simulation
+template <typename T>
+int sim_plans_export(etg_sim* s, PhasePlan<T>* ph, PhasePlan<T>* pe);  // its source/monitor plans
+int sim_check_tables(etg_sim* s, int64_t n_steps);      // tables cover the next n_steps steps
 }  // namespace etg

@@ -28,16 +28,14 @@
 #include <cstring>
 #include <vector>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "etg_tb.h"
 
 namespace etg {
 
 constexpr int TB_THREADS = 256;
-
-template <typename T>
-struct TBDst {
-  T *ex, *ey, *hz, *psi_ex_y, *psi_ey_x, *psi_hz_x, *psi_hz_y;
-};
 
 template <typename T>
 struct TBVec;  // W elements per lane, one 16-byte access
@@ -100,12 +98,7 @@ __device__ __forceinline__ void tb_dft(const MonDesc<T>& d, const TBVec<T> (&val
       if (e < e_lo || e >= e_hi) continue;
       const unsigned dj = (unsigned)(j0 + e - d.jy0);
       if (dj >= (unsigned)d.nym) continue;
-      const int64_t k = (int64_t)di * d.nym + dj;
-      for (int f = 0; f < d.n_f; ++f) {
-        T* acc = d.acc + 2 * (f * nodes + k);
-        acc[0] = add(acc[0], mul(val[t].v[e], phr[2 * f]));
-        acc[1] = add(acc[1], mul(val[t].v[e], phr[2 * f + 1]));
-      }
+      dft_node(d.acc, nodes, (int64_t)di * d.nym + dj, phr, d.n_f, val[t].v[e]);
     }
   }
 }
@@ -137,10 +130,10 @@ __device__ __forceinline__ void tb_inject(const PhasePlan<T>& p, uint32_t rel, T
   }
 }
 
+// One CTA, one tile: load the extended tile, advance it K steps, write the output tile.
 template <typename T, int RPT, int K, bool PML>
-__global__ void __launch_bounds__(TB_THREADS, TBShape<T, RPT, K, PML>::MIN_BLOCKS)
-k_tb_step(SimArgs<T> a, TBDst<T> dst, const int2* __restrict__ tiles, PhasePlan<T> ph,
-          PhasePlan<T> pe, int step_off) {
+__device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst, const int2 tile,
+                                        const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off) {
   using S = TBShape<T, RPT, K, PML>;
   using Vw = TBVec<T>;
   constexpr int W = S::W, ER = S::ER, EC = S::EC, PL = S::PL;
@@ -153,7 +146,6 @@ k_tb_step(SimArgs<T> a, TBDst<T> dst, const int2* __restrict__ tiles, PhasePlan<
   __shared__ uint32_t s_rel[4];  // relevant plan entries: H sources, E sources, H monitors, E monitors
 
   const int lane = threadIdx.x, ty = threadIdx.y;
-  const int2 tile = tiles[blockIdx.x];
   const int R0 = tile.x - K, C0 = tile.y - K;  // global cell of local (0, 0); C0 % W == 0
   const int nx = a.nx, ny = a.ny;
   const int64_t P = a.P;
@@ -414,16 +406,403 @@ k_tb_step(SimArgs<T> a, TBDst<T> dst, const int2* __restrict__ tiles, PhasePlan<
   }
 }
 
+template <typename T, int RPT, int K, bool PML>
+__global__ void __launch_bounds__(TB_THREADS, TBShape<T, RPT, K, PML>::MIN_BLOCKS)
+k_tb_step(const __grid_constant__ SimArgs<T> a, const __grid_constant__ TBDst<T> dst,
+          const int2* __restrict__ tiles, const __grid_constant__ PhasePlan<T> ph,
+          const __grid_constant__ PhasePlan<T> pe, int step_off) {
+  tb_tile<T, RPT, K, PML>(a, dst, tiles[blockIdx.x], ph, pe, step_off);
+}
+
+// Batched form: every tile names its simulation; all simulations advance the same K steps.
+template <typename T, int RPT, int K, bool PML>
+__global__ void __launch_bounds__(TB_THREADS, TBShape<T, RPT, K, PML>::MIN_BLOCKS)
+k_tb_batch(const BatchSim<T>* __restrict__ sims, const int4* __restrict__ tiles, int parity, int step_off) {
+  const int4 t = tiles[blockIdx.x];  // simulation, r0, c0
+  const BatchSim<T>& b = sims[t.x];
+  tb_tile<T, RPT, K, PML>(b.src[parity], b.dst[parity], make_int2(t.y, t.z), b.ph, b.pe, step_off);
+}
+
+// ------------------------------------------------------------------------ persistent TMA variant
+//
+// Two CTAs per SM walk the tile list (interior tiles first, then CPML tiles) with stride
+// gridDim.x. Ex, Ey, Hz, cb_ex and cb_ey of an extended tile arrive by TMA
+// (cp.async.bulk.tensor.2d, zero fill outside the arrays) into the CTA's stage, completion
+// tracked by an mbarrier. The threads copy their cells (fields and cb) to registers at once,
+// so the stage is free again: the next tile's TMA runs while this tile takes its K steps,
+// and the two CTAs of an SM hide each other's barriers. A CPML tile instead fills the stage
+// with its four psi planes and its CPML profiles and fetches the next tile after it.
+// The arithmetic, injection, DFT and trace are those of k_tb_step.
+
+struct TMAMaps {
+  CUtensorMap ex, ey, hz, cbx, cby;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void tma_load_tile(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_addr(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Wait for the stage with an iteration limit; on time-out flag the error, wait once more
+// (bounded) for the copy still in flight, and report failure so the CTA can return.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* flag) {
+  for (uint32_t it = 0; it < (1u << 20); ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (it > 32) __nanosleep(128);
+  }
+  atomicOr(flag, ERRBIT_TIMEOUT);
+  for (uint32_t it = 0; it < (1u << 20); ++it) {
+    if (mbar_try_wait(bar, parity)) break;
+    __nanosleep(128);
+  }
+  return false;
+}
+
+template <typename T, int RPT, int K>
+struct TMAShape {
+  static constexpr int W = TBVec<T>::W;
+  static constexpr int ER = 8 * RPT, EC = 32 * W, OR = ER - 2 * K, OC = EC - 2 * K;
+  static constexpr int PL = ER * EC;
+  static constexpr int STAGE = 5 * PL;       // Ex, Ey, Hz, cb_ex, cb_ey; a CPML tile's psi after the copy
+  static constexpr int PROF = 6 * (ER + EC);  // CPML profiles of a tile: 6 per row, 6 per column
+  static constexpr int XCH = 9 * EC;
+  static constexpr uint32_t TX_BYTES = (uint32_t)(5 * PL * sizeof(T));
+  static constexpr size_t SMEM = (size_t)(STAGE + PROF + 2 * XCH) * sizeof(T) + sizeof(uint64_t) + 128;
+  static_assert(K % W == 0 && OR > 0 && OC > 0, "tile shape");
+  static_assert((PL * sizeof(T)) % 128 == 0, "stage planes stay 128-byte aligned");
+};
+
+template <typename T, int RPT, int K>
+__global__ void __launch_bounds__(TB_THREADS, 2)
+k_tb_tma(const __grid_constant__ TMAMaps maps, const __grid_constant__ SimArgs<T> a,
+         const __grid_constant__ TBDst<T> dst, const int2* __restrict__ tiles, int n_inner, int n_tiles,
+         const __grid_constant__ PhasePlan<T> ph, const __grid_constant__ PhasePlan<T> pe, int step_off) {
+  using S = TMAShape<T, RPT, K>;
+  using Vw = TBVec<T>;
+  constexpr int W = S::W, ER = S::ER, EC = S::EC, PL = S::PL;
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  // TMA destination on a 128-byte boundary whatever the base of dynamic shared memory
+  T* const stage = reinterpret_cast<T*>(tma_smem + ((128u - (smem_addr(tma_smem) & 127u)) & 127u));
+  T* const prof = stage + S::STAGE;  // bxh cxh kxh bxe cxe kxe [ER each], byh cyh kyh bye cye kye [EC each]
+  T* const sHzX = prof + S::PROF;
+  T* const sEyX = sHzX + S::XCH;
+  uint64_t* const mbar = reinterpret_cast<uint64_t*>(sEyX + S::XCH);
+  __shared__ uint32_t s_rel[4];
+
+  const int lane = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + lane;
+  const int nx = a.nx, ny = a.ny;
+  const int64_t P = a.P;
+  const int lj0 = W * lane, lr0 = RPT * ty;
+  if ((int)blockIdx.x >= n_tiles) return;
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (ty == 0) {
+    Vw z;
+    z.zero();
+    z.st(sHzX + lj0);  // the row above every tile
+  }
+  if (ty == 7) {
+    Vw z;
+    z.zero();
+    z.st(sEyX + 8 * EC + lj0);  // the row below every tile
+  }
+  __syncthreads();
+  auto fetch = [&](int k) {  // one thread
+    const int2 t = tiles[k];
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(S::TX_BYTES)
+                 : "memory");
+    const int x = t.y - K, y = t.x - K;
+    tma_load_tile(stage + 0 * PL, &maps.ex, x, y, mbar);
+    tma_load_tile(stage + 1 * PL, &maps.ey, x, y, mbar);
+    tma_load_tile(stage + 2 * PL, &maps.hz, x, y, mbar);
+    tma_load_tile(stage + 3 * PL, &maps.cbx, x, y, mbar);
+    tma_load_tile(stage + 4 * PL, &maps.cby, x, y, mbar);
+  };
+  if (tid == 0) fetch(blockIdx.x);
+  uint32_t parity = 0;
+  const T db = a.db, idx = a.inv_dx, idy = a.inv_dy;
+  const int64_t n_base = *a.step + step_off;
+
+  for (int k = blockIdx.x; k < n_tiles; k += gridDim.x) {
+    const int2 tile = tiles[k];
+    const bool pml = k >= n_inner;
+    const int next = k + gridDim.x;
+    const int R0 = tile.x - K, C0 = tile.y - K, j0 = C0 + lj0, i0 = R0 + lr0;
+    const bool lane_in = j0 >= 0 && j0 + W <= P;
+    T* const sPsi = stage;  // CPML tiles: psi_hz_x, psi_hz_y, psi_ex_y, psi_ey_x after the copy
+    if (ty == 0) {
+      auto src_hits = [&](const PhasePlan<T>& p) {
+        bool hit = false;
+        if (lane < p.n_src) {
+          const SrcDesc<T>& d = p.src[lane];
+          hit = d.i >= R0 && d.i < R0 + ER && d.j >= C0 && d.j < C0 + EC;
+        }
+        return __ballot_sync(0xffffffffu, hit);
+      };
+      auto mon_hits = [&](const PhasePlan<T>& p) {
+        bool hit = false;
+        if (lane < p.n_mon) {
+          const MonDesc<T>& d = p.mon[lane];
+          hit = d.ix0 < tile.x + S::OR && d.ix0 + d.nxm > tile.x && d.jy0 < tile.y + S::OC && d.jy0 + d.nym > tile.y;
+        }
+        return __ballot_sync(0xffffffffu, hit);
+      };
+      const uint32_t r0 = src_hits(ph), r1 = src_hits(pe), r2 = mon_hits(ph), r3 = mon_hits(pe);
+      if (lane == 0) {
+        s_rel[0] = r0;
+        s_rel[1] = r1;
+        s_rel[2] = r2;
+        s_rel[3] = r3;
+      }
+    }
+    if (!mbar_wait_bounded(mbar, parity, a.flag)) return;
+    parity ^= 1;
+    Vw ex[RPT], ey[RPT], hz[RPT], cbx[RPT], cby[RPT];
+#pragma unroll
+    for (int t = 0; t < RPT; ++t) {
+      const int o = (lr0 + t) * EC + lj0;
+      ex[t].ld(stage + 0 * PL + o);
+      ey[t].ld(stage + 1 * PL + o);
+      hz[t].ld(stage + 2 * PL + o);
+      cbx[t].ld(stage + 3 * PL + o);
+      cby[t].ld(stage + 4 * PL + o);
+    }
+    ey[0].st(sEyX + ty * EC + lj0);
+    __syncthreads();  // the stage is copied out
+    if (!pml && next < n_tiles && tid == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      fetch(next);
+    }
+    if (pml) {  // psi planes into the stage, CPML profiles of the tile's rows and columns
+#pragma unroll
+      for (int t = 0; t < RPT; ++t) {
+        const int i = i0 + t;
+        const bool in = lane_in && (unsigned)i <= (unsigned)nx;
+        const int64_t g = (int64_t)i * P + j0;
+        const int o = (lr0 + t) * EC + lj0;
+        Vw p0, p1, p2, p3;
+        if (in) {
+          p0.ld(a.psi_hz_x + g);
+          p1.ld(a.psi_hz_y + g);
+          p2.ld(a.psi_ex_y + g);
+          p3.ld(a.psi_ey_x + g);
+        } else {
+          p0.zero();
+          p1.zero();
+          p2.zero();
+          p3.zero();
+        }
+        p0.st(sPsi + 0 * PL + o);
+        p1.st(sPsi + 1 * PL + o);
+        p2.st(sPsi + 2 * PL + o);
+        p3.st(sPsi + 3 * PL + o);
+      }
+      for (int r = tid; r < ER; r += TB_THREADS) {
+        const int i = R0 + r, ih = min(max(i, 0), nx - 1), ie = min(max(i, 0), nx);
+        prof[0 * ER + r] = a.bx_h[ih];
+        prof[1 * ER + r] = a.cx_h[ih];
+        prof[2 * ER + r] = a.ikx_h[ih];
+        prof[3 * ER + r] = a.bx_e[ie];
+        prof[4 * ER + r] = a.cx_e[ie];
+        prof[5 * ER + r] = a.ikx_e[ie];
+      }
+      for (int c = tid; c < EC; c += TB_THREADS) {
+        const int j = C0 + c, jh = min(max(j, 0), ny - 1), je = min(max(j, 0), ny);
+        T* py = prof + 6 * ER;
+        py[0 * EC + c] = a.by_h[jh];
+        py[1 * EC + c] = a.cy_h[jh];
+        py[2 * EC + c] = a.iky_h[jh];
+        py[3 * EC + c] = a.by_e[je];
+        py[4 * EC + c] = a.cy_e[je];
+        py[5 * EC + c] = a.iky_e[je];
+      }
+      __syncthreads();
+    }
+    const T* const px = prof;           // per tile row
+    const T* const pyc = prof + 6 * ER;  // per tile column
+    const uint32_t relSrcH = s_rel[0], relSrcE = s_rel[1], relMonH = s_rel[2], relMonE = s_rel[3];
+    const int t_lo = max(0, K - lr0), t_hi = min(RPT, ER - K - lr0);
+    const int e_lo = lj0 >= K ? 0 : W, e_hi = lj0 + W <= EC - K ? W : 0;
+    const bool traced = ph.trace.buf && ph.trace.ti0 < tile.x + S::OR && ph.trace.ti0 + ph.trace.tnx > tile.x &&
+                        ph.trace.tj0 < tile.y + S::OC && ph.trace.tj0 + ph.trace.tny > tile.y;
+
+    for (int s = 0; s < K; ++s) {
+      const int64_t n = n_base + s;
+      {  // H half step
+        Vw eyb;
+        eyb.ld(sEyX + (ty + 1) * EC + lj0);
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+          T exr = __shfl_down_sync(0xffffffffu, ex[t].v[0], 1);
+          if (lane == 31) exr = zero<T>();
+#pragma unroll
+          for (int e = 0; e < W; ++e) {
+            const T exn = e < W - 1 ? ex[t].v[e + 1] : exr;
+            const T eyn = t < RPT - 1 ? ey[t + 1].v[e] : eyb.v[e];
+            const T dex_dy = mul(sub(exn, ex[t].v[e]), idy);
+            const T dey_dx = mul(sub(eyn, ey[t].v[e]), idx);
+            if (!pml) {
+              hz[t].v[e] = add(hz[t].v[e], mul(db, sub(add(dex_dy, zero<T>()), add(dey_dx, zero<T>()))));
+            } else {
+              const int i = i0 + t, j = j0 + e, r = lr0 + t, c = lj0 + e;
+              if (i >= 0 && i < nx && j >= 0 && j < ny) {
+                T* pxp = sPsi + 0 * PL + r * EC + c;
+                T* pyp = sPsi + 1 * PL + r * EC + c;
+                const T py = add(mul(pyc[0 * EC + c], *pyp), mul(pyc[1 * EC + c], dex_dy));
+                const T pxv = add(mul(px[0 * ER + r], *pxp), mul(px[1 * ER + r], dey_dx));
+                if (j < a.ys_lo || j >= a.ys_hi) *pyp = py;
+                if (i < a.xs_lo || i >= a.xs_hi) *pxp = pxv;
+                hz[t].v[e] = add(hz[t].v[e], mul(db, sub(add(mul(dex_dy, pyc[2 * EC + c]), py),
+                                                         add(mul(dey_dx, px[2 * ER + r]), pxv))));
+              }
+            }
+          }
+        }
+      }
+      if (relSrcH) tb_inject<T, RPT, W>(ph, relSrcH, ex, ey, hz, i0, j0, n, a.flag);
+      if (relMonH) {
+        for (uint32_t m = relMonH; m; m &= m - 1) {
+          const MonDesc<T>& d = ph.mon[__ffs(m) - 1];
+          const int64_t r = n - d.n0;
+          if (r < 0 || r >= d.rows) atomicOr(a.flag, ERRBIT_TABLE);
+          else tb_dft<T, RPT, W>(d, hz, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
+        }
+      }
+      if (traced) {
+        const TraceDesc<T>& tr = ph.trace;
+        const int64_t r = n - tr.n0;
+        if (r < 0 || r >= tr.rows) {
+          atomicOr(a.flag, ERRBIT_TABLE);
+        } else {
+#pragma unroll
+          for (int t = 0; t < RPT; ++t) {
+            const unsigned di = (unsigned)(i0 + t - tr.ti0);
+            if (t < t_lo || t >= t_hi || di >= (unsigned)tr.tnx) continue;
+#pragma unroll
+            for (int e = 0; e < W; ++e) {
+              const unsigned dj = (unsigned)(j0 + e - tr.tj0);
+              if (e >= e_lo && e < e_hi && dj < (unsigned)tr.tny) tr.buf[(r * tr.tnx + di) * tr.tny + dj] = hz[t].v[e];
+            }
+          }
+        }
+      }
+      hz[RPT - 1].st(sHzX + (ty + 1) * EC + lj0);
+      __syncthreads();
+      {  // E half step
+        Vw hza;
+        hza.ld(sHzX + ty * EC + lj0);
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+          T hzl = __shfl_up_sync(0xffffffffu, hz[t].v[W - 1], 1);
+          if (lane == 0) hzl = zero<T>();
+#pragma unroll
+          for (int e = 0; e < W; ++e) {
+            const T hzp = e > 0 ? hz[t].v[e - 1] : hzl;
+            const T hzu = t > 0 ? hz[t - 1].v[e] : hza.v[e];
+            const T dy = mul(sub(hz[t].v[e], hzp), idy);
+            const T dx = mul(sub(hz[t].v[e], hzu), idx);
+            if (!pml) {
+              ex[t].v[e] = add(ex[t].v[e], mul(cbx[t].v[e], add(dy, zero<T>())));
+              ey[t].v[e] = sub(ey[t].v[e], mul(cby[t].v[e], add(dx, zero<T>())));
+            } else {
+              const int i = i0 + t, j = j0 + e, r = lr0 + t, c = lj0 + e;
+              if (i >= 0 && i < nx && j >= 1 && j <= ny - 1) {
+                T* pp = sPsi + 2 * PL + r * EC + c;
+                const T p = add(mul(pyc[3 * EC + c], *pp), mul(pyc[4 * EC + c], dy));
+                if (j < a.ys_lo || j >= a.ys_hi) *pp = p;
+                ex[t].v[e] = add(ex[t].v[e], mul(cbx[t].v[e], add(mul(dy, pyc[5 * EC + c]), p)));
+              }
+              if (i >= 1 && i <= nx - 1 && j >= 0 && j < ny) {
+                T* pp = sPsi + 3 * PL + r * EC + c;
+                const T p = add(mul(px[3 * ER + r], *pp), mul(px[4 * ER + r], dx));
+                if (i < a.xs_lo || i >= a.xs_hi) *pp = p;
+                ey[t].v[e] = sub(ey[t].v[e], mul(cby[t].v[e], add(mul(dx, px[5 * ER + r]), p)));
+              }
+            }
+          }
+        }
+      }
+      if (relSrcE) tb_inject<T, RPT, W>(pe, relSrcE, ex, ey, hz, i0, j0, n, a.flag);
+      if (relMonE) {
+        for (uint32_t m = relMonE; m; m &= m - 1) {
+          const MonDesc<T>& d = pe.mon[__ffs(m) - 1];
+          const int64_t r = n - d.n0;
+          if (r < 0 || r >= d.rows) atomicOr(a.flag, ERRBIT_TABLE);
+          else if (d.comp == ETG_EX) tb_dft<T, RPT, W>(d, ex, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
+          else tb_dft<T, RPT, W>(d, ey, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
+        }
+      }
+      ey[0].st(sEyX + ty * EC + lj0);
+      __syncthreads();
+    }
+
+    // write the output tile
+    if (e_lo == 0 && e_hi == W && lane_in) {
+#pragma unroll
+      for (int t = 0; t < RPT; ++t) {
+        const int i = i0 + t;
+        if (t < t_lo || t >= t_hi || (unsigned)i > (unsigned)nx) continue;
+        const int64_t g = (int64_t)i * P + j0;
+        ex[t].st(dst.ex + g);
+        ey[t].st(dst.ey + g);
+        hz[t].st(dst.hz + g);
+        if (pml) {
+          const int o = (lr0 + t) * EC + lj0;
+          Vw v;
+          v.ld(sPsi + 0 * PL + o);
+          v.st(dst.psi_hz_x + g);
+          v.ld(sPsi + 1 * PL + o);
+          v.st(dst.psi_hz_y + g);
+          v.ld(sPsi + 2 * PL + o);
+          v.st(dst.psi_ex_y + g);
+          v.ld(sPsi + 3 * PL + o);
+          v.st(dst.psi_ey_x + g);
+        }
+      }
+    }
+    if (pml) {
+      __syncthreads();  // every thread is done with the psi planes in the stage
+      if (next < n_tiles && tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        fetch(next);
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------------------ host side
 
 struct TBConfig {
   int dtype, RPT, K;  // tile rows 8 * RPT, columns 32 * W (128 for f32, 64 for f64), depth K
 };
 
-static constexpr TBConfig kDefault32 = {ETG_F32, 5, 4};
+static constexpr TBConfig kDefault32 = {ETG_F32, 6, 4};
 static constexpr TBConfig kDefault64 = {ETG_F64, 5, 2};
+static constexpr TBConfig kTmaDefault32 = {ETG_F32, 5, 4};
+static constexpr TBConfig kTmaDefault64 = {ETG_F64, 5, 2};
 
 struct TBState {
+  TMAMaps maps[2];          // TMA descriptors of (fields A, cb) and (fields B, cb)
+  bool maps_valid = false;
+  int sms = 0;              // SMs of the device: one persistent CTA each
+  int mode = -1;            // 0: interior + CPML kernels per launch, 1: persistent TMA kernel
   void* alt[7] = {};  // second buffer of each field / psi plane, same pitch
   size_t alt_bytes = 0;
   int2* tiles = nullptr;  // interior tiles first, then CPML tiles
@@ -434,6 +813,12 @@ struct TBState {
   std::map<int64_t, cudaGraphExec_t> graphs;
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+  // per-kernel timing (ETG_OPT_TIMING 2): launches serialised on the main stream, no graphs
+  bool profile = false;
+  cudaEvent_t pev[3] = {};
+  double prof_ms[2] = {};        // interior, CPML
+  int64_t prof_launches[2] = {};
+  int64_t owned_cells[2] = {};   // output cells of one launch of each kernel, inside the grid
 };
 
 TBState* tb_create() { return new TBState; }
@@ -448,6 +833,8 @@ void tb_destroy(TBState* tb) {
   tb_drop_graphs(tb);
   for (void* p : tb->alt) cudaFree(p);
   cudaFree(tb->tiles);
+  for (cudaEvent_t e : tb->pev)
+    if (e) cudaEventDestroy(e);
   if (tb->side) cudaStreamDestroy(tb->side);
   if (tb->fork) cudaEventDestroy(tb->fork);
   if (tb->join) cudaEventDestroy(tb->join);
@@ -483,6 +870,23 @@ static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<
                                   const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                   cudaStream_t s) {
   // interior tiles on the main stream, CPML tiles on a side branch (parallel graph nodes)
+  if (tb->profile) {  // one after the other on s, an event pair around each
+    cudaError_t e = cudaEventRecord(tb->pev[0], s);
+    if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false>(a, d, tb->tiles, tb->n_inner, ph, pe, step_off, s);
+    if (e == cudaSuccess) e = cudaEventRecord(tb->pev[1], s);
+    if (e == cudaSuccess)
+      e = tb_launch_one<T, RPT, K, true>(a, d, tb->tiles + tb->n_inner, tb->n_pml, ph, pe, step_off, s);
+    if (e == cudaSuccess) e = cudaEventRecord(tb->pev[2], s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(tb->pev[2]);
+    float m0 = 0, m1 = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&m0, tb->pev[0], tb->pev[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&m1, tb->pev[1], tb->pev[2]);
+    tb->prof_ms[0] += m0;
+    tb->prof_ms[1] += m1;
+    tb->prof_launches[0] += tb->n_inner > 0;
+    tb->prof_launches[1] += tb->n_pml > 0;
+    return e;
+  }
   cudaError_t e = cudaEventRecord(tb->fork, s);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(tb->side, tb->fork, 0);
   if (e == cudaSuccess)
@@ -538,37 +942,116 @@ struct TBFns {
   cudaError_t (*attrs)();
 };
 
+// cuTensorMapEncodeTiled, looked up through the runtime (no link against libcuda).
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode_tiled = nullptr;
+
+static int get_encoder() {
+  if (g_encode_tiled) return ETG_OK;
+  cudaDriverEntryPointQueryResult q;
+  void* fn = nullptr;
+  ETG_TRY_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+  ETG_REQUIRE(fn && q == cudaDriverEntryPointSuccess, ETG_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  g_encode_tiled = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  return ETG_OK;
+}
+
+// A 2D map over a pitched plane of nx + 2 rows, boxes of ER rows x EC columns, zeros outside.
+template <typename T>
+static int encode_plane(CUtensorMap* m, const void* base, int nx, int64_t P, int ER, int EC) {
+  const cuuint64_t dims[2] = {(cuuint64_t)P, (cuuint64_t)(nx + 2)};
+  const cuuint64_t strides[1] = {(cuuint64_t)(P * sizeof(T))};
+  const cuuint32_t box[2] = {(cuuint32_t)EC, (cuuint32_t)ER};
+  const cuuint32_t es[2] = {1, 1};
+  const CUresult r = g_encode_tiled(m, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                                    2, const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  ETG_REQUIRE(r == CUDA_SUCCESS, ETG_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return ETG_OK;
+}
+
+template <typename T, int RPT, int K>
+static cudaError_t tma_attrs() {
+  return cudaFuncSetAttribute(k_tb_tma<T, RPT, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)TMAShape<T, RPT, K>::SMEM);
+}
+
+// Two persistent launches A -> B -> A covering 2K steps from step_off.
+template <typename T, int RPT, int K>
+static cudaError_t tma_two(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& ph, const PhasePlan<T>& pe,
+                           int step_off, cudaStream_t s) {
+  using S = TMAShape<T, RPT, K>;
+  const SimArgs<T> b = swap_args(a, tb);
+  const int n = tb->n_inner + tb->n_pml, grid = std::min(n, 2 * tb->sms);
+  k_tb_tma<T, RPT, K><<<grid, dim3(32, 8), S::SMEM, s>>>(tb->maps[0], a, as_dst(b), tb->tiles, tb->n_inner, n, ph, pe, step_off);
+  k_tb_tma<T, RPT, K><<<grid, dim3(32, 8), S::SMEM, s>>>(tb->maps[1], b, as_dst(a), tb->tiles, tb->n_inner, n, ph, pe,
+                                                         step_off + K);
+  g_launches += 2;
+  return cudaGetLastError();
+}
+
 // Compiled shapes (rows = 8 * RPT, depth K); the CPML variant's six planes must fit 227 KB.
 #define ETG_TB_SHAPES_F32(X) X(ETG_F32, 4, 4) X(ETG_F32, 5, 4) X(ETG_F32, 6, 4) X(ETG_F32, 8, 4) X(ETG_F32, 8, 8)
 #define ETG_TB_SHAPES_F64(X) X(ETG_F64, 4, 2) X(ETG_F64, 5, 2) X(ETG_F64, 8, 2) X(ETG_F64, 8, 4)
 
+// Shapes of the persistent TMA kernel: two stages of five planes must fit 227 KB.
+#define ETG_TMA_SHAPES_F32(X) X(ETG_F32, 4, 4) X(ETG_F32, 5, 4)
+#define ETG_TMA_SHAPES_F64(X) X(ETG_F64, 4, 2) X(ETG_F64, 5, 2)
+
 template <typename T>
-static TBFns<T> pick(const TBConfig& c) {
+static TBFns<T> pick(const TBConfig& c, int mode) {
 #define ETG_TB_CASE(DT, R, KK) \
   if (c.dtype == DT && c.RPT == R && c.K == KK) return {&tb_two<T, R, KK>, &tb_attrs<T, R, KK>};
-  if constexpr (sizeof(T) == 4) {
-    ETG_TB_SHAPES_F32(ETG_TB_CASE)
+#define ETG_TMA_CASE(DT, R, KK) \
+  if (c.dtype == DT && c.RPT == R && c.K == KK) return {&tma_two<T, R, KK>, &tma_attrs<T, R, KK>};
+  if (mode == 1) {
+    if constexpr (sizeof(T) == 4) {
+      ETG_TMA_SHAPES_F32(ETG_TMA_CASE)
+    } else {
+      ETG_TMA_SHAPES_F64(ETG_TMA_CASE)
+    }
   } else {
-    ETG_TB_SHAPES_F64(ETG_TB_CASE)
+    if constexpr (sizeof(T) == 4) {
+      ETG_TB_SHAPES_F32(ETG_TB_CASE)
+    } else {
+      ETG_TB_SHAPES_F64(ETG_TB_CASE)
+    }
   }
 #undef ETG_TB_CASE
+#undef ETG_TMA_CASE
   return {nullptr, nullptr};
 }
 
-static std::string shapes_text(int dtype) {
+static std::string shapes_text(int dtype, int mode) {
   std::string out;
 #define ETG_TB_NAME(DT, R, KK) \
   if (DT == dtype) out += " " + std::to_string(8 * R) + "x" + std::to_string(DT == ETG_F32 ? 128 : 64) + "/K" + std::to_string(KK);
-  ETG_TB_SHAPES_F32(ETG_TB_NAME)
-  ETG_TB_SHAPES_F64(ETG_TB_NAME)
+  if (mode == 1) {
+    ETG_TMA_SHAPES_F32(ETG_TB_NAME)
+    ETG_TMA_SHAPES_F64(ETG_TB_NAME)
+  } else {
+    ETG_TB_SHAPES_F32(ETG_TB_NAME)
+    ETG_TB_SHAPES_F64(ETG_TB_NAME)
+  }
 #undef ETG_TB_NAME
   return out;
 }
 
 // Interior tiles need their whole extended region in the unit rectangle and off the outer
 // (PEC) edges.
+// Tiles that hold a source node or a monitor node do extra work every step; they go first in
+// their kind's list so that they start early instead of finishing last.
+struct Hot {
+  std::vector<int4> rects;  // x0, y0, x1, y1 (inclusive-exclusive) in cells
+  bool hits(int r0, int c0, int rows, int cols) const {
+    for (const int4& q : rects)
+      if (q.x < r0 + rows && q.z > r0 && q.y < c0 + cols && q.w > c0) return true;
+    return false;
+  }
+};
+
 static void split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_hi, int ER, int EC,
-                        int K, std::vector<int2>* tiles, int* n_inner) {
+                        int K, std::vector<int2>* tiles, int* n_inner, const Hot* hot = nullptr) {
   const int OR = ER - 2 * K, OC = EC - 2 * K;
   const int rlo = std::max(ux_lo, 1), rhi = std::min(ux_hi, nx), clo = std::max(uy_lo, 1), chi = std::min(uy_hi, ny);
   std::vector<int2> inner, pml;
@@ -577,29 +1060,55 @@ static void split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_
       const bool unit = r0 - K >= rlo && r0 + OR + K <= rhi && c0 - K >= clo && c0 + OC + K <= chi;
       (unit ? inner : pml).push_back(make_int2(r0, c0));
     }
+  if (hot) {
+    auto first = [&](std::vector<int2>& v) {
+      std::stable_partition(v.begin(), v.end(),
+                            [&](int2 t) { return hot->hits(t.x - K, t.y - K, ER, EC); });
+    };
+    first(inner);
+    first(pml);
+  }
   *n_inner = (int)inner.size();
   inner.insert(inner.end(), pml.begin(), pml.end());
   *tiles = inner;
 }
 
 template <typename T>
-static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt) {
+static Hot hot_of(const PhasePlan<T>& ph, const PhasePlan<T>& pe) {
+  Hot h;
+  for (const PhasePlan<T>* p : {&ph, &pe}) {
+    for (int k = 0; k < p->n_src; ++k) h.rects.push_back(make_int4(p->src[k].i, p->src[k].j, p->src[k].i + 1, p->src[k].j + 1));
+    for (int k = 0; k < p->n_mon; ++k) {
+      const MonDesc<T>& m = p->mon[k];
+      h.rects.push_back(make_int4(m.ix0, m.jy0, m.ix0 + m.nxm, m.jy0 + m.nym));
+    }
+  }
+  return h;
+}
+
+template <typename T>
+static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt, const Hot& hot) {
   const int dt = (int)sizeof(T);
   const int EC = 32 * TBVec<T>::W;
-  TBConfig want = dt == 4 ? kDefault32 : kDefault64;
+  const int mode = opt[ETG_OPT_KERNEL] == 3 ? 1 : 0;
+  TBConfig want = mode ? (dt == 4 ? kTmaDefault32 : kTmaDefault64) : (dt == 4 ? kDefault32 : kDefault64);
   if (opt[ETG_OPT_TB_DEPTH] > 0) want.K = (int)opt[ETG_OPT_TB_DEPTH];
   if (opt[ETG_OPT_TILE_ROWS] > 0) want.RPT = (int)(opt[ETG_OPT_TILE_ROWS] / 8);
   const bool cols_ok = opt[ETG_OPT_TILE_COLS] == 0 || opt[ETG_OPT_TILE_COLS] == EC;
-  if (!cols_ok || opt[ETG_OPT_TILE_ROWS] % 8 != 0 || !pick<T>(want).two) {
-    set_error("no compiled temporally blocked kernel with tile %lldx%lld and depth %d (have:%s)",
+  if (!cols_ok || opt[ETG_OPT_TILE_ROWS] % 8 != 0 || !pick<T>(want, mode).two) {
+    set_error("no compiled %s kernel with tile %lldx%lld and depth %d (have:%s)",
+              mode ? "persistent TMA" : "temporally blocked",
               (long long)(opt[ETG_OPT_TILE_ROWS] ? opt[ETG_OPT_TILE_ROWS] : 8 * want.RPT),
-              (long long)(opt[ETG_OPT_TILE_COLS] ? opt[ETG_OPT_TILE_COLS] : EC), want.K, shapes_text(dt).c_str());
+              (long long)(opt[ETG_OPT_TILE_COLS] ? opt[ETG_OPT_TILE_COLS] : EC), want.K,
+              shapes_text(dt, mode).c_str());
     return ETG_ERR_ARGUMENT;
   }
-  if (want.RPT != tb->cfg.RPT || want.K != tb->cfg.K || want.dtype != tb->cfg.dtype) {
+  if (want.RPT != tb->cfg.RPT || want.K != tb->cfg.K || want.dtype != tb->cfg.dtype || mode != tb->mode) {
     tb_invalidate(tb);
     tb->cfg = want;
-    ETG_TRY_CUDA(pick<T>(want).attrs());
+    tb->mode = mode;
+    tb->maps_valid = false;
+    ETG_TRY_CUDA(pick<T>(want, mode).attrs());
   }
   const size_t bytes = (size_t)(a.nx + 2) * a.P * sizeof(T);
   if (tb->alt_bytes != bytes) {
@@ -608,6 +1117,7 @@ static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt) {
       cudaFree(p);
       p = nullptr;
     }
+    tb->maps_valid = false;
     for (void*& p : tb->alt) {
       if (cudaMalloc(&p, bytes) != cudaSuccess || cudaMemset(p, 0, bytes) != cudaSuccess) {
         cudaGetLastError();
@@ -625,8 +1135,14 @@ static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt) {
   if (!tb->tiles_valid || tb->nx != a.nx || tb->ny != a.ny) {
     std::vector<int2> inner;
     split_tiles(a.nx, a.ny, a.ux_lo, a.ux_hi, a.uy_lo, a.uy_hi, 8 * tb->cfg.RPT, EC, tb->cfg.K, &inner,
-                &tb->n_inner);
+                &tb->n_inner, &hot);
     tb->n_pml = (int)inner.size() - tb->n_inner;
+    const int OR = 8 * tb->cfg.RPT - 2 * tb->cfg.K, OC = EC - 2 * tb->cfg.K;
+    tb->owned_cells[0] = tb->owned_cells[1] = 0;
+    for (int q = 0; q < (int)inner.size(); ++q) {
+      const int64_t r = std::max(0, std::min(OR, a.nx - inner[q].x)), c = std::max(0, std::min(OC, a.ny - inner[q].y));
+      tb->owned_cells[q < tb->n_inner ? 0 : 1] += r * c;
+    }
     cudaFree(tb->tiles);
     tb->tiles = nullptr;
     ETG_TRY_CUDA(cudaMalloc(&tb->tiles, inner.size() * sizeof(int2)));
@@ -636,20 +1152,48 @@ static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt) {
     tb->tiles_valid = true;
     tb_drop_graphs(tb);
   }
+  if (mode == 1 && !tb->maps_valid) {
+    ETG_REQUIRE(a.P >= EC && a.nx + 2 >= 8 * tb->cfg.RPT, ETG_ERR_ARGUMENT,
+                "the persistent TMA kernel needs a grid of at least %d x %d cells", 8 * tb->cfg.RPT, EC);
+    int rc = get_encoder();
+    if (rc) return rc;
+    int dev = 0;
+    ETG_TRY_CUDA(cudaGetDevice(&dev));
+    ETG_TRY_CUDA(cudaDeviceGetAttribute(&tb->sms, cudaDevAttrMultiProcessorCount, dev));
+    const int ER = 8 * tb->cfg.RPT;
+    const void* fa[3] = {a.ex, a.ey, a.hz};
+    const void* fb[3] = {tb->alt[ETG_EX], tb->alt[ETG_EY], tb->alt[ETG_HZ]};
+    for (int k = 0; k < 2; ++k) {
+      const void* const* f = k == 0 ? fa : fb;
+      TMAMaps& m = tb->maps[k];
+      if ((rc = encode_plane<T>(&m.ex, f[0], a.nx, a.P, ER, EC)) || (rc = encode_plane<T>(&m.ey, f[1], a.nx, a.P, ER, EC)) ||
+          (rc = encode_plane<T>(&m.hz, f[2], a.nx, a.P, ER, EC)) || (rc = encode_plane<T>(&m.cbx, a.cb_ex, a.nx, a.P, ER, EC)) ||
+          (rc = encode_plane<T>(&m.cby, a.cb_ey, a.nx, a.P, ER, EC)))
+        return rc;
+    }
+    tb->maps_valid = true;
+  }
   return ETG_OK;
 }
 
 template <typename T>
 int tb_advance(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& ph, const PhasePlan<T>& pe,
                int64_t n_steps, const int64_t* opt, cudaStream_t s) {
-  int rc = tb_prepare<T>(tb, a, opt);
+  int rc = tb_prepare<T>(tb, a, opt, hot_of(ph, pe));
   if (rc) return rc;
-  const auto two = pick<T>(tb->cfg).two;
+  tb->profile = opt[ETG_OPT_TIMING] == 2 && tb->mode == 0;
+  if (tb->profile) {
+    for (cudaEvent_t& e : tb->pev)
+      if (!e) ETG_TRY_CUDA(cudaEventCreate(&e));
+    tb->prof_ms[0] = tb->prof_ms[1] = 0;
+    tb->prof_launches[0] = tb->prof_launches[1] = 0;
+  }
+  const auto two = pick<T>(tb->cfg, tb->mode).two;
   const int K = tb->cfg.K;
   const int64_t pairs = n_steps / (2 * K);
   const int64_t per_graph = std::max<int64_t>(1, opt[ETG_OPT_GRAPH_STEPS] / (2 * K));
   int64_t done = 0;  // pairs launched
-  if (opt[ETG_OPT_GRAPH_STEPS] > 0 && pairs >= per_graph) {
+  if (opt[ETG_OPT_GRAPH_STEPS] > 0 && pairs >= per_graph && !tb->profile) {
     auto it = tb->graphs.find(per_graph);
     if (it == tb->graphs.end()) {
       cudaGraph_t graph;
@@ -683,6 +1227,14 @@ int tb_advance(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& ph, const P
   return ETG_OK;
 }
 
+void tb_kernel_timing(const TBState* tb, double* ms, int64_t* launches, int64_t* cells) {
+  for (int k = 0; k < 2; ++k) {
+    ms[k] = tb ? tb->prof_ms[k] : 0;
+    launches[k] = tb ? tb->prof_launches[k] : 0;
+    cells[k] = tb ? tb->owned_cells[k] : 0;
+  }
+}
+
 template bool tb_supported<float>(int, int);
 template bool tb_supported<double>(int, int);
 template int tb_advance<float>(TBState*, const SimArgs<float>&, const PhasePlan<float>&,
@@ -696,8 +1248,9 @@ template int tb_advance<double>(TBState*, const SimArgs<double>&, const PhasePla
 
 namespace etg {
 
-void tb_default_shape(int dtype, int* ER, int* EC, int* K) {
-  const TBConfig& c = dtype == ETG_F64 ? kDefault64 : kDefault32;
+void tb_default_shape(int dtype, int* ER, int* EC, int* K, int kernel) {
+  const TBConfig& c = kernel == 3 ? (dtype == ETG_F64 ? kTmaDefault64 : kTmaDefault32)
+                                  : (dtype == ETG_F64 ? kDefault64 : kDefault32);
   *ER = 8 * c.RPT;
   *EC = dtype == ETG_F64 ? 64 : 128;
   *K = c.K;
@@ -729,5 +1282,90 @@ template cudaError_t tb_default_launch<float>(const SimArgs<float>&, const SimAr
                                               int, int, int, cudaStream_t);
 template cudaError_t tb_default_launch<double>(const SimArgs<double>&, const SimArgs<double>&,
                                                const int2*, int, int, int, cudaStream_t);
+
+// ------------------------------------------------------------------------ batched launches
+
+template <typename T, int RPT, int K>
+static cudaError_t batch_pair(const void* sims, const int4* tiles, int n_inner, int n_pml, int parity,
+                              int step_off, cudaStream_t main, cudaStream_t side, cudaEvent_t fork,
+                              cudaEvent_t join) {
+  using SI = TBShape<T, RPT, K, false>;
+  using SP = TBShape<T, RPT, K, true>;
+  const BatchSim<T>* b = (const BatchSim<T>*)sims;
+  cudaError_t e = cudaEventRecord(fork, main);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork, 0);
+  if (e == cudaSuccess && n_pml) {
+    k_tb_batch<T, RPT, K, true><<<n_pml, dim3(32, 8), SP::SMEM, side>>>(b, tiles + n_inner, parity, step_off);
+    g_launches += 1;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && n_inner) {
+    k_tb_batch<T, RPT, K, false><<<n_inner, dim3(32, 8), SI::SMEM, main>>>(b, tiles, parity, step_off);
+    g_launches += 1;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(join, side);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(main, join, 0);
+  return e;
+}
+
+template <typename T, int RPT, int K>
+static cudaError_t batch_attrs() {
+  cudaError_t e = cudaFuncSetAttribute(k_tb_batch<T, RPT, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)TBShape<T, RPT, K, false>::SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_tb_batch<T, RPT, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TBShape<T, RPT, K, true>::SMEM);
+  return e;
+}
+
+template <typename T>
+int tb_batch_pair(int ER, int K, const void* sims, const int4* tiles, int n_inner, int n_pml, int parity,
+                  int step_off, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+#define ETG_BATCH_CASE(DT, R, KK) \
+  if ((int)sizeof(T) == DT && ER == 8 * R && K == KK) {                                                   \
+    ETG_TRY_CUDA((batch_pair<T, R, KK>(sims, tiles, n_inner, n_pml, parity, step_off, main, side, fork, join))); \
+    return ETG_OK;                                                                                         \
+  }
+  if constexpr (sizeof(T) == 4) {
+    ETG_TB_SHAPES_F32(ETG_BATCH_CASE)
+  } else {
+    ETG_TB_SHAPES_F64(ETG_BATCH_CASE)
+  }
+#undef ETG_BATCH_CASE
+  set_error("no compiled batched kernel with %d rows and depth %d", ER, K);
+  return ETG_ERR_ARGUMENT;
+}
+
+template <typename T>
+int tb_batch_attrs(int ER, int K) {
+#define ETG_BATCH_ATTR(DT, R, KK) \
+  if ((int)sizeof(T) == DT && ER == 8 * R && K == KK) {   \
+    ETG_TRY_CUDA((batch_attrs<T, R, KK>()));              \
+    return ETG_OK;                                        \
+  }
+  if constexpr (sizeof(T) == 4) {
+    ETG_TB_SHAPES_F32(ETG_BATCH_ATTR)
+  } else {
+    ETG_TB_SHAPES_F64(ETG_BATCH_ATTR)
+  }
+#undef ETG_BATCH_ATTR
+  set_error("no compiled batched kernel with %d rows and depth %d", ER, K);
+  return ETG_ERR_ARGUMENT;
+}
+
+void tb_split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_hi, int ER, int EC, int K,
+                    const std::vector<int4>& hot, std::vector<int2>* tiles, int* n_inner) {
+  Hot h;
+  h.rects = hot;
+  split_tiles(nx, ny, ux_lo, ux_hi, uy_lo, uy_hi, ER, EC, K, tiles, n_inner, &h);
+}
+
+template int tb_batch_pair<float>(int, int, const void*, const int4*, int, int, int, int, cudaStream_t, cudaStream_t,
+                                  cudaEvent_t, cudaEvent_t);
+template int tb_batch_pair<double>(int, int, const void*, const int4*, int, int, int, int, cudaStream_t, cudaStream_t,
+                                   cudaEvent_t, cudaEvent_t);
+template int tb_batch_attrs<float>(int, int);
+template int tb_batch_attrs<double>(int, int);
 
 }  // namespace etg

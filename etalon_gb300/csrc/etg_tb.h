@@ -9,8 +9,37 @@ namespace etg {
 
 struct TBState;
 
+// Destination planes of one temporally blocked launch.
+template <typename T>
+struct TBDst {
+  T *ex, *ey, *hz, *psi_ex_y, *psi_ey_x, *psi_hz_x, *psi_hz_y;
+};
+
+// One simulation of a batch: its arguments with the fields of either buffer as the source.
+template <typename T>
+struct BatchSim {
+  SimArgs<T> src[2];  // [0]: read A (the simulation's fields), [1]: read B (the second buffer)
+  TBDst<T> dst[2];    // [0]: write B, [1]: write A
+  PhasePlan<T> ph, pe;
+};
+
+// Batched launch pair (interior tiles on `main`, CPML tiles on `side`) of the compiled shape
+// with ER rows and depth K; `sims` is a device array of BatchSim<T>, `tiles` (sim, r0, c0, -)
+// with the interior tiles first.
+template <typename T>
+int tb_batch_pair(int ER, int K, const void* sims, const int4* tiles, int n_inner, int n_pml, int parity,
+                  int step_off, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
+template <typename T>
+int tb_batch_attrs(int ER, int K);
+// Output tiles of one grid, interior tiles first; tiles meeting a `hot` rectangle lead each kind.
+void tb_split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_hi, int ER, int EC, int K,
+                    const std::vector<int4>& hot, std::vector<int2>* tiles, int* n_inner);
+
 TBState* tb_create();
 void tb_destroy(TBState* tb);
+// Interior / CPML kernel time (ms), launches and output cells per launch of the last advance
+// run with ETG_OPT_TIMING 2 (zeros otherwise or before any temporally blocked advance).
+void tb_kernel_timing(const TBState* tb, double* ms, int64_t* launches, int64_t* cells);
 void tb_invalidate(TBState* tb);  // drop cached graphs and plans (pointers changed)
 
 // Whether the temporally blocked path handles a grid of this size.
@@ -27,7 +56,7 @@ int tb_advance(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& ph, const P
 namespace etg {
 
 // Default tile shape of the temporally blocked kernel for a dtype: rows, columns, depth K.
-void tb_default_shape(int dtype, int* ER, int* EC, int* K);
+void tb_default_shape(int dtype, int* ER, int* EC, int* K, int kernel = 0);  // kernel 3: the TMA kernel's
 
 // Tiles of the default shape over a grid: interior tiles first, then CPML tiles.
 void tb_tiles(int dtype, int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_hi,

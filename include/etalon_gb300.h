@@ -151,6 +151,26 @@ int etg_sim_get_option(etg_sim* sim, int option, int64_t* value);
 /* Device-side timing of the last etg_sim_advance (CUDA events on its stream):
  * total milliseconds and the number of kernel launches it made. */
 int etg_sim_last_timing(etg_sim* sim, double* ms, int64_t* launches);
+/* Per-kernel timing of the last advance run with ETG_OPT_TIMING = 2, which launches the
+ * interior-tile and CPML-tile kernels of the temporally blocked path one after the other on
+ * the simulation's stream, without graphs, with a CUDA-event pair around each launch.
+ * Arrays of 2 (interior, CPML): total ms, launches, output cells inside the grid per launch. */
+int etg_sim_kernel_timing(etg_sim* sim, double* ms, int64_t* launches, int64_t* cells);
+
+/* ---------------------------------------------------------------- batch
+ * No counterpart in Etalon (one FDTDSolver per simulation). Steps many resident simulations
+ * of any sizes together, one launch pair per K steps for all of them; each keeps its own
+ * tables, monitors and step index, and its result is bit-identical to its own run. The
+ * simulations must share a precision; the batch does not own them. */
+typedef struct etg_batch etg_batch;
+int etg_batch_create(etg_batch** out, int n_sims, etg_sim* const* sims);
+int etg_batch_destroy(etg_batch* batch);
+/* Advance every simulation n_steps steps (asynchronous; etg_batch_synchronize waits). */
+int etg_batch_advance(etg_batch* batch, int64_t n_steps);
+int etg_batch_synchronize(etg_batch* batch);
+/* ETG_OPT_TB_DEPTH, ETG_OPT_TILE_ROWS, ETG_OPT_GRAPH_STEPS, ETG_OPT_TIMING as for etg_sim. */
+int etg_batch_set_option(etg_batch* batch, int option, int64_t value);
+int etg_batch_last_timing(etg_batch* batch, double* ms, int64_t* launches);
 
 /* ---------------------------------------------------------------- adjoint
  * No counterpart in Etalon. Gradient of an objective J(DFT accumulators) with respect to
@@ -203,13 +223,15 @@ int etg_tb_advance_static(int dtype, int nx, int ny, int64_t pitch, void* ex, vo
                           const void* iky_h, double db, double inv_dx, double inv_dy,
                           int64_t n_steps);
 
-#define ETG_OPT_KERNEL 0        /* 0 = auto, 1 = one step per launch, 2 = temporal blocking */
+#define ETG_OPT_KERNEL 0        /* 0 = auto, 1 = one step per launch, 2 = temporal blocking,
+                                   3 = temporal blocking, persistent CTAs fed by TMA */
 #define ETG_OPT_TB_DEPTH 1      /* steps per launch of the temporally blocked kernel */
 #define ETG_OPT_GRAPH_STEPS 2   /* steps captured per CUDA graph (0 = no graphs) */
 #define ETG_OPT_TILE_ROWS 3     /* tile rows of the temporally blocked kernel */
 #define ETG_OPT_TILE_COLS 4     /* tile columns of the temporally blocked kernel */
 #define ETG_OPT_CHECK_FINITE 5  /* 1 = flag NaN/Inf after each advance */
-#define ETG_OPT_TIMING 6        /* 1 = record CUDA-event timing of each advance */
+#define ETG_OPT_TIMING 6        /* 1 = record CUDA-event timing of each advance,
+                                   2 = also time each temporally blocked kernel launch */
 
 #ifdef __cplusplus
 }

@@ -156,3 +156,79 @@ def dft_inputs(dtype, seed=2):
     phasors = np.exp(1j * rng.uniform(0, 2 * np.pi, 13)).astype(complex_dtype) * 1e-16
     acc = (rng.standard_normal((13, 301)) + 1j * rng.standard_normal((13, 301))) * 1e-15
     return field, index, phasors, acc.astype(complex_dtype)
+
+
+# ----------------------------------------------------------------- seeded synthetic devices
+
+EPS_OXIDE = 2.085
+EPS_SILICON = 12.11
+WIDTH = 0.5  # strip width (µm)
+DEVICE_KINDS = ("bend", "ring", "mmi")
+
+
+def _device_core(kind, X, Y, lx, ly, rng_params):
+    """Boolean silicon mask of a device at node coordinates X, Y (µm, region centred on 0)."""
+    w = WIDTH
+    if kind == "bend":
+        r = min(rng_params["radius"], 0.35 * min(lx, ly))
+        x0, y0 = -r / 2, -r / 2  # input strip along x at y0 up to x0, quarter circle, output along +y
+        rr = np.hypot(X - x0, Y - (y0 + r))
+        arc = (np.abs(rr - r) <= w / 2) & (X >= x0) & (Y <= y0 + r)
+        return arc | ((np.abs(Y - y0) <= w / 2) & (X <= x0)) | ((np.abs(X - (x0 + r)) <= w / 2) & (Y >= y0 + r))
+    if kind == "ring":
+        r = min(rng_params["radius"], 0.4 * min(lx, ly) - w)
+        g = rng_params["gap"]
+        yb = -(r + g + w) / 2  # bus strip along x; ring above it, separated by the gap
+        yc = yb + w + g + r
+        return (np.abs(Y - yb) <= w / 2) | (np.abs(np.hypot(X, Y - yc) - r) <= w / 2)
+    if kind == "mmi":
+        length = min(rng_params["length"], 0.7 * lx)
+        width = min(rng_params["width"], 0.7 * ly)
+        box = (np.abs(X) <= length / 2) & (np.abs(Y) <= width / 2)
+        inp = (np.abs(Y) <= w / 2) & (X < 0)
+        outs = (X > 0) & ((np.abs(Y - width / 4) <= w / 2) | (np.abs(Y + width / 4) <= w / 2))
+        return box | inp | outs
+    raise ValueError(kind)
+
+
+def synthetic_device(seed, precision="single", n_steps=5000, min_cells=256, max_cells=1536, dl=0.02,
+                     n_monitors=4, n_wavelengths=8):  # fmt: skip
+    """One seeded random device on oxide: a waveguide bend (radius 1-5 µm), a ring resonator
+    (radius 2-6 µm, gap 0.1-0.3 µm) or an MMI box (1-8 µm), ε ∈ {2.085, 12.11}.
+
+    Interior nx, ny drawn uniformly in [min_cells, max_cells] (non-square), 12-layer CPML, one
+    Gaussian Hz source in the input strip, ``n_monitors`` point monitors at ``n_wavelengths``
+    wavelengths in 1.5-1.6 µm. Geometry beyond the region continues into the CPML.
+    """
+    rng = np.random.default_rng(seed)
+    nx, ny = (int(v) for v in rng.integers(min_cells, max_cells + 1, 2))
+    lx, ly = nx * dl, ny * dl
+    kind = DEVICE_KINDS[int(rng.integers(0, 3))]
+    params = {"radius": float(rng.uniform(1.0, 5.0) if kind == "bend" else rng.uniform(2.0, 6.0)),
+              "gap": float(rng.uniform(0.1, 0.3)), "length": float(rng.uniform(1.0, 8.0)),
+              "width": float(rng.uniform(1.0, 3.0))}  # fmt: skip
+    grid = ph.yee_grid((lx, ly), dl, 12, 0.99, (0.0, 0.0, 0.0))
+    eps = {}
+    for c in ("Ex", "Ey"):
+        x, y = grid.coords(c)
+        X, Y = np.meshgrid(x, y, indexing="ij")
+        eps[c] = np.where(_device_core(kind, X, Y, lx, ly, params), EPS_SILICON, EPS_OXIDE)
+    if kind == "bend":
+        r = min(params["radius"], 0.35 * min(lx, ly))
+        y_in = -r / 2
+    elif kind == "ring":
+        r = min(params["radius"], 0.4 * min(lx, ly) - WIDTH)
+        y_in = -(r + params["gap"] + WIDTH) / 2
+    else:
+        y_in = 0.0
+    src = PointSource((-0.4 * lx, y_in, 0.0), "Hz", GaussianPulse(1.55, 0.5))
+    wl = list(np.linspace(1.5, 1.6, n_wavelengths))
+    pts = rng.uniform(-0.4, 0.4, (n_monitors, 2)) * np.array([lx, ly])
+    monitors = [DFTMonitor(f"m{k}", wl, center=(float(px), float(py), 0.0)) for k, (px, py) in enumerate(pts)]
+    return ph.te_problem(size=(lx, ly), dl=dl, sources=[src], monitors=monitors, background_eps=EPS_OXIDE,
+                         eps=eps, pml=PMLSpec(layers=12), n_steps=n_steps, precision=precision)  # fmt: skip
+
+
+def synthetic_batch(n=64, seed=2024, **kw):
+    """``n`` seeded synthetic devices (sizes 256²-1536² unless overridden)."""
+    return [synthetic_device(seed * 1000 + k, **kw) for k in range(n)]

@@ -1,0 +1,86 @@
+"""Batched stepping: every simulation of a batch ends bit-identical to its own run (needs a GPU)."""
+
+import numpy as np
+import pytest
+
+from etalon_gb300 import _lib
+from etalon_gb300.batch import Batch
+from etalon_gb300.engine import TEEngine
+from tests import cases
+from tests.golden_io import FIELDS, compare_outputs, count, load
+
+pytestmark = pytest.mark.gpu
+
+
+def _problems(precision):
+    return [cases.config1(precision, n_steps=600), cases.g4_full(precision, n_steps=600),
+            cases.config2(precision, n_steps=600, region=173), cases.small(precision, n_steps=600)]  # fmt: skip
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+@pytest.mark.parametrize("steps", [(600,), (1, 7, 8, 9, 63, 64, 65, 383)])
+def test_batch_equals_individual_runs(gpu, precision, steps):
+    problems = _problems(precision)
+    batch = Batch(problems)
+    for k in steps:
+        batch.advance(k)
+    batch.synchronize()
+    n = sum(steps)
+    for p, e in zip(problems, batch.engines):
+        ref = TEEngine(p, kernel="plain")
+        ref.advance(n)
+        for f in FIELDS:
+            np.testing.assert_array_equal(e.field(f), ref.field(f), err_msg=f)
+        for k in range(len(e.monitors)):
+            np.testing.assert_array_equal(e.dft(k), ref.dft(k))
+        assert e.n == n
+    batch.close()
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_batch_member_matches_reference_fixture(gpu, precision):
+    """The G4 member of a batch reproduces Etalon's own 600-step run bit for bit."""
+    from tests.test_gpu_parity import golden_coeffs
+
+    g = load("g4_full", precision)
+    problems = _problems(precision)
+    batch = Batch(problems)
+    e = batch.engines[1]
+    e.set_coefficients(golden_coeffs(g))
+    for k in range(count(g, "src")):
+        e.set_source_table(k, 0, g[f"src{k}_table"])
+    for k in range(count(g, "mon")):
+        e.set_phasor_table(k, 0, g[f"mon{k}_table"])
+    batch.advance(600)
+    batch.synchronize()
+    assert compare_outputs(g, {f: e.field(f) for f in FIELDS}, [e.dft(k) for k in range(len(e.monitors))]) == []
+    batch.close()
+
+
+def test_batch_fault_injection_is_reported(gpu, monkeypatch):
+    batch = Batch(_problems("single")[:2])
+    monkeypatch.setenv("ETG_FAULT", "etg_batch_advance")
+    with pytest.raises(_lib.EtgError, match="fault injected"):
+        batch.advance(8)
+    batch.close()
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_batch_of_synthetic_devices_vs_live_oracle(gpu, precision):
+    """Uneven seeded devices (bend / ring / MMI) stepped as one batch vs the NumPy oracle."""
+    from tests.test_gpu_parity import _oracle_for
+
+    n = 2 * 8 * 3 + 5  # graph-captured pairs plus a one-step remainder
+    problems = [cases.synthetic_device(s, precision, n_steps=n, min_cells=40, max_cells=300) for s in range(5)]
+    batch = Batch(problems)
+    batch.set_option(_lib.OPT_GRAPH_STEPS, 16)
+    batch.advance(n)
+    batch.synchronize()
+    for p, e in zip(problems, batch.engines):
+        o = _oracle_for(p)
+        o.run(n)
+        for f in FIELDS:
+            np.testing.assert_array_equal(e.field(f), getattr(o, f), err_msg=f)
+        for k, acc in enumerate(o.acc):
+            np.testing.assert_array_equal(e.dft(k), acc)
+    batch.close()

@@ -368,8 +368,8 @@ TB_SHAPES_F32 = [(32, 128, 4), (40, 128, 4), (48, 128, 4), (64, 128, 4), (64, 12
 TB_SHAPES_F64 = [(32, 64, 2), (40, 64, 2), (64, 64, 2), (64, 64, 4)]
 
 
-def _tb_engine(name, precision, g, shape, **kw):
-    e, n = engine_with_reference_inputs(name, precision, g, kernel="tb", **kw)
+def _tb_engine(name, precision, g, shape, kernel="tb", **kw):
+    e, n = engine_with_reference_inputs(name, precision, g, kernel=kernel, **kw)
     rows, cols, k = shape
     e.set_option(_lib.OPT_TILE_ROWS, rows)
     e.set_option(_lib.OPT_TILE_COLS, cols)
@@ -387,6 +387,38 @@ def test_tb_matches_reference(gpu, name, precision, shape):
     e.advance(n)
     e.synchronize()
     assert compare_outputs(g, *engine_outputs(e)) == []
+
+
+TMA_SHAPES = [("single", (32, 128, 4)), ("single", (40, 128, 4)), ("double", (32, 64, 2)), ("double", (40, 64, 2))]
+
+
+@pytest.mark.parametrize("name", ["config1", "g4_full"])
+@pytest.mark.parametrize(("precision", "shape"), TMA_SHAPES)
+def test_tma_matches_reference(gpu, name, precision, shape):
+    """The persistent TMA-fed kernel reproduces Etalon's run bit for bit."""
+    g = load(name, precision)
+    e, n = _tb_engine(name, precision, g, shape, kernel="tma")
+    e.advance(n)
+    e.synchronize()
+    assert compare_outputs(g, *engine_outputs(e)) == []
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_tma_seams_and_config2_prefix(gpu, precision):
+    """TMA kernel: uneven blocks, and the headline grid against the live oracle."""
+    n = 48
+    p = cases.config2(precision, n_steps=n)
+    e = TEEngine(p, kernel="tma", graph_steps=16)
+    for k in (1, 7, 8, 9, 23):
+        e.advance(k)
+    o = _oracle_for(p)
+    workers = min(16, os.cpu_count() or 1)
+    with ThreadPoolExecutor(workers) as pool:
+        o.run(n, pool=pool, bands=workers)
+    for f in FIELDS:
+        np.testing.assert_array_equal(e.field(f), getattr(o, f), err_msg=f)
+    for k, acc in enumerate(o.acc):
+        np.testing.assert_array_equal(e.dft(k), acc)
 
 
 @pytest.mark.parametrize("precision", PRECISIONS)

@@ -72,6 +72,13 @@ SIGNATURES: dict[str, list] = {
     "etg_adj_destroy": [vp],
     "etg_adj_forward": [vp, i64, i64],
     "etg_adj_backward": [vp, C.POINTER(vp), C.POINTER(C.c_double), C.POINTER(C.c_double)],
+    "etg_adj_set_objective": [vp, C.POINTER(vp)],
+    "etg_adj_gradient": [vp, C.POINTER(f64), C.POINTER(f64)],
+    "etg_adj_batch_create": [C.POINTER(vp), i32, C.POINTER(vp)],
+    "etg_adj_batch_destroy": [vp],
+    "etg_adj_batch_set_option": [vp, i32, i64],
+    "etg_adj_batch_forward": [vp, i64, i64],
+    "etg_adj_batch_backward": [vp],
     "etg_tb_advance_static": [i32, i32, i32, i64] + [vp] * 21 + [f64, f64, f64, i64],
 }
 

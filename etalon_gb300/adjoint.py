@@ -101,12 +101,27 @@ class AdjointRunner:
 
     def backward(self, grad_accs: list[np.ndarray | None]) -> tuple[np.ndarray, np.ndarray]:
         """dJ/dcb on the window's Ex and Ey nodes (float64) from dJ/dacc per monitor."""
-        keep = [None if g is None else np.ascontiguousarray(g, dtype=self.problem.complex) for g in grad_accs]
-        ptrs = (C.c_void_p * len(keep))(*[None if g is None else g.ctypes.data for g in keep])
-        d = self.design
-        gx = np.zeros((d.nx, d.ny + 1))
-        gy = np.zeros((d.nx + 1, d.ny))
+        keep, ptrs = self._objective_pointers(grad_accs)
+        gx, gy = self._gradient_buffers()
         call("etg_adj_backward", self._h, ptrs, gx.ctypes.data_as(C.POINTER(C.c_double)),
+             gy.ctypes.data_as(C.POINTER(C.c_double)))  # fmt: skip
+        return gx, gy
+
+    def _objective_pointers(self, grad_accs):
+        keep = [None if g is None else np.ascontiguousarray(g, dtype=self.problem.complex) for g in grad_accs]
+        return keep, (C.c_void_p * len(keep))(*[None if g is None else g.ctypes.data for g in keep])
+
+    def _gradient_buffers(self):
+        d = self.design
+        return np.zeros((d.nx, d.ny + 1)), np.zeros((d.nx + 1, d.ny))
+
+    def set_objective(self, grad_accs: list[np.ndarray | None]) -> None:
+        _, ptrs = self._objective_pointers(grad_accs)
+        call("etg_adj_set_objective", self._h, ptrs)
+
+    def gradient(self) -> tuple[np.ndarray, np.ndarray]:
+        gx, gy = self._gradient_buffers()
+        call("etg_adj_gradient", self._h, gx.ctypes.data_as(C.POINTER(C.c_double)),
              gy.ctypes.data_as(C.POINTER(C.c_double)))  # fmt: skip
         return gx, gy
 
@@ -121,6 +136,88 @@ class AdjointRunner:
             self.close()
         except Exception:
             pass
+
+
+class AdjointBatch:
+    """Forward and reverse passes of many designs at once (etg_adj_batch_*).
+
+    The runners (one precision, one step count and stride, any grid sizes) step together as
+    a batch in the forward pass and share each K-step launch of the reverse sweep; every
+    gradient is bit-identical to the runner's own ``backward``.
+    """
+
+    def __init__(self, runners: list[AdjointRunner]) -> None:
+        if len({(r.problem.n_steps, r.stride, r.problem.precision) for r in runners}) != 1:
+            raise ValueError("the designs of a batch need one step count, one stride and one precision")
+        self.runners = runners
+        handles = (C.c_void_p * len(runners))(*[r._h.value for r in runners])
+        h = C.c_void_p()
+        call("etg_adj_batch_create", C.byref(h), len(runners), handles)
+        self._h = h
+
+    def forward(self) -> list[list[np.ndarray]]:
+        """DFT accumulators of every monitor of every design."""
+        r0 = self.runners[0]
+        call("etg_adj_batch_forward", self._h, r0.problem.n_steps, r0.stride)
+        return [[r.engine.dft(k) for k in range(len(r.engine.monitors))] for r in self.runners]
+
+    def backward(self, grad_accs: list[list[np.ndarray | None]]) -> list[tuple[np.ndarray, np.ndarray]]:
+        """dJ/dcb of every design from its dJ/dacc per monitor."""
+        for r, g in zip(self.runners, grad_accs):
+            r.set_objective(g)
+        call("etg_adj_batch_backward", self._h)
+        return [r.gradient() for r in self.runners]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.lib().etg_adj_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _SimulateBatch(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, batch: AdjointBatch, *eps):
+        cbs = []
+        for r, k in zip(batch.runners, range(0, len(eps), 2)):
+            cbs.append(r.set_eps(eps[k].detach().cpu().numpy(), eps[k + 1].detach().cpu().numpy()))
+        accs = batch.forward()
+        ctx.batch, ctx.cbs = batch, cbs
+        ctx.save_for_backward(*eps)
+        ctx.counts = [len(a) for a in accs]
+        return tuple(torch.as_tensor(np.stack([a.real, a.imag], -1).astype(np.float64)) for per in accs for a in per)
+
+    @staticmethod
+    def backward(ctx, *grads):
+        eps = ctx.saved_tensors
+        per, k = [], 0
+        for c in ctx.counts:
+            per.append([None if t is None else (t[..., 0].numpy() + 1j * t[..., 1].numpy()) for t in grads[k:k + c]])
+            k += c
+        out = []
+        for (gx, gy), (cbx, cby), q in zip(ctx.batch.backward(per), ctx.cbs, range(0, len(eps), 2)):
+            out.append(torch.as_tensor(gx * (-cbx / eps[q].detach().numpy())))
+            out.append(torch.as_tensor(gy * (-cby / eps[q + 1].detach().numpy())))
+        return (None, *out)
+
+
+def simulate_batch(eps_cells: list[torch.Tensor], batch: AdjointBatch) -> list[tuple[torch.Tensor, ...]]:
+    """``simulate`` for every design of a batch: per design, the accumulators of its monitors."""
+    node_eps = []
+    for e, r in zip(eps_cells, batch.runners):
+        node_eps.extend(r.design.node_eps(e, r.static))
+    flat = _SimulateBatch.apply(batch, *node_eps)
+    out, k = [], 0
+    for r in batch.runners:
+        c = len(r.engine.monitors)
+        out.append(tuple(flat[k:k + c]))
+        k += c
+    return out
 
 
 class _Simulate(torch.autograd.Function):

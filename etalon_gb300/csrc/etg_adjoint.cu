@@ -23,6 +23,8 @@
 #include <vector>
 
 #include "etg_sim.h"
+#include "etg_tb.h"
+#include "etg_tb_adj.h"
 
 namespace etg {
 
@@ -190,6 +192,19 @@ __global__ void k_adj_esrc(AdjArgs<T> a, AdjPlan<T> pe, int64_t n) {
   if (j < s.ny) a.ley[g] = a.ley[g] + adj_source(pe, ETG_EY, i, j, n);
 }
 
+// Per-node tables of the adjoint sources: tables[q * n_steps + n] = adj_source(plan, node q, n),
+// the exact sum the one-step kernels add at that node and step.
+template <typename T>
+__global__ void k_adj_tables(AdjPlan<T> plan, const int4* __restrict__ nodes, int n_nodes, int64_t n_steps,
+                             T* __restrict__ tables) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (int64_t)n_nodes * n_steps) return;
+  const int q = (int)(k / n_steps);
+  const int64_t n = k % n_steps;
+  const int4 d = nodes[q];  // i, j, comp
+  tables[k] = adj_source(plan, d.z, d.x, d.y, n);
+}
+
 }  // namespace etg
 
 using namespace etg;
@@ -206,6 +221,16 @@ struct etg_adj {
   void* lpsi[2][4] = {};    // double-buffered lambda psi
   double* grad = nullptr;   // gx then gy
   std::vector<void*> gacc;  // per monitor, device G
+  // temporally blocked sweep: second lambda buffer, tiles, adjoint-source tables
+  void* alt[7] = {};
+  int2* tiles = nullptr;
+  std::vector<int2> h_tiles;
+  int n_inner = 0, n_pml = 0;
+  void* tables = nullptr;
+  size_t tables_bytes = 0;
+  std::vector<int4> hnodes, enodes;  // i, j, comp
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 namespace {
@@ -294,12 +319,62 @@ int copy_state(etg_sim* s, void* const* to, void* const* from) {
   return ETG_OK;
 }
 
-// Reverse steps n_hi-1 … n_lo; the trace buffer holds steps from trace_n0.
+// Arguments of one temporally blocked launch; `to_alt` reads the primary lambda buffers
+// (lambda psi of the current parities) and writes the second buffer, else the reverse.
+template <typename T>
+TBAdjArgs<T> tb_adj_args(etg_adj* A, const SimArgs<T>& sa, int par_e, int par_h, int64_t trace_n0, bool to_alt) {
+  TBAdjArgs<T> a;
+  memset(&a, 0, sizeof a);
+  a.s = sa;
+  void* prim[7] = {A->lam[0], A->lam[1], A->lam[2], A->lpsi[par_h][0], A->lpsi[par_h][1], A->lpsi[par_e][2],
+                   A->lpsi[par_e][3]};
+  for (int k = 0; k < 7; ++k) {
+    a.in[k] = (const T*)(to_alt ? prim[k] : A->alt[k]);
+    a.out[k] = (T*)(to_alt ? A->alt[k] : prim[k]);
+  }
+  a.trace = (const T*)A->trace;
+  a.trace_n0 = trace_n0;
+  a.ti0 = A->ti0;
+  a.tnx = A->tnx;
+  a.tj0 = A->tj0;
+  a.tny = A->tny;
+  a.i0 = A->i0;
+  a.nxd = A->nxd;
+  a.j0 = A->j0;
+  a.nyd = A->nyd;
+  a.gx = A->grad;
+  a.gy = A->grad + (size_t)A->nxd * (A->nyd + 1);
+  const int64_t N = A->n_steps;
+  a.n_hsrc = (int)A->hnodes.size();
+  a.n_esrc = (int)A->enodes.size();
+  for (int q = 0; q < a.n_hsrc; ++q)
+    a.hsrc[q] = AdjSrc<T>{(const T*)A->tables + q * N, A->hnodes[q].x, A->hnodes[q].y, A->hnodes[q].z};
+  for (int q = 0; q < a.n_esrc; ++q)
+    a.esrc[q] = AdjSrc<T>{(const T*)A->tables + (a.n_hsrc + q) * N, A->enodes[q].x, A->enodes[q].y,
+                          A->enodes[q].z};
+  return a;
+}
+
+// Reverse steps n_hi-1 … n_lo; the trace buffer holds steps from trace_n0. Whole pairs of
+// K-step launches of the temporally blocked sweep first (when prepared), the rest one step
+// per launch pair; both give the same bits.
 template <typename T>
 int backward_sweep(etg_adj* A, int64_t n_hi, int64_t n_lo, int64_t trace_n0, int* par_e, int* par_h,
                    const AdjPlan<T>& ph, const AdjPlan<T>& pe) {
   etg_sim* s = A->sim;
   const SimArgs<T> sa = sim_args_of<T>(s);
+  if (A->tiles) {
+    int ER, EC, K;
+    tb_adj_shape(s->dtype, &ER, &EC, &K);
+    const TBAdjArgs<T> to_alt = tb_adj_args<T>(A, sa, *par_e, *par_h, trace_n0, true);
+    const TBAdjArgs<T> back = tb_adj_args<T>(A, sa, *par_e, *par_h, trace_n0, false);
+    for (; n_hi - n_lo >= 2 * K; n_hi -= 2 * K) {
+      int rc = tb_adj_launch<T>(to_alt, A->tiles, A->n_inner, A->n_pml, n_hi, s->stream, A->side, A->fork, A->join);
+      if (rc == ETG_OK)
+        rc = tb_adj_launch<T>(back, A->tiles, A->n_inner, A->n_pml, n_hi - K, s->stream, A->side, A->fork, A->join);
+      if (rc) return rc;
+    }
+  }
   const dim3 block(32, 4);
   const dim3 gre((s->ny + 31) / 32, (s->nx + 3) / 4), grh((s->ny + 1 + 31) / 32, (s->nx + 1 + 3) / 4);
   for (int64_t n = n_hi - 1; n >= n_lo; --n) {
@@ -343,9 +418,125 @@ int build_adj_plans(etg_adj* A, AdjPlan<T>* ph, AdjPlan<T>* pe) {
   return ETG_OK;
 }
 
+void drop_tb(etg_adj* A) {
+  for (void*& p : A->alt) {
+    cudaFree(p);
+    p = nullptr;
+  }
+  cudaFree(A->tiles);
+  A->tiles = nullptr;
+}
+
+// The temporally blocked sweep, unless the simulation is pinned to the one-step kernels or
+// the objective has more adjoint-source nodes than a launch carries: second lambda buffer,
+// tiles (adjoint-source nodes and the design window lead), per-node source tables.
 template <typename T>
-int adj_backward(etg_adj* A, const void* const* grad_acc, double* gx_host, double* gy_host) {
+int prepare_tb(etg_adj* A, const AdjPlan<T>& ph, const AdjPlan<T>& pe) {
   etg_sim* s = A->sim;
+  drop_tb(A);
+  A->hnodes.clear();
+  A->enodes.clear();
+  if (s->opt[ETG_OPT_KERNEL] == 1) return ETG_OK;
+  auto collect = [](const AdjPlan<T>& p, std::vector<int4>* out) {
+    for (int m = 0; m < p.n_mon; ++m) {
+      const AdjMon<T>& d = p.mon[m];
+      for (int a = 0; a < d.nxm; ++a)
+        for (int b = 0; b < d.nym; ++b) {
+          const int4 q = make_int4(d.ix0 + a, d.jy0 + b, d.comp, 0);
+          bool seen = false;
+          for (const int4& o : *out) seen |= o.x == q.x && o.y == q.y && o.z == q.z;
+          if (!seen) out->push_back(q);
+          if (out->size() > (size_t)MAX_SRC_NODES) return false;
+        }
+    }
+    return true;
+  };
+  if (!collect(ph, &A->hnodes) || !collect(pe, &A->enodes)) {
+    A->hnodes.clear();
+    A->enodes.clear();
+    return ETG_OK;  // too many source nodes: one-step sweep
+  }
+  int rc = tb_adj_attrs<T>();
+  if (rc) return rc;
+  const size_t pb = plane_bytes(s);
+  for (void*& p : A->alt) {
+    rc = etg_malloc(&p, pb);
+    if (rc) return rc;
+    ETG_TRY_CUDA(cudaMemsetAsync(p, 0, pb, s->stream));
+  }
+  int ER, EC, K;
+  tb_adj_shape(s->dtype, &ER, &EC, &K);
+  std::vector<int4> hot;
+  for (const int4& q : A->hnodes) hot.push_back(make_int4(q.x, q.y, q.x + 1, q.y + 1));
+  for (const int4& q : A->enodes) hot.push_back(make_int4(q.x, q.y, q.x + 1, q.y + 1));
+  hot.push_back(make_int4(A->i0, A->j0, A->i0 + A->nxd + 1, A->j0 + A->nyd + 1));
+  std::vector<int2> tiles;
+  tb_split_tiles(s->nx, s->ny, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi, ER, EC, K, hot, &tiles, &A->n_inner);
+  A->n_pml = (int)tiles.size() - A->n_inner;
+  A->h_tiles = tiles;
+  rc = etg_malloc((void**)&A->tiles, tiles.size() * sizeof(int2));
+  if (rc) return rc;
+  ETG_TRY_CUDA(cudaMemcpy(A->tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  // adjoint-source tables: H nodes from the H plan, E nodes from the E plan
+  const int64_t N = A->n_steps;
+  const size_t bytes = std::max<size_t>(1, (A->hnodes.size() + A->enodes.size()) * N * sizeof(T));
+  if (A->tables_bytes < bytes) {
+    cudaFree(A->tables);
+    A->tables = nullptr;
+    A->tables_bytes = 0;
+    rc = etg_malloc(&A->tables, bytes);
+    if (rc) return rc;
+    A->tables_bytes = bytes;
+  }
+  for (int which = 0; which < 2; ++which) {
+    const std::vector<int4>& nodes = which == 0 ? A->hnodes : A->enodes;
+    if (nodes.empty()) continue;
+    int4* d_nodes = nullptr;
+    rc = etg_malloc((void**)&d_nodes, nodes.size() * sizeof(int4));
+    if (rc) return rc;
+    ETG_TRY_CUDA(cudaMemcpy(d_nodes, nodes.data(), nodes.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    T* out = (T*)A->tables + (which == 0 ? 0 : A->hnodes.size() * N);
+    const int64_t total = (int64_t)nodes.size() * N;
+    k_adj_tables<T><<<(unsigned)((total + 255) / 256), 256, 0, s->stream>>>(which == 0 ? ph : pe, d_nodes,
+                                                                           (int)nodes.size(), N, out);
+    g_launches += 1;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    cudaFree(d_nodes);
+    ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "adjoint source tables: %s", cudaGetErrorString(e));
+  }
+  if (!A->side) {
+    ETG_TRY_CUDA(cudaStreamCreateWithFlags(&A->side, cudaStreamNonBlocking));
+    ETG_TRY_CUDA(cudaEventCreateWithFlags(&A->fork, cudaEventDisableTiming));
+    ETG_TRY_CUDA(cudaEventCreateWithFlags(&A->join, cudaEventDisableTiming));
+  }
+  return ETG_OK;
+}
+
+// dJ/dacc of every monitor (nullptr: not in the objective), kept on the device.
+int adj_set_objective(etg_adj* A, const void* const* grad_acc) {
+  etg_sim* s = A->sim;
+  for (void*& p : A->gacc) {
+    cudaFree(p);
+    p = nullptr;
+  }
+  A->gacc.assign(s->monitors.size(), nullptr);
+  for (size_t k = 0; k < s->monitors.size(); ++k) {
+    if (!grad_acc || !grad_acc[k]) continue;
+    const Monitor& m = s->monitors[k];
+    const size_t bytes = (size_t)2 * m.n_f * m.nxm * m.nym * s->esize();
+    int rc = etg_malloc(&A->gacc[k], bytes);
+    if (rc) return rc;
+    ETG_TRY_CUDA(cudaMemcpy(A->gacc[k], grad_acc[k], bytes, cudaMemcpyHostToDevice));
+  }
+  return ETG_OK;
+}
+
+// Zero lambda and dJ/dcb, build the adjoint plans, prepare the blocked sweep and add the
+// DFT-E source of the last step; lambda psi parities start at 0.
+template <typename T>
+int adj_begin(etg_adj* A, AdjPlan<T>* ph, AdjPlan<T>* pe) {
+  etg_sim* s = A->sim;
+  ETG_REQUIRE(A->n_steps > 0, ETG_ERR_STATE, "adjoint: run the forward pass first");
   const size_t pb = plane_bytes(s);
   for (int k = 0; k < 3; ++k) {
     int rc = ensure(&A->lam[k], pb);
@@ -362,59 +553,221 @@ int adj_backward(etg_adj* A, const void* const* grad_acc, double* gx_host, doubl
   int rc = ensure((void**)&A->grad, gbytes);
   if (rc) return rc;
   ETG_TRY_CUDA(cudaMemsetAsync(A->grad, 0, gbytes, s->stream));
-  A->gacc.assign(s->monitors.size(), nullptr);
-  for (size_t k = 0; k < s->monitors.size(); ++k) {
-    if (!grad_acc || !grad_acc[k]) continue;
-    const Monitor& m = s->monitors[k];
-    const size_t bytes = (size_t)2 * m.n_f * m.nxm * m.nym * s->esize();
-    rc = etg_malloc(&A->gacc[k], bytes);
-    if (rc) return rc;
-    ETG_TRY_CUDA(cudaMemcpy(A->gacc[k], grad_acc[k], bytes, cudaMemcpyHostToDevice));
-  }
+  if (A->gacc.size() != s->monitors.size()) A->gacc.assign(s->monitors.size(), nullptr);
+  rc = build_adj_plans<T>(A, ph, pe);
+  if (rc == ETG_OK) rc = prepare_tb<T>(A, *ph, *pe);
+  if (rc) return rc;
+  const SimArgs<T> sa = sim_args_of<T>(s);
+  AdjArgs<T> a0 = adj_args<T>(A, sa, 0, 0, 0);
+  const dim3 block(32, 4), grh((s->ny + 1 + 31) / 32, (s->nx + 1 + 3) / 4);
+  k_adj_esrc<T><<<grh, block, 0, s->stream>>>(a0, *pe, A->n_steps - 1);
+  g_launches += 1;
+  ETG_LAUNCH_CHECK();
+  return ETG_OK;
+}
+
+// Restore checkpoint k into the simulation and set it up to re-record the trace of [lo, hi).
+int adj_restore_segment(etg_adj* A, int64_t k, int64_t lo, int64_t hi) {
+  etg_sim* s = A->sim;
+  void* from[7];
+  for (int f = 0; f < 7; ++f) from[f] = (char*)A->ckpt[k] + f * plane_bytes(s);
+  int rc = copy_state(s, s->field, from);
+  if (rc) return rc;
+  ETG_TRY_CUDA(cudaMemcpyAsync(s->d_step, &lo, sizeof lo, cudaMemcpyHostToDevice, s->stream));
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  s->h_step = lo;
+  set_trace(s, A->trace, lo, hi - lo, A);
+  return ETG_OK;
+}
+
+template <typename T>
+int adj_backward(etg_adj* A) {
+  etg_sim* s = A->sim;
   AdjPlan<T> ph, pe;
-  rc = build_adj_plans<T>(A, &ph, &pe);
-  if (rc == ETG_OK) {
-    const SimArgs<T> sa = sim_args_of<T>(s);
-    int par_e = 0, par_h = 0;
-    AdjArgs<T> a0 = adj_args<T>(A, sa, par_e, par_h, 0);
-    const dim3 block(32, 4), grh((s->ny + 1 + 31) / 32, (s->nx + 1 + 3) / 4);
-    k_adj_esrc<T><<<grh, block, 0, s->stream>>>(a0, pe, A->n_steps - 1);
-    g_launches += 1;
-    if (A->stride == 0) {
-      rc = backward_sweep<T>(A, A->n_steps, 0, 0, &par_e, &par_h, ph, pe);
-    } else {
-      const int64_t S = A->stride;
-      const int64_t nseg = (A->n_steps + S - 1) / S;
-      s->monitors_on = false;
-      sim_invalidate(s);
-      for (int64_t k = nseg - 1; k >= 0 && rc == ETG_OK; --k) {
-        const int64_t lo = k * S, hi = std::min(A->n_steps, lo + S);
-        void* from[7];
-        for (int f = 0; f < 7; ++f) from[f] = (char*)A->ckpt[k] + f * plane_bytes(s);
-        rc = copy_state(s, s->field, from);
-        if (rc) break;
-        ETG_TRY_CUDA(cudaMemcpyAsync(s->d_step, &lo, sizeof lo, cudaMemcpyHostToDevice, s->stream));
-        ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
-        s->h_step = lo;
-        set_trace(s, A->trace, lo, hi - lo, A);
-        rc = sim_advance_internal(s, hi - lo);
-        clear_trace(s);
-        if (rc == ETG_OK) rc = backward_sweep<T>(A, hi, lo, lo, &par_e, &par_h, ph, pe);
-      }
-      s->monitors_on = true;
-      sim_invalidate(s);
+  int rc = adj_begin<T>(A, &ph, &pe);
+  if (rc) return rc;
+  int par_e = 0, par_h = 0;
+  if (A->stride == 0) {
+    rc = backward_sweep<T>(A, A->n_steps, 0, 0, &par_e, &par_h, ph, pe);
+  } else {
+    const int64_t S = A->stride;
+    const int64_t nseg = (A->n_steps + S - 1) / S;
+    s->monitors_on = false;
+    sim_invalidate(s);
+    for (int64_t k = nseg - 1; k >= 0 && rc == ETG_OK; --k) {
+      const int64_t lo = k * S, hi = std::min(A->n_steps, lo + S);
+      rc = adj_restore_segment(A, k, lo, hi);
+      if (rc == ETG_OK) rc = sim_advance_internal(s, hi - lo);
+      clear_trace(s);
+      if (rc == ETG_OK) rc = backward_sweep<T>(A, hi, lo, lo, &par_e, &par_h, ph, pe);
     }
+    s->monitors_on = true;
+    sim_invalidate(s);
   }
   ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
-  for (void*& p : A->gacc) {
-    cudaFree(p);
-    p = nullptr;
-  }
-  if (rc) return rc;
+  return rc;
+}
+
+int adj_download(etg_adj* A, double* gx_host, double* gy_host) {
+  ETG_REQUIRE(A->grad, ETG_ERR_STATE, "adjoint: no gradient yet, run the backward pass first");
   ETG_TRY_CUDA(cudaMemcpy(gx_host, A->grad, (size_t)A->nxd * (A->nyd + 1) * sizeof(double), cudaMemcpyDeviceToHost));
   ETG_TRY_CUDA(cudaMemcpy(gy_host, A->grad + (size_t)A->nxd * (A->nyd + 1),
                           (size_t)(A->nxd + 1) * A->nyd * sizeof(double), cudaMemcpyDeviceToHost));
   return ETG_OK;
+}
+
+// Forward pass recording what the gradient needs: the Hz trace of every step (stride 0) or
+// full-state checkpoints every `stride` steps. Resets the simulation first.
+int adj_forward_setup(etg_adj* A, int64_t n_steps, int64_t stride) {
+  etg_sim* s = A->sim;
+  int rc = etg_sim_reset(s);
+  if (rc) return rc;
+  A->n_steps = n_steps;
+  A->stride = stride;
+  const size_t cell_bytes = (size_t)A->tnx * A->tny * s->esize();
+  const int64_t rows = stride == 0 ? n_steps : std::min(stride, n_steps);
+  if (A->trace_cap < rows * cell_bytes) {
+    cudaFree(A->trace);
+    A->trace = nullptr;
+    A->trace_cap = 0;
+    rc = etg_malloc(&A->trace, rows * cell_bytes);
+    if (rc) return rc;
+    A->trace_cap = rows * cell_bytes;
+  }
+  if (stride > 0) {
+    const int64_t nseg = (n_steps + stride - 1) / stride;
+    if ((int64_t)A->ckpt.size() != nseg) {
+      for (void* p : A->ckpt) cudaFree(p);
+      A->ckpt.assign(nseg, nullptr);
+    }
+    for (void*& p : A->ckpt) {
+      if (p) continue;
+      rc = etg_malloc(&p, 7 * plane_bytes(s));
+      if (rc) return rc;
+    }
+  }
+  return ETG_OK;
+}
+
+int adj_save_checkpoint(etg_adj* A, int64_t k) {
+  etg_sim* s = A->sim;
+  void* to[7];
+  for (int f = 0; f < 7; ++f) to[f] = (char*)A->ckpt[k] + f * plane_bytes(s);
+  return copy_state(s, to, s->field);
+}
+
+// ------------------------------------------------------------------ many designs at once
+
+}  // namespace
+
+struct etg_adj_batch {
+  std::vector<etg_adj*> adjs;
+  int dtype = ETG_F32;
+  etg_batch* fwd = nullptr;  // the simulations stepped together
+  void* d_args = nullptr;    // TBAdjArgs<T>[2 n]: reading the primary / the second lambda buffer
+  int4* d_tiles = nullptr;
+  int n_inner = 0, n_pml = 0;
+  cudaStream_t stream = nullptr, side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  int64_t n_steps = 0, stride = 0;
+};
+
+namespace {
+
+// Batched reverse steps n_hi-1 … n_lo of every design: whole K-step launch pairs over the
+// tiles of all designs, then each design's remainder with the one-step kernels.
+template <typename T>
+int batch_sweep(etg_adj_batch* B, int64_t n_hi, int64_t n_lo, int64_t trace_n0, std::vector<int>& par_e,
+                std::vector<int>& par_h, const std::vector<AdjPlan<T>>& ph, const std::vector<AdjPlan<T>>& pe) {
+  const int n = (int)B->adjs.size();
+  int ER, EC, K;
+  tb_adj_shape(B->dtype, &ER, &EC, &K);
+  const int64_t pairs = B->d_tiles ? (n_hi - n_lo) / (2 * K) : 0;
+  if (pairs) {
+    std::vector<TBAdjArgs<T>> args(2 * n);
+    for (int k = 0; k < n; ++k) {
+      etg_adj* A = B->adjs[k];
+      const SimArgs<T> sa = sim_args_of<T>(A->sim);
+      args[2 * k] = tb_adj_args<T>(A, sa, par_e[k], par_h[k], trace_n0, true);
+      args[2 * k + 1] = tb_adj_args<T>(A, sa, par_e[k], par_h[k], trace_n0, false);
+      ETG_TRY_CUDA(cudaStreamSynchronize(A->sim->stream));
+    }
+    ETG_TRY_CUDA(cudaMemcpyAsync(B->d_args, args.data(), args.size() * sizeof(TBAdjArgs<T>), cudaMemcpyHostToDevice,
+                                 B->stream));
+    for (int64_t p = 0; p < pairs; ++p) {
+      const int64_t top = n_hi - 2 * K * p;
+      int rc = tb_adj_batch_launch<T>((const TBAdjArgs<T>*)B->d_args, B->d_tiles, B->n_inner, B->n_pml, 0, top,
+                                      B->stream, B->side, B->fork, B->join);
+      if (rc == ETG_OK)
+        rc = tb_adj_batch_launch<T>((const TBAdjArgs<T>*)B->d_args, B->d_tiles, B->n_inner, B->n_pml, 1, top - K,
+                                    B->stream, B->side, B->fork, B->join);
+      if (rc) return rc;
+    }
+    ETG_TRY_CUDA(cudaStreamSynchronize(B->stream));  // the host copy of args stays alive until here
+  }
+  const int64_t top = n_hi - 2 * K * pairs;
+  for (int k = 0; k < n && top > n_lo; ++k) {
+    int rc = backward_sweep<T>(B->adjs[k], top, n_lo, trace_n0, &par_e[k], &par_h[k], ph[k], pe[k]);
+    if (rc) return rc;
+  }
+  for (etg_adj* A : B->adjs) ETG_TRY_CUDA(cudaStreamSynchronize(A->sim->stream));
+  return ETG_OK;
+}
+
+template <typename T>
+int batch_backward(etg_adj_batch* B) {
+  const int n = (int)B->adjs.size();
+  std::vector<AdjPlan<T>> ph(n), pe(n);
+  bool blocked = true;
+  for (int k = 0; k < n; ++k) {
+    int rc = adj_begin<T>(B->adjs[k], &ph[k], &pe[k]);
+    if (rc) return rc;
+    blocked &= B->adjs[k]->tiles != nullptr;
+  }
+  // one tile list over all designs, interior tiles first
+  cudaFree(B->d_tiles);
+  B->d_tiles = nullptr;
+  if (blocked) {
+    std::vector<int4> inner, pml;
+    for (int k = 0; k < n; ++k) {
+      const etg_adj* A = B->adjs[k];
+      for (int q = 0; q < (int)A->h_tiles.size(); ++q)
+        (q < A->n_inner ? inner : pml).push_back(make_int4(k, A->h_tiles[q].x, A->h_tiles[q].y, 0));
+    }
+    B->n_inner = (int)inner.size();
+    B->n_pml = (int)pml.size();
+    inner.insert(inner.end(), pml.begin(), pml.end());
+    int rc = etg_malloc((void**)&B->d_tiles, inner.size() * sizeof(int4));
+    if (rc) return rc;
+    ETG_TRY_CUDA(cudaMemcpy(B->d_tiles, inner.data(), inner.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    if (!B->d_args) {
+      rc = etg_malloc(&B->d_args, 2 * n * sizeof(TBAdjArgs<T>));
+      if (rc) return rc;
+    }
+  }
+  std::vector<int> par_e(n, 0), par_h(n, 0);
+  if (B->stride == 0) return batch_sweep<T>(B, B->n_steps, 0, 0, par_e, par_h, ph, pe);
+  const int64_t S = B->stride;
+  const int64_t nseg = (B->n_steps + S - 1) / S;
+  for (etg_adj* A : B->adjs) {
+    A->sim->monitors_on = false;
+    sim_invalidate(A->sim);
+  }
+  int rc = ETG_OK;
+  for (int64_t k = nseg - 1; k >= 0 && rc == ETG_OK; --k) {
+    const int64_t lo = k * S, hi = std::min(B->n_steps, lo + S);
+    for (etg_adj* A : B->adjs)
+      if (rc == ETG_OK) rc = adj_restore_segment(A, k, lo, hi);
+    if (rc == ETG_OK) rc = etg_batch_advance(B->fwd, hi - lo);
+    if (rc == ETG_OK) rc = etg_batch_synchronize(B->fwd);
+    for (etg_adj* A : B->adjs) clear_trace(A->sim);
+    if (rc == ETG_OK) rc = batch_sweep<T>(B, hi, lo, lo, par_e, par_h, ph, pe);
+  }
+  for (etg_adj* A : B->adjs) {
+    A->sim->monitors_on = true;
+    sim_invalidate(A->sim);
+  }
+  return rc;
 }
 
 }  // namespace
@@ -461,6 +814,11 @@ int etg_adj_destroy(etg_adj* A) {
     for (void* p : b) cudaFree(p);
   cudaFree(A->grad);
   for (void* p : A->gacc) cudaFree(p);
+  drop_tb(A);
+  cudaFree(A->tables);
+  if (A->fork) cudaEventDestroy(A->fork);
+  if (A->join) cudaEventDestroy(A->join);
+  if (A->side) cudaStreamDestroy(A->side);
   delete A;
   return ETG_OK;
 }
@@ -468,51 +826,133 @@ int etg_adj_destroy(etg_adj* A) {
 int etg_adj_forward(etg_adj* A, int64_t n_steps, int64_t stride) {
   ETG_REQUIRE(A && n_steps > 0 && stride >= 0, ETG_ERR_ARGUMENT, "etg_adj_forward: bad arguments");
   etg_sim* s = A->sim;
-  int rc = etg_sim_reset(s);
+  int rc = adj_forward_setup(A, n_steps, stride);
   if (rc) return rc;
-  A->n_steps = n_steps;
-  A->stride = stride;
-  const size_t cell_bytes = (size_t)A->tnx * A->tny * s->esize();
-  const int64_t rows = stride == 0 ? n_steps : std::min(stride, n_steps);
-  if (A->trace_cap < rows * cell_bytes) {
-    cudaFree(A->trace);
-    A->trace = nullptr;
-    A->trace_cap = 0;
-    rc = etg_malloc(&A->trace, rows * cell_bytes);
-    if (rc) return rc;
-    A->trace_cap = rows * cell_bytes;
-  }
   if (stride == 0) {
     set_trace(s, A->trace, 0, n_steps, A);
     rc = sim_advance_internal(s, n_steps);
     clear_trace(s);
     if (rc) return rc;
   } else {
-    const int64_t nseg = (n_steps + stride - 1) / stride;
-    for (void* p : A->ckpt) cudaFree(p);
-    A->ckpt.assign(nseg, nullptr);
-    const size_t pb = plane_bytes(s);
-    for (int64_t k = 0; k < nseg; ++k) {
-      rc = etg_malloc(&A->ckpt[k], 7 * pb);
-      if (rc) return rc;
-      void* to[7];
-      for (int f = 0; f < 7; ++f) to[f] = (char*)A->ckpt[k] + f * pb;
-      rc = copy_state(s, to, s->field);
-      if (rc) return rc;
-      rc = sim_advance_internal(s, std::min(stride, n_steps - k * stride));
+    for (int64_t k = 0; k < (int64_t)A->ckpt.size(); ++k) {
+      rc = adj_save_checkpoint(A, k);
+      if (rc == ETG_OK) rc = sim_advance_internal(s, std::min(stride, n_steps - k * stride));
       if (rc) return rc;
     }
   }
   return etg_sim_synchronize(s);
 }
 
+int etg_adj_set_objective(etg_adj* A, const void* const* grad_acc) {
+  ETG_REQUIRE(A, ETG_ERR_ARGUMENT, "etg_adj_set_objective: null handle");
+  return adj_set_objective(A, grad_acc);
+}
+
+int etg_adj_gradient(etg_adj* A, double* grad_cb_ex, double* grad_cb_ey) {
+  ETG_REQUIRE(A && grad_cb_ex && grad_cb_ey, ETG_ERR_ARGUMENT, "etg_adj_gradient: null argument");
+  return adj_download(A, grad_cb_ex, grad_cb_ey);
+}
+
 int etg_adj_backward(etg_adj* A, const void* const* grad_acc, double* grad_cb_ex, double* grad_cb_ey) {
   ETG_REQUIRE(A && grad_cb_ex && grad_cb_ey, ETG_ERR_ARGUMENT, "etg_adj_backward: null argument");
   ETG_REQUIRE(A->n_steps > 0, ETG_ERR_STATE, "etg_adj_backward: run etg_adj_forward first");
-  int rc = A->sim->dtype == ETG_F32 ? adj_backward<float>(A, grad_acc, grad_cb_ex, grad_cb_ey)
-                                    : adj_backward<double>(A, grad_acc, grad_cb_ex, grad_cb_ey);
+  int rc = adj_set_objective(A, grad_acc);
   if (rc) return rc;
-  return etg_sim_synchronize(A->sim);
+  rc = A->sim->dtype == ETG_F32 ? adj_backward<float>(A) : adj_backward<double>(A);
+  if (rc) return rc;
+  rc = etg_sim_synchronize(A->sim);
+  if (rc) return rc;
+  return adj_download(A, grad_cb_ex, grad_cb_ey);
+}
+
+int etg_adj_batch_create(etg_adj_batch** out, int n, etg_adj* const* adjs) {
+  ETG_REQUIRE(out && adjs && n > 0, ETG_ERR_ARGUMENT, "etg_adj_batch_create: bad arguments");
+  std::vector<etg_sim*> sims(n);
+  for (int k = 0; k < n; ++k) {
+    ETG_REQUIRE(adjs[k], ETG_ERR_ARGUMENT, "etg_adj_batch_create: design %d is null", k);
+    ETG_REQUIRE(adjs[k]->sim->dtype == adjs[0]->sim->dtype, ETG_ERR_ARGUMENT, "etg_adj_batch_create: mixed precisions");
+    for (int q = 0; q < k; ++q)
+      ETG_REQUIRE(adjs[q]->sim != adjs[k]->sim, ETG_ERR_ARGUMENT, "etg_adj_batch_create: designs %d and %d share a simulation", q, k);
+    sims[k] = adjs[k]->sim;
+  }
+  etg_adj_batch* B = new etg_adj_batch;
+  B->adjs.assign(adjs, adjs + n);
+  B->dtype = adjs[0]->sim->dtype;
+  int rc = etg_batch_create(&B->fwd, n, sims.data());
+  if (rc == ETG_OK &&
+      (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaStreamCreateWithFlags(&B->side, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaEventCreateWithFlags(&B->fork, cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&B->join, cudaEventDisableTiming) != cudaSuccess)) {
+    set_error("etg_adj_batch_create: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = ETG_ERR_CUDA;
+  }
+  if (rc) {
+    etg_adj_batch_destroy(B);
+    return rc;
+  }
+  *out = B;
+  return ETG_OK;
+}
+
+int etg_adj_batch_destroy(etg_adj_batch* B) {
+  if (!B) return ETG_OK;
+  if (B->stream) cudaStreamSynchronize(B->stream);
+  etg_batch_destroy(B->fwd);
+  cudaFree(B->d_args);
+  cudaFree(B->d_tiles);
+  if (B->fork) cudaEventDestroy(B->fork);
+  if (B->join) cudaEventDestroy(B->join);
+  if (B->side) cudaStreamDestroy(B->side);
+  if (B->stream) cudaStreamDestroy(B->stream);
+  delete B;
+  return ETG_OK;
+}
+
+int etg_adj_batch_set_option(etg_adj_batch* B, int option, int64_t value) {
+  ETG_REQUIRE(B, ETG_ERR_ARGUMENT, "etg_adj_batch_set_option: null handle");
+  return etg_batch_set_option(B->fwd, option, value);
+}
+
+int etg_adj_batch_forward(etg_adj_batch* B, int64_t n_steps, int64_t stride) {
+  ETG_REQUIRE(B && n_steps > 0 && stride >= 0, ETG_ERR_ARGUMENT, "etg_adj_batch_forward: bad arguments");
+  for (etg_adj* A : B->adjs) {
+    int rc = adj_forward_setup(A, n_steps, stride);
+    if (rc) return rc;
+  }
+  B->n_steps = n_steps;
+  B->stride = stride;
+  int rc = ETG_OK;
+  if (stride == 0) {
+    for (etg_adj* A : B->adjs) set_trace(A->sim, A->trace, 0, n_steps, A);
+    rc = etg_batch_advance(B->fwd, n_steps);
+    if (rc == ETG_OK) rc = etg_batch_synchronize(B->fwd);
+    for (etg_adj* A : B->adjs) clear_trace(A->sim);
+    return rc;
+  }
+  const int64_t nseg = (n_steps + stride - 1) / stride;
+  for (int64_t k = 0; k < nseg && rc == ETG_OK; ++k) {
+    for (etg_adj* A : B->adjs)
+      if (rc == ETG_OK) rc = adj_save_checkpoint(A, k);
+    if (rc == ETG_OK) rc = etg_batch_advance(B->fwd, std::min(stride, n_steps - k * stride));
+  }
+  if (rc == ETG_OK) rc = etg_batch_synchronize(B->fwd);
+  return rc;
+}
+
+int etg_adj_batch_backward(etg_adj_batch* B) {
+  ETG_REQUIRE(B, ETG_ERR_ARGUMENT, "etg_adj_batch_backward: null handle");
+  ETG_REQUIRE(B->n_steps > 0, ETG_ERR_STATE, "etg_adj_batch_backward: run etg_adj_batch_forward first");
+  for (etg_adj* A : B->adjs)
+    ETG_REQUIRE(A->n_steps == B->n_steps && A->stride == B->stride, ETG_ERR_STATE,
+                "etg_adj_batch_backward: a design was run on its own since the batched forward pass");
+  int rc = B->dtype == ETG_F32 ? batch_backward<float>(B) : batch_backward<double>(B);
+  if (rc) return rc;
+  for (etg_adj* A : B->adjs) {
+    rc = etg_sim_synchronize(A->sim);
+    if (rc) return rc;
+  }
+  return ETG_OK;
 }
 
 }  // extern "C"

@@ -19,6 +19,7 @@ struct etg_batch {
   std::vector<size_t> alt_bytes;
   void* d_sims = nullptr;          // BatchSim<T>[n]
   std::vector<unsigned char> h_sims;
+  std::vector<int4> h_tiles;
   int4* d_tiles = nullptr;
   int n_inner = 0, n_pml = 0, tiles_er = 0, tiles_k = 0;
   int64_t** d_steps = nullptr;     // each simulation's step counter
@@ -42,9 +43,13 @@ void drop_graphs(etg_batch* b) {
   b->graphs.clear();
 }
 
+// Upload the per-simulation arguments when they changed (graphs read them from device
+// memory, so they stay valid) and the tile list when it changed (graphs are rebuilt then:
+// *changed).
 template <typename T>
 int refresh(etg_batch* b, int ER, int K, bool* changed) {
   const int n = (int)b->sims.size();
+  ETG_TRY_CUDA(cudaStreamSynchronize(b->stream));  // no launch still reads the arguments
   std::vector<unsigned char> host((size_t)n * sizeof(BatchSim<T>));
   for (int k = 0; k < n; ++k) {
     etg_sim* s = b->sims[k];
@@ -71,8 +76,8 @@ int refresh(etg_batch* b, int ER, int K, bool* changed) {
     if (rc) return rc;
     memcpy(host.data() + (size_t)k * sizeof e, &e, sizeof e);
   }
-  *changed = host != b->h_sims;
-  if (*changed) {
+  *changed = false;
+  if (host != b->h_sims) {
     if (!b->d_sims) {
       int rc = etg_malloc(&b->d_sims, host.size());
       if (rc) return rc;
@@ -80,7 +85,7 @@ int refresh(etg_batch* b, int ER, int K, bool* changed) {
     ETG_TRY_CUDA(cudaMemcpy(b->d_sims, host.data(), host.size(), cudaMemcpyHostToDevice));
     b->h_sims.swap(host);
   }
-  if (*changed || b->tiles_er != ER || b->tiles_k != K) {
+  {
     std::vector<int4> inner, pml;
     for (int k = 0; k < n; ++k) {
       etg_sim* s = b->sims[k];
@@ -97,17 +102,23 @@ int refresh(etg_batch* b, int ER, int K, bool* changed) {
       tb_split_tiles(s->nx, s->ny, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi, ER, 32 * (sizeof(T) == 4 ? 4 : 2), K, hot, &t, &ni);
       for (int q = 0; q < (int)t.size(); ++q) (q < ni ? inner : pml).push_back(make_int4(k, t[q].x, t[q].y, 0));
     }
-    b->n_inner = (int)inner.size();
-    b->n_pml = (int)pml.size();
+    const int n_inner = (int)inner.size(), n_pml = (int)pml.size();
     inner.insert(inner.end(), pml.begin(), pml.end());
-    cudaFree(b->d_tiles);
-    b->d_tiles = nullptr;
-    int rc = etg_malloc((void**)&b->d_tiles, std::max<size_t>(1, inner.size()) * sizeof(int4));
-    if (rc) return rc;
-    ETG_TRY_CUDA(cudaMemcpy(b->d_tiles, inner.data(), inner.size() * sizeof(int4), cudaMemcpyHostToDevice));
-    b->tiles_er = ER;
-    b->tiles_k = K;
-    *changed = true;
+    const bool same = b->d_tiles && n_inner == b->n_inner && n_pml == b->n_pml && inner.size() == b->h_tiles.size() &&
+                      memcmp(inner.data(), b->h_tiles.data(), inner.size() * sizeof(int4)) == 0;
+    if (!same) {
+      b->n_inner = n_inner;
+      b->n_pml = n_pml;
+      cudaFree(b->d_tiles);
+      b->d_tiles = nullptr;
+      int rc = etg_malloc((void**)&b->d_tiles, std::max<size_t>(1, inner.size()) * sizeof(int4));
+      if (rc) return rc;
+      ETG_TRY_CUDA(cudaMemcpy(b->d_tiles, inner.data(), inner.size() * sizeof(int4), cudaMemcpyHostToDevice));
+      b->h_tiles.swap(inner);
+      b->tiles_er = ER;
+      b->tiles_k = K;
+      *changed = true;
+    }
   }
   return ETG_OK;
 }

@@ -32,39 +32,9 @@
 #include <cudaTypedefs.h>
 
 #include "etg_tb.h"
+#include "etg_tb_dev.cuh"
 
 namespace etg {
-
-constexpr int TB_THREADS = 256;
-
-template <typename T>
-struct TBVec;  // W elements per lane, one 16-byte access
-template <>
-struct TBVec<float> {
-  static constexpr int W = 4;
-  float v[4];
-  __device__ __forceinline__ void ld(const float* p) {
-    const float4 a = *reinterpret_cast<const float4*>(p);
-    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-  }
-  __device__ __forceinline__ void st(float* p) const {
-    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
-  }
-  __device__ __forceinline__ void zero() { v[0] = v[1] = v[2] = v[3] = 0.f; }
-};
-template <>
-struct TBVec<double> {
-  static constexpr int W = 2;
-  double v[2];
-  __device__ __forceinline__ void ld(const double* p) {
-    const double2 a = *reinterpret_cast<const double2*>(p);
-    v[0] = a.x; v[1] = a.y;
-  }
-  __device__ __forceinline__ void st(double* p) const {
-    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
-  }
-  __device__ __forceinline__ void zero() { v[0] = v[1] = 0.0; }
-};
 
 template <typename T, int RPT, int K, bool PML>
 struct TBShape {
@@ -78,9 +48,6 @@ struct TBShape {
   static_assert(K % W == 0, "the halo must keep vectors aligned");
   static_assert(OR > 0 && OC > 0, "halo larger than the tile");
 };
-
-template <typename T>
-__device__ __forceinline__ T zero() { return T(0); }
 
 // acc[f, k] += value * phasor[n, f] for the owned output cells of this thread inside monitor d.
 template <typename T, int RPT, int W>

@@ -1,0 +1,525 @@
+// Temporally blocked reverse sweep of the discrete adjoint: K reverse steps per launch.
+//
+// The one-step adjoint kernels (k_adj_re / k_adj_rh) have the data flow of the forward
+// step mirrored: the lambda-Hz update RE(n) reads the E-node terms of its own node, of the
+// node to its right (j+1) and of the node below (i+1); the lambda-E update RH(n) reads the
+// H-cell terms of its own cell, of the cell to its left (j-1) and of the cell above (i-1).
+// That is the forward's neighbour pattern, so the forward's tiling carries over: a CTA loads
+// an output tile plus a K-cell halo, runs K reverse steps on chip with lambda Ex, Ey, Hz of
+// RPT x W cells per thread in registers, and writes the output tile to the other buffer.
+//
+// Each node's transposed term (gx of an Ex node, gy of an Ey node, hx/hy of an Hz cell) is
+// computed once per step by the thread that owns the node, which also advances the node's
+// lambda-psi; neighbours get it by shuffle (columns) or through shared memory (a warp's first
+// row of gy, last row of hy). The one-step kernels instead recompute a neighbour's term
+// from a second lambda-psi buffer; both evaluate the same expressions in the same order on the
+// same inputs, so the two sweeps give the same bits, and a sweep may mix them freely.
+//
+// dJ/dcb accumulates in float64 in the owning tile, one add per node and step in descending
+// step order, like the one-step kernel; interior tiles keep the running sums of their output
+// cells in shared memory for the launch (read once, written once), CPML tiles add in place. Adjoint sources (the transposed DFT
+// monitors) come as per-node tables and are added wherever a tile holds the node.
+#include <algorithm>
+#include <cstring>
+
+#include "etg_tb_adj.h"
+#include "etg_tb_dev.cuh"
+
+namespace etg {
+
+template <typename T, int RPT, int K, bool PML>
+struct AdjShape {
+  static constexpr int W = TBVec<T>::W;
+  static constexpr int ER = 8 * RPT, EC = 32 * W, OR = ER - 2 * K, OC = EC - 2 * K;
+  static constexpr int PL = ER * EC;
+  static constexpr int PLANES = PML ? 6 : 2;  // cb_ex, cb_ey (+ 4 lambda-psi)
+  static constexpr int XCH = 9 * EC;          // one exchange plane (gy or hy): 8 warps + a zero row
+  // interior tiles also hold the float64 dJ/dcb of their output cells while they run
+  static constexpr int GACC = PML ? 0 : 2 * OR * OC;
+  static constexpr size_t SMEM = ((size_t)PLANES * PL + 2 * XCH) * sizeof(T) + (size_t)GACC * sizeof(double);
+  static constexpr int MIN_BLOCKS = 1;
+  static_assert(K % W == 0, "the halo must keep vectors aligned");
+  static_assert(OR > 0 && OC > 0, "halo larger than the tile");
+};
+
+// lambda += table value of step r for the nodes of `rel` this thread holds.
+template <typename T, int RPT, int W>
+__device__ __forceinline__ void adj_inject(const AdjSrc<T>* src, uint32_t rel, TBVec<T> (&ex)[RPT],
+                                           TBVec<T> (&ey)[RPT], TBVec<T> (&hz)[RPT], int i0, int j0, int64_t r) {
+  for (uint32_t m = rel; m; m &= m - 1) {
+    const AdjSrc<T>& d = src[__ffs(m) - 1];
+    const int t_o = d.i - i0, e_o = d.j - j0;
+    if ((unsigned)t_o >= (unsigned)RPT || (unsigned)e_o >= (unsigned)W) continue;
+    const T v = d.table[r];
+#pragma unroll
+    for (int t = 0; t < RPT; ++t)
+#pragma unroll
+      for (int e = 0; e < W; ++e)
+        if (t == t_o && e == e_o) {
+          if (d.comp == ETG_HZ) hz[t].v[e] = add(hz[t].v[e], v);
+          else if (d.comp == ETG_EX) ex[t].v[e] = add(ex[t].v[e], v);
+          else ey[t].v[e] = add(ey[t].v[e], v);
+        }
+  }
+}
+
+template <typename T, int RPT, int K, bool PML>
+__device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 tile, int64_t n_hi) {
+  using S = AdjShape<T, RPT, K, PML>;
+  using Vw = TBVec<T>;
+  constexpr int W = S::W, ER = S::ER, EC = S::EC, PL = S::PL;
+  extern __shared__ __align__(16) unsigned char adj_smem[];
+  T* const sCbx = reinterpret_cast<T*>(adj_smem);
+  T* const sCby = sCbx + PL;
+  T* const sPsi = sCby + PL;              // CPML tiles: lambda psi_hz_x, psi_hz_y, psi_ex_y, psi_ey_x
+  T* const sGy = sCbx + S::PLANES * PL;   // [k]: gy of warp k's first row; [8] = zeros
+  T* const sHy = sGy + S::XCH;            // [k + 1]: hy of warp k's last row; [0] = zeros
+  // interior tiles: dJ/dcb_ex, dJ/dcb_ey of the output cells ((row - K) * OC + column - K)
+  double* const sGrad = reinterpret_cast<double*>(sHy + S::XCH);
+  __shared__ uint32_t s_rel[2];
+
+  const SimArgs<T>& s = a.s;
+  const int lane = threadIdx.x, ty = threadIdx.y;
+  const int R0 = tile.x - K, C0 = tile.y - K;
+  const int nx = s.nx, ny = s.ny;
+  const int64_t P = s.P;
+  const int lj0 = W * lane, j0 = C0 + lj0;
+  const int lr0 = RPT * ty, i0 = R0 + lr0;
+  const bool lane_in = j0 >= 0 && j0 + W <= P;
+
+  if (ty == 0) {
+    auto hits = [&](const AdjSrc<T>* src, int n) {
+      bool hit = false;
+      if (lane < n) hit = src[lane].i >= R0 && src[lane].i < R0 + ER && src[lane].j >= C0 && src[lane].j < C0 + EC;
+      return __ballot_sync(0xffffffffu, hit);
+    };
+    const uint32_t r0 = hits(a.hsrc, a.n_hsrc), r1 = hits(a.esrc, a.n_esrc);
+    if (lane == 0) {
+      s_rel[0] = r0;
+      s_rel[1] = r1;
+    }
+    Vw z;
+    z.zero();
+    z.st(sHy + lj0);
+  }
+  if (ty == 7) {
+    Vw z;
+    z.zero();
+    z.st(sGy + 8 * EC + lj0);
+  }
+
+  Vw lex[RPT], ley[RPT], lhz[RPT];
+#pragma unroll
+  for (int t = 0; t < RPT; ++t) {
+    const int i = i0 + t;
+    const bool in = lane_in && (unsigned)i <= (unsigned)nx;
+    const int64_t g = (int64_t)i * P + j0;
+    const int o = (lr0 + t) * EC + lj0;
+    Vw cx, cy;
+    if (in) {
+      lex[t].ld(a.in[0] + g);
+      ley[t].ld(a.in[1] + g);
+      lhz[t].ld(a.in[2] + g);
+      cx.ld(s.cb_ex + g);
+      cy.ld(s.cb_ey + g);
+    } else {
+      lex[t].zero();
+      ley[t].zero();
+      lhz[t].zero();
+      cx.zero();
+      cy.zero();
+    }
+    cx.st(sCbx + o);
+    cy.st(sCby + o);
+    if (PML) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        Vw p;
+        if (in) p.ld(a.in[3 + q] + g);
+        else p.zero();
+        p.st(sPsi + q * PL + o);
+      }
+    }
+  }
+  T byh[W], cyh[W], kyh[W], bye[W], cye[W], kye[W];
+  T bxh[RPT], cxh[RPT], kxh[RPT], bxe[RPT], cxe[RPT], kxe[RPT];
+  if (PML) {
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      const int j = min(max(j0 + e, 0), ny - 1), je = min(max(j0 + e, 0), ny);
+      byh[e] = s.by_h[j];
+      cyh[e] = s.cy_h[j];
+      kyh[e] = s.iky_h[j];
+      bye[e] = s.by_e[je];
+      cye[e] = s.cy_e[je];
+      kye[e] = s.iky_e[je];
+    }
+#pragma unroll
+    for (int t = 0; t < RPT; ++t) {
+      const int i = min(max(i0 + t, 0), nx - 1), ie = min(max(i0 + t, 0), nx);
+      bxh[t] = s.bx_h[i];
+      cxh[t] = s.cx_h[i];
+      kxh[t] = s.ikx_h[i];
+      bxe[t] = s.bx_e[ie];
+      cxe[t] = s.cx_e[ie];
+      kxe[t] = s.ikx_e[ie];
+    }
+  }
+  const T db = s.db, idx = s.inv_dx, idy = s.inv_dy;
+
+  // Transposed E update of the Ex node of cell (t, e): dJ/d(dHz/dy); advances lambda psi_ex_y.
+  auto gx_own = [&](int t, int e) -> T {
+    const T lc = mul(sCbx[(lr0 + t) * EC + lj0 + e], lex[t].v[e]);
+    if (!PML) return lc;  // 1/kappa = 1 exactly, no psi
+    const int i = i0 + t, j = j0 + e;
+    if (j < 1 || j > ny - 1 || i < 0 || i >= nx) return zero<T>();
+    if (j < s.ys_lo || j >= s.ys_hi) {
+      T* pp = sPsi + 2 * PL + (lr0 + t) * EC + lj0 + e;
+      const T lpt = add(*pp, lc);
+      *pp = mul(bye[e], lpt);
+      return add(mul(kye[e], lc), mul(cye[e], lpt));
+    }
+    return mul(kye[e], lc);
+  };
+  // Transposed E update of the Ey node: dJ/d(dHz/dx); advances lambda psi_ey_x.
+  auto gy_own = [&](int t, int e) -> T {
+    const T lc = -mul(sCby[(lr0 + t) * EC + lj0 + e], ley[t].v[e]);
+    if (!PML) return lc;
+    const int i = i0 + t, j = j0 + e;
+    if (i < 1 || i > nx - 1 || j < 0 || j >= ny) return zero<T>();
+    if (i < s.xs_lo || i >= s.xs_hi) {
+      T* pp = sPsi + 3 * PL + (lr0 + t) * EC + lj0 + e;
+      const T lpt = add(*pp, lc);
+      *pp = mul(bxe[t], lpt);
+      return add(mul(kxe[t], lc), mul(cxe[t], lpt));
+    }
+    return mul(kxe[t], lc);
+  };
+  // Transposed H update of the Hz cell: dJ/d(dEx/dy), dJ/d(dEy/dx); advances lambda psi_hz_*.
+  auto h_own = [&](int t, int e, T* hx, T* hy) {
+    const T la = mul(db, lhz[t].v[e]);
+    if (!PML) {
+      *hx = la;
+      *hy = -la;
+      return;
+    }
+    const int i = i0 + t, j = j0 + e;
+    if (i < 0 || i >= nx || j < 0 || j >= ny) {
+      *hx = *hy = zero<T>();
+      return;
+    }
+    if (j < s.ys_lo || j >= s.ys_hi) {
+      T* pp = sPsi + 1 * PL + (lr0 + t) * EC + lj0 + e;
+      const T lpt = add(*pp, la);
+      *pp = mul(byh[e], lpt);
+      *hx = add(mul(kyh[e], la), mul(cyh[e], lpt));
+    } else {
+      *hx = mul(kyh[e], la);
+    }
+    if (i < s.xs_lo || i >= s.xs_hi) {
+      T* pp = sPsi + 0 * PL + (lr0 + t) * EC + lj0 + e;
+      const T lpt = sub(*pp, la);
+      *pp = mul(bxh[t], lpt);
+      *hy = add(-mul(kxh[t], la), mul(cxh[t], lpt));
+    } else {
+      *hy = -mul(kxh[t], la);
+    }
+  };
+
+  __syncthreads();  // cb (and lambda psi) staged
+  T gyf[W];         // gy of this warp's first row for the next RE
+#pragma unroll
+  for (int e = 0; e < W; ++e) {
+    gyf[e] = gy_own(0, e);
+    sGy[ty * EC + lj0 + e] = gyf[e];
+  }
+  __syncthreads();
+
+  const uint32_t relH = s_rel[0], relE = s_rel[1];
+  const int t_lo = max(0, K - lr0), t_hi = min(RPT, ER - K - lr0);
+  const int e_lo = lj0 >= K ? 0 : W, e_hi = lj0 + W <= EC - K ? W : 0;
+  const bool designed = a.gx && a.i0 <= tile.x + S::OR - 1 && a.i0 + a.nxd >= tile.x &&
+                        a.j0 <= tile.y + S::OC - 1 && a.j0 + a.nyd >= tile.y;
+  // dJ/dcb slot of output cell (t, e) and component c: global (CPML tiles) or shared memory
+  auto in_gx = [&](int i, int j) { return i >= a.i0 && i < a.i0 + a.nxd && j >= a.j0 && j <= a.j0 + a.nyd; };
+  auto in_gy = [&](int i, int j) { return i >= a.i0 && i <= a.i0 + a.nxd && j >= a.j0 && j < a.j0 + a.nyd; };
+  auto gslot = [&](int t, int e, int c) -> double* {
+    const int i = i0 + t, j = j0 + e;
+    if (PML) return c == 0 ? a.gx + (int64_t)(i - a.i0) * (a.nyd + 1) + (j - a.j0)
+                           : a.gy + (int64_t)(i - a.i0) * a.nyd + (j - a.j0);
+    return sGrad + c * S::OR * S::OC + (lr0 + t - K) * S::OC + (lj0 + e - K);
+  };
+  if (!PML && designed) {  // the running sums of the owned window cells come in once per launch
+#pragma unroll
+    for (int t = 0; t < RPT; ++t) {
+      if (t < t_lo || t >= t_hi) continue;
+#pragma unroll
+      for (int e = 0; e < W; ++e) {
+        if (e < e_lo || e >= e_hi) continue;
+        const int i = i0 + t, j = j0 + e;
+        if (in_gx(i, j)) *gslot(t, e, 0) = a.gx[(int64_t)(i - a.i0) * (a.nyd + 1) + (j - a.j0)];
+        if (in_gy(i, j)) *gslot(t, e, 1) = a.gy[(int64_t)(i - a.i0) * a.nyd + (j - a.j0)];
+      }
+    }
+  }
+
+  for (int st = 0; st < K; ++st) {
+    const int64_t n = n_hi - 1 - st;
+    // ------------------------------------------------ gradient of step n (lambda E of n + 1)
+    if (designed) {
+      const T* tr = a.trace + (n - a.trace_n0) * a.tnx * a.tny;
+#pragma unroll
+      for (int t = 0; t < RPT; ++t) {
+        const int i = i0 + t;
+        if (t < t_lo || t >= t_hi) continue;
+#pragma unroll
+        for (int e = 0; e < W; ++e) {
+          const int j = j0 + e;
+          if (e < e_lo || e >= e_hi) continue;
+          const int ri = i - a.ti0, rj = j - a.tj0;
+          if (in_gx(i, j)) {
+            const T c = add(mul(sub(tr[ri * a.tny + rj], tr[ri * a.tny + rj - 1]), idy), zero<T>());
+            *gslot(t, e, 0) += (double)lex[t].v[e] * (double)c;
+          }
+          if (in_gy(i, j)) {
+            const T c = add(mul(sub(tr[ri * a.tny + rj], tr[(ri - 1) * a.tny + rj]), idx), zero<T>());
+            *gslot(t, e, 1) -= (double)ley[t].v[e] * (double)c;
+          }
+        }
+      }
+    }
+    // ------------------------------------------------ RE(n): lambda Hz
+    {
+      T gyc[W], gyn[W];
+#pragma unroll
+      for (int e = 0; e < W; ++e) gyc[e] = gyf[e];
+#pragma unroll
+      for (int t = 0; t < RPT; ++t) {
+        T gxr[W];
+#pragma unroll
+        for (int e = 0; e < W; ++e) gxr[e] = gx_own(t, e);
+        T gxn = __shfl_down_sync(0xffffffffu, gxr[0], 1);
+        if (lane == 31) gxn = zero<T>();
+        if (t < RPT - 1) {
+#pragma unroll
+          for (int e = 0; e < W; ++e) gyn[e] = gy_own(t + 1, e);
+        } else {
+#pragma unroll
+          for (int e = 0; e < W; ++e) gyn[e] = sGy[(ty + 1) * EC + lj0 + e];
+        }
+#pragma unroll
+        for (int e = 0; e < W; ++e) {
+          const T gx1 = e < W - 1 ? gxr[e + 1] : gxn;
+          const T u = add(add(add(lhz[t].v[e], mul(idy, sub(gxr[e], gx1))), mul(idx, sub(gyc[e], gyn[e]))),
+                          zero<T>());
+          if (!PML) {
+            lhz[t].v[e] = u;
+          } else {
+            const int i = i0 + t, j = j0 + e;
+            if (i >= 0 && i < nx && j >= 0 && j < ny) lhz[t].v[e] = u;
+          }
+          gyc[e] = gyn[e];
+        }
+      }
+    }
+    if (relH) adj_inject<T, RPT, W>(a.hsrc, relH, lex, ley, lhz, i0, j0, n);
+    T hxl[W], hyl[W];  // this warp's last row, computed once and shared
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      h_own(RPT - 1, e, &hxl[e], &hyl[e]);
+      sHy[(ty + 1) * EC + lj0 + e] = hyl[e];
+    }
+    __syncthreads();
+    // ------------------------------------------------ RH(n): lambda E (+ DFT-E term of n - 1)
+    {
+      T hyp[W];
+#pragma unroll
+      for (int e = 0; e < W; ++e) hyp[e] = sHy[ty * EC + lj0 + e];
+#pragma unroll
+      for (int t = 0; t < RPT; ++t) {
+        T hxc[W], hyc[W];
+        if (t < RPT - 1) {
+#pragma unroll
+          for (int e = 0; e < W; ++e) h_own(t, e, &hxc[e], &hyc[e]);
+        } else {
+#pragma unroll
+          for (int e = 0; e < W; ++e) {
+            hxc[e] = hxl[e];
+            hyc[e] = hyl[e];
+          }
+        }
+        T hxp = __shfl_up_sync(0xffffffffu, hxc[W - 1], 1);
+        if (lane == 0) hxp = zero<T>();
+#pragma unroll
+        for (int e = 0; e < W; ++e) {
+          const T hxleft = e > 0 ? hxc[e - 1] : hxp;
+          T vx = add(lex[t].v[e], mul(idy, sub(hxleft, hxc[e])));
+          T vy = add(ley[t].v[e], mul(idx, sub(hyp[e], hyc[e])));
+          if (n >= 1) {
+            vx = add(vx, zero<T>());
+            vy = add(vy, zero<T>());
+          }
+          if (!PML) {
+            lex[t].v[e] = vx;
+            ley[t].v[e] = vy;
+          } else {
+            const int i = i0 + t, j = j0 + e;
+            if (i >= 0 && i < nx && j >= 0 && j <= ny) lex[t].v[e] = vx;
+            if (i >= 0 && i <= nx && j >= 0 && j < ny) ley[t].v[e] = vy;
+          }
+          hyp[e] = hyc[e];
+        }
+      }
+    }
+    if (relE && n >= 1) adj_inject<T, RPT, W>(a.esrc, relE, lex, ley, lhz, i0, j0, n - 1);
+    if (st < K - 1) {
+#pragma unroll
+      for (int e = 0; e < W; ++e) {
+        gyf[e] = gy_own(0, e);
+        sGy[ty * EC + lj0 + e] = gyf[e];
+      }
+    }
+    __syncthreads();
+  }
+
+  if (!PML && designed) {  // running sums back, in the order they were taken
+#pragma unroll
+    for (int t = 0; t < RPT; ++t) {
+      if (t < t_lo || t >= t_hi) continue;
+#pragma unroll
+      for (int e = 0; e < W; ++e) {
+        if (e < e_lo || e >= e_hi) continue;
+        const int i = i0 + t, j = j0 + e;
+        if (in_gx(i, j)) a.gx[(int64_t)(i - a.i0) * (a.nyd + 1) + (j - a.j0)] = *gslot(t, e, 0);
+        if (in_gy(i, j)) a.gy[(int64_t)(i - a.i0) * a.nyd + (j - a.j0)] = *gslot(t, e, 1);
+      }
+    }
+  }
+  if (e_lo != 0 || e_hi != W || !lane_in) return;
+#pragma unroll
+  for (int t = 0; t < RPT; ++t) {
+    const int i = i0 + t;
+    if (t < t_lo || t >= t_hi || (unsigned)i > (unsigned)nx) continue;
+    const int64_t g = (int64_t)i * P + j0;
+    lex[t].st(a.out[0] + g);
+    ley[t].st(a.out[1] + g);
+    lhz[t].st(a.out[2] + g);
+    if (PML) {  // lambda psi stays +0 outside its strips in both buffers
+      const int o = (lr0 + t) * EC + lj0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        Vw v;
+        v.ld(sPsi + q * PL + o);
+        v.st(a.out[3 + q] + g);
+      }
+    }
+  }
+}
+
+template <typename T, int RPT, int K, bool PML>
+__global__ void __launch_bounds__(TB_THREADS, 1)
+k_tb_adj(const __grid_constant__ TBAdjArgs<T> a, const int2* __restrict__ tiles, int64_t n_hi) {
+  tb_adj_tile<T, RPT, K, PML>(a, tiles[blockIdx.x], n_hi);
+}
+
+template <typename T, int RPT, int K, bool PML>
+__global__ void __launch_bounds__(TB_THREADS, 1)
+k_tb_adj_batch(const TBAdjArgs<T>* __restrict__ args, const int4* __restrict__ tiles, int parity, int64_t n_hi) {
+  const int4 t = tiles[blockIdx.x];  // simulation, r0, c0
+  tb_adj_tile<T, RPT, K, PML>(args[2 * t.x + parity], make_int2(t.y, t.z), n_hi);
+}
+
+// ------------------------------------------------------------------------ host side
+
+// Compiled shapes: the forward's default tile of each dtype.
+template <typename T>
+struct AdjCfg;
+template <>
+struct AdjCfg<float> {
+  static constexpr int RPT = 6, K = 4;
+};
+template <>
+struct AdjCfg<double> {
+  static constexpr int RPT = 5, K = 2;
+};
+
+void tb_adj_shape(int dtype, int* ER, int* EC, int* K) {
+  if (dtype == ETG_F64) {
+    *ER = 8 * AdjCfg<double>::RPT;
+    *EC = 32 * TBVec<double>::W;
+    *K = AdjCfg<double>::K;
+  } else {
+    *ER = 8 * AdjCfg<float>::RPT;
+    *EC = 32 * TBVec<float>::W;
+    *K = AdjCfg<float>::K;
+  }
+}
+
+template <typename T>
+int tb_adj_attrs() {
+  constexpr int RPT = AdjCfg<T>::RPT, K = AdjCfg<T>::K;
+  ETG_TRY_CUDA(cudaFuncSetAttribute(k_tb_adj<T, RPT, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)AdjShape<T, RPT, K, false>::SMEM));
+  ETG_TRY_CUDA(cudaFuncSetAttribute(k_tb_adj<T, RPT, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)AdjShape<T, RPT, K, true>::SMEM));
+  ETG_TRY_CUDA(cudaFuncSetAttribute(k_tb_adj_batch<T, RPT, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)AdjShape<T, RPT, K, false>::SMEM));
+  ETG_TRY_CUDA(cudaFuncSetAttribute(k_tb_adj_batch<T, RPT, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)AdjShape<T, RPT, K, true>::SMEM));
+  return ETG_OK;
+}
+
+template <typename T>
+int tb_adj_launch(const TBAdjArgs<T>& a, const int2* tiles, int n_inner, int n_pml, int64_t n_hi,
+                  cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+  constexpr int RPT = AdjCfg<T>::RPT, K = AdjCfg<T>::K;
+  ETG_TRY_CUDA(cudaEventRecord(fork, main));
+  ETG_TRY_CUDA(cudaStreamWaitEvent(side, fork, 0));
+  if (n_pml) {
+    k_tb_adj<T, RPT, K, true><<<n_pml, dim3(32, 8), AdjShape<T, RPT, K, true>::SMEM, side>>>(a, tiles + n_inner, n_hi);
+    g_launches += 1;
+  }
+  if (n_inner) {
+    k_tb_adj<T, RPT, K, false><<<n_inner, dim3(32, 8), AdjShape<T, RPT, K, false>::SMEM, main>>>(a, tiles, n_hi);
+    g_launches += 1;
+  }
+  ETG_TRY_CUDA(cudaGetLastError());
+  ETG_TRY_CUDA(cudaEventRecord(join, side));
+  ETG_TRY_CUDA(cudaStreamWaitEvent(main, join, 0));
+  return ETG_OK;
+}
+
+template <typename T>
+int tb_adj_batch_launch(const TBAdjArgs<T>* args, const int4* tiles, int n_inner, int n_pml, int parity,
+                        int64_t n_hi, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+  constexpr int RPT = AdjCfg<T>::RPT, K = AdjCfg<T>::K;
+  ETG_TRY_CUDA(cudaEventRecord(fork, main));
+  ETG_TRY_CUDA(cudaStreamWaitEvent(side, fork, 0));
+  if (n_pml) {
+    k_tb_adj_batch<T, RPT, K, true><<<n_pml, dim3(32, 8), AdjShape<T, RPT, K, true>::SMEM, side>>>(
+        args, tiles + n_inner, parity, n_hi);
+    g_launches += 1;
+  }
+  if (n_inner) {
+    k_tb_adj_batch<T, RPT, K, false><<<n_inner, dim3(32, 8), AdjShape<T, RPT, K, false>::SMEM, main>>>(
+        args, tiles, parity, n_hi);
+    g_launches += 1;
+  }
+  ETG_TRY_CUDA(cudaGetLastError());
+  ETG_TRY_CUDA(cudaEventRecord(join, side));
+  ETG_TRY_CUDA(cudaStreamWaitEvent(main, join, 0));
+  return ETG_OK;
+}
+
+template int tb_adj_attrs<float>();
+template int tb_adj_attrs<double>();
+template int tb_adj_launch<float>(const TBAdjArgs<float>&, const int2*, int, int, int64_t, cudaStream_t, cudaStream_t,
+                                  cudaEvent_t, cudaEvent_t);
+template int tb_adj_launch<double>(const TBAdjArgs<double>&, const int2*, int, int, int64_t, cudaStream_t,
+                                   cudaStream_t, cudaEvent_t, cudaEvent_t);
+template int tb_adj_batch_launch<float>(const TBAdjArgs<float>*, const int4*, int, int, int, int64_t, cudaStream_t,
+                                        cudaStream_t, cudaEvent_t, cudaEvent_t);
+template int tb_adj_batch_launch<double>(const TBAdjArgs<double>*, const int4*, int, int, int, int64_t, cudaStream_t,
+                                         cudaStream_t, cudaEvent_t, cudaEvent_t);
+
+}  // namespace etg

@@ -1,0 +1,53 @@
+// Temporally blocked reverse sweep of the discrete adjoint (K reverse steps per launch).
+#pragma once
+
+#include "etg_sim.h"
+
+namespace etg {
+
+// One adjoint source node: lambda(comp at i, j) += table[n] at reverse step n (H nodes) or
+// table[n - 1] (E nodes, the DFT-E term of step n - 1). The table holds, for every step, the
+// sum over the objective's monitors of Re(G)·Re(ph) + Im(G)·Im(ph) in the order the one-step
+// adjoint kernel adds them.
+template <typename T>
+struct AdjSrc {
+  const T* table;
+  int i, j, comp;
+};
+
+// Everything one temporally blocked adjoint launch reads and writes. Lambda planes are
+// pitched like the fields: in/out[0..2] = lambda Ex, Ey, Hz; [3..6] = lambda psi_hz_x,
+// psi_hz_y, psi_ex_y, psi_ey_x.
+template <typename T>
+struct TBAdjArgs {
+  SimArgs<T> s;  // geometry, coefficients and strips (its field pointers are not used)
+  const T* in[7];
+  T* out[7];
+  const T* trace;  // Hz^(n+1/2) on [ti0, ti0+tnx) x [tj0, tj0+tny) per step, from trace_n0
+  int64_t trace_n0;
+  int ti0, tnx, tj0, tny;
+  int i0, nxd, j0, nyd;  // design cells
+  double *gx, *gy;       // dJ/dcb_ex (nxd, nyd+1), dJ/dcb_ey (nxd+1, nyd)
+  int n_hsrc, n_esrc;
+  AdjSrc<T> hsrc[MAX_SRC_NODES], esrc[MAX_SRC_NODES];
+};
+
+// Tile shape of the adjoint kernels of a dtype (rows ER, columns EC, depth K).
+void tb_adj_shape(int dtype, int* ER, int* EC, int* K);
+
+template <typename T>
+int tb_adj_attrs();
+
+// Reverse steps n_hi-1 … n_hi-K of one simulation: interior tiles on `main`, CPML tiles on
+// `side` (fork/join through the two events), tiles[0, n_inner) interior.
+template <typename T>
+int tb_adj_launch(const TBAdjArgs<T>& a, const int2* tiles, int n_inner, int n_pml, int64_t n_hi,
+                  cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
+
+// The same for a batch: args is a device array of 2 TBAdjArgs per simulation (reading the
+// primary or the second buffer), tiles (sim, r0, c0, -) with the interior tiles first.
+template <typename T>
+int tb_adj_batch_launch(const TBAdjArgs<T>* args, const int4* tiles, int n_inner, int n_pml, int parity,
+                        int64_t n_hi, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
+
+}  // namespace etg

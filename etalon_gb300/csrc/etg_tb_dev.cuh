@@ -1,0 +1,42 @@
+// Device-side pieces shared by the temporally blocked kernels (forward and adjoint).
+#pragma once
+
+#include "etg_sim.h"
+
+namespace etg {
+
+constexpr int TB_THREADS = 256;  // 8 warps of 32 lanes per tile
+
+template <typename T>
+struct TBVec;  // W elements per lane, one 16-byte access
+template <>
+struct TBVec<float> {
+  static constexpr int W = 4;
+  float v[4];
+  __device__ __forceinline__ void ld(const float* p) {
+    const float4 a = *reinterpret_cast<const float4*>(p);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  }
+  __device__ __forceinline__ void st(float* p) const {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+  __device__ __forceinline__ void zero() { v[0] = v[1] = v[2] = v[3] = 0.f; }
+};
+template <>
+struct TBVec<double> {
+  static constexpr int W = 2;
+  double v[2];
+  __device__ __forceinline__ void ld(const double* p) {
+    const double2 a = *reinterpret_cast<const double2*>(p);
+    v[0] = a.x; v[1] = a.y;
+  }
+  __device__ __forceinline__ void st(double* p) const {
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+  }
+  __device__ __forceinline__ void zero() { v[0] = v[1] = 0.0; }
+};
+
+template <typename T>
+__device__ __forceinline__ T zero() { return T(0); }
+
+}  // namespace etg

@@ -189,6 +189,22 @@ int etg_adj_forward(etg_adj* adj, int64_t n_steps, int64_t stride);
  * dJ/dcb_ex (nxd, nyd+1) and dJ/dcb_ey (nxd+1, nyd) in float64. The simulation's fields are
  * left in an unspecified state. */
 int etg_adj_backward(etg_adj* adj, const void* const* grad_acc, double* grad_cb_ex, double* grad_cb_ey);
+/* The two halves of etg_adj_backward, for batches: set the objective's dJ/dacc (kept on the
+ * device until replaced), and read dJ/dcb after a backward pass. */
+int etg_adj_set_objective(etg_adj* adj, const void* const* grad_acc);
+int etg_adj_gradient(etg_adj* adj, double* grad_cb_ex, double* grad_cb_ey);
+/* Many designs at once (one adjoint context per simulation, one precision): the forward
+ * passes step together as an etg_batch, and the reverse sweeps run as one set of K-step
+ * launches over the tiles of every design. Each design's gradient is bit-identical to its
+ * own etg_adj_backward. forward(n_steps, stride) as etg_adj_forward for every design; set
+ * each design's objective, call backward, then read each gradient with etg_adj_gradient. */
+typedef struct etg_adj_batch etg_adj_batch;
+int etg_adj_batch_create(etg_adj_batch** out, int n, etg_adj* const* adjs);
+int etg_adj_batch_destroy(etg_adj_batch* batch);
+/* Options of the forward batch (ETG_OPT_TB_DEPTH, ETG_OPT_TILE_ROWS, ETG_OPT_GRAPH_STEPS). */
+int etg_adj_batch_set_option(etg_adj_batch* batch, int option, int64_t value);
+int etg_adj_batch_forward(etg_adj_batch* batch, int64_t n_steps, int64_t stride);
+int etg_adj_batch_backward(etg_adj_batch* batch);
 
 /* ---------------------------------------------------------------- no-allocation advance
  * Has no counterpart in Etalon. For callers that cannot allocate device memory when they

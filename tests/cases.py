@@ -232,3 +232,48 @@ def synthetic_device(seed, precision="single", n_steps=5000, min_cells=256, max_
 def synthetic_batch(n=64, seed=2024, **kw):
     """``n`` seeded synthetic devices (sizes 256²-1536² unless overridden)."""
     return [synthetic_device(seed * 1000 + k, **kw) for k in range(n)]
+
+
+def smooth_design(nx, ny, seed, sigma=3.0):
+    """Per-cell ε in [2.085, 12.11] from a seeded uniform field smoothed with a Gaussian of
+    ``sigma`` cells, rescaled to [0, 1] before mapping to ε."""
+    from scipy.ndimage import gaussian_filter
+
+    u = gaussian_filter(np.random.default_rng(seed).uniform(0.0, 1.0, (nx, ny)), sigma, mode="reflect")
+    u = (u - u.min()) / max(u.max() - u.min(), 1e-30)
+    return EPS_OXIDE + (EPS_SILICON - EPS_OXIDE) * u
+
+
+def adjoint_device(precision="single", n_steps=20000, region=1200, design=100, dl=0.02, n_wavelengths=3):
+    """Single-design adjoint workload: ``region``² cells at dl + 12-layer CPML, oxide, input and
+    output Si strips (0.5 µm) along x meeting a ``design``² cell window at the centre; Hz source
+    in the input strip, Hz point monitor in the output strip at 1.50/1.55/1.60 µm (3 λ) or
+    ``n_wavelengths`` evenly in 1.5-1.6 µm. Returns (problem, (x0, y0, wx, wy) of the window)."""
+    side = region * dl
+    half = design * dl / 2
+    eps_box = side / 2 + 1.0
+    strips = [Box((-(eps_box + half) / 2, 0.0, 0.0), (eps_box - half, WIDTH, 0.22), EPS_SILICON),
+              Box(((eps_box + half) / 2, 0.0, 0.0), (eps_box - half, WIDTH, 0.22), EPS_SILICON)]  # fmt: skip
+    wl = [1.50, 1.55, 1.60] if n_wavelengths == 3 else list(np.linspace(1.5, 1.6, n_wavelengths))
+    p = ph.te_problem(
+        size=(side, side), dl=dl, background_eps=EPS_OXIDE, boxes=strips, pml=PMLSpec(layers=12),
+        sources=[PointSource((-0.35 * side, 0.0, 0.0), "Hz", GaussianPulse(1.55, 0.5))],
+        monitors=[DFTMonitor("out", wl, center=(0.35 * side + 0.011, 0.007, 0.0), components=("Hz",))],
+        n_steps=n_steps, precision=precision,
+    )  # fmt: skip
+    return p, (0.0, 0.0, design * dl - 1e-6, design * dl - 1e-6)
+
+
+def adjoint_variants(n=32, seed=5, precision="single", n_steps=10000, min_cells=512, max_cells=1024,
+                     min_design=50, max_design=150):  # fmt: skip
+    """``n`` seeded design variants for batched gradients: square regions of min-max cells per
+    side, design windows of min-max cells per side with smoothed random ε, 8 wavelengths in
+    1.5-1.6 µm. Returns [(problem, (x0, y0, wx, wy) of the window, ε cells (float64))]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        region = int(rng.integers(min_cells, max_cells + 1))
+        design = int(rng.integers(min_design, max_design + 1))
+        p, win = adjoint_device(precision, n_steps=n_steps, region=region, design=design, n_wavelengths=8)
+        out.append((p, win, design, seed * 1000 + k))
+    return out

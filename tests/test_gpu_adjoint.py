@@ -123,3 +123,91 @@ def test_eps_gradient_matches_central_differences(gpu):
         fd = (vals[0] - vals[1]) / (2 * h)
         assert grad[a, b] == pytest.approx(fd, rel=1e-3, abs=1e-6 * np.abs(grad).max())
     r.close()
+
+
+def _large_problem(precision, n_steps=400):
+    """216×166 cells (a strip through a 1.2×1.0 µm design window): interior and CPML tiles."""
+    return ph.te_problem(
+        size=(8.0, 6.0), dl=0.04, background_eps=2.085,
+        boxes=[ph.Box((0.0, 0.0, 0.0), (9.0, 0.5, 1.0), 12.11)],
+        pml=ph.PMLSpec(layers=10),
+        sources=[ph.PointSource((-3.0, 0.0, 0.0), "Hz", ph.GaussianPulse(1.55, 0.5))],
+        monitors=[ph.DFTMonitor("out", [1.50, 1.55, 1.60], center=(3.03, 0.02, 0.0), components=("Hz",)),
+                  ph.DFTMonitor("e", [1.55], center=(2.51, 0.33, 0.0), components=("Ex", "Ey"))],
+        n_steps=n_steps, precision=precision,
+    )  # fmt: skip
+
+
+def _gpu_grad_all(p, design, **kw):
+    """J = Σ over every monitor component of Σ_f |F|² (H and E adjoint sources)."""
+    r = AdjointRunner(p, design, **kw)
+    sx, sy = design.node_windows()
+    r.set_eps(p.eps["Ex"][sx], p.eps["Ey"][sy])
+    accs = r.forward()
+    grads = []
+    for acc_np, sampling in zip(accs, p.samplings):
+        acc = torch.as_tensor(np.stack([acc_np.real, acc_np.imag], -1).astype(np.float64)).requires_grad_(True)
+        point_power(acc, sampling).backward()
+        grads.append(acc.grad[..., 0].numpy() + 1j * acc.grad[..., 1].numpy())
+    gx, gy = r.backward(grads)
+    r.close()
+    return gx, gy
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_blocked_adjoint_sweep_equals_one_step_sweep_bitwise(gpu, precision):
+    """The temporally blocked reverse sweep gives the one-step kernels' bits, H and E sources."""
+    p = _large_problem(precision)
+    d = DesignRegion.from_box(p, (0.0, 0.0), (1.2, 1.0))
+    for stride in (0, 37):
+        a = _gpu_grad_all(p, d, stride=stride)
+        b = _gpu_grad_all(p, d, stride=stride, kernel="plain")
+        assert np.abs(a[0]).max() > 0 and np.abs(a[1]).max() > 0
+        np.testing.assert_array_equal(a[0], b[0])
+        np.testing.assert_array_equal(a[1], b[1])
+
+
+def test_blocked_adjoint_float32_within_1e3_of_float64(gpu):
+    p64, p32 = _large_problem("double"), _large_problem("single")
+    d = DesignRegion.from_box(p64, (0.0, 0.0), (1.2, 1.0))
+    ref = _gpu_grad_all(p64, d, kernel="plain")
+    got = _gpu_grad_all(p32, d)
+    assert _rel(got[0], ref[0]) < 1e-3 and _rel(got[1], ref[1]) < 1e-3
+
+
+def _variant(seed, precision, n_steps=900):
+    """A small seeded design variant: uneven region, design window of uneven size; the pulse
+    reaches the output monitor well within the run."""
+    from tests import cases
+
+    rng = np.random.default_rng(seed)
+    region, design = int(rng.integers(70, 130)), int(rng.integers(12, 30))
+    p, win = cases.adjoint_device(precision, n_steps=n_steps, region=region, design=design, n_wavelengths=4)
+    d = DesignRegion.from_box(p, win[:2], win[2:])
+    return p, d, torch.as_tensor(cases.smooth_design(d.nx, d.ny, seed))
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+@pytest.mark.parametrize("stride", [0, 23])
+def test_batched_gradients_equal_single_design_gradients(gpu, precision, stride):
+    from etalon_gb300.adjoint import AdjointBatch, simulate_batch
+
+    variants = [_variant(s, precision) for s in range(4)]
+    singles = []
+    for p, d, eps0 in variants:
+        r = AdjointRunner(p, d, stride=stride)
+        eps = eps0.clone().requires_grad_(True)
+        point_power(simulate(eps, r)[0], p.samplings[0]).backward()
+        singles.append(eps.grad.numpy().copy())
+        r.close()
+    runners = [AdjointRunner(p, d, stride=stride) for p, d, _ in variants]
+    batch = AdjointBatch(runners)
+    eps = [e.clone().requires_grad_(True) for _, _, e in variants]
+    outs = simulate_batch(eps, batch)
+    sum(point_power(o[0], v[0].samplings[0]) for o, v in zip(outs, variants)).backward()
+    for e, ref in zip(eps, singles):
+        assert np.abs(ref).max() > 0
+        np.testing.assert_array_equal(e.grad.numpy(), ref)
+    batch.close()
+    for r in runners:
+        r.close()

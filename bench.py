@@ -335,7 +335,11 @@ def run_ours(args, world, rank, local) -> None:
                       f"NumPy oracle in {threads} row bands",
         }  # fmt: skip
     if not args.no_batched:
-        out["batched"] = batched_line(args, local)
+        out["batched"] = batched_line(args, local, world, rank)
+    if not args.no_adjoint:
+        if world == 1:  # one grid: replicas would only repeat it
+            out["adjoint"] = adjoint_line(args)
+        out["batched_adjoint"] = batched_adjoint_line(args, world, rank)
     if args.fp64:
         out["fp64"] = fp64_line(args, local)
     if rank == 0:
@@ -412,21 +416,22 @@ def get_option(e, option: int) -> int:
     return int(v.value)
 
 
-def batched_line(args, local) -> dict:
+def batched_line(args, local, world=1, rank=0) -> dict:
     """64 seeded synthetic devices (bends, rings, MMIs; interiors 256-1536 cells per axis,
     12-layer CPML, one Hz source, 4 point monitors x 8 wavelengths), float32, 5000 time steps,
     stepped together by one Batch: tiles of all 64 in each launch, CUDA graphs per step block."""
     import torch
 
-    from etalon_gb300 import _lib, autotune
+    from etalon_gb300 import autotune
     from etalon_gb300.batch import Batch
+    from etalon_gb300.shard import shard
     from tests import cases
 
-    problems = cases.synthetic_batch(64, n_steps=args.batch_time_steps)
+    every = cases.synthetic_batch(64, n_steps=args.batch_time_steps)
+    problems = shard(every, [p.grid.n_cells for p in every], rank, world)  # no exchange between ranks
     b = Batch(problems)
     choice = autotune.tune_batch(b)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
-    cells = sum(p.grid.n_cells for p in problems)
     ms, launches = [], 0
     for k in range(3):
         b.reset()
@@ -438,12 +443,137 @@ def batched_line(args, local) -> dict:
             ms.append(t)
             launches += n
     b.close()
-    t = sum(ms) / len(ms)
+    t = reduce_max(world, sum(ms) / len(ms))
+    cells = sum(p.grid.n_cells for p in every)
     return {"metric": "cell-updates/s (64 synthetic devices 256^2-1536^2 + CPML, fp32, one batch)",
             "value": cells * args.batch_time_steps / (t / 1e3), "unit": UNIT, "ms_per_run": t,
-            "sims": len(problems), "cells": cells, "time_steps": args.batch_time_steps,
+            "sims": len(every), "cells": cells, "time_steps": args.batch_time_steps,
+            "sharding": f"{world} rank(s), devices balanced by cells, no exchange",
             "tile_rows_depth": list(choice), "gpu_launches_per_run": launches // len(ms),
             "runs_timed": len(ms), "l2": "flushed before each run"}  # fmt: skip
+
+
+def _gradient_once(runner, problem, eps0) -> tuple[float, np.ndarray]:
+    """One gradient through the public API (simulate + backward), wall time with syncs."""
+    import torch
+
+    from etalon_gb300 import _lib
+    from etalon_gb300.adjoint import point_power, simulate
+
+    eps = eps0.clone().requires_grad_(True)
+    _lib.call("etg_synchronize")
+    t = time.perf_counter()
+    point_power(simulate(eps, runner)[0], problem.samplings[0]).backward()
+    _lib.call("etg_synchronize")
+    return time.perf_counter() - t, eps.grad.numpy().copy()
+
+
+def adjoint_line(args) -> dict:
+    """dJ/dε of one 100×100-cell design in a 1224² grid (1200² + CPML), 20 000 steps, √N
+    checkpoints, J = Σ_λ |DFT Hz|² at an output point (3 λ): gradients per second through
+    simulate() + backward(), temporally blocked kernels against the one-step kernels, and the
+    float32 gradient's error against the float64 one."""
+    import torch
+
+    from etalon_gb300.adjoint import AdjointRunner, DesignRegion
+    from tests import cases
+
+    n = args.adjoint_time_steps
+    out = {"metric": "gradient evaluations/s (1224^2, 100x100 design, sqrt-N checkpoints, fp32)", "time_steps": n}
+    grads = {}
+    for name, precision, kernel, stride in (("blocked", "single", "auto", None), ("trace", "single", "auto", 0),
+                                            ("one_step", "single", "plain", None), ("fp64", "double", "auto", None)):
+        p, win = cases.adjoint_device(precision, n_steps=n)
+        d = DesignRegion.from_box(p, win[:2], win[2:])
+        eps0 = torch.as_tensor(cases.smooth_design(d.nx, d.ny, 0))
+        r = AdjointRunner(p, d, stride=AdjointRunner.sqrt_stride(n) if stride is None else stride, kernel=kernel)
+        reps = 1 if name == "fp64" else 2
+        ts = []
+        for _ in range(reps + 1):
+            t, g = _gradient_once(r, p, eps0)
+            ts.append(t)
+        r.close()
+        grads[name] = g
+        out[f"{name}_s_per_gradient"] = min(ts[1:])
+    out["value"] = 1.0 / out["blocked_s_per_gradient"]
+    out["unit"] = "gradients/s"
+    out["one_step_kernels_value"] = 1.0 / out["one_step_s_per_gradient"]
+    out["trace_mode_value"] = 1.0 / out["trace_s_per_gradient"]
+    ref = grads["fp64"]
+    out["rel_err_vs_fp64"] = float(np.abs(grads["blocked"] - ref).max() / np.abs(ref).max())
+    out["blocked_equals_one_step_bits"] = bool(np.array_equal(grads["blocked"], grads["one_step"]))
+    return out
+
+
+def batched_adjoint_line(args, world=1, rank=0) -> dict:
+    """32 seeded design variants (regions 512-1024 cells per side + CPML, design windows 50-150
+    cells, 8 λ, 10 000 steps): all forward and reverse passes run as one batch; gradients per
+    second against the same 32 designs run one at a time on the one-step kernels with √N
+    checkpoints (the single-design workload's plain path)."""
+    import torch
+
+    from etalon_gb300 import _lib
+    from etalon_gb300.adjoint import AdjointBatch, AdjointRunner, DesignRegion, point_power, simulate_batch
+    from tests import cases
+
+    n = args.batch_adjoint_time_steps
+    from etalon_gb300.shard import shard
+
+    variants = cases.adjoint_variants(32, n_steps=n)
+    variants = shard(variants, [v[0].grid.n_cells for v in variants], rank, world)  # no exchange
+    items, designs = [], []
+    for p, win, design, seed in variants:
+        d = DesignRegion.from_box(p, win[:2], win[2:])
+        items.append((p, d, torch.as_tensor(cases.smooth_design(d.nx, d.ny, seed))))
+        designs.append(design)
+    S = AdjointRunner.sqrt_stride(n)
+    out = {"metric": "gradient evaluations/s (32 designs 512^2-1024^2, 50^2-150^2 windows, 8 wavelengths, fp32)",
+           "unit": "gradients/s", "time_steps": n}  # fmt: skip
+    grads = {}
+    for name, stride in (("trace", 0), ("checkpoints", S)):
+        runners = [AdjointRunner(p, d, stride=stride) for p, d, _ in items]
+        b = AdjointBatch(runners)
+        ts = []
+        for _ in range(3):
+            eps = [e.clone().requires_grad_(True) for _, _, e in items]
+            _lib.call("etg_synchronize")
+            t = time.perf_counter()
+            outs = simulate_batch(eps, b)
+            sum(point_power(o[0], it[0].samplings[0]) for o, it in zip(outs, items)).backward()
+            _lib.call("etg_synchronize")
+            ts.append(time.perf_counter() - t)
+        grads[name] = [e.grad.numpy().copy() for e in eps]
+        b.close()
+        for r in runners:
+            r.close()
+        out[f"batched_{name}_s"] = reduce_max(world, min(ts[1:]))
+    total, one = 0.0, []
+    for p, d, e0 in items:  # the baseline: one design at a time, one-step kernels, √N checkpoints
+        r = AdjointRunner(p, d, stride=S, kernel="plain")
+        t, g = _gradient_once(r, p, e0)
+        total += t
+        one.append(g)
+        r.close()
+    total = reduce_max(world, total)
+    out["one_at_a_time_one_step_s"] = total
+    out["designs"] = 32
+    out["sharding"] = f"{world} rank(s), designs balanced by cells, no exchange"
+    out["value"] = 32 / out["batched_trace_s"]
+    out["checkpoints_value"] = 32 / out["batched_checkpoints_s"]
+    out["one_at_a_time_value"] = 32 / total
+    out["speedup_vs_one_at_a_time"] = total / out["batched_trace_s"]
+    out["checkpoints_speedup_vs_one_at_a_time"] = total / out["batched_checkpoints_s"]
+    out["batched_equals_one_at_a_time_bits"] = bool(all(np.array_equal(a, b) for a, b in zip(grads["trace"], one)))
+    errs = []
+    for (p, d, e0), g32, design in list(zip(items, grads["trace"], designs))[:2]:  # float64, two designs
+        p64, win = cases.adjoint_device("double", n_steps=n, region=p.grid.nx - 24, design=design, n_wavelengths=8)
+        r = AdjointRunner(p64, DesignRegion.from_box(p64, win[:2], win[2:]), stride=S)
+        _, g64 = _gradient_once(r, p64, e0)
+        r.close()
+        errs.append(float(np.abs(g32 - g64).max() / np.abs(g64).max()))
+    out["rel_err_vs_fp64"] = max(errs)
+    out["rel_err_designs"] = len(errs)
+    return out
 
 
 def fp64_line(args, local) -> dict:
@@ -481,6 +611,9 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-device batched line")
     ap.add_argument("--batch-time-steps", type=int, default=5000)
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the gradient lines")
+    ap.add_argument("--adjoint-time-steps", type=int, default=20000)
+    ap.add_argument("--batch-adjoint-time-steps", type=int, default=10000)
     ap.add_argument("--fp64", action="store_true", help="add a float64 line of the same workload")
     args = ap.parse_args()
     os.environ["ETG_BENCH_IMPL"] = args.impl

@@ -20,9 +20,8 @@ from . import _lib
 
 # (kernel, tile rows, steps per launch); tile columns follow from the precision
 CANDIDATES = {
-    "single": [("tb", 48, 4), ("tb", 64, 4), ("tb", 32, 4), ("tb", 40, 4), ("tb", 64, 8), ("tma", 32, 4),
-               ("plain", 0, 0)],
-    "double": [("tb", 40, 2), ("tb", 32, 2), ("tb", 64, 2), ("tma", 32, 2), ("plain", 0, 0)],
+    "single": [("tb", 48, 4), ("tb", 64, 4), ("tb", 40, 4), ("tma", 40, 4), ("plain", 0, 0)],
+    "double": [("tb", 40, 2), ("tb", 32, 2), ("tma", 40, 2), ("plain", 0, 0)],
 }  # fmt: skip
 
 
@@ -100,8 +99,7 @@ def _get(engine, option: int) -> int:
     return v.value
 
 
-BATCH_CANDIDATES = {"single": [(48, 4), (40, 4), (32, 4), (64, 4), (64, 8)],
-                    "double": [(40, 2), (32, 2), (64, 2)]}  # fmt: skip
+BATCH_CANDIDATES = {"single": [(48, 4), (40, 4), (64, 4)], "double": [(40, 2), (32, 2)]}
 
 
 def tune_batch(batch, *, steps: int = 64, reps: int = 2) -> tuple[int, int]:

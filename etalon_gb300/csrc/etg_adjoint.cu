@@ -18,6 +18,7 @@
 // full-state checkpoints every S ~ sqrt(N) steps and re-records it segment by segment in the
 // reverse sweep ("checkpoint" mode); both give the same bits.
 #include <algorithm>
+#include <map>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -209,6 +210,9 @@ __global__ void k_adj_tables(AdjPlan<T> plan, const int4* __restrict__ nodes, in
 
 using namespace etg;
 
+// Launch pairs per captured block of the batched reverse sweep.
+constexpr int64_t kBatchPairsPerGraph = 4;
+
 struct etg_adj {
   etg_sim* sim = nullptr;
   int i0 = 0, nxd = 0, j0 = 0, nyd = 0;
@@ -231,6 +235,12 @@ struct etg_adj {
   std::vector<int4> hnodes, enodes;  // i, j, comp
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+  int64_t* d_ctl = nullptr;                      // top step of the launch block, trace origin
+  std::map<int64_t, cudaGraphExec_t> graphs;     // key: pairs per graph * 2 + lambda-psi parity
+  etg_batch* fwd1 = nullptr;                     // segment recompute with the plans in device memory
+  void* ltrace = nullptr;                        // lambda E of the window per step of a launch block
+  int64_t ltrace_slots = 0;
+  void* d_args1 = nullptr;                       // device copy of the block's TBAdjArgs (gradient kernel)
 };
 
 namespace {
@@ -322,7 +332,7 @@ int copy_state(etg_sim* s, void* const* to, void* const* from) {
 // Arguments of one temporally blocked launch; `to_alt` reads the primary lambda buffers
 // (lambda psi of the current parities) and writes the second buffer, else the reverse.
 template <typename T>
-TBAdjArgs<T> tb_adj_args(etg_adj* A, const SimArgs<T>& sa, int par_e, int par_h, int64_t trace_n0, bool to_alt) {
+TBAdjArgs<T> tb_adj_args(etg_adj* A, const SimArgs<T>& sa, int par_e, int par_h, const int64_t* ctl, bool to_alt) {
   TBAdjArgs<T> a;
   memset(&a, 0, sizeof a);
   a.s = sa;
@@ -333,7 +343,7 @@ TBAdjArgs<T> tb_adj_args(etg_adj* A, const SimArgs<T>& sa, int par_e, int par_h,
     a.out[k] = (T*)(to_alt ? A->alt[k] : prim[k]);
   }
   a.trace = (const T*)A->trace;
-  a.trace_n0 = trace_n0;
+  a.ctl = ctl;
   a.ti0 = A->ti0;
   a.tnx = A->tnx;
   a.tj0 = A->tj0;
@@ -344,6 +354,7 @@ TBAdjArgs<T> tb_adj_args(etg_adj* A, const SimArgs<T>& sa, int par_e, int par_h,
   a.nyd = A->nyd;
   a.gx = A->grad;
   a.gy = A->grad + (size_t)A->nxd * (A->nyd + 1);
+  a.ltrace = (T*)A->ltrace;
   const int64_t N = A->n_steps;
   a.n_hsrc = (int)A->hnodes.size();
   a.n_esrc = (int)A->enodes.size();
@@ -363,17 +374,63 @@ int backward_sweep(etg_adj* A, int64_t n_hi, int64_t n_lo, int64_t trace_n0, int
                    const AdjPlan<T>& ph, const AdjPlan<T>& pe) {
   etg_sim* s = A->sim;
   const SimArgs<T> sa = sim_args_of<T>(s);
-  if (A->tiles) {
-    int ER, EC, K;
-    tb_adj_shape(s->dtype, &ER, &EC, &K);
-    const TBAdjArgs<T> to_alt = tb_adj_args<T>(A, sa, *par_e, *par_h, trace_n0, true);
-    const TBAdjArgs<T> back = tb_adj_args<T>(A, sa, *par_e, *par_h, trace_n0, false);
-    for (; n_hi - n_lo >= 2 * K; n_hi -= 2 * K) {
-      int rc = tb_adj_launch<T>(to_alt, A->tiles, A->n_inner, A->n_pml, n_hi, s->stream, A->side, A->fork, A->join);
+  int ER, EC, K;
+  tb_adj_shape(s->dtype, &ER, &EC, &K);
+  const int64_t pairs = A->tiles ? (n_hi - n_lo) / (2 * K) : 0;
+  if (pairs) {  // K-step launch pairs, captured in graphs of per_graph pairs
+    const int64_t ctl[2] = {n_hi, trace_n0};
+    ETG_TRY_CUDA(cudaMemcpyAsync(A->d_ctl, ctl, sizeof ctl, cudaMemcpyHostToDevice, s->stream));
+    const TBAdjArgs<T> to_alt = tb_adj_args<T>(A, sa, *par_e, *par_h, A->d_ctl, true);
+    const TBAdjArgs<T> back = tb_adj_args<T>(A, sa, *par_e, *par_h, A->d_ctl, false);
+    ETG_TRY_CUDA(cudaMemcpyAsync(A->d_args1, &to_alt, sizeof to_alt, cudaMemcpyHostToDevice, s->stream));
+    const int64_t nodes = (int64_t)A->nxd * (A->nyd + 1) + (int64_t)(A->nxd + 1) * A->nyd;
+    auto block_end = [&](int64_t n_pairs) {  // dJ/dcb of the block's steps, then the next block
+      tb_adj_grad<T>((const TBAdjArgs<T>*)A->d_args1, 1, 1, nodes, (int)(2 * K * n_pairs), s->stream);
+      tb_adj_ctl_add(A->d_ctl, -2 * K * n_pairs, s->stream);
+    };
+    auto pair = [&](int64_t p) {
+      int rc = tb_adj_launch<T>(to_alt, A->tiles, A->n_inner, A->n_pml, (int)(2 * K * p), s->stream, A->side, A->fork,
+                                A->join);
       if (rc == ETG_OK)
-        rc = tb_adj_launch<T>(back, A->tiles, A->n_inner, A->n_pml, n_hi - K, s->stream, A->side, A->fork, A->join);
-      if (rc) return rc;
+        rc = tb_adj_launch<T>(back, A->tiles, A->n_inner, A->n_pml, (int)(2 * K * p + K), s->stream, A->side,
+                              A->fork, A->join);
+      return rc;
+    };
+    const int64_t per_graph = std::max<int64_t>(1, s->opt[ETG_OPT_GRAPH_STEPS] / (2 * K));
+    int64_t done = 0;
+    if (s->opt[ETG_OPT_GRAPH_STEPS] > 0 && pairs >= per_graph) {
+      const int64_t key = 2 * per_graph + *par_e;
+      auto it = A->graphs.find(key);
+      if (it == A->graphs.end()) {
+        cudaGraph_t graph;
+        ETG_TRY_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = ETG_OK;
+        for (int64_t p = 0; p < per_graph && rc == ETG_OK; ++p) rc = pair(p);
+        if (rc == ETG_OK) block_end(per_graph);
+        cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+        if (rc) return rc;
+        ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "adjoint graph capture failed: %s", cudaGetErrorString(e));
+        cudaGraphExec_t exec;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "adjoint graph instantiate failed: %s", cudaGetErrorString(e));
+        it = A->graphs.emplace(key, exec).first;
+      }
+      for (; done + per_graph <= pairs; done += per_graph) {
+        ETG_TRY_CUDA(cudaGraphLaunch(it->second, s->stream));
+        g_launches += 4 * per_graph + 2;
+      }
     }
+    while (done < pairs) {  // without graphs, blocks of at most per_graph pairs
+      const int64_t c = std::min(per_graph, pairs - done);
+      for (int64_t p = 0; p < c; ++p) {
+        int rc = pair(p);
+        if (rc) return rc;
+      }
+      block_end(c);
+      done += c;
+    }
+    n_hi -= 2 * K * pairs;
   }
   const dim3 block(32, 4);
   const dim3 gre((s->ny + 31) / 32, (s->nx + 3) / 4), grh((s->ny + 1 + 31) / 32, (s->nx + 1 + 3) / 4);
@@ -419,6 +476,8 @@ int build_adj_plans(etg_adj* A, AdjPlan<T>* ph, AdjPlan<T>* pe) {
 }
 
 void drop_tb(etg_adj* A) {
+  for (auto& kv : A->graphs) cudaGraphExecDestroy(kv.second);
+  A->graphs.clear();
   for (void*& p : A->alt) {
     cudaFree(p);
     p = nullptr;
@@ -433,10 +492,14 @@ void drop_tb(etg_adj* A) {
 template <typename T>
 int prepare_tb(etg_adj* A, const AdjPlan<T>& ph, const AdjPlan<T>& pe) {
   etg_sim* s = A->sim;
-  drop_tb(A);
+  for (auto& kv : A->graphs) cudaGraphExecDestroy(kv.second);  // arguments change every pass
+  A->graphs.clear();
   A->hnodes.clear();
   A->enodes.clear();
-  if (s->opt[ETG_OPT_KERNEL] == 1) return ETG_OK;
+  if (s->opt[ETG_OPT_KERNEL] == 1) {
+    drop_tb(A);
+    return ETG_OK;
+  }
   auto collect = [](const AdjPlan<T>& p, std::vector<int4>* out) {
     for (int m = 0; m < p.n_mon; ++m) {
       const AdjMon<T>& d = p.mon[m];
@@ -454,14 +517,38 @@ int prepare_tb(etg_adj* A, const AdjPlan<T>& ph, const AdjPlan<T>& pe) {
   if (!collect(ph, &A->hnodes) || !collect(pe, &A->enodes)) {
     A->hnodes.clear();
     A->enodes.clear();
+    drop_tb(A);
     return ETG_OK;  // too many source nodes: one-step sweep
   }
   int rc = tb_adj_attrs<T>();
   if (rc) return rc;
-  const size_t pb = plane_bytes(s);
-  for (void*& p : A->alt) {
-    rc = etg_malloc(&p, pb);
+  if (!A->d_ctl) {
+    rc = etg_malloc((void**)&A->d_ctl, 2 * sizeof(int64_t));
     if (rc) return rc;
+  }
+  if (!A->d_args1) {
+    rc = etg_malloc(&A->d_args1, sizeof(TBAdjArgs<T>));
+    if (rc) return rc;
+  }
+  {  // lambda E of the window for every step of the largest launch block (graph or batch)
+    int ER, EC, K;
+    tb_adj_shape(s->dtype, &ER, &EC, &K);
+    const int64_t slots = 2 * K * std::max<int64_t>({1, s->opt[ETG_OPT_GRAPH_STEPS] / (2 * K), kBatchPairsPerGraph});
+    if (slots > A->ltrace_slots) {
+      cudaFree(A->ltrace);
+      A->ltrace = nullptr;
+      A->ltrace_slots = 0;
+      rc = etg_malloc(&A->ltrace, (size_t)slots * 2 * (A->nxd + 1) * (A->nyd + 1) * sizeof(T));
+      if (rc) return rc;
+      A->ltrace_slots = slots;
+    }
+  }
+  const size_t pb = plane_bytes(s);
+  for (void*& p : A->alt) {  // kept from pass to pass; lambda psi must start at +0 in both buffers
+    if (!p) {
+      rc = etg_malloc(&p, pb);
+      if (rc) return rc;
+    }
     ETG_TRY_CUDA(cudaMemsetAsync(p, 0, pb, s->stream));
   }
   int ER, EC, K;
@@ -473,10 +560,15 @@ int prepare_tb(etg_adj* A, const AdjPlan<T>& ph, const AdjPlan<T>& pe) {
   std::vector<int2> tiles;
   tb_split_tiles(s->nx, s->ny, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi, ER, EC, K, hot, &tiles, &A->n_inner);
   A->n_pml = (int)tiles.size() - A->n_inner;
-  A->h_tiles = tiles;
-  rc = etg_malloc((void**)&A->tiles, tiles.size() * sizeof(int2));
-  if (rc) return rc;
-  ETG_TRY_CUDA(cudaMemcpy(A->tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  if (!A->tiles || tiles.size() != A->h_tiles.size() ||
+      memcmp(tiles.data(), A->h_tiles.data(), tiles.size() * sizeof(int2)) != 0) {
+    cudaFree(A->tiles);
+    A->tiles = nullptr;
+    rc = etg_malloc((void**)&A->tiles, tiles.size() * sizeof(int2));
+    if (rc) return rc;
+    ETG_TRY_CUDA(cudaMemcpy(A->tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    A->h_tiles = tiles;
+  }
   // adjoint-source tables: H nodes from the H plan, E nodes from the E plan
   const int64_t N = A->n_steps;
   const size_t bytes = std::max<size_t>(1, (A->hnodes.size() + A->enodes.size()) * N * sizeof(T));
@@ -594,10 +686,20 @@ int adj_backward(etg_adj* A) {
     const int64_t nseg = (A->n_steps + S - 1) / S;
     s->monitors_on = false;
     sim_invalidate(s);
+    // the blocked path recomputes through a one-simulation batch, whose plans live in device
+    // memory: moving the trace origin per segment then needs no new graphs
+    if (A->tiles && !A->fwd1) rc = etg_batch_create(&A->fwd1, 1, &s);
     for (int64_t k = nseg - 1; k >= 0 && rc == ETG_OK; --k) {
       const int64_t lo = k * S, hi = std::min(A->n_steps, lo + S);
       rc = adj_restore_segment(A, k, lo, hi);
-      if (rc == ETG_OK) rc = sim_advance_internal(s, hi - lo);
+      if (rc == ETG_OK) {
+        if (A->tiles) {
+          rc = etg_batch_advance(A->fwd1, hi - lo);
+          if (rc == ETG_OK) rc = etg_batch_synchronize(A->fwd1);
+        } else {
+          rc = sim_advance_internal(s, hi - lo);
+        }
+      }
       clear_trace(s);
       if (rc == ETG_OK) rc = backward_sweep<T>(A, hi, lo, lo, &par_e, &par_h, ph, pe);
     }
@@ -670,6 +772,8 @@ struct etg_adj_batch {
   cudaStream_t stream = nullptr, side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
   int64_t n_steps = 0, stride = 0;
+  int64_t* d_ctl = nullptr;                   // top step of the launch block, trace origin
+  std::map<int64_t, cudaGraphExec_t> graphs;  // key: pairs per graph
 };
 
 namespace {
@@ -688,20 +792,61 @@ int batch_sweep(etg_adj_batch* B, int64_t n_hi, int64_t n_lo, int64_t trace_n0, 
     for (int k = 0; k < n; ++k) {
       etg_adj* A = B->adjs[k];
       const SimArgs<T> sa = sim_args_of<T>(A->sim);
-      args[2 * k] = tb_adj_args<T>(A, sa, par_e[k], par_h[k], trace_n0, true);
-      args[2 * k + 1] = tb_adj_args<T>(A, sa, par_e[k], par_h[k], trace_n0, false);
+      args[2 * k] = tb_adj_args<T>(A, sa, par_e[k], par_h[k], B->d_ctl, true);
+      args[2 * k + 1] = tb_adj_args<T>(A, sa, par_e[k], par_h[k], B->d_ctl, false);
       ETG_TRY_CUDA(cudaStreamSynchronize(A->sim->stream));
     }
+    const int64_t ctl[2] = {n_hi, trace_n0};
+    ETG_TRY_CUDA(cudaMemcpyAsync(B->d_ctl, ctl, sizeof ctl, cudaMemcpyHostToDevice, B->stream));
     ETG_TRY_CUDA(cudaMemcpyAsync(B->d_args, args.data(), args.size() * sizeof(TBAdjArgs<T>), cudaMemcpyHostToDevice,
                                  B->stream));
-    for (int64_t p = 0; p < pairs; ++p) {
-      const int64_t top = n_hi - 2 * K * p;
-      int rc = tb_adj_batch_launch<T>((const TBAdjArgs<T>*)B->d_args, B->d_tiles, B->n_inner, B->n_pml, 0, top,
-                                      B->stream, B->side, B->fork, B->join);
+    const TBAdjArgs<T>* d_args = (const TBAdjArgs<T>*)B->d_args;
+    int64_t max_nodes = 0;
+    for (const etg_adj* A : B->adjs)
+      max_nodes = std::max<int64_t>(max_nodes, (int64_t)A->nxd * (A->nyd + 1) + (int64_t)(A->nxd + 1) * A->nyd);
+    auto block_end = [&](int64_t n_pairs) {
+      tb_adj_grad<T>(d_args, 2, n, max_nodes, (int)(2 * K * n_pairs), B->stream);
+      tb_adj_ctl_add(B->d_ctl, -2 * K * n_pairs, B->stream);
+    };
+    auto pair = [&](int64_t p) {
+      int rc = tb_adj_batch_launch<T>(d_args, B->d_tiles, B->n_inner, B->n_pml, 0, (int)(2 * K * p), B->stream,
+                                      B->side, B->fork, B->join);
       if (rc == ETG_OK)
-        rc = tb_adj_batch_launch<T>((const TBAdjArgs<T>*)B->d_args, B->d_tiles, B->n_inner, B->n_pml, 1, top - K,
-                                    B->stream, B->side, B->fork, B->join);
-      if (rc) return rc;
+        rc = tb_adj_batch_launch<T>(d_args, B->d_tiles, B->n_inner, B->n_pml, 1, (int)(2 * K * p + K), B->stream,
+                                    B->side, B->fork, B->join);
+      return rc;
+    };
+    const int64_t per_graph = kBatchPairsPerGraph;
+    int64_t done = 0;
+    if (pairs >= per_graph) {
+      auto it = B->graphs.find(per_graph);
+      if (it == B->graphs.end()) {
+        cudaGraph_t graph;
+        ETG_TRY_CUDA(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = ETG_OK;
+        for (int64_t p = 0; p < per_graph && rc == ETG_OK; ++p) rc = pair(p);
+        if (rc == ETG_OK) block_end(per_graph);
+        cudaError_t e = cudaStreamEndCapture(B->stream, &graph);
+        if (rc) return rc;
+        ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "batched adjoint graph capture failed: %s", cudaGetErrorString(e));
+        cudaGraphExec_t exec;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "batched adjoint graph instantiate failed: %s",
+                    cudaGetErrorString(e));
+        it = B->graphs.emplace(per_graph, exec).first;
+      }
+      for (; done + per_graph <= pairs; done += per_graph) {
+        ETG_TRY_CUDA(cudaGraphLaunch(it->second, B->stream));
+        g_launches += 4 * per_graph + 2;
+      }
+    }
+    if (done < pairs) {
+      for (int64_t p = 0; done + p < pairs; ++p) {
+        int rc = pair(p);
+        if (rc) return rc;
+      }
+      block_end(pairs - done);
     }
     ETG_TRY_CUDA(cudaStreamSynchronize(B->stream));  // the host copy of args stays alive until here
   }
@@ -724,15 +869,22 @@ int batch_backward(etg_adj_batch* B) {
     if (rc) return rc;
     blocked &= B->adjs[k]->tiles != nullptr;
   }
-  // one tile list over all designs, interior tiles first
+  // one tile list over all designs, interior tiles first (graphs hold its address)
+  for (auto& kv : B->graphs) cudaGraphExecDestroy(kv.second);
+  B->graphs.clear();
   cudaFree(B->d_tiles);
   B->d_tiles = nullptr;
+  if (!B->d_ctl) {
+    int rc = etg_malloc((void**)&B->d_ctl, 2 * sizeof(int64_t));
+    if (rc) return rc;
+  }
   if (blocked) {
     std::vector<int4> inner, pml;
     for (int k = 0; k < n; ++k) {
       const etg_adj* A = B->adjs[k];
       for (int q = 0; q < (int)A->h_tiles.size(); ++q)
-        (q < A->n_inner ? inner : pml).push_back(make_int4(k, A->h_tiles[q].x, A->h_tiles[q].y, 0));
+        (q < A->n_inner ? inner : pml)
+            .push_back(make_int4(k, tb_tile_row(A->h_tiles[q]), A->h_tiles[q].y, tb_tile_kind(A->h_tiles[q])));
     }
     B->n_inner = (int)inner.size();
     B->n_pml = (int)pml.size();
@@ -815,6 +967,10 @@ int etg_adj_destroy(etg_adj* A) {
   cudaFree(A->grad);
   for (void* p : A->gacc) cudaFree(p);
   drop_tb(A);
+  etg_batch_destroy(A->fwd1);
+  cudaFree(A->d_ctl);
+  cudaFree(A->ltrace);
+  cudaFree(A->d_args1);
   cudaFree(A->tables);
   if (A->fork) cudaEventDestroy(A->fork);
   if (A->join) cudaEventDestroy(A->join);
@@ -899,6 +1055,8 @@ int etg_adj_batch_destroy(etg_adj_batch* B) {
   if (!B) return ETG_OK;
   if (B->stream) cudaStreamSynchronize(B->stream);
   etg_batch_destroy(B->fwd);
+  for (auto& kv : B->graphs) cudaGraphExecDestroy(kv.second);
+  cudaFree(B->d_ctl);
   cudaFree(B->d_args);
   cudaFree(B->d_tiles);
   if (B->fork) cudaEventDestroy(B->fork);

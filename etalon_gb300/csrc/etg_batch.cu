@@ -100,7 +100,8 @@ int refresh(etg_batch* b, int ER, int K, bool* changed) {
       std::vector<int2> t;
       int ni = 0;
       tb_split_tiles(s->nx, s->ny, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi, ER, 32 * (sizeof(T) == 4 ? 4 : 2), K, hot, &t, &ni);
-      for (int q = 0; q < (int)t.size(); ++q) (q < ni ? inner : pml).push_back(make_int4(k, t[q].x, t[q].y, 0));
+      for (int q = 0; q < (int)t.size(); ++q)
+        (q < ni ? inner : pml).push_back(make_int4(k, tb_tile_row(t[q]), t[q].y, tb_tile_kind(t[q])));
     }
     const int n_inner = (int)inner.size(), n_pml = (int)pml.size();
     inner.insert(inner.end(), pml.begin(), pml.end());
@@ -276,6 +277,7 @@ int etg_batch_advance(etg_batch* b, int64_t n_steps) {
   for (etg_sim* s : b->sims) {
     ETG_TRY_CUDA(cudaStreamWaitEvent(s->stream, b->done, 0));
     s->h_step += n_steps;
+    s->psi_dirty = true;
   }
   return ETG_OK;
 }

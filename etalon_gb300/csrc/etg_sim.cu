@@ -249,6 +249,7 @@ int sim_advance_internal(etg_sim* s, int64_t n_steps) {
   if (n_steps == 0) return ETG_OK;
   int rc = check_tables(s, n_steps);
   if (rc) return rc;
+  s->psi_dirty = true;
   rc = s->dtype == ETG_F32 ? advance_dispatch<float>(s, n_steps) : advance_dispatch<double>(s, n_steps);
   if (rc) return rc;
   s->h_step += n_steps;
@@ -368,6 +369,12 @@ int etg_sim_set_coefficients(etg_sim* s, const void* cb_ex, const void* cb_ey, c
   for (int k = 0; k < 12; ++k) {
     ETG_REQUIRE(c[k], ETG_ERR_ARGUMENT, "etg_sim_set_coefficients: null 1D array %d", k);
     ETG_TRY_CUDA(cudaMemcpy(s->c1d[k], c[k], len[k] * s->esize(), cudaMemcpyHostToDevice));
+  }
+  // psi may be non-zero wherever it was live since the last reset: those rows and columns
+  // stay strips whatever the new coefficients say
+  if (s->psi_dirty) {
+    for (int k = 0; k <= s->nx; ++k) s->psi_live_x[k] |= s->live_x[k];
+    for (int k = 0; k <= s->ny; ++k) s->psi_live_y[k] |= s->live_y[k];
   }
   // live CPML rows/columns: psi_hz_x (h, i < nx), psi_ey_x (e, 1 <= i <= nx-1), same for y
   std::fill(s->live_x.begin(), s->live_x.end(), 0);
@@ -574,6 +581,7 @@ int etg_sim_set_dft(etg_sim* s, int monitor, const void* host) {
 
 int etg_sim_reset(etg_sim* s) {
   ETG_REQUIRE(s, ETG_ERR_ARGUMENT, "etg_sim_reset: null handle");
+  s->psi_dirty = false;
   std::fill(s->psi_live_x.begin(), s->psi_live_x.end(), 0);
   std::fill(s->psi_live_y.begin(), s->psi_live_y.end(), 0);
   update_strips(s);
@@ -590,6 +598,7 @@ int etg_sim_advance(etg_sim* s, int64_t n_steps) {
   const bool timing = s->opt[ETG_OPT_TIMING] != 0;
   const int64_t launches0 = g_launches;
   if (timing) ETG_TRY_CUDA(cudaEventRecord(s->ev0, s->stream));
+  s->psi_dirty = true;
   rc = s->dtype == ETG_F32 ? advance_dispatch<float>(s, n_steps) : advance_dispatch<double>(s, n_steps);
   if (rc) return rc;
   if (s->opt[ETG_OPT_CHECK_FINITE]) {

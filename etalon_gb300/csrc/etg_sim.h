@@ -144,6 +144,7 @@ struct etg_sim {
   bool have_coeffs = false;
   // rows / columns whose psi may be non-zero (from c != 0, b outside (0, inf) or uploaded psi)
   std::vector<char> live_x, live_y, psi_live_x, psi_live_y;
+  bool psi_dirty = false;  // stepped since the last reset: psi may be non-zero in the live rows
   std::vector<char> nonunit_x, nonunit_y;  // rows / columns whose CPML terms are not "+ 0"
   int xs_lo = 0, xs_hi = 0, ys_lo = 0, ys_hi = 0;
   int ux_lo = 0, ux_hi = 0, uy_lo = 0, uy_hi = 0;

@@ -36,15 +36,21 @@
 
 namespace etg {
 
-template <typename T, int RPT, int K, bool PML>
+// Tile kinds: KIND_INNER (unit rectangle, lean update), KIND_X (CPML only across rows: the
+// tile's columns are unit), KIND_Y (CPML only across columns), KIND_XY (both: corners).
+constexpr int KIND_INNER = 0, KIND_X = 1, KIND_Y = 2, KIND_XY = 3;
+constexpr int KIND_SHIFT = 28;  // CPML tile lists carry the kind in bits 28-29 of the row
+
+template <typename T, int RPT, int K, int KIND>
 struct TBShape {
   static constexpr int W = TBVec<T>::W;
   static constexpr int ER = 8 * RPT, EC = 32 * W, OR = ER - 2 * K, OC = EC - 2 * K;
   static constexpr int PL = ER * EC;                    // one plane: cb or psi
-  static constexpr int PLANES = PML ? 6 : 2;            // cb_ex, cb_ey (+ 4 psi)
+  // cb_ex, cb_ey, then psi_hz_x, psi_ey_x (x kinds), then psi_hz_y, psi_ex_y (y kinds)
+  static constexpr int PLANES = 2 + ((KIND & KIND_X) ? 2 : 0) + ((KIND & KIND_Y) ? 2 : 0);
   static constexpr int XCH = 9 * EC;                    // one exchange buffer: 8 warps + a zero row
   static constexpr size_t SMEM = ((size_t)PLANES * PL + 2 * XCH) * sizeof(T);
-  static constexpr int MIN_BLOCKS = PML ? 1 : (RPT <= 5 ? 2 : 1);
+  static constexpr int MIN_BLOCKS = KIND ? 1 : (RPT <= 5 ? 2 : 1);
   static_assert(K % W == 0, "the halo must keep vectors aligned");
   static_assert(OR > 0 && OC > 0, "halo larger than the tile");
 };
@@ -98,16 +104,24 @@ __device__ __forceinline__ void tb_inject(const PhasePlan<T>& p, uint32_t rel, T
 }
 
 // One CTA, one tile: load the extended tile, advance it K steps, write the output tile.
-template <typename T, int RPT, int K, bool PML>
+//
+// CPML tiles come in three kinds. In an X tile every column of the extended region lies in
+// the unit range of the y coefficients, so the y terms take the lean form; rows outside the
+// x strips have no psi and their x terms reduce to d·(1/kappa) + 0 (b·0 + 0·d = +0 for
+// finite d); only strip rows read and write psi. Y tiles are the same with rows and columns
+// exchanged, XY tiles (corners) run the full expression everywhere. All give Etalon's bits.
+template <typename T, int RPT, int K, int KIND>
 __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst, const int2 tile,
                                         const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off) {
-  using S = TBShape<T, RPT, K, PML>;
+  using S = TBShape<T, RPT, K, KIND>;
   using Vw = TBVec<T>;
   constexpr int W = S::W, ER = S::ER, EC = S::EC, PL = S::PL;
+  constexpr bool PML = KIND != KIND_INNER, PX = (KIND & KIND_X) != 0, PY = (KIND & KIND_Y) != 0;
   extern __shared__ __align__(16) unsigned char tb_smem[];
   T* const sCbx = reinterpret_cast<T*>(tb_smem);
   T* const sCby = sCbx + PL;
-  T* const sPsi = sCby + PL;                     // CPML tiles: psi_hz_x, psi_hz_y, psi_ex_y, psi_ey_x
+  T* const sPsiX = sCby + PL;                    // x kinds: psi_hz_x, psi_ey_x
+  T* const sPsiY = sPsiX + (PX ? 2 * PL : 0);    // y kinds: psi_hz_y, psi_ex_y
   T* const sHzX = sCbx + S::PLANES * PL;         // [k = ty + 1]: last-row Hz of warp ty; [0] = zeros
   T* const sEyX = sHzX + S::XCH;                 // [k = ty]: first-row Ey of warp ty; [8] = zeros
   __shared__ uint32_t s_rel[4];  // relevant plan entries: H sources, E sources, H monitors, E monitors
@@ -179,30 +193,38 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
     }
     cx.st(sCbx + o);
     cy.st(sCby + o);
-    if (PML) {
-      Vw p0, p1, p2, p3;
-      if (in) {
+    // psi only where it can be non-zero: x strips for psi_*_x, y strips for psi_*_y; the
+    // update never reads it anywhere else (XY tiles read all of it)
+    if (PX) {
+      Vw p0, p1;
+      if (in && (KIND == KIND_XY || i < a.xs_lo || i >= a.xs_hi)) {
         p0.ld(a.psi_hz_x + g);
-        p1.ld(a.psi_hz_y + g);
-        p2.ld(a.psi_ex_y + g);
-        p3.ld(a.psi_ey_x + g);
+        p1.ld(a.psi_ey_x + g);
       } else {
         p0.zero();
         p1.zero();
-        p2.zero();
-        p3.zero();
       }
-      p0.st(sPsi + 0 * PL + o);
-      p1.st(sPsi + 1 * PL + o);
-      p2.st(sPsi + 2 * PL + o);
-      p3.st(sPsi + 3 * PL + o);
+      p0.st(sPsiX + o);
+      p1.st(sPsiX + PL + o);
+    }
+    if (PY) {
+      Vw p0, p1;
+      if (in && (KIND == KIND_XY || j0 < a.ys_lo || j0 + W > a.ys_hi)) {
+        p0.ld(a.psi_hz_y + g);
+        p1.ld(a.psi_ex_y + g);
+      } else {
+        p0.zero();
+        p1.zero();
+      }
+      p0.st(sPsiY + o);
+      p1.st(sPsiY + PL + o);
     }
   }
   ey[0].st(sEyX + ty * EC + lj0);
   // CPML tiles: this thread's profiles in registers (columns per lane, rows per warp)
   T byh[W], cyh[W], kyh[W], bye[W], cye[W], kye[W];
   T bxh[RPT], cxh[RPT], kxh[RPT], bxe[RPT], cxe[RPT], kxe[RPT];
-  if (PML) {
+  if (PY) {
 #pragma unroll
     for (int e = 0; e < W; ++e) {
       const int j = min(max(j0 + e, 0), ny - 1), je = min(max(j0 + e, 0), ny);
@@ -213,6 +235,8 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
       cye[e] = a.cy_e[je];
       kye[e] = a.iky_e[je];
     }
+  }
+  if (PX) {
 #pragma unroll
     for (int t = 0; t < RPT; ++t) {
       const int i = min(max(i0 + t, 0), nx - 1), ie = min(max(i0 + t, 0), nx);
@@ -254,14 +278,30 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
             hz[t].v[e] = add(hz[t].v[e], mul(db, sub(add(dex_dy, zero<T>()), add(dey_dx, zero<T>()))));
           } else {
             const int i = i0 + t, j = j0 + e;
-            if (i >= 0 && i < nx && j >= 0 && j < ny) {
-              T* pxp = sPsi + 0 * PL + (lr0 + t) * EC + lj0 + e;
-              T* pyp = sPsi + 1 * PL + (lr0 + t) * EC + lj0 + e;
-              const T py = add(mul(byh[e], *pyp), mul(cyh[e], dex_dy));
-              const T px = add(mul(bxh[t], *pxp), mul(cxh[t], dey_dx));
-              if (j < a.ys_lo || j >= a.ys_hi) *pyp = py;
-              if (i < a.xs_lo || i >= a.xs_hi) *pxp = px;
-              hz[t].v[e] = add(hz[t].v[e], mul(db, sub(add(mul(dex_dy, kyh[e]), py), add(mul(dey_dx, kxh[t]), px))));
+            const bool xs = i < a.xs_lo || i >= a.xs_hi, ys = j < a.ys_lo || j >= a.ys_hi;
+            if ((!PX || (i >= 0 && i < nx)) && (!PY || (j >= 0 && j < ny))) {
+              T ty_ = add(dex_dy, zero<T>()), tx_ = add(dey_dx, zero<T>());
+              if (PY) {
+                if (KIND == KIND_XY || ys) {
+                  T* pyp = sPsiY + (lr0 + t) * EC + lj0 + e;
+                  const T py = add(mul(byh[e], *pyp), mul(cyh[e], dex_dy));
+                  if (ys) *pyp = py;
+                  ty_ = add(mul(dex_dy, kyh[e]), py);
+                } else {
+                  ty_ = add(mul(dex_dy, kyh[e]), zero<T>());
+                }
+              }
+              if (PX) {
+                if (KIND == KIND_XY || xs) {
+                  T* pxp = sPsiX + (lr0 + t) * EC + lj0 + e;
+                  const T px = add(mul(bxh[t], *pxp), mul(cxh[t], dey_dx));
+                  if (xs) *pxp = px;
+                  tx_ = add(mul(dey_dx, kxh[t]), px);
+                } else {
+                  tx_ = add(mul(dey_dx, kxh[t]), zero<T>());
+                }
+              }
+              hz[t].v[e] = add(hz[t].v[e], mul(db, sub(ty_, tx_)));
             }
           }
         }
@@ -318,17 +358,34 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
             ey[t].v[e] = sub(ey[t].v[e], mul(cy.v[e], add(dx, zero<T>())));
           } else {
             const int i = i0 + t, j = j0 + e;
-            if (i >= 0 && i < nx && j >= 1 && j <= ny - 1) {
-              T* pp = sPsi + 2 * PL + (lr0 + t) * EC + lj0 + e;
-              const T p = add(mul(bye[e], *pp), mul(cye[e], dy));
-              if (j < a.ys_lo || j >= a.ys_hi) *pp = p;
-              ex[t].v[e] = add(ex[t].v[e], mul(cx.v[e], add(mul(dy, kye[e]), p)));
+            const bool xs = i < a.xs_lo || i >= a.xs_hi, ys = j < a.ys_lo || j >= a.ys_hi;
+            if ((!PX || (i >= 0 && i < nx)) && (!PY || (j >= 1 && j <= ny - 1))) {
+              T term = add(dy, zero<T>());
+              if (PY) {
+                if (KIND == KIND_XY || ys) {
+                  T* pp = sPsiY + PL + (lr0 + t) * EC + lj0 + e;
+                  const T p = add(mul(bye[e], *pp), mul(cye[e], dy));
+                  if (ys) *pp = p;
+                  term = add(mul(dy, kye[e]), p);
+                } else {
+                  term = add(mul(dy, kye[e]), zero<T>());
+                }
+              }
+              ex[t].v[e] = add(ex[t].v[e], mul(cx.v[e], term));
             }
-            if (i >= 1 && i <= nx - 1 && j >= 0 && j < ny) {
-              T* pp = sPsi + 3 * PL + (lr0 + t) * EC + lj0 + e;
-              const T p = add(mul(bxe[t], *pp), mul(cxe[t], dx));
-              if (i < a.xs_lo || i >= a.xs_hi) *pp = p;
-              ey[t].v[e] = sub(ey[t].v[e], mul(cy.v[e], add(mul(dx, kxe[t]), p)));
+            if ((!PX || (i >= 1 && i <= nx - 1)) && (!PY || (j >= 0 && j < ny))) {
+              T term = add(dx, zero<T>());
+              if (PX) {
+                if (KIND == KIND_XY || xs) {
+                  T* pp = sPsiX + PL + (lr0 + t) * EC + lj0 + e;
+                  const T p = add(mul(bxe[t], *pp), mul(cxe[t], dx));
+                  if (xs) *pp = p;
+                  term = add(mul(dx, kxe[t]), p);
+                } else {
+                  term = add(mul(dx, kxe[t]), zero<T>());
+                }
+              }
+              ey[t].v[e] = sub(ey[t].v[e], mul(cy.v[e], term));
             }
           }
         }
@@ -358,36 +415,68 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
     ex[t].st(dst.ex + g);
     ey[t].st(dst.ey + g);
     hz[t].st(dst.hz + g);
-    if (PML) {  // psi stays +0 outside its strips in both buffers, so whole vectors are copied
-      const int o = (lr0 + t) * EC + lj0;
+    // psi stays +0 outside its strips in both buffers: strip rows (x) and vectors that
+    // meet a strip column (y) are written, as whole vectors
+    const int o = (lr0 + t) * EC + lj0;
+    if (PX && (KIND == KIND_XY || i < a.xs_lo || i >= a.xs_hi)) {
       Vw v;
-      v.ld(sPsi + 0 * PL + o);
+      v.ld(sPsiX + o);
       v.st(dst.psi_hz_x + g);
-      v.ld(sPsi + 1 * PL + o);
-      v.st(dst.psi_hz_y + g);
-      v.ld(sPsi + 2 * PL + o);
-      v.st(dst.psi_ex_y + g);
-      v.ld(sPsi + 3 * PL + o);
+      v.ld(sPsiX + PL + o);
       v.st(dst.psi_ey_x + g);
+    }
+    if (PY && (KIND == KIND_XY || j0 < a.ys_lo || j0 + W > a.ys_hi)) {
+      Vw v;
+      v.ld(sPsiY + o);
+      v.st(dst.psi_hz_y + g);
+      v.ld(sPsiY + PL + o);
+      v.st(dst.psi_ex_y + g);
     }
   }
 }
 
+// Shared memory of a launch of the interior kernel (PML false) or the CPML kernel (the
+// largest CPML kind).
 template <typename T, int RPT, int K, bool PML>
-__global__ void __launch_bounds__(TB_THREADS, TBShape<T, RPT, K, PML>::MIN_BLOCKS)
+constexpr size_t tb_smem() {
+  return TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER>::SMEM;
+}
+
+template <typename T, int RPT, int K, bool PML>
+__global__ void __launch_bounds__(TB_THREADS, TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER>::MIN_BLOCKS)
 k_tb_step(const __grid_constant__ SimArgs<T> a, const __grid_constant__ TBDst<T> dst,
           const int2* __restrict__ tiles, const __grid_constant__ PhasePlan<T> ph,
           const __grid_constant__ PhasePlan<T> pe, int step_off) {
-  tb_tile<T, RPT, K, PML>(a, dst, tiles[blockIdx.x], ph, pe, step_off);
+  const int2 t = tiles[blockIdx.x];
+  if (!PML) {
+    tb_tile<T, RPT, K, KIND_INNER>(a, dst, t, ph, pe, step_off);
+    return;
+  }
+  const int2 u = make_int2(t.x & ((1 << KIND_SHIFT) - 1), t.y);
+  switch (t.x >> KIND_SHIFT) {
+    case KIND_X: tb_tile<T, RPT, K, KIND_X>(a, dst, u, ph, pe, step_off); break;
+    case KIND_Y: tb_tile<T, RPT, K, KIND_Y>(a, dst, u, ph, pe, step_off); break;
+    default: tb_tile<T, RPT, K, KIND_XY>(a, dst, u, ph, pe, step_off); break;
+  }
 }
 
-// Batched form: every tile names its simulation; all simulations advance the same K steps.
+// Batched form: every tile names its simulation (and, for CPML tiles, its kind in .w); all
+// simulations advance the same K steps.
 template <typename T, int RPT, int K, bool PML>
-__global__ void __launch_bounds__(TB_THREADS, TBShape<T, RPT, K, PML>::MIN_BLOCKS)
+__global__ void __launch_bounds__(TB_THREADS, TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER>::MIN_BLOCKS)
 k_tb_batch(const BatchSim<T>* __restrict__ sims, const int4* __restrict__ tiles, int parity, int step_off) {
-  const int4 t = tiles[blockIdx.x];  // simulation, r0, c0
+  const int4 t = tiles[blockIdx.x];  // simulation, r0, c0, kind
   const BatchSim<T>& b = sims[t.x];
-  tb_tile<T, RPT, K, PML>(b.src[parity], b.dst[parity], make_int2(t.y, t.z), b.ph, b.pe, step_off);
+  const int2 u = make_int2(t.y, t.z);
+  if (!PML) {
+    tb_tile<T, RPT, K, KIND_INNER>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off);
+    return;
+  }
+  switch (t.w) {
+    case KIND_X: tb_tile<T, RPT, K, KIND_X>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off); break;
+    case KIND_Y: tb_tile<T, RPT, K, KIND_Y>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off); break;
+    default: tb_tile<T, RPT, K, KIND_XY>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off); break;
+  }
 }
 
 // ------------------------------------------------------------------------ persistent TMA variant
@@ -492,7 +581,7 @@ k_tb_tma(const __grid_constant__ TMAMaps maps, const __grid_constant__ SimArgs<T
   }
   __syncthreads();
   auto fetch = [&](int k) {  // one thread
-    const int2 t = tiles[k];
+    const int2 t = make_int2(tiles[k].x & ((1 << KIND_SHIFT) - 1), tiles[k].y);
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(S::TX_BYTES)
                  : "memory");
     const int x = t.y - K, y = t.x - K;
@@ -508,7 +597,7 @@ k_tb_tma(const __grid_constant__ TMAMaps maps, const __grid_constant__ SimArgs<T
   const int64_t n_base = *a.step + step_off;
 
   for (int k = blockIdx.x; k < n_tiles; k += gridDim.x) {
-    const int2 tile = tiles[k];
+    const int2 tile = make_int2(tiles[k].x & ((1 << KIND_SHIFT) - 1), tiles[k].y);
     const bool pml = k >= n_inner;
     const int next = k + gridDim.x;
     const int R0 = tile.x - K, C0 = tile.y - K, j0 = C0 + lj0, i0 = R0 + lr0;
@@ -818,7 +907,7 @@ void tb_invalidate(TBState* tb) {
 // rather than HBM bounds the step, and the halo recomputation would cost more than it saves.
 template <typename T>
 bool tb_supported(int nx, int ny) {
-  return sizeof(T) == 4 && nx >= 64 && ny >= 64;
+  return nx >= 64 && ny >= 64;  // both precisions: blocked beats one step per launch from here up
 }
 
 template <typename T, int RPT, int K, bool PML>
@@ -826,8 +915,7 @@ static cudaError_t tb_launch_one(const SimArgs<T>& a, const TBDst<T>& d, const i
                                  const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                  cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  using S = TBShape<T, RPT, K, PML>;
-  k_tb_step<T, RPT, K, PML><<<n, dim3(32, 8), S::SMEM, s>>>(a, d, tiles, ph, pe, step_off);
+  k_tb_step<T, RPT, K, PML><<<n, dim3(32, 8), tb_smem<T, RPT, K, PML>(), s>>>(a, d, tiles, ph, pe, step_off);
   g_launches += 1;
   return cudaGetLastError();
 }
@@ -896,10 +984,10 @@ static cudaError_t tb_two(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& 
 template <typename T, int RPT, int K>
 static cudaError_t tb_attrs() {
   cudaError_t e = cudaFuncSetAttribute(k_tb_step<T, RPT, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)TBShape<T, RPT, K, false>::SMEM);
+                                       (int)tb_smem<T, RPT, K, false>());
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_tb_step<T, RPT, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)TBShape<T, RPT, K, true>::SMEM);
+                             (int)tb_smem<T, RPT, K, true>());
   return e;
 }
 
@@ -958,12 +1046,12 @@ static cudaError_t tma_two(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>&
 }
 
 // Compiled shapes (rows = 8 * RPT, depth K); the CPML variant's six planes must fit 227 KB.
-#define ETG_TB_SHAPES_F32(X) X(ETG_F32, 4, 4) X(ETG_F32, 5, 4) X(ETG_F32, 6, 4) X(ETG_F32, 8, 4) X(ETG_F32, 8, 8)
-#define ETG_TB_SHAPES_F64(X) X(ETG_F64, 4, 2) X(ETG_F64, 5, 2) X(ETG_F64, 8, 2) X(ETG_F64, 8, 4)
+#define ETG_TB_SHAPES_F32(X) X(ETG_F32, 5, 4) X(ETG_F32, 6, 4) X(ETG_F32, 8, 4)
+#define ETG_TB_SHAPES_F64(X) X(ETG_F64, 4, 2) X(ETG_F64, 5, 2)
 
 // Shapes of the persistent TMA kernel: two stages of five planes must fit 227 KB.
-#define ETG_TMA_SHAPES_F32(X) X(ETG_F32, 4, 4) X(ETG_F32, 5, 4)
-#define ETG_TMA_SHAPES_F64(X) X(ETG_F64, 4, 2) X(ETG_F64, 5, 2)
+#define ETG_TMA_SHAPES_F32(X) X(ETG_F32, 5, 4)
+#define ETG_TMA_SHAPES_F64(X) X(ETG_F64, 5, 2)
 
 template <typename T>
 static TBFns<T> pick(const TBConfig& c, int mode) {
@@ -1024,13 +1112,19 @@ static void split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_
   std::vector<int2> inner, pml;
   for (int r0 = 0; r0 <= nx; r0 += OR)
     for (int c0 = 0; c0 <= ny; c0 += OC) {
-      const bool unit = r0 - K >= rlo && r0 + OR + K <= rhi && c0 - K >= clo && c0 + OC + K <= chi;
-      (unit ? inner : pml).push_back(make_int2(r0, c0));
+      const bool ux = r0 - K >= rlo && r0 + OR + K <= rhi, uy = c0 - K >= clo && c0 + OC + K <= chi;
+      if (ux && uy) {
+        inner.push_back(make_int2(r0, c0));
+      } else {  // unit columns: CPML across rows only (X); unit rows: across columns only (Y)
+        const int kind = uy ? KIND_X : ux ? KIND_Y : KIND_XY;
+        pml.push_back(make_int2(r0 | (kind << KIND_SHIFT), c0));
+      }
     }
   if (hot) {
     auto first = [&](std::vector<int2>& v) {
-      std::stable_partition(v.begin(), v.end(),
-                            [&](int2 t) { return hot->hits(t.x - K, t.y - K, ER, EC); });
+      std::stable_partition(v.begin(), v.end(), [&](int2 t) {
+        return hot->hits((t.x & ((1 << KIND_SHIFT) - 1)) - K, t.y - K, ER, EC);
+      });
     };
     first(inner);
     first(pml);
@@ -1107,7 +1201,8 @@ static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt, cons
     const int OR = 8 * tb->cfg.RPT - 2 * tb->cfg.K, OC = EC - 2 * tb->cfg.K;
     tb->owned_cells[0] = tb->owned_cells[1] = 0;
     for (int q = 0; q < (int)inner.size(); ++q) {
-      const int64_t r = std::max(0, std::min(OR, a.nx - inner[q].x)), c = std::max(0, std::min(OC, a.ny - inner[q].y));
+      const int64_t r = std::max(0, std::min(OR, a.nx - tb_tile_row(inner[q]))),
+                    c = std::max(0, std::min(OC, a.ny - inner[q].y));
       tb->owned_cells[q < tb->n_inner ? 0 : 1] += r * c;
     }
     cudaFree(tb->tiles);
@@ -1256,18 +1351,18 @@ template <typename T, int RPT, int K>
 static cudaError_t batch_pair(const void* sims, const int4* tiles, int n_inner, int n_pml, int parity,
                               int step_off, cudaStream_t main, cudaStream_t side, cudaEvent_t fork,
                               cudaEvent_t join) {
-  using SI = TBShape<T, RPT, K, false>;
-  using SP = TBShape<T, RPT, K, true>;
   const BatchSim<T>* b = (const BatchSim<T>*)sims;
   cudaError_t e = cudaEventRecord(fork, main);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork, 0);
   if (e == cudaSuccess && n_pml) {
-    k_tb_batch<T, RPT, K, true><<<n_pml, dim3(32, 8), SP::SMEM, side>>>(b, tiles + n_inner, parity, step_off);
+    k_tb_batch<T, RPT, K, true><<<n_pml, dim3(32, 8), tb_smem<T, RPT, K, true>(), side>>>(b, tiles + n_inner, parity,
+                                                                                         step_off);
     g_launches += 1;
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && n_inner) {
-    k_tb_batch<T, RPT, K, false><<<n_inner, dim3(32, 8), SI::SMEM, main>>>(b, tiles, parity, step_off);
+    k_tb_batch<T, RPT, K, false><<<n_inner, dim3(32, 8), tb_smem<T, RPT, K, false>(), main>>>(b, tiles, parity,
+                                                                                              step_off);
     g_launches += 1;
     e = cudaGetLastError();
   }
@@ -1279,10 +1374,10 @@ static cudaError_t batch_pair(const void* sims, const int4* tiles, int n_inner, 
 template <typename T, int RPT, int K>
 static cudaError_t batch_attrs() {
   cudaError_t e = cudaFuncSetAttribute(k_tb_batch<T, RPT, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)TBShape<T, RPT, K, false>::SMEM);
+                                       (int)tb_smem<T, RPT, K, false>());
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_tb_batch<T, RPT, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)TBShape<T, RPT, K, true>::SMEM);
+                             (int)tb_smem<T, RPT, K, true>());
   return e;
 }
 

@@ -32,8 +32,13 @@ int tb_batch_pair(int ER, int K, const void* sims, const int4* tiles, int n_inne
 template <typename T>
 int tb_batch_attrs(int ER, int K);
 // Output tiles of one grid, interior tiles first; tiles meeting a `hot` rectangle lead each kind.
+// A CPML tile carries its kind (1: CPML across rows, 2: across columns, 3: both) in bits
+// 28-29 of .x (tb_tile_row and tb_tile_kind take it apart).
 void tb_split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_hi, int ER, int EC, int K,
                     const std::vector<int4>& hot, std::vector<int2>* tiles, int* n_inner);
+
+inline int tb_tile_row(int2 t) { return t.x & ((1 << 28) - 1); }
+inline int tb_tile_kind(int2 t) { return t.x >> 28; }
 
 TBState* tb_create();
 void tb_destroy(TBState* tb);

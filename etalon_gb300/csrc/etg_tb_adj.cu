@@ -15,9 +15,10 @@
 // from a second lambda-psi buffer; both evaluate the same expressions in the same order on the
 // same inputs, so the two sweeps give the same bits, and a sweep may mix them freely.
 //
-// dJ/dcb accumulates in float64 in the owning tile, one add per node and step in descending
-// step order, like the one-step kernel; interior tiles keep the running sums of their output
-// cells in shared memory for the launch (read once, written once), CPML tiles add in place. Adjoint sources (the transposed DFT
+// dJ/dcb: the tiles over the design window record lambda E of the window at every step
+// (float, one slot per step of the launch block); k_adj_grad then adds the block's terms in
+// float64, one thread per node, in descending step order like the one-step kernel. Doing the
+// float64 sums in the few window tiles themselves made them the stragglers of every launch. Adjoint sources (the transposed DFT
 // monitors) come as per-node tables and are added wherever a tile holds the node.
 #include <algorithm>
 #include <cstring>
@@ -27,16 +28,19 @@
 
 namespace etg {
 
-template <typename T, int RPT, int K, bool PML>
+// Tile kinds as in the forward kernels: 0 interior, 1 CPML across rows (X), 2 across
+// columns (Y), 3 both; CPML tile lists carry the kind in bits 28-29 of the row (int2) or in .w.
+constexpr int AKIND_X = 1, AKIND_Y = 2, AKIND_XY = 3, AKIND_SHIFT = 28;
+
+template <typename T, int RPT, int K, int KIND>
 struct AdjShape {
   static constexpr int W = TBVec<T>::W;
   static constexpr int ER = 8 * RPT, EC = 32 * W, OR = ER - 2 * K, OC = EC - 2 * K;
   static constexpr int PL = ER * EC;
-  static constexpr int PLANES = PML ? 6 : 2;  // cb_ex, cb_ey (+ 4 lambda-psi)
+  // cb_ex, cb_ey, then lambda psi_hz_x, psi_ey_x (x kinds), then psi_hz_y, psi_ex_y (y kinds)
+  static constexpr int PLANES = 2 + ((KIND & AKIND_X) ? 2 : 0) + ((KIND & AKIND_Y) ? 2 : 0);
   static constexpr int XCH = 9 * EC;          // one exchange plane (gy or hy): 8 warps + a zero row
-  // interior tiles also hold the float64 dJ/dcb of their output cells while they run
-  static constexpr int GACC = PML ? 0 : 2 * OR * OC;
-  static constexpr size_t SMEM = ((size_t)PLANES * PL + 2 * XCH) * sizeof(T) + (size_t)GACC * sizeof(double);
+  static constexpr size_t SMEM = ((size_t)PLANES * PL + 2 * XCH) * sizeof(T);
   static constexpr int MIN_BLOCKS = 1;
   static_assert(K % W == 0, "the halo must keep vectors aligned");
   static_assert(OR > 0 && OC > 0, "halo larger than the tile");
@@ -63,19 +67,22 @@ __device__ __forceinline__ void adj_inject(const AdjSrc<T>* src, uint32_t rel, T
   }
 }
 
-template <typename T, int RPT, int K, bool PML>
-__device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 tile, int64_t n_hi) {
-  using S = AdjShape<T, RPT, K, PML>;
+// CPML tiles of kind X (Y) have unit y (x) coefficients on every column (row) and advance
+// lambda psi only on strip rows (columns), as the forward kernels do; XY tiles (corners)
+// evaluate the one-step kernels' full expressions everywhere.
+template <typename T, int RPT, int K, int KIND>
+__device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 tile, int step_off) {
+  using S = AdjShape<T, RPT, K, KIND>;
   using Vw = TBVec<T>;
   constexpr int W = S::W, ER = S::ER, EC = S::EC, PL = S::PL;
+  constexpr bool PML = KIND != 0, PX = (KIND & AKIND_X) != 0, PY = (KIND & AKIND_Y) != 0;
   extern __shared__ __align__(16) unsigned char adj_smem[];
   T* const sCbx = reinterpret_cast<T*>(adj_smem);
   T* const sCby = sCbx + PL;
-  T* const sPsi = sCby + PL;              // CPML tiles: lambda psi_hz_x, psi_hz_y, psi_ex_y, psi_ey_x
+  T* const sPsiX = sCby + PL;                   // x kinds: lambda psi_hz_x, psi_ey_x
+  T* const sPsiY = sPsiX + (PX ? 2 * PL : 0);   // y kinds: lambda psi_hz_y, psi_ex_y
   T* const sGy = sCbx + S::PLANES * PL;   // [k]: gy of warp k's first row; [8] = zeros
   T* const sHy = sGy + S::XCH;            // [k + 1]: hy of warp k's last row; [0] = zeros
-  // interior tiles: dJ/dcb_ex, dJ/dcb_ey of the output cells ((row - K) * OC + column - K)
-  double* const sGrad = reinterpret_cast<double*>(sHy + S::XCH);
   __shared__ uint32_t s_rel[2];
 
   const SimArgs<T>& s = a.s;
@@ -131,19 +138,34 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
     }
     cx.st(sCbx + o);
     cy.st(sCby + o);
-    if (PML) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        Vw p;
-        if (in) p.ld(a.in[3 + q] + g);
-        else p.zero();
-        p.st(sPsi + q * PL + o);
+    if (PX) {  // strip rows only (every row in corner tiles)
+      Vw p0, p1;
+      if (in && (KIND == AKIND_XY || i < s.xs_lo || i >= s.xs_hi)) {
+        p0.ld(a.in[3] + g);  // lambda psi_hz_x
+        p1.ld(a.in[6] + g);  // lambda psi_ey_x
+      } else {
+        p0.zero();
+        p1.zero();
       }
+      p0.st(sPsiX + o);
+      p1.st(sPsiX + PL + o);
+    }
+    if (PY) {  // vectors meeting a strip column only
+      Vw p0, p1;
+      if (in && (KIND == AKIND_XY || j0 < s.ys_lo || j0 + W > s.ys_hi)) {
+        p0.ld(a.in[4] + g);  // lambda psi_hz_y
+        p1.ld(a.in[5] + g);  // lambda psi_ex_y
+      } else {
+        p0.zero();
+        p1.zero();
+      }
+      p0.st(sPsiY + o);
+      p1.st(sPsiY + PL + o);
     }
   }
   T byh[W], cyh[W], kyh[W], bye[W], cye[W], kye[W];
   T bxh[RPT], cxh[RPT], kxh[RPT], bxe[RPT], cxe[RPT], kxe[RPT];
-  if (PML) {
+  if (PY) {
 #pragma unroll
     for (int e = 0; e < W; ++e) {
       const int j = min(max(j0 + e, 0), ny - 1), je = min(max(j0 + e, 0), ny);
@@ -154,6 +176,8 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
       cye[e] = s.cy_e[je];
       kye[e] = s.iky_e[je];
     }
+  }
+  if (PX) {
 #pragma unroll
     for (int t = 0; t < RPT; ++t) {
       const int i = min(max(i0 + t, 0), nx - 1), ie = min(max(i0 + t, 0), nx);
@@ -166,15 +190,19 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
     }
   }
   const T db = s.db, idx = s.inv_dx, idy = s.inv_dy;
+  const int64_t n_hi = a.ctl[0] - step_off, trace_n0 = a.ctl[1];
 
   // Transposed E update of the Ex node of cell (t, e): dJ/d(dHz/dy); advances lambda psi_ex_y.
-  auto gx_own = [&](int t, int e) -> T {
-    const T lc = mul(sCbx[(lr0 + t) * EC + lj0 + e], lex[t].v[e]);
+  // (the one-step kernel's "iky·lc" with 1/kappa = 1 exactly is lc itself; the domain checks
+  // a kind's rows or columns always pass are left out)
+  auto gx_own = [&](int t, int e, T cb) -> T {
+    const T lc = mul(cb, lex[t].v[e]);
     if (!PML) return lc;  // 1/kappa = 1 exactly, no psi
     const int i = i0 + t, j = j0 + e;
-    if (j < 1 || j > ny - 1 || i < 0 || i >= nx) return zero<T>();
+    if ((PY && (j < 1 || j > ny - 1)) || (PX && (i < 0 || i >= nx))) return zero<T>();
+    if (!PY) return lc;
     if (j < s.ys_lo || j >= s.ys_hi) {
-      T* pp = sPsi + 2 * PL + (lr0 + t) * EC + lj0 + e;
+      T* pp = sPsiY + PL + (lr0 + t) * EC + lj0 + e;
       const T lpt = add(*pp, lc);
       *pp = mul(bye[e], lpt);
       return add(mul(kye[e], lc), mul(cye[e], lpt));
@@ -182,13 +210,14 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
     return mul(kye[e], lc);
   };
   // Transposed E update of the Ey node: dJ/d(dHz/dx); advances lambda psi_ey_x.
-  auto gy_own = [&](int t, int e) -> T {
-    const T lc = -mul(sCby[(lr0 + t) * EC + lj0 + e], ley[t].v[e]);
+  auto gy_own = [&](int t, int e, T cb) -> T {
+    const T lc = -mul(cb, ley[t].v[e]);
     if (!PML) return lc;
     const int i = i0 + t, j = j0 + e;
-    if (i < 1 || i > nx - 1 || j < 0 || j >= ny) return zero<T>();
+    if ((PX && (i < 1 || i > nx - 1)) || (PY && (j < 0 || j >= ny))) return zero<T>();
+    if (!PX) return lc;
     if (i < s.xs_lo || i >= s.xs_hi) {
-      T* pp = sPsi + 3 * PL + (lr0 + t) * EC + lj0 + e;
+      T* pp = sPsiX + PL + (lr0 + t) * EC + lj0 + e;
       const T lpt = add(*pp, lc);
       *pp = mul(bxe[t], lpt);
       return add(mul(kxe[t], lc), mul(cxe[t], lpt));
@@ -204,20 +233,24 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
       return;
     }
     const int i = i0 + t, j = j0 + e;
-    if (i < 0 || i >= nx || j < 0 || j >= ny) {
+    if ((PX && (i < 0 || i >= nx)) || (PY && (j < 0 || j >= ny))) {
       *hx = *hy = zero<T>();
       return;
     }
-    if (j < s.ys_lo || j >= s.ys_hi) {
-      T* pp = sPsi + 1 * PL + (lr0 + t) * EC + lj0 + e;
+    if (!PY) {
+      *hx = la;
+    } else if (j < s.ys_lo || j >= s.ys_hi) {
+      T* pp = sPsiY + (lr0 + t) * EC + lj0 + e;
       const T lpt = add(*pp, la);
       *pp = mul(byh[e], lpt);
       *hx = add(mul(kyh[e], la), mul(cyh[e], lpt));
     } else {
       *hx = mul(kyh[e], la);
     }
-    if (i < s.xs_lo || i >= s.xs_hi) {
-      T* pp = sPsi + 0 * PL + (lr0 + t) * EC + lj0 + e;
+    if (!PX) {
+      *hy = -la;
+    } else if (i < s.xs_lo || i >= s.xs_hi) {
+      T* pp = sPsiX + (lr0 + t) * EC + lj0 + e;
       const T lpt = sub(*pp, la);
       *pp = mul(bxh[t], lpt);
       *hy = add(-mul(kxh[t], la), mul(cxh[t], lpt));
@@ -228,63 +261,41 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
 
   __syncthreads();  // cb (and lambda psi) staged
   T gyf[W];         // gy of this warp's first row for the next RE
+  {
+    Vw cy;
+    cy.ld(sCby + lr0 * EC + lj0);
 #pragma unroll
-  for (int e = 0; e < W; ++e) {
-    gyf[e] = gy_own(0, e);
-    sGy[ty * EC + lj0 + e] = gyf[e];
+    for (int e = 0; e < W; ++e) gyf[e] = gy_own(0, e, cy.v[e]);
+    Vw g;
+#pragma unroll
+    for (int e = 0; e < W; ++e) g.v[e] = gyf[e];
+    g.st(sGy + ty * EC + lj0);
   }
   __syncthreads();
 
   const uint32_t relH = s_rel[0], relE = s_rel[1];
   const int t_lo = max(0, K - lr0), t_hi = min(RPT, ER - K - lr0);
   const int e_lo = lj0 >= K ? 0 : W, e_hi = lj0 + W <= EC - K ? W : 0;
-  const bool designed = a.gx && a.i0 <= tile.x + S::OR - 1 && a.i0 + a.nxd >= tile.x &&
+  const bool designed = a.ltrace && a.i0 <= tile.x + S::OR - 1 && a.i0 + a.nxd >= tile.x &&
                         a.j0 <= tile.y + S::OC - 1 && a.j0 + a.nyd >= tile.y;
-  // dJ/dcb slot of output cell (t, e) and component c: global (CPML tiles) or shared memory
-  auto in_gx = [&](int i, int j) { return i >= a.i0 && i < a.i0 + a.nxd && j >= a.j0 && j <= a.j0 + a.nyd; };
-  auto in_gy = [&](int i, int j) { return i >= a.i0 && i <= a.i0 + a.nxd && j >= a.j0 && j < a.j0 + a.nyd; };
-  auto gslot = [&](int t, int e, int c) -> double* {
-    const int i = i0 + t, j = j0 + e;
-    if (PML) return c == 0 ? a.gx + (int64_t)(i - a.i0) * (a.nyd + 1) + (j - a.j0)
-                           : a.gy + (int64_t)(i - a.i0) * a.nyd + (j - a.j0);
-    return sGrad + c * S::OR * S::OC + (lr0 + t - K) * S::OC + (lj0 + e - K);
-  };
-  if (!PML && designed) {  // the running sums of the owned window cells come in once per launch
-#pragma unroll
-    for (int t = 0; t < RPT; ++t) {
-      if (t < t_lo || t >= t_hi) continue;
-#pragma unroll
-      for (int e = 0; e < W; ++e) {
-        if (e < e_lo || e >= e_hi) continue;
-        const int i = i0 + t, j = j0 + e;
-        if (in_gx(i, j)) *gslot(t, e, 0) = a.gx[(int64_t)(i - a.i0) * (a.nyd + 1) + (j - a.j0)];
-        if (in_gy(i, j)) *gslot(t, e, 1) = a.gy[(int64_t)(i - a.i0) * a.nyd + (j - a.j0)];
-      }
-    }
-  }
+  const int wy = a.nyd + 1;
+  const int64_t wbox = (int64_t)(a.nxd + 1) * wy;
 
   for (int st = 0; st < K; ++st) {
     const int64_t n = n_hi - 1 - st;
-    // ------------------------------------------------ gradient of step n (lambda E of n + 1)
+    // ------------------------------------------------ lambda E of n + 1 on the window, for dJ/dcb
     if (designed) {
-      const T* tr = a.trace + (n - a.trace_n0) * a.tnx * a.tny;
+      T* lt = a.ltrace + (a.ctl[0] - 1 - n) * 2 * wbox;
 #pragma unroll
       for (int t = 0; t < RPT; ++t) {
-        const int i = i0 + t;
-        if (t < t_lo || t >= t_hi) continue;
+        const int di = i0 + t - a.i0;
+        if (t < t_lo || t >= t_hi || (unsigned)di > (unsigned)a.nxd) continue;
 #pragma unroll
         for (int e = 0; e < W; ++e) {
-          const int j = j0 + e;
-          if (e < e_lo || e >= e_hi) continue;
-          const int ri = i - a.ti0, rj = j - a.tj0;
-          if (in_gx(i, j)) {
-            const T c = add(mul(sub(tr[ri * a.tny + rj], tr[ri * a.tny + rj - 1]), idy), zero<T>());
-            *gslot(t, e, 0) += (double)lex[t].v[e] * (double)c;
-          }
-          if (in_gy(i, j)) {
-            const T c = add(mul(sub(tr[ri * a.tny + rj], tr[(ri - 1) * a.tny + rj]), idx), zero<T>());
-            *gslot(t, e, 1) -= (double)ley[t].v[e] * (double)c;
-          }
+          const int dj = j0 + e - a.j0;
+          if (e < e_lo || e >= e_hi || (unsigned)dj > (unsigned)a.nyd) continue;
+          lt[(int64_t)di * wy + dj] = lex[t].v[e];
+          lt[wbox + (int64_t)di * wy + dj] = ley[t].v[e];
         }
       }
     }
@@ -296,16 +307,22 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
 #pragma unroll
       for (int t = 0; t < RPT; ++t) {
         T gxr[W];
+        Vw cx;
+        cx.ld(sCbx + (lr0 + t) * EC + lj0);
 #pragma unroll
-        for (int e = 0; e < W; ++e) gxr[e] = gx_own(t, e);
+        for (int e = 0; e < W; ++e) gxr[e] = gx_own(t, e, cx.v[e]);
         T gxn = __shfl_down_sync(0xffffffffu, gxr[0], 1);
         if (lane == 31) gxn = zero<T>();
         if (t < RPT - 1) {
+          Vw cy;
+          cy.ld(sCby + (lr0 + t + 1) * EC + lj0);
 #pragma unroll
-          for (int e = 0; e < W; ++e) gyn[e] = gy_own(t + 1, e);
+          for (int e = 0; e < W; ++e) gyn[e] = gy_own(t + 1, e, cy.v[e]);
         } else {
+          Vw g;
+          g.ld(sGy + (ty + 1) * EC + lj0);
 #pragma unroll
-          for (int e = 0; e < W; ++e) gyn[e] = sGy[(ty + 1) * EC + lj0 + e];
+          for (int e = 0; e < W; ++e) gyn[e] = g.v[e];
         }
 #pragma unroll
         for (int e = 0; e < W; ++e) {
@@ -316,7 +333,7 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
             lhz[t].v[e] = u;
           } else {
             const int i = i0 + t, j = j0 + e;
-            if (i >= 0 && i < nx && j >= 0 && j < ny) lhz[t].v[e] = u;
+            if ((!PX || (i >= 0 && i < nx)) && (!PY || (j >= 0 && j < ny))) lhz[t].v[e] = u;
           }
           gyc[e] = gyn[e];
         }
@@ -324,17 +341,25 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
     }
     if (relH) adj_inject<T, RPT, W>(a.hsrc, relH, lex, ley, lhz, i0, j0, n);
     T hxl[W], hyl[W];  // this warp's last row, computed once and shared
+    {
+      Vw g;
 #pragma unroll
-    for (int e = 0; e < W; ++e) {
-      h_own(RPT - 1, e, &hxl[e], &hyl[e]);
-      sHy[(ty + 1) * EC + lj0 + e] = hyl[e];
+      for (int e = 0; e < W; ++e) {
+        h_own(RPT - 1, e, &hxl[e], &hyl[e]);
+        g.v[e] = hyl[e];
+      }
+      g.st(sHy + (ty + 1) * EC + lj0);
     }
     __syncthreads();
     // ------------------------------------------------ RH(n): lambda E (+ DFT-E term of n - 1)
     {
       T hyp[W];
+      {
+        Vw g;
+        g.ld(sHy + ty * EC + lj0);
 #pragma unroll
-      for (int e = 0; e < W; ++e) hyp[e] = sHy[ty * EC + lj0 + e];
+        for (int e = 0; e < W; ++e) hyp[e] = g.v[e];
+      }
 #pragma unroll
       for (int t = 0; t < RPT; ++t) {
         T hxc[W], hyc[W];
@@ -364,8 +389,8 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
             ley[t].v[e] = vy;
           } else {
             const int i = i0 + t, j = j0 + e;
-            if (i >= 0 && i < nx && j >= 0 && j <= ny) lex[t].v[e] = vx;
-            if (i >= 0 && i <= nx && j >= 0 && j < ny) ley[t].v[e] = vy;
+            if ((!PX || (i >= 0 && i < nx)) && (!PY || (j >= 0 && j <= ny))) lex[t].v[e] = vx;
+            if ((!PX || (i >= 0 && i <= nx)) && (!PY || (j >= 0 && j < ny))) ley[t].v[e] = vy;
           }
           hyp[e] = hyc[e];
         }
@@ -373,28 +398,18 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
     }
     if (relE && n >= 1) adj_inject<T, RPT, W>(a.esrc, relE, lex, ley, lhz, i0, j0, n - 1);
     if (st < K - 1) {
+      Vw cy, g;
+      cy.ld(sCby + lr0 * EC + lj0);
 #pragma unroll
       for (int e = 0; e < W; ++e) {
-        gyf[e] = gy_own(0, e);
-        sGy[ty * EC + lj0 + e] = gyf[e];
+        gyf[e] = gy_own(0, e, cy.v[e]);
+        g.v[e] = gyf[e];
       }
+      g.st(sGy + ty * EC + lj0);
     }
     __syncthreads();
   }
 
-  if (!PML && designed) {  // running sums back, in the order they were taken
-#pragma unroll
-    for (int t = 0; t < RPT; ++t) {
-      if (t < t_lo || t >= t_hi) continue;
-#pragma unroll
-      for (int e = 0; e < W; ++e) {
-        if (e < e_lo || e >= e_hi) continue;
-        const int i = i0 + t, j = j0 + e;
-        if (in_gx(i, j)) a.gx[(int64_t)(i - a.i0) * (a.nyd + 1) + (j - a.j0)] = *gslot(t, e, 0);
-        if (in_gy(i, j)) a.gy[(int64_t)(i - a.i0) * a.nyd + (j - a.j0)] = *gslot(t, e, 1);
-      }
-    }
-  }
   if (e_lo != 0 || e_hi != W || !lane_in) return;
 #pragma unroll
   for (int t = 0; t < RPT; ++t) {
@@ -404,29 +419,105 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
     lex[t].st(a.out[0] + g);
     ley[t].st(a.out[1] + g);
     lhz[t].st(a.out[2] + g);
-    if (PML) {  // lambda psi stays +0 outside its strips in both buffers
-      const int o = (lr0 + t) * EC + lj0;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        Vw v;
-        v.ld(sPsi + q * PL + o);
-        v.st(a.out[3 + q] + g);
-      }
+    // lambda psi stays +0 outside its strips in both buffers
+    const int o = (lr0 + t) * EC + lj0;
+    if (PX && (KIND == AKIND_XY || i < s.xs_lo || i >= s.xs_hi)) {
+      Vw v;
+      v.ld(sPsiX + o);
+      v.st(a.out[3] + g);
+      v.ld(sPsiX + PL + o);
+      v.st(a.out[6] + g);
+    }
+    if (PY && (KIND == AKIND_XY || j0 < s.ys_lo || j0 + W > s.ys_hi)) {
+      Vw v;
+      v.ld(sPsiY + o);
+      v.st(a.out[4] + g);
+      v.ld(sPsiY + PL + o);
+      v.st(a.out[5] + g);
     }
   }
 }
 
 template <typename T, int RPT, int K, bool PML>
-__global__ void __launch_bounds__(TB_THREADS, 1)
-k_tb_adj(const __grid_constant__ TBAdjArgs<T> a, const int2* __restrict__ tiles, int64_t n_hi) {
-  tb_adj_tile<T, RPT, K, PML>(a, tiles[blockIdx.x], n_hi);
+constexpr size_t adj_smem() {
+  return PML ? AdjShape<T, RPT, K, AKIND_XY>::SMEM : AdjShape<T, RPT, K, 0>::SMEM;
+}
+
+template <typename T, int RPT, int K, bool PML>
+__device__ __forceinline__ void adj_dispatch(const TBAdjArgs<T>& a, int r0, int c0, int kind, int step_off) {
+  const int2 u = make_int2(r0, c0);
+  if (!PML) {
+    tb_adj_tile<T, RPT, K, 0>(a, u, step_off);
+    return;
+  }
+  switch (kind) {
+    case AKIND_X: tb_adj_tile<T, RPT, K, AKIND_X>(a, u, step_off); break;
+    case AKIND_Y: tb_adj_tile<T, RPT, K, AKIND_Y>(a, u, step_off); break;
+    default: tb_adj_tile<T, RPT, K, AKIND_XY>(a, u, step_off); break;
+  }
 }
 
 template <typename T, int RPT, int K, bool PML>
 __global__ void __launch_bounds__(TB_THREADS, 1)
-k_tb_adj_batch(const TBAdjArgs<T>* __restrict__ args, const int4* __restrict__ tiles, int parity, int64_t n_hi) {
-  const int4 t = tiles[blockIdx.x];  // simulation, r0, c0
-  tb_adj_tile<T, RPT, K, PML>(args[2 * t.x + parity], make_int2(t.y, t.z), n_hi);
+k_tb_adj(const __grid_constant__ TBAdjArgs<T> a, const int2* __restrict__ tiles, int step_off) {
+  const int2 t = tiles[blockIdx.x];
+  adj_dispatch<T, RPT, K, PML>(a, t.x & ((1 << AKIND_SHIFT) - 1), t.y, t.x >> AKIND_SHIFT, step_off);
+}
+
+template <typename T, int RPT, int K, bool PML>
+__global__ void __launch_bounds__(TB_THREADS, 1)
+k_tb_adj_batch(const TBAdjArgs<T>* __restrict__ args, const int4* __restrict__ tiles, int parity, int step_off) {
+  const int4 t = tiles[blockIdx.x];  // simulation, r0, c0, kind
+  adj_dispatch<T, RPT, K, PML>(args[2 * t.x + parity], t.y, t.z, t.w, step_off);
+}
+
+__global__ void k_adj_ctl_add(int64_t* ctl, int64_t delta) { ctl[0] += delta; }
+
+// dJ/dcb += the window's terms of steps ctl[0]-1 … ctl[0]-n_slots for design blockIdx.y
+// (args[stride * design]): one thread per Ex or Ey node, float64, in descending step order —
+// the one-step kernel's additions in its order, spread over the whole GPU.
+template <typename T>
+__global__ void k_adj_grad(const TBAdjArgs<T>* __restrict__ args, int stride, int n_slots) {
+  const TBAdjArgs<T>& a = args[stride * blockIdx.y];
+  const int nx_ = a.nxd, ny_ = a.nyd, wy = ny_ + 1;
+  const int64_t n_ex = (int64_t)nx_ * wy, n_ey = (int64_t)(nx_ + 1) * ny_;
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n_ex + n_ey) return;
+  const bool is_ex = q < n_ex;
+  const int64_t qq = is_ex ? q : q - n_ex;
+  const int di = (int)(is_ex ? qq / wy : qq / ny_), dj = (int)(is_ex ? qq % wy : qq % ny_);
+  const int ri = di + a.i0 - a.ti0, rj = dj + a.j0 - a.tj0;
+  const int64_t wbox = (int64_t)(nx_ + 1) * wy, top = a.ctl[0], n0 = a.ctl[1];
+  double* const gp = is_ex ? a.gx + qq : a.gy + qq;
+  double g = *gp;
+  const T idx = a.s.inv_dx, idy = a.s.inv_dy;
+  for (int k = 0; k < n_slots; ++k) {
+    const T* tr = a.trace + (top - 1 - k - n0) * a.tnx * a.tny;
+    const T* lt = a.ltrace + (int64_t)k * 2 * wbox;
+    if (is_ex) {
+      const T c = add(mul(sub(tr[ri * a.tny + rj], tr[ri * a.tny + rj - 1]), idy), zero<T>());
+      g += (double)lt[(int64_t)di * wy + dj] * (double)c;
+    } else {
+      const T c = add(mul(sub(tr[ri * a.tny + rj], tr[(ri - 1) * a.tny + rj]), idx), zero<T>());
+      g -= (double)lt[wbox + (int64_t)di * wy + dj] * (double)c;
+    }
+  }
+  *gp = g;
+}
+
+template <typename T>
+void tb_adj_grad(const TBAdjArgs<T>* args, int stride, int n_designs, int64_t max_nodes, int n_slots, cudaStream_t s) {
+  const dim3 grid((unsigned)((max_nodes + 127) / 128), (unsigned)n_designs);
+  k_adj_grad<T><<<grid, 128, 0, s>>>(args, stride, n_slots);
+  g_launches += 1;
+}
+
+template void tb_adj_grad<float>(const TBAdjArgs<float>*, int, int, int64_t, int, cudaStream_t);
+template void tb_adj_grad<double>(const TBAdjArgs<double>*, int, int, int64_t, int, cudaStream_t);
+
+void tb_adj_ctl_add(int64_t* ctl, int64_t delta, cudaStream_t s) {
+  k_adj_ctl_add<<<1, 1, 0, s>>>(ctl, delta);
+  g_launches += 1;
 }
 
 // ------------------------------------------------------------------------ host side
@@ -459,28 +550,28 @@ template <typename T>
 int tb_adj_attrs() {
   constexpr int RPT = AdjCfg<T>::RPT, K = AdjCfg<T>::K;
   ETG_TRY_CUDA(cudaFuncSetAttribute(k_tb_adj<T, RPT, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)AdjShape<T, RPT, K, false>::SMEM));
+                                    (int)adj_smem<T, RPT, K, false>()));
   ETG_TRY_CUDA(cudaFuncSetAttribute(k_tb_adj<T, RPT, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)AdjShape<T, RPT, K, true>::SMEM));
+                                    (int)adj_smem<T, RPT, K, true>()));
   ETG_TRY_CUDA(cudaFuncSetAttribute(k_tb_adj_batch<T, RPT, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)AdjShape<T, RPT, K, false>::SMEM));
+                                    (int)adj_smem<T, RPT, K, false>()));
   ETG_TRY_CUDA(cudaFuncSetAttribute(k_tb_adj_batch<T, RPT, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)AdjShape<T, RPT, K, true>::SMEM));
+                                    (int)adj_smem<T, RPT, K, true>()));
   return ETG_OK;
 }
 
 template <typename T>
-int tb_adj_launch(const TBAdjArgs<T>& a, const int2* tiles, int n_inner, int n_pml, int64_t n_hi,
+int tb_adj_launch(const TBAdjArgs<T>& a, const int2* tiles, int n_inner, int n_pml, int step_off,
                   cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
   constexpr int RPT = AdjCfg<T>::RPT, K = AdjCfg<T>::K;
   ETG_TRY_CUDA(cudaEventRecord(fork, main));
   ETG_TRY_CUDA(cudaStreamWaitEvent(side, fork, 0));
   if (n_pml) {
-    k_tb_adj<T, RPT, K, true><<<n_pml, dim3(32, 8), AdjShape<T, RPT, K, true>::SMEM, side>>>(a, tiles + n_inner, n_hi);
+    k_tb_adj<T, RPT, K, true><<<n_pml, dim3(32, 8), adj_smem<T, RPT, K, true>(), side>>>(a, tiles + n_inner, step_off);
     g_launches += 1;
   }
   if (n_inner) {
-    k_tb_adj<T, RPT, K, false><<<n_inner, dim3(32, 8), AdjShape<T, RPT, K, false>::SMEM, main>>>(a, tiles, n_hi);
+    k_tb_adj<T, RPT, K, false><<<n_inner, dim3(32, 8), adj_smem<T, RPT, K, false>(), main>>>(a, tiles, step_off);
     g_launches += 1;
   }
   ETG_TRY_CUDA(cudaGetLastError());
@@ -491,18 +582,18 @@ int tb_adj_launch(const TBAdjArgs<T>& a, const int2* tiles, int n_inner, int n_p
 
 template <typename T>
 int tb_adj_batch_launch(const TBAdjArgs<T>* args, const int4* tiles, int n_inner, int n_pml, int parity,
-                        int64_t n_hi, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+                        int step_off, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
   constexpr int RPT = AdjCfg<T>::RPT, K = AdjCfg<T>::K;
   ETG_TRY_CUDA(cudaEventRecord(fork, main));
   ETG_TRY_CUDA(cudaStreamWaitEvent(side, fork, 0));
   if (n_pml) {
-    k_tb_adj_batch<T, RPT, K, true><<<n_pml, dim3(32, 8), AdjShape<T, RPT, K, true>::SMEM, side>>>(
-        args, tiles + n_inner, parity, n_hi);
+    k_tb_adj_batch<T, RPT, K, true><<<n_pml, dim3(32, 8), adj_smem<T, RPT, K, true>(), side>>>(
+        args, tiles + n_inner, parity, step_off);
     g_launches += 1;
   }
   if (n_inner) {
-    k_tb_adj_batch<T, RPT, K, false><<<n_inner, dim3(32, 8), AdjShape<T, RPT, K, false>::SMEM, main>>>(
-        args, tiles, parity, n_hi);
+    k_tb_adj_batch<T, RPT, K, false><<<n_inner, dim3(32, 8), adj_smem<T, RPT, K, false>(), main>>>(
+        args, tiles, parity, step_off);
     g_launches += 1;
   }
   ETG_TRY_CUDA(cudaGetLastError());
@@ -513,13 +604,13 @@ int tb_adj_batch_launch(const TBAdjArgs<T>* args, const int4* tiles, int n_inner
 
 template int tb_adj_attrs<float>();
 template int tb_adj_attrs<double>();
-template int tb_adj_launch<float>(const TBAdjArgs<float>&, const int2*, int, int, int64_t, cudaStream_t, cudaStream_t,
+template int tb_adj_launch<float>(const TBAdjArgs<float>&, const int2*, int, int, int, cudaStream_t, cudaStream_t,
                                   cudaEvent_t, cudaEvent_t);
-template int tb_adj_launch<double>(const TBAdjArgs<double>&, const int2*, int, int, int64_t, cudaStream_t,
-                                   cudaStream_t, cudaEvent_t, cudaEvent_t);
-template int tb_adj_batch_launch<float>(const TBAdjArgs<float>*, const int4*, int, int, int, int64_t, cudaStream_t,
+template int tb_adj_launch<double>(const TBAdjArgs<double>&, const int2*, int, int, int, cudaStream_t, cudaStream_t,
+                                   cudaEvent_t, cudaEvent_t);
+template int tb_adj_batch_launch<float>(const TBAdjArgs<float>*, const int4*, int, int, int, int, cudaStream_t,
                                         cudaStream_t, cudaEvent_t, cudaEvent_t);
-template int tb_adj_batch_launch<double>(const TBAdjArgs<double>*, const int4*, int, int, int, int64_t, cudaStream_t,
+template int tb_adj_batch_launch<double>(const TBAdjArgs<double>*, const int4*, int, int, int, int, cudaStream_t,
                                          cudaStream_t, cudaEvent_t, cudaEvent_t);
 
 }  // namespace etg

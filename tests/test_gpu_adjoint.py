@@ -211,3 +211,41 @@ def test_batched_gradients_equal_single_design_gradients(gpu, precision, stride)
     batch.close()
     for r in runners:
         r.close()
+
+
+def test_single_design_workload_gradient_vs_central_differences(gpu):
+    """The 1224² single-design workload (100×100 cells of smoothed random ε, 3 λ), shortened to
+    3000 steps: float64 dJ/dε of 20 random design cells against central differences (h = 1e-3
+    relative), and the float32 blocked gradient within 1e-3 of the float64 one."""
+    from tests import cases
+
+    n = 3000
+    p64, win = cases.adjoint_device("double", n_steps=n)
+    d = DesignRegion.from_box(p64, win[:2], win[2:])
+    eps0 = torch.as_tensor(cases.smooth_design(d.nx, d.ny, 0))
+    r = AdjointRunner(p64, d, stride=AdjointRunner.sqrt_stride(n))
+    eps = eps0.clone().requires_grad_(True)
+    point_power(simulate(eps, r)[0], p64.samplings[0]).backward()
+    g64 = eps.grad.numpy().copy()
+    assert np.abs(g64).max() > 0
+    rng = np.random.default_rng(11)
+    cells = rng.choice(d.nx * d.ny, 20, replace=False)
+    scale = np.abs(g64).max()
+    for q in cells:
+        a, b = divmod(int(q), d.ny)
+        h = 1e-3 * float(eps0[a, b])
+        vals = []
+        for sign in (1, -1):
+            e = eps0.clone()
+            e[a, b] += sign * h
+            with torch.no_grad():
+                vals.append(float(point_power(simulate(e, r)[0], p64.samplings[0])))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        assert g64[a, b] == pytest.approx(fd, rel=1e-3, abs=1e-4 * scale)
+    r.close()
+    p32, _ = cases.adjoint_device("single", n_steps=n)
+    r32 = AdjointRunner(p32, d, stride=AdjointRunner.sqrt_stride(n))
+    eps = eps0.clone().requires_grad_(True)
+    point_power(simulate(eps, r32)[0], p32.samplings[0]).backward()
+    r32.close()
+    assert _rel(eps.grad.numpy(), g64) < 1e-3

@@ -235,6 +235,9 @@ struct etg_adj {
   std::vector<int4> hnodes, enodes;  // i, j, comp
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+  cudaStream_t sides[3] = {};                    // one branch per CPML kind
+  cudaEvent_t joins[3] = {};
+  int n_kind[3] = {};                            // CPML tiles of each kind (the list is sorted by kind)
   int64_t* d_ctl = nullptr;                      // top step of the launch block, trace origin
   std::map<int64_t, cudaGraphExec_t> graphs;     // key: pairs per graph * 2 + lambda-psi parity
   etg_batch* fwd1 = nullptr;                     // segment recompute with the plans in device memory
@@ -389,11 +392,11 @@ int backward_sweep(etg_adj* A, int64_t n_hi, int64_t n_lo, int64_t trace_n0, int
       tb_adj_ctl_add(A->d_ctl, -2 * K * n_pairs, s->stream);
     };
     auto pair = [&](int64_t p) {
-      int rc = tb_adj_launch<T>(to_alt, A->tiles, A->n_inner, A->n_pml, (int)(2 * K * p), s->stream, A->side, A->fork,
-                                A->join);
+      int rc = tb_adj_launch<T>(to_alt, A->tiles, A->n_inner, A->n_kind, (int)(2 * K * p), s->stream, A->sides,
+                                A->fork, A->joins);
       if (rc == ETG_OK)
-        rc = tb_adj_launch<T>(back, A->tiles, A->n_inner, A->n_pml, (int)(2 * K * p + K), s->stream, A->side,
-                              A->fork, A->join);
+        rc = tb_adj_launch<T>(back, A->tiles, A->n_inner, A->n_kind, (int)(2 * K * p + K), s->stream, A->sides,
+                              A->fork, A->joins);
       return rc;
     };
     const int64_t per_graph = std::max<int64_t>(1, s->opt[ETG_OPT_GRAPH_STEPS] / (2 * K));
@@ -560,6 +563,8 @@ int prepare_tb(etg_adj* A, const AdjPlan<T>& ph, const AdjPlan<T>& pe) {
   std::vector<int2> tiles;
   tb_split_tiles(s->nx, s->ny, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi, ER, EC, K, hot, &tiles, &A->n_inner);
   A->n_pml = (int)tiles.size() - A->n_inner;
+  for (int k = 0; k < 3; ++k) A->n_kind[k] = 0;
+  for (int q = A->n_inner; q < (int)tiles.size(); ++q) A->n_kind[tb_tile_kind(tiles[q]) - 1] += 1;
   if (!A->tiles || tiles.size() != A->h_tiles.size() ||
       memcmp(tiles.data(), A->h_tiles.data(), tiles.size() * sizeof(int2)) != 0) {
     cudaFree(A->tiles);
@@ -600,6 +605,10 @@ int prepare_tb(etg_adj* A, const AdjPlan<T>& ph, const AdjPlan<T>& pe) {
     ETG_TRY_CUDA(cudaStreamCreateWithFlags(&A->side, cudaStreamNonBlocking));
     ETG_TRY_CUDA(cudaEventCreateWithFlags(&A->fork, cudaEventDisableTiming));
     ETG_TRY_CUDA(cudaEventCreateWithFlags(&A->join, cudaEventDisableTiming));
+    for (int k = 0; k < 3; ++k) {
+      ETG_TRY_CUDA(cudaStreamCreateWithFlags(&A->sides[k], cudaStreamNonBlocking));
+      ETG_TRY_CUDA(cudaEventCreateWithFlags(&A->joins[k], cudaEventDisableTiming));
+    }
   }
   return ETG_OK;
 }
@@ -771,6 +780,9 @@ struct etg_adj_batch {
   int n_inner = 0, n_pml = 0;
   cudaStream_t stream = nullptr, side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+  cudaStream_t sides[3] = {};  // one branch per CPML kind
+  cudaEvent_t joins[3] = {};
+  int n_kind[3] = {};
   int64_t n_steps = 0, stride = 0;
   int64_t* d_ctl = nullptr;                   // top step of the launch block, trace origin
   std::map<int64_t, cudaGraphExec_t> graphs;  // key: pairs per graph
@@ -809,11 +821,11 @@ int batch_sweep(etg_adj_batch* B, int64_t n_hi, int64_t n_lo, int64_t trace_n0, 
       tb_adj_ctl_add(B->d_ctl, -2 * K * n_pairs, B->stream);
     };
     auto pair = [&](int64_t p) {
-      int rc = tb_adj_batch_launch<T>(d_args, B->d_tiles, B->n_inner, B->n_pml, 0, (int)(2 * K * p), B->stream,
-                                      B->side, B->fork, B->join);
+      int rc = tb_adj_batch_launch<T>(d_args, B->d_tiles, B->n_inner, B->n_kind, 0, (int)(2 * K * p), B->stream,
+                                      B->sides, B->fork, B->joins);
       if (rc == ETG_OK)
-        rc = tb_adj_batch_launch<T>(d_args, B->d_tiles, B->n_inner, B->n_pml, 1, (int)(2 * K * p + K), B->stream,
-                                    B->side, B->fork, B->join);
+        rc = tb_adj_batch_launch<T>(d_args, B->d_tiles, B->n_inner, B->n_kind, 1, (int)(2 * K * p + K), B->stream,
+                                    B->sides, B->fork, B->joins);
       return rc;
     };
     const int64_t per_graph = kBatchPairsPerGraph;
@@ -886,6 +898,9 @@ int batch_backward(etg_adj_batch* B) {
         (q < A->n_inner ? inner : pml)
             .push_back(make_int4(k, tb_tile_row(A->h_tiles[q]), A->h_tiles[q].y, tb_tile_kind(A->h_tiles[q])));
     }
+    std::stable_sort(pml.begin(), pml.end(), [](const int4& p, const int4& q) { return p.w < q.w; });
+    for (int k = 0; k < 3; ++k) B->n_kind[k] = 0;
+    for (const int4& q : pml) B->n_kind[q.w - 1] += 1;
     B->n_inner = (int)inner.size();
     B->n_pml = (int)pml.size();
     inner.insert(inner.end(), pml.begin(), pml.end());
@@ -975,6 +990,10 @@ int etg_adj_destroy(etg_adj* A) {
   if (A->fork) cudaEventDestroy(A->fork);
   if (A->join) cudaEventDestroy(A->join);
   if (A->side) cudaStreamDestroy(A->side);
+  for (int k = 0; k < 3; ++k) {
+    if (A->sides[k]) cudaStreamDestroy(A->sides[k]);
+    if (A->joins[k]) cudaEventDestroy(A->joins[k]);
+  }
   delete A;
   return ETG_OK;
 }
@@ -1039,7 +1058,13 @@ int etg_adj_batch_create(etg_adj_batch** out, int n, etg_adj* const* adjs) {
       (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess ||
        cudaStreamCreateWithFlags(&B->side, cudaStreamNonBlocking) != cudaSuccess ||
        cudaEventCreateWithFlags(&B->fork, cudaEventDisableTiming) != cudaSuccess ||
-       cudaEventCreateWithFlags(&B->join, cudaEventDisableTiming) != cudaSuccess)) {
+       cudaEventCreateWithFlags(&B->join, cudaEventDisableTiming) != cudaSuccess ||
+       cudaStreamCreateWithFlags(&B->sides[0], cudaStreamNonBlocking) != cudaSuccess ||
+       cudaStreamCreateWithFlags(&B->sides[1], cudaStreamNonBlocking) != cudaSuccess ||
+       cudaStreamCreateWithFlags(&B->sides[2], cudaStreamNonBlocking) != cudaSuccess ||
+       cudaEventCreateWithFlags(&B->joins[0], cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&B->joins[1], cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&B->joins[2], cudaEventDisableTiming) != cudaSuccess)) {
     set_error("etg_adj_batch_create: %s", cudaGetErrorString(cudaGetLastError()));
     rc = ETG_ERR_CUDA;
   }
@@ -1062,6 +1087,10 @@ int etg_adj_batch_destroy(etg_adj_batch* B) {
   if (B->fork) cudaEventDestroy(B->fork);
   if (B->join) cudaEventDestroy(B->join);
   if (B->side) cudaStreamDestroy(B->side);
+  for (int k = 0; k < 3; ++k) {
+    if (B->sides[k]) cudaStreamDestroy(B->sides[k]);
+    if (B->joins[k]) cudaEventDestroy(B->joins[k]);
+  }
   if (B->stream) cudaStreamDestroy(B->stream);
   delete B;
   return ETG_OK;

@@ -22,9 +22,14 @@ struct etg_batch {
   std::vector<int4> h_tiles;
   int4* d_tiles = nullptr;
   int n_inner = 0, n_pml = 0, tiles_er = 0, tiles_k = 0;
+  int64_t dft_work = 0;  // largest sampled monitor (frequencies x nodes) of any simulation
+  int dft_mon = 0;       // most monitor components of any simulation
   int64_t** d_steps = nullptr;     // each simulation's step counter
   cudaStream_t stream = nullptr, side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, ev0 = nullptr, ev1 = nullptr, done = nullptr;
+  cudaStream_t sides[3] = {};  // one branch per CPML kind
+  cudaEvent_t joins[3] = {};
+  int n_kind[3] = {};
   int64_t opt[8] = {0, 0, 32, 0, 0, 0, 0, 0};
   std::map<int64_t, cudaGraphExec_t> graphs;
   double last_ms = 0;
@@ -50,6 +55,8 @@ template <typename T>
 int refresh(etg_batch* b, int ER, int K, bool* changed) {
   const int n = (int)b->sims.size();
   ETG_TRY_CUDA(cudaStreamSynchronize(b->stream));  // no launch still reads the arguments
+  b->dft_work = 0;
+  b->dft_mon = 0;
   std::vector<unsigned char> host((size_t)n * sizeof(BatchSim<T>));
   for (int k = 0; k < n; ++k) {
     etg_sim* s = b->sims[k];
@@ -72,9 +79,14 @@ int refresh(etg_batch* b, int ER, int K, bool* changed) {
     e.src[1] = bb;
     e.dst[0] = TBDst<T>{bb.ex, bb.ey, bb.hz, bb.psi_ex_y, bb.psi_ey_x, bb.psi_hz_x, bb.psi_hz_y};
     e.dst[1] = TBDst<T>{a.ex, a.ey, a.hz, a.psi_ex_y, a.psi_ey_x, a.psi_hz_x, a.psi_hz_y};
-    int rc = sim_plans_export<T>(s, &e.ph, &e.pe);
+    int rc = sim_plans_export<T>(s, &e.ph, &e.pe, std::max<int64_t>(16, b->opt[ETG_OPT_GRAPH_STEPS]));
     if (rc) return rc;
     memcpy(host.data() + (size_t)k * sizeof e, &e, sizeof e);
+    b->dft_mon = std::max(b->dft_mon, e.ph.n_mon + e.pe.n_mon);
+    for (int m = 0; m < e.ph.n_mon + e.pe.n_mon; ++m) {
+      const MonDesc<T>& d = m < e.ph.n_mon ? e.ph.mon[m] : e.pe.mon[m - e.ph.n_mon];
+      if (d.samp) b->dft_work = std::max<int64_t>(b->dft_work, (int64_t)d.nxm * d.nym * d.n_f);
+    }
   }
   *changed = false;
   if (host != b->h_sims) {
@@ -103,6 +115,10 @@ int refresh(etg_batch* b, int ER, int K, bool* changed) {
       for (int q = 0; q < (int)t.size(); ++q)
         (q < ni ? inner : pml).push_back(make_int4(k, tb_tile_row(t[q]), t[q].y, tb_tile_kind(t[q])));
     }
+    // CPML tiles grouped by kind over every simulation (one kernel per kind)
+    std::stable_sort(pml.begin(), pml.end(), [](const int4& p, const int4& q) { return p.w < q.w; });
+    int n_kind[3] = {0, 0, 0};
+    for (const int4& q : pml) n_kind[q.w - 1] += 1;
     const int n_inner = (int)inner.size(), n_pml = (int)pml.size();
     inner.insert(inner.end(), pml.begin(), pml.end());
     const bool same = b->d_tiles && n_inner == b->n_inner && n_pml == b->n_pml && inner.size() == b->h_tiles.size() &&
@@ -110,6 +126,7 @@ int refresh(etg_batch* b, int ER, int K, bool* changed) {
     if (!same) {
       b->n_inner = n_inner;
       b->n_pml = n_pml;
+      for (int k = 0; k < 3; ++k) b->n_kind[k] = n_kind[k];
       cudaFree(b->d_tiles);
       b->d_tiles = nullptr;
       int rc = etg_malloc((void**)&b->d_tiles, std::max<size_t>(1, inner.size()) * sizeof(int4));
@@ -130,7 +147,8 @@ int batch_advance(etg_batch* b, int64_t n_steps) {
   tb_default_shape((int)sizeof(T), &ER, &EC, &K);
   if (b->opt[ETG_OPT_TILE_ROWS] > 0) ER = (int)b->opt[ETG_OPT_TILE_ROWS];
   if (b->opt[ETG_OPT_TB_DEPTH] > 0) K = (int)b->opt[ETG_OPT_TB_DEPTH];
-  int rc = tb_batch_attrs<T>(ER, K);
+  const int NW = b->opt[ETG_OPT_TB_WARPS] > 0 ? (int)b->opt[ETG_OPT_TB_WARPS] : 8;
+  int rc = tb_batch_attrs<T>(ER, K, NW);
   if (rc) return rc;
   bool changed = false;
   rc = refresh<T>(b, ER, K, &changed);
@@ -140,16 +158,26 @@ int batch_advance(etg_batch* b, int64_t n_steps) {
   const int64_t pairs = n_steps / (2 * K);
   const int64_t per_graph = std::max<int64_t>(1, b->opt[ETG_OPT_GRAPH_STEPS] / (2 * K));
   auto pair = [&](int64_t p) -> int {
-    int r = tb_batch_pair<T>(ER, K, b->d_sims, b->d_tiles, b->n_inner, b->n_pml, 0, (int)(2 * K * p), b->stream,
-                             b->side, b->fork, b->join);
+    int r = tb_batch_pair<T>(ER, K, NW, b->d_sims, b->d_tiles, b->n_inner, b->n_kind, 0, (int)(2 * K * p),
+                             b->stream, b->sides, b->fork, b->joins);
     if (r == ETG_OK)
-      r = tb_batch_pair<T>(ER, K, b->d_sims, b->d_tiles, b->n_inner, b->n_pml, 1, (int)(2 * K * p + K), b->stream,
-                           b->side, b->fork, b->join);
+      r = tb_batch_pair<T>(ER, K, NW, b->d_sims, b->d_tiles, b->n_inner, b->n_kind, 1, (int)(2 * K * p + K),
+                           b->stream, b->sides, b->fork, b->joins);
     return r;
   };
   auto add_steps = [&](int64_t k) {
     k_batch_step_add<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_steps, n, k);
     g_launches += 1;
+  };
+  // a block: up to per_graph launch pairs, the DFT of the block's samples, the step counters
+  auto block = [&](int64_t n_pairs) -> int {
+    int r = ETG_OK;
+    for (int64_t p = 0; p < n_pairs && r == ETG_OK; ++p) r = pair(p);
+    if (r == ETG_OK) {
+      tb_batch_dft<T>(b->d_sims, n, b->dft_work, b->dft_mon, (int)(2 * K * n_pairs), b->stream);
+      add_steps(2 * K * n_pairs);
+    }
+    return r;
   };
   int64_t done = 0;
   if (b->opt[ETG_OPT_GRAPH_STEPS] > 0 && pairs >= per_graph) {
@@ -157,9 +185,7 @@ int batch_advance(etg_batch* b, int64_t n_steps) {
     if (it == b->graphs.end()) {
       cudaGraph_t graph;
       ETG_TRY_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-      int r = ETG_OK;
-      for (int64_t p = 0; p < per_graph && r == ETG_OK; ++p) r = pair(p);
-      if (r == ETG_OK) add_steps(2 * K * per_graph);
+      const int r = block(per_graph);
       cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
       if (r) return r;
       ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "batch graph capture failed: %s", cudaGetErrorString(e));
@@ -171,15 +197,14 @@ int batch_advance(etg_batch* b, int64_t n_steps) {
     }
     for (; done + per_graph <= pairs; done += per_graph) {
       ETG_TRY_CUDA(cudaGraphLaunch(it->second, b->stream));
-      g_launches += 4 * per_graph + 1;
+      g_launches += 4 * per_graph + 2;
     }
   }
-  if (done < pairs) {
-    for (int64_t p = 0; done + p < pairs; ++p) {
-      rc = pair(p);
-      if (rc) return rc;
-    }
-    add_steps(2 * K * (pairs - done));
+  while (done < pairs) {
+    const int64_t c = std::min(per_graph, pairs - done);
+    rc = block(c);
+    if (rc) return rc;
+    done += c;
   }
   const int64_t rem = n_steps - 2 * K * pairs;  // one-step kernels, simulation by simulation
   if (rem) {
@@ -222,6 +247,12 @@ int etg_batch_create(etg_batch** out, int n_sims, etg_sim* const* sims) {
        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
        cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess ||
        cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess ||
+       cudaStreamCreateWithFlags(&b->sides[0], cudaStreamNonBlocking) != cudaSuccess ||
+       cudaStreamCreateWithFlags(&b->sides[1], cudaStreamNonBlocking) != cudaSuccess ||
+       cudaStreamCreateWithFlags(&b->sides[2], cudaStreamNonBlocking) != cudaSuccess ||
+       cudaEventCreateWithFlags(&b->joins[0], cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&b->joins[1], cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&b->joins[2], cudaEventDisableTiming) != cudaSuccess ||
        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)) {
     set_error("etg_batch_create: %s", cudaGetErrorString(cudaGetLastError()));
     rc = ETG_ERR_CUDA;
@@ -245,6 +276,10 @@ int etg_batch_destroy(etg_batch* b) {
   for (cudaEvent_t e : {b->fork, b->join, b->ev0, b->ev1, b->done})
     if (e) cudaEventDestroy(e);
   if (b->side) cudaStreamDestroy(b->side);
+  for (int k = 0; k < 3; ++k) {
+    if (b->sides[k]) cudaStreamDestroy(b->sides[k]);
+    if (b->joins[k]) cudaEventDestroy(b->joins[k]);
+  }
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return ETG_OK;

@@ -96,8 +96,10 @@ SimArgs<T> sim_args(etg_sim* s) {
   return a;
 }
 
+// sample_slots > 0: monitors record their samples for blocks of up to sample_slots steps
+// (temporally blocked kernels) instead of accumulating in place.
 template <typename T>
-int build_plans(etg_sim* s, PhasePlan<T>* ph, PhasePlan<T>* pe) {
+int build_plans(etg_sim* s, PhasePlan<T>* ph, PhasePlan<T>* pe, int64_t sample_slots = 0) {
   memset(ph, 0, sizeof *ph);
   memset(pe, 0, sizeof *pe);
   for (const Source& src : s->sources) {
@@ -124,14 +126,23 @@ int build_plans(etg_sim* s, PhasePlan<T>* ph, PhasePlan<T>* pe) {
     ph->trace.tj0 = s->trace_tj0;
     ph->trace.tny = s->trace_tny;
   }
-  for (const Monitor& m : s->monitors) {
+  for (Monitor& m : s->monitors) {
     if (!s->monitors_on) break;
+    if (sample_slots > m.samp_slots) {
+      cudaFree(m.samp);
+      m.samp = nullptr;
+      m.samp_slots = 0;
+      int rc = etg_malloc(&m.samp, (size_t)sample_slots * m.nxm * m.nym * s->esize());
+      if (rc) return rc;
+      m.samp_slots = sample_slots;
+    }
     PhasePlan<T>* p = m.comp == ETG_HZ ? ph : pe;
     ETG_REQUIRE(p->n_mon < MAX_MONITORS, ETG_ERR_ARGUMENT,
                 "more than %d monitor components in one half step", MAX_MONITORS);
     MonDesc<T>& d = p->mon[p->n_mon++];
     d.acc = (T*)m.acc;
     d.table = (const T*)m.table;
+    d.samp = sample_slots > 0 ? (T*)m.samp : nullptr;
     d.n0 = m.n0;
     d.rows = m.rows;
     d.ix0 = m.ix0;
@@ -199,9 +210,9 @@ int advance_plain(etg_sim* s, int64_t n_steps) {
 template <typename T>
 int advance_dispatch(etg_sim* s, int64_t n_steps) {
   const int64_t kernel = s->opt[ETG_OPT_KERNEL];
-  if (kernel == 2 || kernel == 3 || (kernel == 0 && tb_supported<T>(s->nx, s->ny))) {
-    PhasePlan<T> ph, pe;
-    int rc = build_plans<T>(s, &ph, &pe);
+  if (kernel == 2 || kernel == 3 || kernel == 4 || (kernel == 0 && tb_supported<T>(s->nx, s->ny))) {
+    PhasePlan<T> ph, pe;  // the TMA kernel accumulates in place; the others sample per block
+    int rc = build_plans<T>(s, &ph, &pe, kernel == 3 ? 0 : sim_sample_slots(s));
     if (rc) return rc;
     if (!s->tb) s->tb = tb_create();
     return tb_advance<T>(s->tb, sim_args<T>(s), ph, pe, n_steps, s->opt, s->stream);
@@ -267,16 +278,18 @@ SimArgs<T> sim_args_export(etg_sim* s) {
 }
 
 template <typename T>
-int sim_plans_export(etg_sim* s, PhasePlan<T>* ph, PhasePlan<T>* pe) {
-  return build_plans<T>(s, ph, pe);
+int sim_plans_export(etg_sim* s, PhasePlan<T>* ph, PhasePlan<T>* pe, int64_t sample_slots) {
+  return build_plans<T>(s, ph, pe, sample_slots);
 }
+
+int64_t sim_sample_slots(const etg_sim* s) { return std::max<int64_t>(16, s->opt[ETG_OPT_GRAPH_STEPS]); }
 
 int sim_check_tables(etg_sim* s, int64_t n_steps) { return check_tables(s, n_steps); }
 
 template SimArgs<float> sim_args_export<float>(etg_sim*);
 template SimArgs<double> sim_args_export<double>(etg_sim*);
-template int sim_plans_export<float>(etg_sim*, PhasePlan<float>*, PhasePlan<float>*);
-template int sim_plans_export<double>(etg_sim*, PhasePlan<double>*, PhasePlan<double>*);
+template int sim_plans_export<float>(etg_sim*, PhasePlan<float>*, PhasePlan<float>*, int64_t);
+template int sim_plans_export<double>(etg_sim*, PhasePlan<double>*, PhasePlan<double>*, int64_t);
 
 }  // namespace etg
 
@@ -343,6 +356,7 @@ int etg_sim_destroy(etg_sim* s) {
   for (Monitor& m : s->monitors) {
     cudaFree(m.acc);
     cudaFree(m.table);
+    cudaFree(m.samp);
   }
   cudaFree(s->d_step);
   cudaFree(s->d_flag);
@@ -667,6 +681,7 @@ int etg_sim_set_option(etg_sim* s, int option, int64_t value) {
 int etg_sim_get_option(etg_sim* s, int option, int64_t* value) {
   ETG_REQUIRE(s && value && option >= 0 && option < 8, ETG_ERR_ARGUMENT, "etg_sim_get_option: bad option");
   *value = s->opt[option];
+  if (*value == 0 && option == ETG_OPT_TB_WARPS) *value = 8;
   if (*value == 0 && (option == ETG_OPT_TB_DEPTH || option == ETG_OPT_TILE_ROWS || option == ETG_OPT_TILE_COLS)) {
     int er, ec, k;  // the default tile shape of this dtype
     tb_default_shape(s->dtype, &er, &ec, &k, (int)s->opt[ETG_OPT_KERNEL]);

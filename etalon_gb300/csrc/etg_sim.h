@@ -24,6 +24,8 @@ template <typename T>
 struct MonDesc {
   T* acc;          // (n_f, nxm*nym) complex
   const T* table;  // (rows, n_f) complex
+  T* samp;         // temporally blocked kernels: field values [step of the block][node], summed
+                   // into acc after the block by k_dft_block; nullptr: accumulate in place
   int64_t n0, rows;
   int ix0, nxm, jy0, nym, n_f, comp;
 };
@@ -125,7 +127,35 @@ struct Monitor {
   void* acc = nullptr;    // (n_f, nxm*nym) complex
   void* table = nullptr;  // (rows, n_f) complex
   int64_t n0 = 0, rows = 0;
+  void* samp = nullptr;   // field samples of one launch block (samp_slots steps x nodes)
+  int64_t samp_slots = 0;
 };
+
+// acc[f, k] += samples of steps step0 … step0 + n_slots - 1 times their phasors, in step order:
+// for one thread's (frequency, node) the same additions as dft_node makes step by step.
+template <typename T>
+__device__ __forceinline__ void dft_block_node(const MonDesc<T>& d, int64_t q, int64_t step0, int n_slots,
+                                               int* flag) {
+  const int64_t nodes = (int64_t)d.nxm * d.nym;
+  if (!d.samp || q >= nodes * d.n_f) return;
+  const int f = (int)(q / nodes);
+  const int64_t k = q % nodes;
+  T* a = d.acc + 2 * ((int64_t)f * nodes + k);
+  T re = a[0], im = a[1];
+  for (int slot = 0; slot < n_slots; ++slot) {
+    const int64_t r = step0 + slot - d.n0;
+    if (r < 0 || r >= d.rows) {
+      atomicOr(flag, ERRBIT_TABLE);
+      continue;
+    }
+    const T v = d.samp[(int64_t)slot * nodes + k];
+    const T* ph = d.table + 2 * (r * d.n_f + f);
+    re = add(re, mul(v, __ldg(ph)));
+    im = add(im, mul(v, __ldg(ph + 1)));
+  }
+  a[0] = re;
+  a[1] = im;
+}
 
 }  // namespace etg
 
@@ -179,6 +209,8 @@ void sim_invalidate(etg_sim* s);                        // drop graphs after a c
 template <typename T>
 SimArgs<T> sim_args_export(etg_sim* s);                 // kernel arguments of the simulation
 template <typename T>
-int sim_plans_export(etg_sim* s, PhasePlan<T>* ph, PhasePlan<T>* pe);  // its source/monitor plans
+int sim_plans_export(etg_sim* s, PhasePlan<T>* ph, PhasePlan<T>* pe,  // its source/monitor plans;
+                     int64_t sample_slots = 0);                        // > 0: monitors sample per block
+int64_t sim_sample_slots(const etg_sim* s);             // block length the sample buffers must hold
 int sim_check_tables(etg_sim* s, int64_t n_steps);      // tables cover the next n_steps steps
 }  // namespace etg

@@ -41,16 +41,16 @@ namespace etg {
 constexpr int KIND_INNER = 0, KIND_X = 1, KIND_Y = 2, KIND_XY = 3;
 constexpr int KIND_SHIFT = 28;  // CPML tile lists carry the kind in bits 28-29 of the row
 
-template <typename T, int RPT, int K, int KIND>
+template <typename T, int RPT, int K, int KIND, int NW = 8>
 struct TBShape {
   static constexpr int W = TBVec<T>::W;
-  static constexpr int ER = 8 * RPT, EC = 32 * W, OR = ER - 2 * K, OC = EC - 2 * K;
+  static constexpr int ER = NW * RPT, EC = 32 * W, OR = ER - 2 * K, OC = EC - 2 * K;
   static constexpr int PL = ER * EC;                    // one plane: cb or psi
   // cb_ex, cb_ey, then psi_hz_x, psi_ey_x (x kinds), then psi_hz_y, psi_ex_y (y kinds)
   static constexpr int PLANES = 2 + ((KIND & KIND_X) ? 2 : 0) + ((KIND & KIND_Y) ? 2 : 0);
-  static constexpr int XCH = 9 * EC;                    // one exchange buffer: 8 warps + a zero row
+  static constexpr int XCH = (NW + 1) * EC;             // one exchange buffer: NW warps + a zero row
   static constexpr size_t SMEM = ((size_t)PLANES * PL + 2 * XCH) * sizeof(T);
-  static constexpr int MIN_BLOCKS = KIND ? 1 : (RPT <= 5 ? 2 : 1);
+  static constexpr int MIN_BLOCKS = KIND || NW != 8 ? 1 : (RPT <= 5 ? 2 : 1);
   static_assert(K % W == 0, "the halo must keep vectors aligned");
   static_assert(OR > 0 && OC > 0, "halo larger than the tile");
 };
@@ -72,6 +72,26 @@ __device__ __forceinline__ void tb_dft(const MonDesc<T>& d, const TBVec<T> (&val
       const unsigned dj = (unsigned)(j0 + e - d.jy0);
       if (dj >= (unsigned)d.nym) continue;
       dft_node(d.acc, nodes, (int64_t)di * d.nym + dj, phr, d.n_f, val[t].v[e]);
+    }
+  }
+}
+
+// Record this thread's owned nodes of monitor d in its sample slot (summed by k_dft_block).
+template <typename T, int RPT, int W>
+__device__ __forceinline__ void tb_sample(const MonDesc<T>& d, const TBVec<T> (&val)[RPT], int i0, int j0,
+                                          int t_lo, int t_hi, int e_lo, int e_hi, int slot) {
+  const int64_t nodes = (int64_t)d.nxm * d.nym;
+  T* out = d.samp + (int64_t)slot * nodes;
+#pragma unroll
+  for (int t = 0; t < RPT; ++t) {
+    if (t < t_lo || t >= t_hi) continue;
+    const unsigned di = (unsigned)(i0 + t - d.ix0);
+    if (di >= (unsigned)d.nxm) continue;
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      if (e < e_lo || e >= e_hi) continue;
+      const unsigned dj = (unsigned)(j0 + e - d.jy0);
+      if (dj < (unsigned)d.nym) out[(int64_t)di * d.nym + dj] = val[t].v[e];
     }
   }
 }
@@ -108,22 +128,37 @@ __device__ __forceinline__ void tb_inject(const PhasePlan<T>& p, uint32_t rel, T
 // CPML tiles come in three kinds. In an X tile every column of the extended region lies in
 // the unit range of the y coefficients, so the y terms take the lean form; rows outside the
 // x strips have no psi and their x terms reduce to d·(1/kappa) + 0 (b·0 + 0·d = +0 for
-// finite d); only strip rows read and write psi. Y tiles are the same with rows and columns
-// exchanged, XY tiles (corners) run the full expression everywhere. All give Etalon's bits.
-template <typename T, int RPT, int K, int KIND>
+// finite d), a test that is uniform across a warp (one warp, one row); only strip rows read
+// and write psi. Y tiles have unit x terms; their strip columns fall across the lanes of every
+// warp, so all columns evaluate the full y expression (psi = +0 outside the strips gives the
+// same bits) and only the psi store is predicated. XY tiles (corners) run the full
+// expression everywhere. All give Etalon's bits.
+struct TBNoHook {
+  __device__ void operator()() const {}
+};
+
+// STAGED (interior tiles of the persistent kernel): Ex, Ey, Hz of the extended tile are
+// already in shared memory at `stage` (three planes) and cb at `cb_s` (two planes), placed
+// there by TMA; the exchange rows live at `xch_s`. `after_load` runs on every thread right
+// after the barrier that ends the load phase, when the stage is free again.
+template <typename T, int RPT, int K, int KIND, bool STAGED = false, typename Hook = TBNoHook, int NW = 8>
 __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst, const int2 tile,
-                                        const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off) {
-  using S = TBShape<T, RPT, K, KIND>;
+                                        const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
+                                        const T* stage = nullptr, T* cb_s = nullptr, T* xch_s = nullptr,
+                                        Hook after_load = Hook()) {
+  using S = TBShape<T, RPT, K, KIND, NW>;
   using Vw = TBVec<T>;
   constexpr int W = S::W, ER = S::ER, EC = S::EC, PL = S::PL;
   constexpr bool PML = KIND != KIND_INNER, PX = (KIND & KIND_X) != 0, PY = (KIND & KIND_Y) != 0;
+  static_assert(!STAGED || !PML, "only interior tiles are staged");
+  static_assert(!STAGED || NW == 8, "the staged layout is for 8 warps");
   extern __shared__ __align__(16) unsigned char tb_smem[];
-  T* const sCbx = reinterpret_cast<T*>(tb_smem);
+  T* const sCbx = STAGED ? cb_s : reinterpret_cast<T*>(tb_smem);
   T* const sCby = sCbx + PL;
   T* const sPsiX = sCby + PL;                    // x kinds: psi_hz_x, psi_ey_x
   T* const sPsiY = sPsiX + (PX ? 2 * PL : 0);    // y kinds: psi_hz_y, psi_ex_y
-  T* const sHzX = sCbx + S::PLANES * PL;         // [k = ty + 1]: last-row Hz of warp ty; [0] = zeros
-  T* const sEyX = sHzX + S::XCH;                 // [k = ty]: first-row Ey of warp ty; [8] = zeros
+  T* const sHzX = STAGED ? xch_s : sCbx + S::PLANES * PL;  // [k = ty + 1]: last-row Hz of warp ty; [0] = zeros
+  T* const sEyX = sHzX + S::XCH;                 // [k = ty]: first-row Ey of warp ty; [NW] = zeros
   __shared__ uint32_t s_rel[4];  // relevant plan entries: H sources, E sources, H monitors, E monitors
 
   const int lane = threadIdx.x, ty = threadIdx.y;
@@ -163,10 +198,10 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
     z.zero();
     z.st(sHzX + lj0);  // the row above the tile
   }
-  if (ty == 7) {
+  if (ty == NW - 1) {
     Vw z;
     z.zero();
-    z.st(sEyX + 8 * EC + lj0);  // the row below the tile
+    z.st(sEyX + NW * EC + lj0);  // the row below the tile
   }
 
   // load the extended tile: fields to registers, cb (and psi) to shared memory
@@ -177,6 +212,12 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
     const bool in = lane_in && (unsigned)i <= (unsigned)nx;
     const int64_t g = (int64_t)i * P + j0;
     const int o = li * EC + lj0;
+    if (STAGED) {  // the whole extended region of an interior tile lies inside the grid
+      ex[t].ld(stage + 0 * PL + o);
+      ey[t].ld(stage + 1 * PL + o);
+      hz[t].ld(stage + 2 * PL + o);
+      continue;
+    }
     Vw cx, cy;
     if (in) {
       ex[t].ld(a.ex + g);
@@ -249,6 +290,7 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
     }
   }
   __syncthreads();
+  after_load();
   const uint32_t relSrcH = s_rel[0], relSrcE = s_rel[1], relMonH = s_rel[2], relMonE = s_rel[3];
   const int64_t n_base = *a.step + step_off;
   const T db = a.db, idx = a.inv_dx, idy = a.inv_dy;
@@ -268,6 +310,13 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
       for (int t = 0; t < RPT; ++t) {
         T exr = __shfl_down_sync(0xffffffffu, ex[t].v[0], 1);
         if (lane == 31) exr = zero<T>();
+        // CPML tiles: this row's psi as one 16-byte vector per lane. Outside the strips psi
+        // is +0 and its update b*0 + 0*d is +0 again, so whole vectors go back unchanged there.
+        const int ir = i0 + t;
+        const bool xrow = KIND == KIND_XY || ir < a.xs_lo || ir >= a.xs_hi;
+        Vw pyv, pxv;
+        if (PY) pyv.ld(sPsiY + (lr0 + t) * EC + lj0);
+        if (PX && xrow) pxv.ld(sPsiX + (lr0 + t) * EC + lj0);
 #pragma unroll
         for (int e = 0; e < W; ++e) {
           const T exn = e < W - 1 ? ex[t].v[e + 1] : exr;
@@ -277,25 +326,18 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
           if (!PML) {
             hz[t].v[e] = add(hz[t].v[e], mul(db, sub(add(dex_dy, zero<T>()), add(dey_dx, zero<T>()))));
           } else {
-            const int i = i0 + t, j = j0 + e;
-            const bool xs = i < a.xs_lo || i >= a.xs_hi, ys = j < a.ys_lo || j >= a.ys_hi;
+            const int i = ir, j = j0 + e;
             if ((!PX || (i >= 0 && i < nx)) && (!PY || (j >= 0 && j < ny))) {
               T ty_ = add(dex_dy, zero<T>()), tx_ = add(dey_dx, zero<T>());
-              if (PY) {
-                if (KIND == KIND_XY || ys) {
-                  T* pyp = sPsiY + (lr0 + t) * EC + lj0 + e;
-                  const T py = add(mul(byh[e], *pyp), mul(cyh[e], dex_dy));
-                  if (ys) *pyp = py;
-                  ty_ = add(mul(dex_dy, kyh[e]), py);
-                } else {
-                  ty_ = add(mul(dex_dy, kyh[e]), zero<T>());
-                }
+              if (PY) {  // every column alike: no divergence between strip and other lanes
+                const T py = add(mul(byh[e], pyv.v[e]), mul(cyh[e], dex_dy));
+                pyv.v[e] = py;
+                ty_ = add(mul(dex_dy, kyh[e]), py);
               }
               if (PX) {
-                if (KIND == KIND_XY || xs) {
-                  T* pxp = sPsiX + (lr0 + t) * EC + lj0 + e;
-                  const T px = add(mul(bxh[t], *pxp), mul(cxh[t], dey_dx));
-                  if (xs) *pxp = px;
+                if (xrow) {
+                  const T px = add(mul(bxh[t], pxv.v[e]), mul(cxh[t], dey_dx));
+                  pxv.v[e] = px;
                   tx_ = add(mul(dey_dx, kxh[t]), px);
                 } else {
                   tx_ = add(mul(dey_dx, kxh[t]), zero<T>());
@@ -305,14 +347,17 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
             }
           }
         }
+        if (PY) pyv.st(sPsiY + (lr0 + t) * EC + lj0);
+        if (PX && xrow) pxv.st(sPsiX + (lr0 + t) * EC + lj0);
       }
     }
     if (relSrcH) tb_inject<T, RPT, W>(ph, relSrcH, ex, ey, hz, i0, j0, n, a.flag);
-    if (relMonH) {  // DFT of H at (n + 1/2) dt, owned nodes only
+    if (relMonH) {  // DFT of H at (n + 1/2) dt, owned nodes only (or their samples)
       for (uint32_t m = relMonH; m; m &= m - 1) {
         const MonDesc<T>& d = ph.mon[__ffs(m) - 1];
         const int64_t r = n - d.n0;
-        if (r < 0 || r >= d.rows) atomicOr(a.flag, ERRBIT_TABLE);
+        if (d.samp) tb_sample<T, RPT, W>(d, hz, i0, j0, t_lo, t_hi, e_lo, e_hi, step_off + s);
+        else if (r < 0 || r >= d.rows) atomicOr(a.flag, ERRBIT_TABLE);
         else tb_dft<T, RPT, W>(d, hz, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
       }
     }
@@ -347,6 +392,11 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
         Vw cx, cy;
         cx.ld(sCbx + (lr0 + t) * EC + lj0);
         cy.ld(sCby + (lr0 + t) * EC + lj0);
+        const int ir = i0 + t;
+        const bool xrow = KIND == KIND_XY || ir < a.xs_lo || ir >= a.xs_hi;
+        Vw pyv, pxv;  // psi_ex_y, psi_ey_x of this row (CPML tiles)
+        if (PY) pyv.ld(sPsiY + PL + (lr0 + t) * EC + lj0);
+        if (PX && xrow) pxv.ld(sPsiX + PL + (lr0 + t) * EC + lj0);
 #pragma unroll
         for (int e = 0; e < W; ++e) {
           const T hzp = e > 0 ? hz[t].v[e - 1] : hzl;
@@ -357,29 +407,22 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
             ex[t].v[e] = add(ex[t].v[e], mul(cx.v[e], add(dy, zero<T>())));
             ey[t].v[e] = sub(ey[t].v[e], mul(cy.v[e], add(dx, zero<T>())));
           } else {
-            const int i = i0 + t, j = j0 + e;
-            const bool xs = i < a.xs_lo || i >= a.xs_hi, ys = j < a.ys_lo || j >= a.ys_hi;
+            const int i = ir, j = j0 + e;
             if ((!PX || (i >= 0 && i < nx)) && (!PY || (j >= 1 && j <= ny - 1))) {
               T term = add(dy, zero<T>());
-              if (PY) {
-                if (KIND == KIND_XY || ys) {
-                  T* pp = sPsiY + PL + (lr0 + t) * EC + lj0 + e;
-                  const T p = add(mul(bye[e], *pp), mul(cye[e], dy));
-                  if (ys) *pp = p;
-                  term = add(mul(dy, kye[e]), p);
-                } else {
-                  term = add(mul(dy, kye[e]), zero<T>());
-                }
+              if (PY) {  // every column alike
+                const T p = add(mul(bye[e], pyv.v[e]), mul(cye[e], dy));
+                pyv.v[e] = p;
+                term = add(mul(dy, kye[e]), p);
               }
               ex[t].v[e] = add(ex[t].v[e], mul(cx.v[e], term));
             }
             if ((!PX || (i >= 1 && i <= nx - 1)) && (!PY || (j >= 0 && j < ny))) {
               T term = add(dx, zero<T>());
               if (PX) {
-                if (KIND == KIND_XY || xs) {
-                  T* pp = sPsiX + PL + (lr0 + t) * EC + lj0 + e;
-                  const T p = add(mul(bxe[t], *pp), mul(cxe[t], dx));
-                  if (xs) *pp = p;
+                if (xrow) {
+                  const T p = add(mul(bxe[t], pxv.v[e]), mul(cxe[t], dx));
+                  pxv.v[e] = p;
                   term = add(mul(dx, kxe[t]), p);
                 } else {
                   term = add(mul(dx, kxe[t]), zero<T>());
@@ -389,16 +432,25 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
             }
           }
         }
+        if (PY) pyv.st(sPsiY + PL + (lr0 + t) * EC + lj0);
+        if (PX && xrow) pxv.st(sPsiX + PL + (lr0 + t) * EC + lj0);
       }
     }
     if (relSrcE) tb_inject<T, RPT, W>(pe, relSrcE, ex, ey, hz, i0, j0, n, a.flag);
-    if (relMonE) {  // DFT of E at (n + 1) dt
+    if (relMonE) {  // DFT of E at (n + 1) dt (or the samples)
       for (uint32_t m = relMonE; m; m &= m - 1) {
         const MonDesc<T>& d = pe.mon[__ffs(m) - 1];
         const int64_t r = n - d.n0;
-        if (r < 0 || r >= d.rows) atomicOr(a.flag, ERRBIT_TABLE);
-        else if (d.comp == ETG_EX) tb_dft<T, RPT, W>(d, ex, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
-        else tb_dft<T, RPT, W>(d, ey, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
+        if (d.samp) {
+          if (d.comp == ETG_EX) tb_sample<T, RPT, W>(d, ex, i0, j0, t_lo, t_hi, e_lo, e_hi, step_off + s);
+          else tb_sample<T, RPT, W>(d, ey, i0, j0, t_lo, t_hi, e_lo, e_hi, step_off + s);
+        } else if (r < 0 || r >= d.rows) {
+          atomicOr(a.flag, ERRBIT_TABLE);
+        } else if (d.comp == ETG_EX) {
+          tb_dft<T, RPT, W>(d, ex, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
+        } else {
+          tb_dft<T, RPT, W>(d, ey, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
+        }
       }
     }
     ey[0].st(sEyX + ty * EC + lj0);
@@ -437,45 +489,70 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
 
 // Shared memory of a launch of the interior kernel (PML false) or the CPML kernel (the
 // largest CPML kind).
-template <typename T, int RPT, int K, bool PML>
+template <typename T, int RPT, int K, bool PML, int NW = 8>
 constexpr size_t tb_smem() {
-  return TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER>::SMEM;
+  return TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER, NW>::SMEM;
 }
 
-template <typename T, int RPT, int K, bool PML>
-__global__ void __launch_bounds__(TB_THREADS, TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER>::MIN_BLOCKS)
+template <typename T, int RPT, int K, int KIND, int NW>
+__device__ __forceinline__ void tb_tile_nw(const SimArgs<T>& a, const TBDst<T>& dst, const int2 tile,
+                                           const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off) {
+  tb_tile<T, RPT, K, KIND, false, TBNoHook, NW>(a, dst, tile, ph, pe, step_off);
+}
+
+template <typename T, int RPT, int K, bool PML, int NW = 8>
+__global__ void __launch_bounds__(32 * NW, TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER, NW>::MIN_BLOCKS)
 k_tb_step(const __grid_constant__ SimArgs<T> a, const __grid_constant__ TBDst<T> dst,
           const int2* __restrict__ tiles, const __grid_constant__ PhasePlan<T> ph,
           const __grid_constant__ PhasePlan<T> pe, int step_off) {
   const int2 t = tiles[blockIdx.x];
   if (!PML) {
-    tb_tile<T, RPT, K, KIND_INNER>(a, dst, t, ph, pe, step_off);
+    tb_tile_nw<T, RPT, K, KIND_INNER, NW>(a, dst, t, ph, pe, step_off);
     return;
   }
   const int2 u = make_int2(t.x & ((1 << KIND_SHIFT) - 1), t.y);
   switch (t.x >> KIND_SHIFT) {
-    case KIND_X: tb_tile<T, RPT, K, KIND_X>(a, dst, u, ph, pe, step_off); break;
-    case KIND_Y: tb_tile<T, RPT, K, KIND_Y>(a, dst, u, ph, pe, step_off); break;
-    default: tb_tile<T, RPT, K, KIND_XY>(a, dst, u, ph, pe, step_off); break;
+    case KIND_X: tb_tile_nw<T, RPT, K, KIND_X, NW>(a, dst, u, ph, pe, step_off); break;
+    case KIND_Y: tb_tile_nw<T, RPT, K, KIND_Y, NW>(a, dst, u, ph, pe, step_off); break;
+    default: tb_tile_nw<T, RPT, K, KIND_XY, NW>(a, dst, u, ph, pe, step_off); break;
   }
+}
+
+// One CPML kind per kernel: each kernel then holds one tile body, which keeps the code of a
+// launch within the instruction cache (the three bodies in one kernel did not fit).
+template <typename T, int RPT, int K, int KIND, int NW = 8>
+__global__ void __launch_bounds__(32 * NW, 1)
+k_tb_kind(const __grid_constant__ SimArgs<T> a, const __grid_constant__ TBDst<T> dst,
+          const int2* __restrict__ tiles, const __grid_constant__ PhasePlan<T> ph,
+          const __grid_constant__ PhasePlan<T> pe, int step_off) {
+  const int2 t = tiles[blockIdx.x];
+  tb_tile_nw<T, RPT, K, KIND, NW>(a, dst, make_int2(t.x & ((1 << KIND_SHIFT) - 1), t.y), ph, pe, step_off);
+}
+
+template <typename T, int RPT, int K, int KIND, int NW = 8>
+__global__ void __launch_bounds__(32 * NW, 1)
+k_tb_batch_kind(const BatchSim<T>* __restrict__ sims, const int4* __restrict__ tiles, int parity, int step_off) {
+  const int4 t = tiles[blockIdx.x];  // simulation, r0, c0, kind
+  const BatchSim<T>& b = sims[t.x];
+  tb_tile_nw<T, RPT, K, KIND, NW>(b.src[parity], b.dst[parity], make_int2(t.y, t.z), b.ph, b.pe, step_off);
 }
 
 // Batched form: every tile names its simulation (and, for CPML tiles, its kind in .w); all
 // simulations advance the same K steps.
-template <typename T, int RPT, int K, bool PML>
-__global__ void __launch_bounds__(TB_THREADS, TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER>::MIN_BLOCKS)
+template <typename T, int RPT, int K, bool PML, int NW = 8>
+__global__ void __launch_bounds__(32 * NW, TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER, NW>::MIN_BLOCKS)
 k_tb_batch(const BatchSim<T>* __restrict__ sims, const int4* __restrict__ tiles, int parity, int step_off) {
   const int4 t = tiles[blockIdx.x];  // simulation, r0, c0, kind
   const BatchSim<T>& b = sims[t.x];
   const int2 u = make_int2(t.y, t.z);
   if (!PML) {
-    tb_tile<T, RPT, K, KIND_INNER>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off);
+    tb_tile_nw<T, RPT, K, KIND_INNER, NW>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off);
     return;
   }
   switch (t.w) {
-    case KIND_X: tb_tile<T, RPT, K, KIND_X>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off); break;
-    case KIND_Y: tb_tile<T, RPT, K, KIND_Y>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off); break;
-    default: tb_tile<T, RPT, K, KIND_XY>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off); break;
+    case KIND_X: tb_tile_nw<T, RPT, K, KIND_X, NW>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off); break;
+    case KIND_Y: tb_tile_nw<T, RPT, K, KIND_Y, NW>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off); break;
+    default: tb_tile_nw<T, RPT, K, KIND_XY, NW>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off); break;
   }
 }
 
@@ -843,16 +920,185 @@ k_tb_tma(const __grid_constant__ TMAMaps maps, const __grid_constant__ SimArgs<T
   }
 }
 
+// ------------------------------------------------------------------------ block DFT
+//
+// Tiles that hold monitor nodes record them per step (tb_sample); after each block of
+// launches one thread per (monitor, frequency, node) adds the block's samples to its
+// accumulator in step order. Done in the tile itself, those serial read-modify-writes made
+// the monitor tiles the longest of every launch.
+
+template <typename T>
+__global__ void k_dft_block(const __grid_constant__ PhasePlan<T> ph, const __grid_constant__ PhasePlan<T> pe,
+                            const int64_t* __restrict__ step, int n_slots, int* flag) {
+  const int m = blockIdx.y;
+  const MonDesc<T>& d = m < ph.n_mon ? ph.mon[m] : pe.mon[m - ph.n_mon];
+  dft_block_node(d, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, *step, n_slots, flag);
+}
+
+template <typename T>
+__global__ void k_dft_block_batch(const BatchSim<T>* __restrict__ sims, int n_slots) {
+  const BatchSim<T>& b = sims[blockIdx.y];
+  const int m = blockIdx.z;
+  if (m >= b.ph.n_mon + b.pe.n_mon) return;
+  const MonDesc<T>& d = m < b.ph.n_mon ? b.ph.mon[m] : b.pe.mon[m - b.ph.n_mon];
+  dft_block_node(d, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, *b.src[0].step, n_slots, b.src[0].flag);
+}
+
+// Largest (frequencies x nodes) of the sampled monitors of a plan pair; 0 when none samples.
+template <typename T>
+static int64_t sampled_work(const PhasePlan<T>& ph, const PhasePlan<T>& pe, int* n_mon) {
+  int64_t w = 0;
+  *n_mon = ph.n_mon + pe.n_mon;
+  for (int m = 0; m < *n_mon; ++m) {
+    const MonDesc<T>& d = m < ph.n_mon ? ph.mon[m] : pe.mon[m - ph.n_mon];
+    if (d.samp) w = std::max<int64_t>(w, (int64_t)d.nxm * d.nym * d.n_f);
+  }
+  return w;
+}
+
+template <typename T>
+void launch_dft_block(const SimArgs<T>& a, const PhasePlan<T>& ph, const PhasePlan<T>& pe, int n_slots,
+                      cudaStream_t s) {
+  int n_mon = 0;
+  const int64_t w = sampled_work(ph, pe, &n_mon);
+  if (w == 0 || n_slots == 0) return;
+  k_dft_block<T><<<dim3((unsigned)((w + 127) / 128), (unsigned)n_mon), 128, 0, s>>>(ph, pe, a.step, n_slots, a.flag);
+  g_launches += 1;
+}
+
+template <typename T>
+void tb_batch_dft(const void* sims, int n_sims, int64_t max_work, int max_mon, int n_slots, cudaStream_t s) {
+  if (max_work == 0 || n_slots == 0) return;
+  const dim3 grid((unsigned)((max_work + 127) / 128), (unsigned)n_sims, (unsigned)max_mon);
+  k_dft_block_batch<T><<<grid, 128, 0, s>>>((const BatchSim<T>*)sims, n_slots);
+  g_launches += 1;
+}
+
+template void tb_batch_dft<float>(const void*, int, int64_t, int, int, cudaStream_t);
+template void tb_batch_dft<double>(const void*, int, int64_t, int, int, cudaStream_t);
+
+// ------------------------------------------------------------------------ persistent pipelined kernel
+//
+// One CTA per SM claims tiles from a device counter until none is left: CPML tiles first
+// (the long ones, each loading itself), then interior tiles. While an interior tile runs its
+// K steps, TMA brings the next interior tile's Ex, Ey, Hz into the stage and its cb into the
+// other cb buffer, so the load of every interior tile but a CTA's first is hidden behind the
+// previous tile's work. With no register cap (one CTA per SM) the tile body is the same code
+// as k_tb_step's. The claim counter resets itself: the last CTA out zeroes it.
+
+template <typename T, int RPT, int K>
+struct PipeShape {
+  static constexpr int W = TBVec<T>::W, ER = 8 * RPT, EC = 32 * W, PL = ER * EC, XCH = 9 * EC;
+  static constexpr size_t STAGE = 3 * (size_t)PL * sizeof(T);  // Ex, Ey, Hz of the next tile
+  static constexpr size_t CBUF = 4 * (size_t)PL * sizeof(T);   // cb_ex, cb_ey of two tiles
+  static constexpr size_t XCHB = 2 * (size_t)XCH * sizeof(T);
+  static constexpr uint32_t TX = (uint32_t)(5 * PL * sizeof(T));
+  static constexpr size_t CPML = TBShape<T, RPT, K, KIND_XY>::SMEM;
+  static constexpr size_t SMEM = 128 + (STAGE + CBUF + XCHB > CPML ? STAGE + CBUF + XCHB : CPML) + 16;
+  static_assert((PL * sizeof(T)) % 128 == 0, "stage planes stay 128-byte aligned");
+};
+
+template <typename T, int RPT, int K>
+__global__ void __launch_bounds__(TB_THREADS, 1)
+k_tb_pipe(const __grid_constant__ TMAMaps maps, const __grid_constant__ SimArgs<T> a,
+          const __grid_constant__ TBDst<T> dst, const int2* __restrict__ tiles, int n_inner, int n_pml,
+          unsigned* __restrict__ ctr, const __grid_constant__ PhasePlan<T> ph,
+          const __grid_constant__ PhasePlan<T> pe, int step_off) {
+  using S = PipeShape<T, RPT, K>;
+  constexpr int PL = S::PL;
+  extern __shared__ __align__(128) unsigned char pipe_smem[];
+  unsigned char* const base = pipe_smem + ((128u - (smem_addr(pipe_smem) & 127u)) & 127u);
+  T* const stage = reinterpret_cast<T*>(base);
+  T* const cbuf = reinterpret_cast<T*>(base + S::STAGE);
+  T* const xch = reinterpret_cast<T*>(base + S::STAGE + S::CBUF);
+  // past both layouts (a CPML tile uses the dynamic shared memory from its start)
+  uint64_t* const mbar = reinterpret_cast<uint64_t*>(pipe_smem + S::SMEM - 16);
+  __shared__ int s_next, s_pending, s_ok;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const int n_all = n_pml + n_inner;
+
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto fetch = [&](int k_inner, int buf) {  // one thread: interior tile k_inner into stage, cb buffer buf
+    const int2 t = tiles[k_inner];
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(S::TX)
+                 : "memory");
+    const int x = t.y - K, y = t.x - K;
+    tma_load_tile(stage + 0 * PL, &maps.ex, x, y, mbar);
+    tma_load_tile(stage + 1 * PL, &maps.ey, x, y, mbar);
+    tma_load_tile(stage + 2 * PL, &maps.hz, x, y, mbar);
+    tma_load_tile(cbuf + (2 * buf) * PL, &maps.cbx, x, y, mbar);
+    tma_load_tile(cbuf + (2 * buf + 1) * PL, &maps.cby, x, y, mbar);
+  };
+  // claim the next tile; prefetch it into cb buffer `buf` when it is interior and `may_fetch`
+  auto claim = [&](int buf, bool may_fetch) {
+    if (tid == 0) {
+      const int k = (int)atomicAdd(ctr, 1u);
+      s_next = k;
+      s_pending = 0;
+      if (may_fetch && k >= n_pml && k < n_all) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        fetch(k - n_pml, buf);
+        s_pending = 1;
+      }
+    }
+  };
+  claim(0, true);
+  __syncthreads();
+  int cur = s_next, pending = s_pending, buf = 0;
+  uint32_t parity = 0;
+  while (cur < n_all) {
+    if (cur < n_pml) {  // a CPML tile loads itself; nothing can be staged meanwhile
+      const int2 raw = tiles[n_inner + cur];
+      const int2 u = make_int2(raw.x & ((1 << KIND_SHIFT) - 1), raw.y);
+      auto hook = [&]() { claim(buf, false); };
+      switch (raw.x >> KIND_SHIFT) {
+        case KIND_X: tb_tile<T, RPT, K, KIND_X>(a, dst, u, ph, pe, step_off, nullptr, nullptr, nullptr, hook); break;
+        case KIND_Y: tb_tile<T, RPT, K, KIND_Y>(a, dst, u, ph, pe, step_off, nullptr, nullptr, nullptr, hook); break;
+        default: tb_tile<T, RPT, K, KIND_XY>(a, dst, u, ph, pe, step_off, nullptr, nullptr, nullptr, hook); break;
+      }
+    } else {
+      if (!pending && tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        fetch(cur - n_pml, buf);
+      }
+      if (tid == 0) s_ok = 1;
+      __syncthreads();
+      if (!mbar_wait_bounded(mbar, parity, a.flag)) s_ok = 0;
+      parity ^= 1;
+      if (!__syncthreads_and(s_ok)) break;  // the copy never landed: flagged, leave uniformly
+      const int2 tile = tiles[cur - n_pml];
+      auto hook = [&]() { claim(buf ^ 1, true); };
+      tb_tile<T, RPT, K, KIND_INNER, true>(a, dst, tile, ph, pe, step_off, stage, cbuf + 2 * buf * PL, xch, hook);
+      buf ^= 1;
+    }
+    __syncthreads();  // s_next, s_pending published; cb buffer and exchange rows free
+    cur = s_next;
+    pending = s_pending;
+  }
+  if (tid == 0) {  // the last CTA out resets the claim counter for the next launch
+    __threadfence();
+    if (atomicAdd(ctr + 1, 1u) == gridDim.x - 1) {
+      ctr[0] = 0;
+      ctr[1] = 0;
+      __threadfence();
+    }
+  }
+}
+
 // ------------------------------------------------------------------------ host side
 
 struct TBConfig {
-  int dtype, RPT, K;  // tile rows 8 * RPT, columns 32 * W (128 for f32, 64 for f64), depth K
+  int dtype, RPT, K, NW;  // tile rows NW * RPT, columns 32 * W (128 for f32, 64 for f64), depth K, NW warps
 };
 
-static constexpr TBConfig kDefault32 = {ETG_F32, 6, 4};
-static constexpr TBConfig kDefault64 = {ETG_F64, 5, 2};
-static constexpr TBConfig kTmaDefault32 = {ETG_F32, 5, 4};
-static constexpr TBConfig kTmaDefault64 = {ETG_F64, 5, 2};
+static constexpr TBConfig kDefault32 = {ETG_F32, 6, 4, 8};
+static constexpr TBConfig kDefault64 = {ETG_F64, 5, 2, 8};
+static constexpr TBConfig kTmaDefault32 = {ETG_F32, 5, 4, 8};
+static constexpr TBConfig kTmaDefault64 = {ETG_F64, 5, 2, 8};
 
 struct TBState {
   TMAMaps maps[2];          // TMA descriptors of (fields A, cb) and (fields B, cb)
@@ -863,18 +1109,23 @@ struct TBState {
   size_t alt_bytes = 0;
   int2* tiles = nullptr;  // interior tiles first, then CPML tiles
   int n_inner = 0, n_pml = 0;
-  TBConfig cfg = {0, 0, 0};
+  TBConfig cfg = {0, 0, 0, 0};
   int nx = -1, ny = -1;
   bool tiles_valid = false;
   std::map<int64_t, cudaGraphExec_t> graphs;
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+  cudaStream_t sides[3] = {};    // one branch per CPML kind
+  cudaEvent_t joins[3] = {};
   // per-kernel timing (ETG_OPT_TIMING 2): launches serialised on the main stream, no graphs
   bool profile = false;
-  cudaEvent_t pev[3] = {};
+  cudaEvent_t pev[7] = {};
   double prof_ms[2] = {};        // interior, CPML
+  double prof_kind_ms[3] = {};   // CPML tiles of each kind launched alone: X, Y, XY
   int64_t prof_launches[2] = {};
-  int64_t owned_cells[2] = {};   // output cells of one launch of each kernel, inside the grid
+  int64_t owned_cells[5] = {};   // output cells of one launch: interior, CPML, and per CPML kind
+  int n_kind[3] = {};            // CPML tiles of each kind (the CPML list is sorted by kind)
+  unsigned* ctr = nullptr;       // persistent pipelined kernel: claim counters of the two launches
 };
 
 TBState* tb_create() { return new TBState; }
@@ -889,9 +1140,14 @@ void tb_destroy(TBState* tb) {
   tb_drop_graphs(tb);
   for (void* p : tb->alt) cudaFree(p);
   cudaFree(tb->tiles);
+  cudaFree(tb->ctr);
   for (cudaEvent_t e : tb->pev)
     if (e) cudaEventDestroy(e);
   if (tb->side) cudaStreamDestroy(tb->side);
+  for (int k = 0; k < 3; ++k) {
+    if (tb->sides[k]) cudaStreamDestroy(tb->sides[k]);
+    if (tb->joins[k]) cudaEventDestroy(tb->joins[k]);
+  }
   if (tb->fork) cudaEventDestroy(tb->fork);
   if (tb->join) cudaEventDestroy(tb->join);
   delete tb;
@@ -910,45 +1166,87 @@ bool tb_supported(int nx, int ny) {
   return nx >= 64 && ny >= 64;  // both precisions: blocked beats one step per launch from here up
 }
 
-template <typename T, int RPT, int K, bool PML>
+template <typename T, int RPT, int K, bool PML, int NW = 8>
 static cudaError_t tb_launch_one(const SimArgs<T>& a, const TBDst<T>& d, const int2* tiles, int n,
                                  const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                  cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  k_tb_step<T, RPT, K, PML><<<n, dim3(32, 8), tb_smem<T, RPT, K, PML>(), s>>>(a, d, tiles, ph, pe, step_off);
+  k_tb_step<T, RPT, K, PML, NW><<<n, dim3(32, NW), tb_smem<T, RPT, K, PML, NW>(), s>>>(a, d, tiles, ph, pe, step_off);
   g_launches += 1;
   return cudaGetLastError();
 }
 
-template <typename T, int RPT, int K>
+// CPML tiles, one kernel per kind on its own side stream (tiles sorted X, Y, XY from `tiles`).
+template <typename T, int RP, int K>
+static cudaError_t tb_launch_kinds(const SimArgs<T>& a, const TBDst<T>& d, const int2* tiles, const int* n_kind,
+                                   const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
+                                   cudaStream_t const* side) {
+  cudaError_t e = cudaSuccess;
+  const int2* t = tiles;
+  if (n_kind[0] && e == cudaSuccess) {
+    k_tb_kind<T, RP, K, KIND_X><<<n_kind[0], dim3(32, 8), TBShape<T, RP, K, KIND_X>::SMEM, side[0]>>>(a, d, t, ph, pe,
+                                                                                                    step_off);
+    g_launches += 1;
+    e = cudaGetLastError();
+  }
+  t += n_kind[0];
+  if (n_kind[1] && e == cudaSuccess) {
+    k_tb_kind<T, RP, K, KIND_Y><<<n_kind[1], dim3(32, 8), TBShape<T, RP, K, KIND_Y>::SMEM, side[1]>>>(a, d, t, ph, pe,
+                                                                                                    step_off);
+    g_launches += 1;
+    e = cudaGetLastError();
+  }
+  t += n_kind[1];
+  if (n_kind[2] && e == cudaSuccess) {
+    k_tb_kind<T, RP, K, KIND_XY><<<n_kind[2], dim3(32, 8), TBShape<T, RP, K, KIND_XY>::SMEM, side[2]>>>(a, d, t, ph,
+                                                                                                      pe, step_off);
+    g_launches += 1;
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+template <typename T, int RPT, int K, int NW = 8>
 static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<T>& d,
                                   const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                   cudaStream_t s) {
+  constexpr int RP = RPT * NW / 8;  // CPML tiles: 8 warps over the same rows
   // interior tiles on the main stream, CPML tiles on a side branch (parallel graph nodes)
-  if (tb->profile) {  // one after the other on s, an event pair around each
+  if (tb->profile) {  // one after the other on s, an event pair around each kernel
     cudaError_t e = cudaEventRecord(tb->pev[0], s);
-    if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false>(a, d, tb->tiles, tb->n_inner, ph, pe, step_off, s);
-    if (e == cudaSuccess) e = cudaEventRecord(tb->pev[1], s);
-    if (e == cudaSuccess)
-      e = tb_launch_one<T, RPT, K, true>(a, d, tb->tiles + tb->n_inner, tb->n_pml, ph, pe, step_off, s);
-    if (e == cudaSuccess) e = cudaEventRecord(tb->pev[2], s);
-    if (e == cudaSuccess) e = cudaEventSynchronize(tb->pev[2]);
-    float m0 = 0, m1 = 0;
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&m0, tb->pev[0], tb->pev[1]);
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&m1, tb->pev[1], tb->pev[2]);
-    tb->prof_ms[0] += m0;
-    tb->prof_ms[1] += m1;
+    if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW>(a, d, tb->tiles, tb->n_inner, ph, pe, step_off, s);
+    const int2* t = tb->tiles + tb->n_inner;
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+      int only[3] = {0, 0, 0};
+      only[k] = tb->n_kind[k];
+      e = cudaEventRecord(tb->pev[1 + k], s);
+      if (e == cudaSuccess) {
+        cudaStream_t ss[3] = {s, s, s};
+        e = tb_launch_kinds<T, RP, K>(a, d, t, only, ph, pe, step_off, ss);
+      }
+      t += tb->n_kind[k];
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(tb->pev[4], s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(tb->pev[4]);
+    float m[4] = {};
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventElapsedTime(&m[k], tb->pev[k], tb->pev[k + 1]);
+    tb->prof_ms[0] += m[0];
+    tb->prof_ms[1] += m[1] + m[2] + m[3];
+    for (int k = 0; k < 3; ++k) tb->prof_kind_ms[k] += m[1 + k];
     tb->prof_launches[0] += tb->n_inner > 0;
     tb->prof_launches[1] += tb->n_pml > 0;
     return e;
   }
+  // CPML kinds on three side branches, interior tiles on the main stream (parallel graph nodes)
   cudaError_t e = cudaEventRecord(tb->fork, s);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(tb->side, tb->fork, 0);
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(tb->sides[k], tb->fork, 0);
   if (e == cudaSuccess)
-    e = tb_launch_one<T, RPT, K, true>(a, d, tb->tiles + tb->n_inner, tb->n_pml, ph, pe, step_off, tb->side);
-  if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false>(a, d, tb->tiles, tb->n_inner, ph, pe, step_off, s);
-  if (e == cudaSuccess) e = cudaEventRecord(tb->join, tb->side);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, tb->join, 0);
+    e = tb_launch_kinds<T, RP, K>(a, d, tb->tiles + tb->n_inner, tb->n_kind, ph, pe, step_off, tb->sides);
+  if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW>(a, d, tb->tiles, tb->n_inner, ph, pe, step_off, s);
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+    e = cudaEventRecord(tb->joins[k], tb->sides[k]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, tb->joins[k], 0);
+  }
   return e;
 }
 
@@ -971,23 +1269,33 @@ static TBDst<T> as_dst(const SimArgs<T>& a) {
 }
 
 // Two launches A -> B -> A covering 2K steps from step_off.
-template <typename T, int RPT, int K>
+template <typename T, int RPT, int K, int NW = 8>
 static cudaError_t tb_two(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& ph,
                           const PhasePlan<T>& pe, int step_off, cudaStream_t s) {
   const SimArgs<T> b = swap_args(a, tb);
-  cudaError_t e = tb_launch_pair<T, RPT, K>(tb, a, as_dst(b), ph, pe, step_off, s);
-  if (e == cudaSuccess) e = tb_launch_pair<T, RPT, K>(tb, b, as_dst(a), ph, pe, step_off + K, s);
+  cudaError_t e = tb_launch_pair<T, RPT, K, NW>(tb, a, as_dst(b), ph, pe, step_off, s);
+  if (e == cudaSuccess) e = tb_launch_pair<T, RPT, K, NW>(tb, b, as_dst(a), ph, pe, step_off + K, s);
   return e;
 }
 
 // Dynamic shared memory above 48 KB must be allowed per kernel, before any launch or capture.
-template <typename T, int RPT, int K>
+template <typename T, int RPT, int K, int NW = 8>
 static cudaError_t tb_attrs() {
-  cudaError_t e = cudaFuncSetAttribute(k_tb_step<T, RPT, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)tb_smem<T, RPT, K, false>());
+  cudaError_t e = cudaFuncSetAttribute(k_tb_step<T, RPT, K, false, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)tb_smem<T, RPT, K, false, NW>());
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_tb_step<T, RPT, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)tb_smem<T, RPT, K, true>());
+    e = cudaFuncSetAttribute(k_tb_step<T, RPT * NW / 8, K, true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tb_smem<T, RPT * NW / 8, K, true, 8>());
+  constexpr int RP = RPT * NW / 8;
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_tb_kind<T, RP, K, KIND_X>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TBShape<T, RP, K, KIND_X>::SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_tb_kind<T, RP, K, KIND_Y>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TBShape<T, RP, K, KIND_Y>::SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_tb_kind<T, RP, K, KIND_XY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TBShape<T, RP, K, KIND_XY>::SMEM);
   return e;
 }
 
@@ -1045,21 +1353,55 @@ static cudaError_t tma_two(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>&
   return cudaGetLastError();
 }
 
+template <typename T, int RPT, int K>
+static cudaError_t pipe_attrs() {
+  return cudaFuncSetAttribute(k_tb_pipe<T, RPT, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)PipeShape<T, RPT, K>::SMEM);
+}
+
+// Two persistent pipelined launches A -> B -> A covering 2K steps from step_off, one CTA per SM.
+template <typename T, int RPT, int K>
+static cudaError_t pipe_two(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& ph, const PhasePlan<T>& pe,
+                            int step_off, cudaStream_t s) {
+  using S = PipeShape<T, RPT, K>;
+  const SimArgs<T> b = swap_args(a, tb);
+  k_tb_pipe<T, RPT, K><<<tb->sms, dim3(32, 8), S::SMEM, s>>>(tb->maps[0], a, as_dst(b), tb->tiles, tb->n_inner,
+                                                             tb->n_pml, tb->ctr, ph, pe, step_off);
+  k_tb_pipe<T, RPT, K><<<tb->sms, dim3(32, 8), S::SMEM, s>>>(tb->maps[1], b, as_dst(a), tb->tiles, tb->n_inner,
+                                                             tb->n_pml, tb->ctr + 2, ph, pe, step_off + K);
+  g_launches += 2;
+  return cudaGetLastError();
+}
+
 // Compiled shapes (rows = 8 * RPT, depth K); the CPML variant's six planes must fit 227 KB.
-#define ETG_TB_SHAPES_F32(X) X(ETG_F32, 5, 4) X(ETG_F32, 6, 4) X(ETG_F32, 8, 4)
-#define ETG_TB_SHAPES_F64(X) X(ETG_F64, 4, 2) X(ETG_F64, 5, 2)
+// X(dtype, rows per warp, depth, warps)
+// (CPML tiles always run 8 warps on the same tile: rows per warp NW * RPT / 8)
+#define ETG_TB_SHAPES_F32(X) X(ETG_F32, 5, 4, 8) X(ETG_F32, 6, 4, 8) X(ETG_F32, 8, 4, 8) X(ETG_F32, 3, 4, 16)
+#define ETG_TB_SHAPES_F64(X) X(ETG_F64, 4, 2, 8) X(ETG_F64, 5, 2, 8)
 
 // Shapes of the persistent TMA kernel: two stages of five planes must fit 227 KB.
 #define ETG_TMA_SHAPES_F32(X) X(ETG_F32, 5, 4)
 #define ETG_TMA_SHAPES_F64(X) X(ETG_F64, 5, 2)
 
+// Shapes of the persistent pipelined kernel: stage, two cb buffers and exchange rows must fit.
+#define ETG_PIPE_SHAPES_F32(X) X(ETG_F32, 5, 4) X(ETG_F32, 6, 4)
+#define ETG_PIPE_SHAPES_F64(X) X(ETG_F64, 4, 2) X(ETG_F64, 5, 2)
+
 template <typename T>
 static TBFns<T> pick(const TBConfig& c, int mode) {
-#define ETG_TB_CASE(DT, R, KK) \
-  if (c.dtype == DT && c.RPT == R && c.K == KK) return {&tb_two<T, R, KK>, &tb_attrs<T, R, KK>};
+#define ETG_TB_CASE(DT, R, KK, NWW) \
+  if (c.dtype == DT && c.RPT == R && c.K == KK && c.NW == NWW) return {&tb_two<T, R, KK, NWW>, &tb_attrs<T, R, KK, NWW>};
 #define ETG_TMA_CASE(DT, R, KK) \
-  if (c.dtype == DT && c.RPT == R && c.K == KK) return {&tma_two<T, R, KK>, &tma_attrs<T, R, KK>};
-  if (mode == 1) {
+  if (c.dtype == DT && c.RPT == R && c.K == KK && c.NW == 8) return {&tma_two<T, R, KK>, &tma_attrs<T, R, KK>};
+#define ETG_PIPE_CASE(DT, R, KK) \
+  if (c.dtype == DT && c.RPT == R && c.K == KK && c.NW == 8) return {&pipe_two<T, R, KK>, &pipe_attrs<T, R, KK>};
+  if (mode == 2) {
+    if constexpr (sizeof(T) == 4) {
+      ETG_PIPE_SHAPES_F32(ETG_PIPE_CASE)
+    } else {
+      ETG_PIPE_SHAPES_F64(ETG_PIPE_CASE)
+    }
+  } else if (mode == 1) {
     if constexpr (sizeof(T) == 4) {
       ETG_TMA_SHAPES_F32(ETG_TMA_CASE)
     } else {
@@ -1074,6 +1416,7 @@ static TBFns<T> pick(const TBConfig& c, int mode) {
   }
 #undef ETG_TB_CASE
 #undef ETG_TMA_CASE
+#undef ETG_PIPE_CASE
   return {nullptr, nullptr};
 }
 
@@ -1081,14 +1424,22 @@ static std::string shapes_text(int dtype, int mode) {
   std::string out;
 #define ETG_TB_NAME(DT, R, KK) \
   if (DT == dtype) out += " " + std::to_string(8 * R) + "x" + std::to_string(DT == ETG_F32 ? 128 : 64) + "/K" + std::to_string(KK);
-  if (mode == 1) {
+#define ETG_TB_NAME4(DT, R, KK, NWW)                                                                              \
+  if (DT == dtype)                                                                                                \
+    out += " " + std::to_string(NWW * R) + "x" + std::to_string(DT == ETG_F32 ? 128 : 64) + "/K" + std::to_string(KK) + \
+           "/" + std::to_string(NWW) + "w";
+  if (mode == 2) {
+    ETG_PIPE_SHAPES_F32(ETG_TB_NAME)
+    ETG_PIPE_SHAPES_F64(ETG_TB_NAME)
+  } else if (mode == 1) {
     ETG_TMA_SHAPES_F32(ETG_TB_NAME)
     ETG_TMA_SHAPES_F64(ETG_TB_NAME)
   } else {
-    ETG_TB_SHAPES_F32(ETG_TB_NAME)
-    ETG_TB_SHAPES_F64(ETG_TB_NAME)
+    ETG_TB_SHAPES_F32(ETG_TB_NAME4)
+    ETG_TB_SHAPES_F64(ETG_TB_NAME4)
   }
 #undef ETG_TB_NAME
+#undef ETG_TB_NAME4
   return out;
 }
 
@@ -1120,14 +1471,18 @@ static void split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_
         pml.push_back(make_int2(r0 | (kind << KIND_SHIFT), c0));
       }
     }
+  // CPML tiles grouped by kind (X, Y, XY), so that each kind is one contiguous range
+  std::stable_sort(pml.begin(), pml.end(), [](int2 p, int2 q) { return (p.x >> KIND_SHIFT) < (q.x >> KIND_SHIFT); });
   if (hot) {
-    auto first = [&](std::vector<int2>& v) {
-      std::stable_partition(v.begin(), v.end(), [&](int2 t) {
-        return hot->hits((t.x & ((1 << KIND_SHIFT) - 1)) - K, t.y - K, ER, EC);
-      });
+    auto first = [&](std::vector<int2>::iterator b, std::vector<int2>::iterator e) {
+      std::stable_partition(b, e, [&](int2 t) { return hot->hits((t.x & ((1 << KIND_SHIFT) - 1)) - K, t.y - K, ER, EC); });
     };
-    first(inner);
-    first(pml);
+    first(inner.begin(), inner.end());
+    for (int kind = KIND_X; kind <= KIND_XY; ++kind) {
+      auto b = std::find_if(pml.begin(), pml.end(), [&](int2 t) { return (t.x >> KIND_SHIFT) == kind; });
+      auto e = std::find_if(b, pml.end(), [&](int2 t) { return (t.x >> KIND_SHIFT) != kind; });
+      first(b, e);
+    }
   }
   *n_inner = (int)inner.size();
   inner.insert(inner.end(), pml.begin(), pml.end());
@@ -1151,20 +1506,25 @@ template <typename T>
 static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt, const Hot& hot) {
   const int dt = (int)sizeof(T);
   const int EC = 32 * TBVec<T>::W;
-  const int mode = opt[ETG_OPT_KERNEL] == 3 ? 1 : 0;
-  TBConfig want = mode ? (dt == 4 ? kTmaDefault32 : kTmaDefault64) : (dt == 4 ? kDefault32 : kDefault64);
+  const int mode = opt[ETG_OPT_KERNEL] == 3 ? 1 : opt[ETG_OPT_KERNEL] == 4 ? 2 : 0;
+  TBConfig want = mode == 1 ? (dt == 4 ? kTmaDefault32 : kTmaDefault64) : (dt == 4 ? kDefault32 : kDefault64);
   if (opt[ETG_OPT_TB_DEPTH] > 0) want.K = (int)opt[ETG_OPT_TB_DEPTH];
-  if (opt[ETG_OPT_TILE_ROWS] > 0) want.RPT = (int)(opt[ETG_OPT_TILE_ROWS] / 8);
+  if (opt[ETG_OPT_TB_WARPS] > 0 && opt[ETG_OPT_TB_WARPS] != want.NW) {  // same rows, other split
+    want.RPT = want.RPT * want.NW / (int)opt[ETG_OPT_TB_WARPS];
+    want.NW = (int)opt[ETG_OPT_TB_WARPS];
+  }
+  if (opt[ETG_OPT_TILE_ROWS] > 0) want.RPT = (int)(opt[ETG_OPT_TILE_ROWS] / want.NW);
   const bool cols_ok = opt[ETG_OPT_TILE_COLS] == 0 || opt[ETG_OPT_TILE_COLS] == EC;
-  if (!cols_ok || opt[ETG_OPT_TILE_ROWS] % 8 != 0 || !pick<T>(want, mode).two) {
+  if (!cols_ok || opt[ETG_OPT_TILE_ROWS] % want.NW != 0 || !pick<T>(want, mode).two) {
     set_error("no compiled %s kernel with tile %lldx%lld and depth %d (have:%s)",
-              mode ? "persistent TMA" : "temporally blocked",
+              mode == 1 ? "persistent TMA" : mode == 2 ? "persistent pipelined" : "temporally blocked",
               (long long)(opt[ETG_OPT_TILE_ROWS] ? opt[ETG_OPT_TILE_ROWS] : 8 * want.RPT),
               (long long)(opt[ETG_OPT_TILE_COLS] ? opt[ETG_OPT_TILE_COLS] : EC), want.K,
               shapes_text(dt, mode).c_str());
     return ETG_ERR_ARGUMENT;
   }
-  if (want.RPT != tb->cfg.RPT || want.K != tb->cfg.K || want.dtype != tb->cfg.dtype || mode != tb->mode) {
+  if (want.RPT != tb->cfg.RPT || want.K != tb->cfg.K || want.NW != tb->cfg.NW || want.dtype != tb->cfg.dtype ||
+      mode != tb->mode) {
     tb_invalidate(tb);
     tb->cfg = want;
     tb->mode = mode;
@@ -1192,18 +1552,28 @@ static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt, cons
     ETG_TRY_CUDA(cudaStreamCreateWithFlags(&tb->side, cudaStreamNonBlocking));
     ETG_TRY_CUDA(cudaEventCreateWithFlags(&tb->fork, cudaEventDisableTiming));
     ETG_TRY_CUDA(cudaEventCreateWithFlags(&tb->join, cudaEventDisableTiming));
+    for (int k = 0; k < 3; ++k) {
+      ETG_TRY_CUDA(cudaStreamCreateWithFlags(&tb->sides[k], cudaStreamNonBlocking));
+      ETG_TRY_CUDA(cudaEventCreateWithFlags(&tb->joins[k], cudaEventDisableTiming));
+    }
   }
   if (!tb->tiles_valid || tb->nx != a.nx || tb->ny != a.ny) {
     std::vector<int2> inner;
-    split_tiles(a.nx, a.ny, a.ux_lo, a.ux_hi, a.uy_lo, a.uy_hi, 8 * tb->cfg.RPT, EC, tb->cfg.K, &inner,
+    split_tiles(a.nx, a.ny, a.ux_lo, a.ux_hi, a.uy_lo, a.uy_hi, tb->cfg.NW * tb->cfg.RPT, EC, tb->cfg.K, &inner,
                 &tb->n_inner, &hot);
     tb->n_pml = (int)inner.size() - tb->n_inner;
-    const int OR = 8 * tb->cfg.RPT - 2 * tb->cfg.K, OC = EC - 2 * tb->cfg.K;
-    tb->owned_cells[0] = tb->owned_cells[1] = 0;
+    const int OR = tb->cfg.NW * tb->cfg.RPT - 2 * tb->cfg.K, OC = EC - 2 * tb->cfg.K;
+    for (int64_t& c : tb->owned_cells) c = 0;
+    for (int& c : tb->n_kind) c = 0;
     for (int q = 0; q < (int)inner.size(); ++q) {
       const int64_t r = std::max(0, std::min(OR, a.nx - tb_tile_row(inner[q]))),
                     c = std::max(0, std::min(OC, a.ny - inner[q].y));
       tb->owned_cells[q < tb->n_inner ? 0 : 1] += r * c;
+      if (q >= tb->n_inner) {
+        const int kind = tb_tile_kind(inner[q]);
+        tb->owned_cells[1 + kind] += r * c;
+        tb->n_kind[kind - 1] += 1;
+      }
     }
     cudaFree(tb->tiles);
     tb->tiles = nullptr;
@@ -1214,9 +1584,13 @@ static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt, cons
     tb->tiles_valid = true;
     tb_drop_graphs(tb);
   }
-  if (mode == 1 && !tb->maps_valid) {
+  if (mode == 2 && !tb->ctr) {
+    ETG_TRY_CUDA(cudaMalloc(&tb->ctr, 4 * sizeof(unsigned)));
+    ETG_TRY_CUDA(cudaMemset(tb->ctr, 0, 4 * sizeof(unsigned)));
+  }
+  if (mode >= 1 && !tb->maps_valid) {
     ETG_REQUIRE(a.P >= EC && a.nx + 2 >= 8 * tb->cfg.RPT, ETG_ERR_ARGUMENT,
-                "the persistent TMA kernel needs a grid of at least %d x %d cells", 8 * tb->cfg.RPT, EC);
+                "the persistent kernels need a grid of at least %d x %d cells", 8 * tb->cfg.RPT, EC);
     int rc = get_encoder();
     if (rc) return rc;
     int dev = 0;
@@ -1248,38 +1622,46 @@ int tb_advance(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& ph, const P
     for (cudaEvent_t& e : tb->pev)
       if (!e) ETG_TRY_CUDA(cudaEventCreate(&e));
     tb->prof_ms[0] = tb->prof_ms[1] = 0;
+    tb->prof_kind_ms[0] = tb->prof_kind_ms[1] = tb->prof_kind_ms[2] = 0;
     tb->prof_launches[0] = tb->prof_launches[1] = 0;
   }
   const auto two = pick<T>(tb->cfg, tb->mode).two;
   const int K = tb->cfg.K;
   const int64_t pairs = n_steps / (2 * K);
   const int64_t per_graph = std::max<int64_t>(1, opt[ETG_OPT_GRAPH_STEPS] / (2 * K));
+  // a block: up to per_graph launch pairs, the DFT of the block's samples, the step counter
+  auto block = [&](int64_t n_pairs) -> cudaError_t {
+    cudaError_t e = cudaSuccess;
+    for (int64_t p = 0; p < n_pairs && e == cudaSuccess; ++p) e = two(tb, a, ph, pe, (int)(2 * K * p), s);
+    if (e == cudaSuccess) launch_dft_block<T>(a, ph, pe, (int)(2 * K * n_pairs), s);
+    if (e == cudaSuccess) launch_step_add<T>(a, 2 * K * n_pairs, s);
+    return e == cudaSuccess ? cudaGetLastError() : e;
+  };
   int64_t done = 0;  // pairs launched
   if (opt[ETG_OPT_GRAPH_STEPS] > 0 && pairs >= per_graph && !tb->profile) {
     auto it = tb->graphs.find(per_graph);
     if (it == tb->graphs.end()) {
       cudaGraph_t graph;
       ETG_TRY_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      cudaError_t e = cudaSuccess;
-      for (int64_t p = 0; p < per_graph && e == cudaSuccess; ++p) e = two(tb, a, ph, pe, (int)(2 * K * p), s);
-      if (e == cudaSuccess) launch_step_add<T>(a, 2 * K * per_graph, s);
+      const cudaError_t e = block(per_graph);
       cudaError_t e2 = cudaStreamEndCapture(s, &graph);
       ETG_REQUIRE(e == cudaSuccess && e2 == cudaSuccess, ETG_ERR_CUDA, "temporal-blocking graph capture failed: %s",
                   cudaGetErrorString(e != cudaSuccess ? e : e2));
       cudaGraphExec_t exec;
-      e = cudaGraphInstantiate(&exec, graph, 0);
+      e2 = cudaGraphInstantiate(&exec, graph, 0);
       cudaGraphDestroy(graph);
-      ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+      ETG_REQUIRE(e2 == cudaSuccess, ETG_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e2));
       it = tb->graphs.emplace(per_graph, exec).first;
     }
     for (; done + per_graph <= pairs; done += per_graph) {
       ETG_TRY_CUDA(cudaGraphLaunch(it->second, s));
-      g_launches += 4 * per_graph + 1;
+      g_launches += 4 * per_graph + 2;
     }
   }
-  if (done < pairs) {
-    for (int64_t p = 0; done + p < pairs; ++p) ETG_TRY_CUDA(two(tb, a, ph, pe, (int)(2 * K * p), s));
-    launch_step_add<T>(a, 2 * K * (pairs - done), s);
+  while (done < pairs) {
+    const int64_t c = std::min(per_graph, pairs - done);
+    ETG_TRY_CUDA(block(c));
+    done += c;
   }
   // the remainder (< 2K steps) with the one-step kernels, in place on the primary buffer
   const int64_t rem = n_steps - 2 * K * pairs;
@@ -1290,9 +1672,9 @@ int tb_advance(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& ph, const P
 }
 
 void tb_kernel_timing(const TBState* tb, double* ms, int64_t* launches, int64_t* cells) {
-  for (int k = 0; k < 2; ++k) {
-    ms[k] = tb ? tb->prof_ms[k] : 0;
-    launches[k] = tb ? tb->prof_launches[k] : 0;
+  for (int k = 0; k < 5; ++k) {
+    ms[k] = !tb ? 0 : k < 2 ? tb->prof_ms[k] : tb->prof_kind_ms[k - 2];
+    launches[k] = !tb ? 0 : k < 2 ? tb->prof_launches[k] : (tb->n_kind[k - 2] ? tb->prof_launches[1] : 0);
     cells[k] = tb ? tb->owned_cells[k] : 0;
   }
 }
@@ -1330,6 +1712,7 @@ cudaError_t tb_default_launch(const SimArgs<T>& src, const SimArgs<T>& dst, cons
                               int n_inner, int n_pml, int step_off, cudaStream_t s) {
   constexpr TBConfig c = sizeof(T) == 4 ? kDefault32 : kDefault64;
   constexpr int RPT = c.RPT, K = c.K;
+  static_assert(c.NW == 8, "the default shape is 8 warps");
   PhasePlan<T> none;
   memset(&none, 0, sizeof none);
   cudaError_t e = tb_attrs<T, RPT, K>();
@@ -1347,47 +1730,68 @@ template cudaError_t tb_default_launch<double>(const SimArgs<double>&, const Sim
 
 // ------------------------------------------------------------------------ batched launches
 
-template <typename T, int RPT, int K>
-static cudaError_t batch_pair(const void* sims, const int4* tiles, int n_inner, int n_pml, int parity,
-                              int step_off, cudaStream_t main, cudaStream_t side, cudaEvent_t fork,
-                              cudaEvent_t join) {
+template <typename T, int RP, int K, int KIND>
+static cudaError_t batch_kind(const BatchSim<T>* b, const int4* tiles, int n, int parity, int step_off,
+                              cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  k_tb_batch_kind<T, RP, K, KIND><<<n, dim3(32, 8), TBShape<T, RP, K, KIND>::SMEM, s>>>(b, tiles, parity, step_off);
+  g_launches += 1;
+  return cudaGetLastError();
+}
+
+template <typename T, int RPT, int K, int NW>
+static cudaError_t batch_pair(const void* sims, const int4* tiles, int n_inner, const int* n_kind, int parity,
+                              int step_off, cudaStream_t main, const cudaStream_t* sides, cudaEvent_t fork,
+                              const cudaEvent_t* joins) {
+  constexpr int RP = RPT * NW / 8;  // CPML tiles: 8 warps over the same rows, one kernel per kind
   const BatchSim<T>* b = (const BatchSim<T>*)sims;
   cudaError_t e = cudaEventRecord(fork, main);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork, 0);
-  if (e == cudaSuccess && n_pml) {
-    k_tb_batch<T, RPT, K, true><<<n_pml, dim3(32, 8), tb_smem<T, RPT, K, true>(), side>>>(b, tiles + n_inner, parity,
-                                                                                         step_off);
-    g_launches += 1;
-    e = cudaGetLastError();
-  }
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(sides[k], fork, 0);
+  const int4* t = tiles + n_inner;
+  if (e == cudaSuccess) e = batch_kind<T, RP, K, KIND_X>(b, t, n_kind[0], parity, step_off, sides[0]);
+  t += n_kind[0];
+  if (e == cudaSuccess) e = batch_kind<T, RP, K, KIND_Y>(b, t, n_kind[1], parity, step_off, sides[1]);
+  t += n_kind[1];
+  if (e == cudaSuccess) e = batch_kind<T, RP, K, KIND_XY>(b, t, n_kind[2], parity, step_off, sides[2]);
   if (e == cudaSuccess && n_inner) {
-    k_tb_batch<T, RPT, K, false><<<n_inner, dim3(32, 8), tb_smem<T, RPT, K, false>(), main>>>(b, tiles, parity,
-                                                                                              step_off);
+    k_tb_batch<T, RPT, K, false, NW><<<n_inner, dim3(32, NW), tb_smem<T, RPT, K, false, NW>(), main>>>(
+        b, tiles, parity, step_off);
     g_launches += 1;
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = cudaEventRecord(join, side);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(main, join, 0);
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+    e = cudaEventRecord(joins[k], sides[k]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(main, joins[k], 0);
+  }
   return e;
 }
 
-template <typename T, int RPT, int K>
+template <typename T, int RPT, int K, int NW>
 static cudaError_t batch_attrs() {
-  cudaError_t e = cudaFuncSetAttribute(k_tb_batch<T, RPT, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)tb_smem<T, RPT, K, false>());
+  constexpr int RP = RPT * NW / 8;
+  cudaError_t e = cudaFuncSetAttribute(k_tb_batch<T, RPT, K, false, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)tb_smem<T, RPT, K, false, NW>());
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_tb_batch<T, RPT, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)tb_smem<T, RPT, K, true>());
+    e = cudaFuncSetAttribute(k_tb_batch_kind<T, RP, K, KIND_X>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TBShape<T, RP, K, KIND_X>::SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_tb_batch_kind<T, RP, K, KIND_Y>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TBShape<T, RP, K, KIND_Y>::SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_tb_batch_kind<T, RP, K, KIND_XY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TBShape<T, RP, K, KIND_XY>::SMEM);
   return e;
 }
 
 template <typename T>
-int tb_batch_pair(int ER, int K, const void* sims, const int4* tiles, int n_inner, int n_pml, int parity,
-                  int step_off, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
-#define ETG_BATCH_CASE(DT, R, KK) \
-  if ((int)sizeof(T) == DT && ER == 8 * R && K == KK) {                                                   \
-    ETG_TRY_CUDA((batch_pair<T, R, KK>(sims, tiles, n_inner, n_pml, parity, step_off, main, side, fork, join))); \
-    return ETG_OK;                                                                                         \
+int tb_batch_pair(int ER, int K, int NW, const void* sims, const int4* tiles, int n_inner, const int* n_kind,
+                  int parity, int step_off, cudaStream_t main, const cudaStream_t* sides, cudaEvent_t fork,
+                  const cudaEvent_t* joins) {
+#define ETG_BATCH_CASE(DT, R, KK, NWW)                                                                           \
+  if ((int)sizeof(T) == DT && ER == NWW * R && K == KK && NW == NWW) {                                           \
+    ETG_TRY_CUDA(                                                                                                \
+        (batch_pair<T, R, KK, NWW>(sims, tiles, n_inner, n_kind, parity, step_off, main, sides, fork, joins))); \
+    return ETG_OK;                                                                                               \
   }
   if constexpr (sizeof(T) == 4) {
     ETG_TB_SHAPES_F32(ETG_BATCH_CASE)
@@ -1395,16 +1799,16 @@ int tb_batch_pair(int ER, int K, const void* sims, const int4* tiles, int n_inne
     ETG_TB_SHAPES_F64(ETG_BATCH_CASE)
   }
 #undef ETG_BATCH_CASE
-  set_error("no compiled batched kernel with %d rows and depth %d", ER, K);
+  set_error("no compiled batched kernel with %d rows, depth %d and %d warps", ER, K, NW);
   return ETG_ERR_ARGUMENT;
 }
 
 template <typename T>
-int tb_batch_attrs(int ER, int K) {
-#define ETG_BATCH_ATTR(DT, R, KK) \
-  if ((int)sizeof(T) == DT && ER == 8 * R && K == KK) {   \
-    ETG_TRY_CUDA((batch_attrs<T, R, KK>()));              \
-    return ETG_OK;                                        \
+int tb_batch_attrs(int ER, int K, int NW) {
+#define ETG_BATCH_ATTR(DT, R, KK, NWW)                             \
+  if ((int)sizeof(T) == DT && ER == NWW * R && K == KK && NW == NWW) { \
+    ETG_TRY_CUDA((batch_attrs<T, R, KK, NWW>()));                  \
+    return ETG_OK;                                                 \
   }
   if constexpr (sizeof(T) == 4) {
     ETG_TB_SHAPES_F32(ETG_BATCH_ATTR)
@@ -1412,7 +1816,7 @@ int tb_batch_attrs(int ER, int K) {
     ETG_TB_SHAPES_F64(ETG_BATCH_ATTR)
   }
 #undef ETG_BATCH_ATTR
-  set_error("no compiled batched kernel with %d rows and depth %d", ER, K);
+  set_error("no compiled batched kernel with %d rows, depth %d and %d warps", ER, K, NW);
   return ETG_ERR_ARGUMENT;
 }
 
@@ -1423,11 +1827,11 @@ void tb_split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_hi, 
   split_tiles(nx, ny, ux_lo, ux_hi, uy_lo, uy_hi, ER, EC, K, tiles, n_inner, &h);
 }
 
-template int tb_batch_pair<float>(int, int, const void*, const int4*, int, int, int, int, cudaStream_t, cudaStream_t,
-                                  cudaEvent_t, cudaEvent_t);
-template int tb_batch_pair<double>(int, int, const void*, const int4*, int, int, int, int, cudaStream_t, cudaStream_t,
-                                   cudaEvent_t, cudaEvent_t);
-template int tb_batch_attrs<float>(int, int);
-template int tb_batch_attrs<double>(int, int);
+template int tb_batch_pair<float>(int, int, int, const void*, const int4*, int, const int*, int, int, cudaStream_t,
+                                  const cudaStream_t*, cudaEvent_t, const cudaEvent_t*);
+template int tb_batch_pair<double>(int, int, int, const void*, const int4*, int, const int*, int, int, cudaStream_t,
+                                   const cudaStream_t*, cudaEvent_t, const cudaEvent_t*);
+template int tb_batch_attrs<float>(int, int, int);
+template int tb_batch_attrs<double>(int, int, int);
 
 }  // namespace etg

@@ -23,14 +23,20 @@ struct BatchSim {
   PhasePlan<T> ph, pe;
 };
 
-// Batched launch pair (interior tiles on `main`, CPML tiles on `side`) of the compiled shape
-// with ER rows and depth K; `sims` is a device array of BatchSim<T>, `tiles` (sim, r0, c0, -)
-// with the interior tiles first.
+// Batched launch pair (interior tiles on `main`, the CPML tiles of each kind on its side
+// stream) of the compiled shape with ER rows, depth K and NW warps; `sims` is a device array of
+// BatchSim<T>, `tiles` (sim, r0, c0, kind): interior tiles first, then n_kind[0..2] tiles of
+// kinds X, Y, XY.
 template <typename T>
-int tb_batch_pair(int ER, int K, const void* sims, const int4* tiles, int n_inner, int n_pml, int parity,
-                  int step_off, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
+int tb_batch_pair(int ER, int K, int NW, const void* sims, const int4* tiles, int n_inner, const int* n_kind,
+                  int parity, int step_off, cudaStream_t main, const cudaStream_t* sides, cudaEvent_t fork,
+                  const cudaEvent_t* joins);
 template <typename T>
-int tb_batch_attrs(int ER, int K);
+int tb_batch_attrs(int ER, int K, int NW);
+// Block DFT of a batch: every simulation's sampled monitors (at most max_mon per simulation,
+// at most max_work frequencies x nodes each) summed over the block's n_slots steps.
+template <typename T>
+void tb_batch_dft(const void* sims, int n_sims, int64_t max_work, int max_mon, int n_slots, cudaStream_t s);
 // Output tiles of one grid, interior tiles first; tiles meeting a `hot` rectangle lead each kind.
 // A CPML tile carries its kind (1: CPML across rows, 2: across columns, 3: both) in bits
 // 28-29 of .x (tb_tile_row and tb_tile_kind take it apart).
@@ -42,8 +48,9 @@ inline int tb_tile_kind(int2 t) { return t.x >> 28; }
 
 TBState* tb_create();
 void tb_destroy(TBState* tb);
-// Interior / CPML kernel time (ms), launches and output cells per launch of the last advance
-// run with ETG_OPT_TIMING 2 (zeros otherwise or before any temporally blocked advance).
+// Kernel time (ms), launches and output cells per launch of the last advance run with
+// ETG_OPT_TIMING 2, for [interior, CPML, CPML X tiles alone, Y alone, XY alone] (zeros
+// otherwise or before any temporally blocked advance).
 void tb_kernel_timing(const TBState* tb, double* ms, int64_t* launches, int64_t* cells);
 void tb_invalidate(TBState* tb);  // drop cached graphs and plans (pointers changed)
 

@@ -195,68 +195,92 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
   // Transposed E update of the Ex node of cell (t, e): dJ/d(dHz/dy); advances lambda psi_ex_y.
   // (the one-step kernel's "iky·lc" with 1/kappa = 1 exactly is lc itself; the domain checks
   // a kind's rows or columns always pass are left out)
-  auto gx_own = [&](int t, int e, T cb) -> T {
-    const T lc = mul(cb, lex[t].v[e]);
-    if (!PML) return lc;  // 1/kappa = 1 exactly, no psi
-    const int i = i0 + t, j = j0 + e;
-    if ((PY && (j < 1 || j > ny - 1)) || (PX && (i < 0 || i >= nx))) return zero<T>();
-    if (!PY) return lc;
-    if (j < s.ys_lo || j >= s.ys_hi) {
-      T* pp = sPsiY + PL + (lr0 + t) * EC + lj0 + e;
-      const T lpt = add(*pp, lc);
-      *pp = mul(bye[e], lpt);
-      return add(mul(kye[e], lc), mul(cye[e], lpt));
+  // Each works on one row of this thread's W nodes with that row's lambda psi as one 16-byte
+  // vector in registers (the nodes outside the strips keep theirs untouched).
+  auto gx_row = [&](int t, const Vw& cb, T* out) {  // Ex nodes; advances lambda psi_ex_y
+    Vw lp;
+    if (PY) lp.ld(sPsiY + PL + (lr0 + t) * EC + lj0);
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      const T lc = mul(cb.v[e], lex[t].v[e]);
+      const int i = i0 + t, j = j0 + e;
+      if (!PML || !PY) {
+        out[e] = (PX && (i < 0 || i >= nx)) ? zero<T>() : lc;  // 1/kappa = 1 exactly, no psi
+      } else if ((j < 1 || j > ny - 1) || (PX && (i < 0 || i >= nx))) {
+        out[e] = zero<T>();
+      } else if (j < s.ys_lo || j >= s.ys_hi) {
+        const T lpt = add(lp.v[e], lc);
+        lp.v[e] = mul(bye[e], lpt);
+        out[e] = add(mul(kye[e], lc), mul(cye[e], lpt));
+      } else {
+        out[e] = mul(kye[e], lc);
+      }
     }
-    return mul(kye[e], lc);
+    if (PY) lp.st(sPsiY + PL + (lr0 + t) * EC + lj0);
   };
-  // Transposed E update of the Ey node: dJ/d(dHz/dx); advances lambda psi_ey_x.
-  auto gy_own = [&](int t, int e, T cb) -> T {
-    const T lc = -mul(cb, ley[t].v[e]);
-    if (!PML) return lc;
-    const int i = i0 + t, j = j0 + e;
-    if ((PX && (i < 1 || i > nx - 1)) || (PY && (j < 0 || j >= ny))) return zero<T>();
-    if (!PX) return lc;
-    if (i < s.xs_lo || i >= s.xs_hi) {
-      T* pp = sPsiX + PL + (lr0 + t) * EC + lj0 + e;
-      const T lpt = add(*pp, lc);
-      *pp = mul(bxe[t], lpt);
-      return add(mul(kxe[t], lc), mul(cxe[t], lpt));
+  auto gy_row = [&](int t, const Vw& cb, T* out) {  // Ey nodes; advances lambda psi_ey_x
+    const int i = i0 + t;
+    const bool xrow = PX && (i < s.xs_lo || i >= s.xs_hi);
+    Vw lp;
+    if (xrow) lp.ld(sPsiX + PL + (lr0 + t) * EC + lj0);
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      const T lc = -mul(cb.v[e], ley[t].v[e]);
+      const int j = j0 + e;
+      if (!PML || !PX) {
+        out[e] = (PY && (j < 0 || j >= ny)) ? zero<T>() : lc;
+      } else if ((i < 1 || i > nx - 1) || (PY && (j < 0 || j >= ny))) {
+        out[e] = zero<T>();
+      } else if (xrow) {
+        const T lpt = add(lp.v[e], lc);
+        lp.v[e] = mul(bxe[t], lpt);
+        out[e] = add(mul(kxe[t], lc), mul(cxe[t], lpt));
+      } else {
+        out[e] = mul(kxe[t], lc);
+      }
     }
-    return mul(kxe[t], lc);
+    if (xrow) lp.st(sPsiX + PL + (lr0 + t) * EC + lj0);
   };
-  // Transposed H update of the Hz cell: dJ/d(dEx/dy), dJ/d(dEy/dx); advances lambda psi_hz_*.
-  auto h_own = [&](int t, int e, T* hx, T* hy) {
-    const T la = mul(db, lhz[t].v[e]);
-    if (!PML) {
-      *hx = la;
-      *hy = -la;
-      return;
+  auto h_row = [&](int t, T* hx, T* hy) {  // Hz cells; advances lambda psi_hz_y, psi_hz_x
+    const int i = i0 + t;
+    const bool xrow = PX && (i < s.xs_lo || i >= s.xs_hi);
+    Vw ly, lx;
+    if (PY) ly.ld(sPsiY + (lr0 + t) * EC + lj0);
+    if (xrow) lx.ld(sPsiX + (lr0 + t) * EC + lj0);
+#pragma unroll
+    for (int e = 0; e < W; ++e) {
+      const T la = mul(db, lhz[t].v[e]);
+      const int j = j0 + e;
+      if (!PML) {
+        hx[e] = la;
+        hy[e] = -la;
+        continue;
+      }
+      if ((PX && (i < 0 || i >= nx)) || (PY && (j < 0 || j >= ny))) {
+        hx[e] = hy[e] = zero<T>();
+        continue;
+      }
+      if (!PY) {
+        hx[e] = la;
+      } else if (j < s.ys_lo || j >= s.ys_hi) {
+        const T lpt = add(ly.v[e], la);
+        ly.v[e] = mul(byh[e], lpt);
+        hx[e] = add(mul(kyh[e], la), mul(cyh[e], lpt));
+      } else {
+        hx[e] = mul(kyh[e], la);
+      }
+      if (!PX) {
+        hy[e] = -la;
+      } else if (xrow) {
+        const T lpt = sub(lx.v[e], la);
+        lx.v[e] = mul(bxh[t], lpt);
+        hy[e] = add(-mul(kxh[t], la), mul(cxh[t], lpt));
+      } else {
+        hy[e] = -mul(kxh[t], la);
+      }
     }
-    const int i = i0 + t, j = j0 + e;
-    if ((PX && (i < 0 || i >= nx)) || (PY && (j < 0 || j >= ny))) {
-      *hx = *hy = zero<T>();
-      return;
-    }
-    if (!PY) {
-      *hx = la;
-    } else if (j < s.ys_lo || j >= s.ys_hi) {
-      T* pp = sPsiY + (lr0 + t) * EC + lj0 + e;
-      const T lpt = add(*pp, la);
-      *pp = mul(byh[e], lpt);
-      *hx = add(mul(kyh[e], la), mul(cyh[e], lpt));
-    } else {
-      *hx = mul(kyh[e], la);
-    }
-    if (!PX) {
-      *hy = -la;
-    } else if (i < s.xs_lo || i >= s.xs_hi) {
-      T* pp = sPsiX + (lr0 + t) * EC + lj0 + e;
-      const T lpt = sub(*pp, la);
-      *pp = mul(bxh[t], lpt);
-      *hy = add(-mul(kxh[t], la), mul(cxh[t], lpt));
-    } else {
-      *hy = -mul(kxh[t], la);
-    }
+    if (PY) ly.st(sPsiY + (lr0 + t) * EC + lj0);
+    if (xrow) lx.st(sPsiX + (lr0 + t) * EC + lj0);
   };
 
   __syncthreads();  // cb (and lambda psi) staged
@@ -265,7 +289,7 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
     Vw cy;
     cy.ld(sCby + lr0 * EC + lj0);
 #pragma unroll
-    for (int e = 0; e < W; ++e) gyf[e] = gy_own(0, e, cy.v[e]);
+    gy_row(0, cy, gyf);
     Vw g;
 #pragma unroll
     for (int e = 0; e < W; ++e) g.v[e] = gyf[e];
@@ -309,15 +333,13 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
         T gxr[W];
         Vw cx;
         cx.ld(sCbx + (lr0 + t) * EC + lj0);
-#pragma unroll
-        for (int e = 0; e < W; ++e) gxr[e] = gx_own(t, e, cx.v[e]);
+        gx_row(t, cx, gxr);
         T gxn = __shfl_down_sync(0xffffffffu, gxr[0], 1);
         if (lane == 31) gxn = zero<T>();
         if (t < RPT - 1) {
           Vw cy;
           cy.ld(sCby + (lr0 + t + 1) * EC + lj0);
-#pragma unroll
-          for (int e = 0; e < W; ++e) gyn[e] = gy_own(t + 1, e, cy.v[e]);
+          gy_row(t + 1, cy, gyn);
         } else {
           Vw g;
           g.ld(sGy + (ty + 1) * EC + lj0);
@@ -343,11 +365,9 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
     T hxl[W], hyl[W];  // this warp's last row, computed once and shared
     {
       Vw g;
+      h_row(RPT - 1, hxl, hyl);
 #pragma unroll
-      for (int e = 0; e < W; ++e) {
-        h_own(RPT - 1, e, &hxl[e], &hyl[e]);
-        g.v[e] = hyl[e];
-      }
+      for (int e = 0; e < W; ++e) g.v[e] = hyl[e];
       g.st(sHy + (ty + 1) * EC + lj0);
     }
     __syncthreads();
@@ -364,8 +384,7 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
       for (int t = 0; t < RPT; ++t) {
         T hxc[W], hyc[W];
         if (t < RPT - 1) {
-#pragma unroll
-          for (int e = 0; e < W; ++e) h_own(t, e, &hxc[e], &hyc[e]);
+          h_row(t, hxc, hyc);
         } else {
 #pragma unroll
           for (int e = 0; e < W; ++e) {
@@ -400,11 +419,9 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
     if (st < K - 1) {
       Vw cy, g;
       cy.ld(sCby + lr0 * EC + lj0);
+      gy_row(0, cy, gyf);
 #pragma unroll
-      for (int e = 0; e < W; ++e) {
-        gyf[e] = gy_own(0, e, cy.v[e]);
-        g.v[e] = gyf[e];
-      }
+      for (int e = 0; e < W; ++e) g.v[e] = gyf[e];
       g.st(sGy + ty * EC + lj0);
     }
     __syncthreads();
@@ -469,6 +486,21 @@ __global__ void __launch_bounds__(TB_THREADS, 1)
 k_tb_adj_batch(const TBAdjArgs<T>* __restrict__ args, const int4* __restrict__ tiles, int parity, int step_off) {
   const int4 t = tiles[blockIdx.x];  // simulation, r0, c0, kind
   adj_dispatch<T, RPT, K, PML>(args[2 * t.x + parity], t.y, t.z, t.w, step_off);
+}
+
+// One CPML kind per kernel (one tile body per kernel keeps each launch's code small).
+template <typename T, int RPT, int K, int KIND>
+__global__ void __launch_bounds__(TB_THREADS, 1)
+k_tb_adj_kind(const __grid_constant__ TBAdjArgs<T> a, const int2* __restrict__ tiles, int step_off) {
+  const int2 t = tiles[blockIdx.x];
+  tb_adj_tile<T, RPT, K, KIND>(a, make_int2(t.x & ((1 << AKIND_SHIFT) - 1), t.y), step_off);
+}
+
+template <typename T, int RPT, int K, int KIND>
+__global__ void __launch_bounds__(TB_THREADS, 1)
+k_tb_adj_batch_kind(const TBAdjArgs<T>* __restrict__ args, const int4* __restrict__ tiles, int parity, int step_off) {
+  const int4 t = tiles[blockIdx.x];  // simulation, r0, c0, kind
+  tb_adj_tile<T, RPT, K, KIND>(args[2 * t.x + parity], make_int2(t.y, t.z), step_off);
 }
 
 __global__ void k_adj_ctl_add(int64_t* ctl, int64_t delta) { ctl[0] += delta; }
@@ -557,17 +589,40 @@ int tb_adj_attrs() {
                                     (int)adj_smem<T, RPT, K, false>()));
   ETG_TRY_CUDA(cudaFuncSetAttribute(k_tb_adj_batch<T, RPT, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)adj_smem<T, RPT, K, true>()));
+#define ETG_ADJ_KIND_ATTR(KD)                                                                             \
+  ETG_TRY_CUDA(cudaFuncSetAttribute(k_tb_adj_kind<T, RPT, K, KD>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                    (int)AdjShape<T, RPT, K, KD>::SMEM));                                  \
+  ETG_TRY_CUDA(cudaFuncSetAttribute(k_tb_adj_batch_kind<T, RPT, K, KD>,                                  \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AdjShape<T, RPT, K, KD>::SMEM));
+  ETG_ADJ_KIND_ATTR(AKIND_X)
+  ETG_ADJ_KIND_ATTR(AKIND_Y)
+  ETG_ADJ_KIND_ATTR(AKIND_XY)
+#undef ETG_ADJ_KIND_ATTR
   return ETG_OK;
 }
 
 template <typename T>
-int tb_adj_launch(const TBAdjArgs<T>& a, const int2* tiles, int n_inner, int n_pml, int step_off,
-                  cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+int tb_adj_launch(const TBAdjArgs<T>& a, const int2* tiles, int n_inner, const int* n_kind, int step_off,
+                  cudaStream_t main, const cudaStream_t* sides, cudaEvent_t fork, const cudaEvent_t* joins) {
   constexpr int RPT = AdjCfg<T>::RPT, K = AdjCfg<T>::K;
   ETG_TRY_CUDA(cudaEventRecord(fork, main));
-  ETG_TRY_CUDA(cudaStreamWaitEvent(side, fork, 0));
-  if (n_pml) {
-    k_tb_adj<T, RPT, K, true><<<n_pml, dim3(32, 8), adj_smem<T, RPT, K, true>(), side>>>(a, tiles + n_inner, step_off);
+  for (int k = 0; k < 3; ++k) ETG_TRY_CUDA(cudaStreamWaitEvent(sides[k], fork, 0));
+  const int2* t = tiles + n_inner;
+  if (n_kind[0]) {
+    k_tb_adj_kind<T, RPT, K, AKIND_X><<<n_kind[0], dim3(32, 8), AdjShape<T, RPT, K, AKIND_X>::SMEM, sides[0]>>>(
+        a, t, step_off);
+    g_launches += 1;
+  }
+  t += n_kind[0];
+  if (n_kind[1]) {
+    k_tb_adj_kind<T, RPT, K, AKIND_Y><<<n_kind[1], dim3(32, 8), AdjShape<T, RPT, K, AKIND_Y>::SMEM, sides[1]>>>(
+        a, t, step_off);
+    g_launches += 1;
+  }
+  t += n_kind[1];
+  if (n_kind[2]) {
+    k_tb_adj_kind<T, RPT, K, AKIND_XY><<<n_kind[2], dim3(32, 8), AdjShape<T, RPT, K, AKIND_XY>::SMEM, sides[2]>>>(
+        a, t, step_off);
     g_launches += 1;
   }
   if (n_inner) {
@@ -575,42 +630,60 @@ int tb_adj_launch(const TBAdjArgs<T>& a, const int2* tiles, int n_inner, int n_p
     g_launches += 1;
   }
   ETG_TRY_CUDA(cudaGetLastError());
-  ETG_TRY_CUDA(cudaEventRecord(join, side));
-  ETG_TRY_CUDA(cudaStreamWaitEvent(main, join, 0));
+  for (int k = 0; k < 3; ++k) {
+    ETG_TRY_CUDA(cudaEventRecord(joins[k], sides[k]));
+    ETG_TRY_CUDA(cudaStreamWaitEvent(main, joins[k], 0));
+  }
   return ETG_OK;
 }
 
 template <typename T>
-int tb_adj_batch_launch(const TBAdjArgs<T>* args, const int4* tiles, int n_inner, int n_pml, int parity,
-                        int step_off, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
+int tb_adj_batch_launch(const TBAdjArgs<T>* args, const int4* tiles, int n_inner, const int* n_kind, int parity,
+                        int step_off, cudaStream_t main, const cudaStream_t* sides, cudaEvent_t fork,
+                        const cudaEvent_t* joins) {
   constexpr int RPT = AdjCfg<T>::RPT, K = AdjCfg<T>::K;
   ETG_TRY_CUDA(cudaEventRecord(fork, main));
-  ETG_TRY_CUDA(cudaStreamWaitEvent(side, fork, 0));
-  if (n_pml) {
-    k_tb_adj_batch<T, RPT, K, true><<<n_pml, dim3(32, 8), adj_smem<T, RPT, K, true>(), side>>>(
-        args, tiles + n_inner, parity, step_off);
+  for (int k = 0; k < 3; ++k) ETG_TRY_CUDA(cudaStreamWaitEvent(sides[k], fork, 0));
+  const int4* t = tiles + n_inner;
+  if (n_kind[0]) {
+    k_tb_adj_batch_kind<T, RPT, K, AKIND_X><<<n_kind[0], dim3(32, 8), AdjShape<T, RPT, K, AKIND_X>::SMEM, sides[0]>>>(
+        args, t, parity, step_off);
+    g_launches += 1;
+  }
+  t += n_kind[0];
+  if (n_kind[1]) {
+    k_tb_adj_batch_kind<T, RPT, K, AKIND_Y><<<n_kind[1], dim3(32, 8), AdjShape<T, RPT, K, AKIND_Y>::SMEM, sides[1]>>>(
+        args, t, parity, step_off);
+    g_launches += 1;
+  }
+  t += n_kind[1];
+  if (n_kind[2]) {
+    k_tb_adj_batch_kind<T, RPT, K, AKIND_XY>
+        <<<n_kind[2], dim3(32, 8), AdjShape<T, RPT, K, AKIND_XY>::SMEM, sides[2]>>>(args, t, parity, step_off);
     g_launches += 1;
   }
   if (n_inner) {
-    k_tb_adj_batch<T, RPT, K, false><<<n_inner, dim3(32, 8), adj_smem<T, RPT, K, false>(), main>>>(
-        args, tiles, parity, step_off);
+    k_tb_adj_batch<T, RPT, K, false><<<n_inner, dim3(32, 8), adj_smem<T, RPT, K, false>(), main>>>(args, tiles, parity,
+                                                                                                 step_off);
     g_launches += 1;
   }
   ETG_TRY_CUDA(cudaGetLastError());
-  ETG_TRY_CUDA(cudaEventRecord(join, side));
-  ETG_TRY_CUDA(cudaStreamWaitEvent(main, join, 0));
+  for (int k = 0; k < 3; ++k) {
+    ETG_TRY_CUDA(cudaEventRecord(joins[k], sides[k]));
+    ETG_TRY_CUDA(cudaStreamWaitEvent(main, joins[k], 0));
+  }
   return ETG_OK;
 }
 
 template int tb_adj_attrs<float>();
 template int tb_adj_attrs<double>();
-template int tb_adj_launch<float>(const TBAdjArgs<float>&, const int2*, int, int, int, cudaStream_t, cudaStream_t,
-                                  cudaEvent_t, cudaEvent_t);
-template int tb_adj_launch<double>(const TBAdjArgs<double>&, const int2*, int, int, int, cudaStream_t, cudaStream_t,
-                                   cudaEvent_t, cudaEvent_t);
-template int tb_adj_batch_launch<float>(const TBAdjArgs<float>*, const int4*, int, int, int, int, cudaStream_t,
-                                        cudaStream_t, cudaEvent_t, cudaEvent_t);
-template int tb_adj_batch_launch<double>(const TBAdjArgs<double>*, const int4*, int, int, int, int, cudaStream_t,
-                                         cudaStream_t, cudaEvent_t, cudaEvent_t);
+template int tb_adj_launch<float>(const TBAdjArgs<float>&, const int2*, int, const int*, int, cudaStream_t,
+                                  const cudaStream_t*, cudaEvent_t, const cudaEvent_t*);
+template int tb_adj_launch<double>(const TBAdjArgs<double>&, const int2*, int, const int*, int, cudaStream_t,
+                                   const cudaStream_t*, cudaEvent_t, const cudaEvent_t*);
+template int tb_adj_batch_launch<float>(const TBAdjArgs<float>*, const int4*, int, const int*, int, int,
+                                        cudaStream_t, const cudaStream_t*, cudaEvent_t, const cudaEvent_t*);
+template int tb_adj_batch_launch<double>(const TBAdjArgs<double>*, const int4*, int, const int*, int, int,
+                                         cudaStream_t, const cudaStream_t*, cudaEvent_t, const cudaEvent_t*);
 
 }  // namespace etg

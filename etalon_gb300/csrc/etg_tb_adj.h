@@ -41,17 +41,20 @@ template <typename T>
 int tb_adj_attrs();
 
 // Reverse steps n_hi-1 … n_hi-K of one simulation, n_hi = ctl[0] - step_off: interior tiles
-// on `main`, CPML tiles on `side` (fork/join through the two events), tiles[0, n_inner)
-// interior. Capturable in a CUDA graph: the step comes from device memory.
+// (tiles[0, n_inner)) on `main`, then n_kind[0..2] CPML tiles of kinds X, Y, XY, each kind on
+// its side stream (fork/join through the events). Capturable in a CUDA graph: the step comes
+// from device memory.
 template <typename T>
-int tb_adj_launch(const TBAdjArgs<T>& a, const int2* tiles, int n_inner, int n_pml, int step_off,
-                  cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
+int tb_adj_launch(const TBAdjArgs<T>& a, const int2* tiles, int n_inner, const int* n_kind, int step_off,
+                  cudaStream_t main, const cudaStream_t* sides, cudaEvent_t fork, const cudaEvent_t* joins);
 
 // The same for a batch: args is a device array of 2 TBAdjArgs per simulation (reading the
-// primary or the second buffer), tiles (sim, r0, c0, kind) with the interior tiles first.
+// primary or the second buffer), tiles (sim, r0, c0, kind): interior tiles, then the CPML
+// tiles sorted by kind.
 template <typename T>
-int tb_adj_batch_launch(const TBAdjArgs<T>* args, const int4* tiles, int n_inner, int n_pml, int parity,
-                        int step_off, cudaStream_t main, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
+int tb_adj_batch_launch(const TBAdjArgs<T>* args, const int4* tiles, int n_inner, const int* n_kind, int parity,
+                        int step_off, cudaStream_t main, const cudaStream_t* sides, cudaEvent_t fork,
+                        const cudaEvent_t* joins);
 
 // ctl[0] += delta (one thread), for the end of a captured block of launches.
 void tb_adj_ctl_add(int64_t* ctl, int64_t delta, cudaStream_t s);

@@ -202,7 +202,7 @@ class TEEngine:
         call("etg_sim_set_option", self._h, option, int(value))
 
     def set_kernel(self, kernel: str) -> None:
-        self.set_option(_lib.OPT_KERNEL, {"auto": 0, "plain": 1, "tb": 2, "tma": 3}[kernel])
+        self.set_option(_lib.OPT_KERNEL, {"auto": 0, "plain": 1, "tb": 2, "tma": 3, "pipe": 4}[kernel])
 
     def last_timing(self) -> tuple[float, int]:
         ms, launches = C.c_double(), C.c_int64()
@@ -210,11 +210,13 @@ class TEEngine:
         return ms.value, launches.value
 
     def kernel_timing(self) -> dict[str, tuple[float, int, int]]:
-        """{"interior"|"cpml": (total ms, launches, output cells per launch)} of the last
-        advance run with option TIMING = 2 (temporally blocked kernels timed one by one)."""
-        ms, launches, cells = (C.c_double * 2)(), (C.c_int64 * 2)(), (C.c_int64 * 2)()
+        """{"interior"|"cpml"|"cpml_x"|"cpml_y"|"cpml_xy": (total ms, launches, output cells per
+        launch)} of the last advance run with option TIMING = 2 (temporally blocked kernels
+        timed one by one; each CPML kind also alone)."""
+        ms, launches, cells = (C.c_double * 5)(), (C.c_int64 * 5)(), (C.c_int64 * 5)()
         call("etg_sim_kernel_timing", self._h, ms, launches, cells)
-        return {k: (ms[i], launches[i], cells[i]) for i, k in enumerate(("interior", "cpml"))}
+        names = ("interior", "cpml", "cpml_x", "cpml_y", "cpml_xy")
+        return {k: (ms[i], launches[i], cells[i]) for i, k in enumerate(names)}
 
     def close(self) -> None:
         h = getattr(self, "_h", None)

@@ -153,8 +153,10 @@ int etg_sim_get_option(etg_sim* sim, int option, int64_t* value);
 int etg_sim_last_timing(etg_sim* sim, double* ms, int64_t* launches);
 /* Per-kernel timing of the last advance run with ETG_OPT_TIMING = 2, which launches the
  * interior-tile and CPML-tile kernels of the temporally blocked path one after the other on
- * the simulation's stream, without graphs, with a CUDA-event pair around each launch.
- * Arrays of 2 (interior, CPML): total ms, launches, output cells inside the grid per launch. */
+ * the simulation's stream, without graphs, with a CUDA-event pair around each launch, then
+ * each kind of CPML tile once more on its own (same inputs, same outputs). Arrays of 5
+ * (interior, CPML, CPML tiles across rows, across columns, corners): total ms, launches,
+ * output cells inside the grid per launch. */
 int etg_sim_kernel_timing(etg_sim* sim, double* ms, int64_t* launches, int64_t* cells);
 
 /* ---------------------------------------------------------------- batch
@@ -240,12 +242,16 @@ int etg_tb_advance_static(int dtype, int nx, int ny, int64_t pitch, void* ex, vo
                           int64_t n_steps);
 
 #define ETG_OPT_KERNEL 0        /* 0 = auto, 1 = one step per launch, 2 = temporal blocking,
-                                   3 = temporal blocking, persistent CTAs fed by TMA */
+                                   3 = temporal blocking, persistent CTAs fed by TMA (two per SM),
+                                   4 = temporal blocking, one persistent CTA per SM claiming tiles,
+                                       the next interior tile staged by TMA during the current one */
 #define ETG_OPT_TB_DEPTH 1      /* steps per launch of the temporally blocked kernel */
 #define ETG_OPT_GRAPH_STEPS 2   /* steps captured per CUDA graph (0 = no graphs) */
 #define ETG_OPT_TILE_ROWS 3     /* tile rows of the temporally blocked kernel */
 #define ETG_OPT_TILE_COLS 4     /* tile columns of the temporally blocked kernel */
 #define ETG_OPT_CHECK_FINITE 5  /* 1 = flag NaN/Inf after each advance */
+#define ETG_OPT_TB_WARPS 7      /* warps per CTA of the temporally blocked kernel (0: 8); the
+                                   tile has TILE_ROWS / TB_WARPS rows per warp */
 #define ETG_OPT_TIMING 6        /* 1 = record CUDA-event timing of each advance,
                                    2 = also time each temporally blocked kernel launch */
 

@@ -364,16 +364,18 @@ def _oracle_for(p):
 
 # ----------------------------------------------------------------- temporal blocking
 
-TB_SHAPES_F32 = [(40, 128, 4), (48, 128, 4), (64, 128, 4)]
+TB_SHAPES_F32 = [(40, 128, 4), (48, 128, 4), (64, 128, 4), (48, 128, 4, 16)]  # (rows, cols, K[, warps])
 TB_SHAPES_F64 = [(32, 64, 2), (40, 64, 2)]
 
 
 def _tb_engine(name, precision, g, shape, kernel="tb", **kw):
     e, n = engine_with_reference_inputs(name, precision, g, kernel=kernel, **kw)
-    rows, cols, k = shape
+    rows, cols, k = shape[:3]
     e.set_option(_lib.OPT_TILE_ROWS, rows)
     e.set_option(_lib.OPT_TILE_COLS, cols)
     e.set_option(_lib.OPT_TB_DEPTH, k)
+    if len(shape) > 3:
+        e.set_option(_lib.OPT_TB_WARPS, shape[3])
     return e, n
 
 
@@ -506,3 +508,82 @@ def test_coefficient_change_after_stepping_keeps_old_strips(gpu, kernel):
     o.run(40)
     for f in FIELDS:
         np.testing.assert_array_equal(e.field(f), getattr(o, f), err_msg=f)
+
+
+PIPE_SHAPES = [("single", (40, 128, 4)), ("single", (48, 128, 4)), ("double", (32, 64, 2)), ("double", (40, 64, 2))]
+
+
+@pytest.mark.parametrize("name", ["config1", "g4_full"])
+@pytest.mark.parametrize(("precision", "shape"), PIPE_SHAPES)
+def test_pipelined_kernel_matches_reference(gpu, name, precision, shape):
+    """The persistent pipelined kernel (tile claims, TMA-staged interior tiles) gives Etalon's bits."""
+    g = load(name, precision)
+    e, n = _tb_engine(name, precision, g, shape, kernel="pipe")
+    e.advance(n)
+    e.synchronize()
+    assert compare_outputs(g, *engine_outputs(e)) == []
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_pipelined_kernel_seams_and_headline_grid(gpu, precision):
+    """Uneven blocks on the 2024² grid (many interior tiles per CTA) against the live oracle."""
+    n = 48
+    p = cases.config2(precision, n_steps=n)
+    e = TEEngine(p, kernel="pipe", graph_steps=16)
+    for k in (1, 7, 8, 9, 23):
+        e.advance(k)
+    o = _oracle_for(p)
+    workers = min(16, os.cpu_count() or 1)
+    with ThreadPoolExecutor(workers) as pool:
+        o.run(n, pool=pool, bands=workers)
+    for f in FIELDS:
+        np.testing.assert_array_equal(e.field(f), getattr(o, f), err_msg=f)
+    for k, acc in enumerate(o.acc):
+        np.testing.assert_array_equal(e.dft(k), acc)
+
+
+@pytest.mark.parametrize("region", [137, 211])
+def test_pipelined_kernel_odd_grids(gpu, region):
+    n = 40
+    p = cases.config2("single", n_steps=n, region=region)
+    e = TEEngine(p, kernel="pipe")
+    e.advance(n)
+    o = _oracle_for(p)
+    o.run(n)
+    for f in FIELDS:
+        np.testing.assert_array_equal(e.field(f), getattr(o, f), err_msg=f)
+
+
+@pytest.mark.parametrize("precision", ["single"])
+def test_sixteen_warp_tiles_on_headline_grid(gpu, precision):
+    """48×128 tiles run by 16 warps of 3 rows (CPML tiles by 8 warps of 6): live oracle, 2024²."""
+    n = 40
+    p = cases.config2(precision, n_steps=n)
+    e = TEEngine(p, kernel="tb", graph_steps=16)
+    e.set_option(_lib.OPT_TB_WARPS, 16)
+    for k in (3, 8, 29):
+        e.advance(k)
+    o = _oracle_for(p)
+    workers = min(16, os.cpu_count() or 1)
+    with ThreadPoolExecutor(workers) as pool:
+        o.run(n, pool=pool, bands=workers)
+    for f in FIELDS:
+        np.testing.assert_array_equal(e.field(f), getattr(o, f), err_msg=f)
+    for k, acc in enumerate(o.acc):
+        np.testing.assert_array_equal(e.dft(k), acc)
+
+
+def test_sixteen_warp_batch_matches_single_runs(gpu):
+    from etalon_gb300.batch import Batch
+
+    problems = [cases.synthetic_device(s, "single", n_steps=90, min_cells=60, max_cells=400) for s in range(4)]
+    batch = Batch(problems)
+    batch.set_option(_lib.OPT_TB_WARPS, 16)
+    batch.advance(90)
+    batch.synchronize()
+    for p, e in zip(problems, batch.engines):
+        ref = TEEngine(p, kernel="plain")
+        ref.advance(90)
+        for f in FIELDS:
+            np.testing.assert_array_equal(e.field(f), ref.field(f), err_msg=f)
+    batch.close()

@@ -142,7 +142,8 @@ __device__ __forceinline__ void dft_block_node(const MonDesc<T>& d, int64_t q, i
   const int64_t k = q % nodes;
   T* a = d.acc + 2 * ((int64_t)f * nodes + k);
   T re = a[0], im = a[1];
-  for (int slot = 0; slot < n_slots; ++slot) {
+#pragma unroll 8
+  for (int slot = 0; slot < n_slots; ++slot) {  // (loads of later slots issue ahead of the sums)
     const int64_t r = step0 + slot - d.n0;
     if (r < 0 || r >= d.rows) {
       atomicOr(flag, ERRBIT_TABLE);

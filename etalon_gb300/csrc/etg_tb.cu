@@ -326,25 +326,27 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
           if (!PML) {
             hz[t].v[e] = add(hz[t].v[e], mul(db, sub(add(dex_dy, zero<T>()), add(dey_dx, zero<T>()))));
           } else {
+            // computed for every cell and kept only inside the domain: selects, not branches,
+            // so the cells of a row stay independent instructions
             const int i = ir, j = j0 + e;
-            if ((!PX || (i >= 0 && i < nx)) && (!PY || (j >= 0 && j < ny))) {
-              T ty_ = add(dex_dy, zero<T>()), tx_ = add(dey_dx, zero<T>());
-              if (PY) {  // every column alike: no divergence between strip and other lanes
-                const T py = add(mul(byh[e], pyv.v[e]), mul(cyh[e], dex_dy));
-                pyv.v[e] = py;
-                ty_ = add(mul(dex_dy, kyh[e]), py);
-              }
-              if (PX) {
-                if (xrow) {
-                  const T px = add(mul(bxh[t], pxv.v[e]), mul(cxh[t], dey_dx));
-                  pxv.v[e] = px;
-                  tx_ = add(mul(dey_dx, kxh[t]), px);
-                } else {
-                  tx_ = add(mul(dey_dx, kxh[t]), zero<T>());
-                }
-              }
-              hz[t].v[e] = add(hz[t].v[e], mul(db, sub(ty_, tx_)));
+            const bool in = (!PX || (i >= 0 && i < nx)) && (!PY || (j >= 0 && j < ny));
+            T ty_ = add(dex_dy, zero<T>()), tx_ = add(dey_dx, zero<T>());
+            if (PY) {  // every column alike: no divergence between strip and other lanes
+              const T py = add(mul(byh[e], pyv.v[e]), mul(cyh[e], dex_dy));
+              pyv.v[e] = in ? py : pyv.v[e];
+              ty_ = add(mul(dex_dy, kyh[e]), py);
             }
+            if (PX) {
+              if (xrow) {
+                const T px = add(mul(bxh[t], pxv.v[e]), mul(cxh[t], dey_dx));
+                pxv.v[e] = in ? px : pxv.v[e];
+                tx_ = add(mul(dey_dx, kxh[t]), px);
+              } else {
+                tx_ = add(mul(dey_dx, kxh[t]), zero<T>());
+              }
+            }
+            const T h1 = add(hz[t].v[e], mul(db, sub(ty_, tx_)));
+            hz[t].v[e] = in ? h1 : hz[t].v[e];
           }
         }
         if (PY) pyv.st(sPsiY + (lr0 + t) * EC + lj0);
@@ -406,29 +408,33 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
           if (!PML) {
             ex[t].v[e] = add(ex[t].v[e], mul(cx.v[e], add(dy, zero<T>())));
             ey[t].v[e] = sub(ey[t].v[e], mul(cy.v[e], add(dx, zero<T>())));
-          } else {
+          } else {  // as in the H half step: every cell computed, kept inside the domain
             const int i = ir, j = j0 + e;
-            if ((!PX || (i >= 0 && i < nx)) && (!PY || (j >= 1 && j <= ny - 1))) {
+            const bool in_x = (!PX || (i >= 0 && i < nx)) && (!PY || (j >= 1 && j <= ny - 1));
+            const bool in_y = (!PX || (i >= 1 && i <= nx - 1)) && (!PY || (j >= 0 && j < ny));
+            {
               T term = add(dy, zero<T>());
               if (PY) {  // every column alike
                 const T p = add(mul(bye[e], pyv.v[e]), mul(cye[e], dy));
-                pyv.v[e] = p;
+                pyv.v[e] = in_x ? p : pyv.v[e];
                 term = add(mul(dy, kye[e]), p);
               }
-              ex[t].v[e] = add(ex[t].v[e], mul(cx.v[e], term));
+              const T e1 = add(ex[t].v[e], mul(cx.v[e], term));
+              ex[t].v[e] = in_x ? e1 : ex[t].v[e];
             }
-            if ((!PX || (i >= 1 && i <= nx - 1)) && (!PY || (j >= 0 && j < ny))) {
+            {
               T term = add(dx, zero<T>());
               if (PX) {
                 if (xrow) {
                   const T p = add(mul(bxe[t], pxv.v[e]), mul(cxe[t], dx));
-                  pxv.v[e] = p;
+                  pxv.v[e] = in_y ? p : pxv.v[e];
                   term = add(mul(dx, kxe[t]), p);
                 } else {
                   term = add(mul(dx, kxe[t]), zero<T>());
                 }
               }
-              ey[t].v[e] = sub(ey[t].v[e], mul(cy.v[e], term));
+              const T e1 = sub(ey[t].v[e], mul(cy.v[e], term));
+              ey[t].v[e] = in_y ? e1 : ey[t].v[e];
             }
           }
         }

@@ -197,23 +197,26 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
   // a kind's rows or columns always pass are left out)
   // Each works on one row of this thread's W nodes with that row's lambda psi as one 16-byte
   // vector in registers (the nodes outside the strips keep theirs untouched).
+  // Per-column tests (strip, domain) are selects between expressions computed for every
+  // column, not branches, so the columns stay independent instructions; each selected
+  // expression is the one-step kernel's.
   auto gx_row = [&](int t, const Vw& cb, T* out) {  // Ex nodes; advances lambda psi_ex_y
     Vw lp;
     if (PY) lp.ld(sPsiY + PL + (lr0 + t) * EC + lj0);
+    const int i = i0 + t;
+    const bool row_in = !PX || (i >= 0 && i < nx);
 #pragma unroll
     for (int e = 0; e < W; ++e) {
       const T lc = mul(cb.v[e], lex[t].v[e]);
-      const int i = i0 + t, j = j0 + e;
+      const int j = j0 + e;
       if (!PML || !PY) {
-        out[e] = (PX && (i < 0 || i >= nx)) ? zero<T>() : lc;  // 1/kappa = 1 exactly, no psi
-      } else if ((j < 1 || j > ny - 1) || (PX && (i < 0 || i >= nx))) {
-        out[e] = zero<T>();
-      } else if (j < s.ys_lo || j >= s.ys_hi) {
-        const T lpt = add(lp.v[e], lc);
-        lp.v[e] = mul(bye[e], lpt);
-        out[e] = add(mul(kye[e], lc), mul(cye[e], lpt));
+        out[e] = row_in ? lc : zero<T>();  // 1/kappa = 1 exactly, no psi
       } else {
-        out[e] = mul(kye[e], lc);
+        const bool in = row_in && j >= 1 && j <= ny - 1, strip = j < s.ys_lo || j >= s.ys_hi;
+        const T lpt = add(lp.v[e], lc);
+        const T with_psi = add(mul(kye[e], lc), mul(cye[e], lpt)), without = mul(kye[e], lc);
+        lp.v[e] = in && strip ? mul(bye[e], lpt) : lp.v[e];
+        out[e] = !in ? zero<T>() : strip ? with_psi : without;
       }
     }
     if (PY) lp.st(sPsiY + PL + (lr0 + t) * EC + lj0);
@@ -221,22 +224,22 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
   auto gy_row = [&](int t, const Vw& cb, T* out) {  // Ey nodes; advances lambda psi_ey_x
     const int i = i0 + t;
     const bool xrow = PX && (i < s.xs_lo || i >= s.xs_hi);
+    const bool row_in = !PX || (i >= 1 && i <= nx - 1);
     Vw lp;
     if (xrow) lp.ld(sPsiX + PL + (lr0 + t) * EC + lj0);
 #pragma unroll
     for (int e = 0; e < W; ++e) {
       const T lc = -mul(cb.v[e], ley[t].v[e]);
       const int j = j0 + e;
+      const bool in = row_in && (!PY || (j >= 0 && j < ny));
       if (!PML || !PX) {
-        out[e] = (PY && (j < 0 || j >= ny)) ? zero<T>() : lc;
-      } else if ((i < 1 || i > nx - 1) || (PY && (j < 0 || j >= ny))) {
-        out[e] = zero<T>();
+        out[e] = in ? lc : zero<T>();
       } else if (xrow) {
         const T lpt = add(lp.v[e], lc);
-        lp.v[e] = mul(bxe[t], lpt);
-        out[e] = add(mul(kxe[t], lc), mul(cxe[t], lpt));
+        lp.v[e] = in ? mul(bxe[t], lpt) : lp.v[e];
+        out[e] = in ? add(mul(kxe[t], lc), mul(cxe[t], lpt)) : zero<T>();
       } else {
-        out[e] = mul(kxe[t], lc);
+        out[e] = in ? mul(kxe[t], lc) : zero<T>();
       }
     }
     if (xrow) lp.st(sPsiX + PL + (lr0 + t) * EC + lj0);
@@ -244,6 +247,7 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
   auto h_row = [&](int t, T* hx, T* hy) {  // Hz cells; advances lambda psi_hz_y, psi_hz_x
     const int i = i0 + t;
     const bool xrow = PX && (i < s.xs_lo || i >= s.xs_hi);
+    const bool row_in = !PX || (i >= 0 && i < nx);
     Vw ly, lx;
     if (PY) ly.ld(sPsiY + (lr0 + t) * EC + lj0);
     if (xrow) lx.ld(sPsiX + (lr0 + t) * EC + lj0);
@@ -256,28 +260,27 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
         hy[e] = -la;
         continue;
       }
-      if ((PX && (i < 0 || i >= nx)) || (PY && (j < 0 || j >= ny))) {
-        hx[e] = hy[e] = zero<T>();
-        continue;
-      }
+      const bool in = row_in && (!PY || (j >= 0 && j < ny));
+      T vx, vy;
       if (!PY) {
-        hx[e] = la;
-      } else if (j < s.ys_lo || j >= s.ys_hi) {
-        const T lpt = add(ly.v[e], la);
-        ly.v[e] = mul(byh[e], lpt);
-        hx[e] = add(mul(kyh[e], la), mul(cyh[e], lpt));
+        vx = la;
       } else {
-        hx[e] = mul(kyh[e], la);
+        const bool strip = j < s.ys_lo || j >= s.ys_hi;
+        const T lpt = add(ly.v[e], la);
+        ly.v[e] = in && strip ? mul(byh[e], lpt) : ly.v[e];
+        vx = strip ? add(mul(kyh[e], la), mul(cyh[e], lpt)) : mul(kyh[e], la);
       }
       if (!PX) {
-        hy[e] = -la;
+        vy = -la;
       } else if (xrow) {
         const T lpt = sub(lx.v[e], la);
-        lx.v[e] = mul(bxh[t], lpt);
-        hy[e] = add(-mul(kxh[t], la), mul(cxh[t], lpt));
+        lx.v[e] = in ? mul(bxh[t], lpt) : lx.v[e];
+        vy = add(-mul(kxh[t], la), mul(cxh[t], lpt));
       } else {
-        hy[e] = -mul(kxh[t], la);
+        vy = -mul(kxh[t], la);
       }
+      hx[e] = in ? vx : zero<T>();
+      hy[e] = in ? vy : zero<T>();
     }
     if (PY) ly.st(sPsiY + (lr0 + t) * EC + lj0);
     if (xrow) lx.st(sPsiX + (lr0 + t) * EC + lj0);

@@ -132,27 +132,40 @@ struct Monitor {
 };
 
 // acc[f, k] += samples of steps step0 … step0 + n_slots - 1 times their phasors, in step order:
-// for one thread's (frequency, node) the same additions as dft_node makes step by step.
+// for one thread's (frequency, node) the same additions as dft_node makes step by step. The
+// table range is checked once for the block; samples and phasors of 8 steps are loaded
+// before their 8 sums, so the loads overlap instead of waiting one by one.
 template <typename T>
 __device__ __forceinline__ void dft_block_node(const MonDesc<T>& d, int64_t q, int64_t step0, int n_slots,
                                                int* flag) {
   const int64_t nodes = (int64_t)d.nxm * d.nym;
   if (!d.samp || q >= nodes * d.n_f) return;
+  const int64_t r0 = step0 - d.n0;
+  if (r0 < 0 || r0 + n_slots > d.rows) {
+    atomicOr(flag, ERRBIT_TABLE);
+    return;
+  }
   const int f = (int)(q / nodes);
   const int64_t k = q % nodes;
   T* a = d.acc + 2 * ((int64_t)f * nodes + k);
   T re = a[0], im = a[1];
-#pragma unroll 8
-  for (int slot = 0; slot < n_slots; ++slot) {  // (loads of later slots issue ahead of the sums)
-    const int64_t r = step0 + slot - d.n0;
-    if (r < 0 || r >= d.rows) {
-      atomicOr(flag, ERRBIT_TABLE);
-      continue;
-    }
-    const T v = d.samp[(int64_t)slot * nodes + k];
-    const T* ph = d.table + 2 * (r * d.n_f + f);
-    re = add(re, mul(v, __ldg(ph)));
-    im = add(im, mul(v, __ldg(ph + 1)));
+  const T* smp = d.samp + k;
+  const T* ph = d.table + 2 * (r0 * d.n_f + f);
+  for (int s0 = 0; s0 < n_slots; s0 += 8) {
+    T v[8], pr[8], pi[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (s0 + u < n_slots) {
+        v[u] = smp[(int64_t)(s0 + u) * nodes];
+        pr[u] = __ldg(ph + 2 * (int64_t)(s0 + u) * d.n_f);
+        pi[u] = __ldg(ph + 2 * (int64_t)(s0 + u) * d.n_f + 1);
+      }
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (s0 + u < n_slots) {
+        re = add(re, mul(v[u], pr[u]));
+        im = add(im, mul(v[u], pi[u]));
+      }
   }
   a[0] = re;
   a[1] = im;

@@ -1004,7 +1004,7 @@ struct PipeShape {
   static_assert((PL * sizeof(T)) % 128 == 0, "stage planes stay 128-byte aligned");
 };
 
-template <typename T, int RPT, int K>
+template <typename T, int RPT, int K, bool WITH_CPML = true>
 __global__ void __launch_bounds__(TB_THREADS, 1)
 k_tb_pipe(const __grid_constant__ TMAMaps maps, const __grid_constant__ SimArgs<T> a,
           const __grid_constant__ TBDst<T> dst, const int2* __restrict__ tiles, int n_inner, int n_pml,
@@ -1057,7 +1057,7 @@ k_tb_pipe(const __grid_constant__ TMAMaps maps, const __grid_constant__ SimArgs<
   int cur = s_next, pending = s_pending, buf = 0;
   uint32_t parity = 0;
   while (cur < n_all) {
-    if (cur < n_pml) {  // a CPML tile loads itself; nothing can be staged meanwhile
+    if (WITH_CPML && cur < n_pml) {  // a CPML tile loads itself; nothing can be staged meanwhile
       const int2 raw = tiles[n_inner + cur];
       const int2 u = make_int2(raw.x & ((1 << KIND_SHIFT) - 1), raw.y);
       auto hook = [&]() { claim(buf, false); };
@@ -1361,22 +1361,39 @@ static cudaError_t tma_two(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>&
 
 template <typename T, int RPT, int K>
 static cudaError_t pipe_attrs() {
-  return cudaFuncSetAttribute(k_tb_pipe<T, RPT, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)PipeShape<T, RPT, K>::SMEM);
+  cudaError_t e = cudaFuncSetAttribute(k_tb_pipe<T, RPT, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)PipeShape<T, RPT, K>::SMEM);
+  if (e == cudaSuccess) e = tb_attrs<T, RPT, K, 8>();  // the per-kind CPML kernels beside it
+  return e;
 }
 
-// Two persistent pipelined launches A -> B -> A covering 2K steps from step_off, one CTA per SM.
+// Two persistent pipelined launches A -> B -> A covering 2K steps from step_off, one CTA per SM
+// on the interior tiles; the CPML tiles run as their per-kind kernels on the side branches,
+// launched first, and the persistent CTAs take the SMs as those free them.
 template <typename T, int RPT, int K>
 static cudaError_t pipe_two(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& ph, const PhasePlan<T>& pe,
                             int step_off, cudaStream_t s) {
   using S = PipeShape<T, RPT, K>;
   const SimArgs<T> b = swap_args(a, tb);
-  k_tb_pipe<T, RPT, K><<<tb->sms, dim3(32, 8), S::SMEM, s>>>(tb->maps[0], a, as_dst(b), tb->tiles, tb->n_inner,
-                                                             tb->n_pml, tb->ctr, ph, pe, step_off);
-  k_tb_pipe<T, RPT, K><<<tb->sms, dim3(32, 8), S::SMEM, s>>>(tb->maps[1], b, as_dst(a), tb->tiles, tb->n_inner,
-                                                             tb->n_pml, tb->ctr + 2, ph, pe, step_off + K);
-  g_launches += 2;
-  return cudaGetLastError();
+  for (int half = 0; half < 2; ++half) {
+    const SimArgs<T>& src = half ? b : a;
+    const TBDst<T> d = as_dst(half ? a : b);
+    const int off = step_off + half * K;
+    cudaError_t e = cudaEventRecord(tb->fork, s);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(tb->sides[k], tb->fork, 0);
+    if (e == cudaSuccess) e = tb_launch_kinds<T, RPT, K>(src, d, tb->tiles + tb->n_inner, tb->n_kind, ph, pe, off, tb->sides);
+    if (e != cudaSuccess) return e;
+    k_tb_pipe<T, RPT, K, false><<<tb->sms, dim3(32, 8), S::SMEM, s>>>(tb->maps[half], src, d, tb->tiles, tb->n_inner, 0,
+                                                                    tb->ctr + 2 * half, ph, pe, off);
+    g_launches += 1;
+    e = cudaGetLastError();
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+      e = cudaEventRecord(tb->joins[k], tb->sides[k]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s, tb->joins[k], 0);
+    }
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 // Compiled shapes (rows = 8 * RPT, depth K); the CPML variant's six planes must fit 227 KB.

@@ -379,15 +379,16 @@ def kernel_roofline(e, p) -> dict:
                  "output_cells_per_launch": cells, "launch_ms": launch_ms, "launches_timed": launches,
                  "cpml_kernel": {"launch_ms": cp_ms / max(cp_launches, 1), "output_cells_per_launch": cp_cells},
                  "timing": "CUDA events around each launch, one extra run of the workload, kernels serialised"}
-        tag = "k_tb_step_interior"
-    elif kind == 3:  # persistent TMA kernel: the run's device time over its launches
+        tag = f"k_tb_step_interior_{rows}x{128 if s == 4 else 64}"
+    elif kind in (3, 4):  # persistent kernels: the run's device time over its launches
         e.reset()
         e.advance(p.n_steps)
         total, _ = e.last_timing()
         n_launch = 2 * (p.n_steps // (2 * depth))
         launch_ms = total / max(n_launch, 1)
         bytes_launch = algorithmic_bytes_per_step(p) * depth
-        extra = {"kernel": f"k_tb_tma<{rows // 8},{depth}>", "steps_per_launch": depth, "launch_ms": launch_ms,
+        extra = {"kernel": f"{'k_tb_tma' if kind == 3 else 'k_tb_pipe'}<{rows // 8},{depth}>", "steps_per_launch": depth,
+                 "launch_ms": launch_ms,
                  "timing": "CUDA events around the run, divided by its launches"}
         tag = "k_tb_tma"
     else:  # one-step kernels: the timed run's own device time
@@ -606,7 +607,7 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="single", choices=["single", "double"])
     ap.add_argument("--time-steps", type=int, default=10000)
-    ap.add_argument("--kernel", default="tuned", choices=["tuned", "auto", "plain", "tb"])
+    ap.add_argument("--kernel", default="auto", choices=["auto", "tuned", "plain", "tb", "pipe"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-device batched line")

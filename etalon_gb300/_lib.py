@@ -41,11 +41,16 @@ SIGNATURES: dict[str, list] = {
     "etg_update_e_te": [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, f64, f64],
     "etg_accumulate_dft": [i32, i32, i32, vp, vp, vp, vp],
     "etg_scatter_sub": [i32, i64, i32, vp, vp, vp, vp],
+    "etg_sum_sq": [i32, i64, i64, i64, vp, vp, C.POINTER(f64)],
+    "etg_block_mean": [i32, i64, i64, i64, vp, i32, i32, i32, vp],
+    "etg_cast": [i32, i32, i64, vp, vp],
     "etg_sim_create": [C.POINTER(vp), i32, i32, i32],
     "etg_sim_destroy": [vp],
     "etg_sim_set_coefficients": [vp] + [vp] * 14 + [f64, f64, f64],
     "etg_sim_add_source": [vp, i32, i32, vp, vp, i64, i64, vp],
     "etg_sim_set_cb_window": [vp, i32, i32, i32, i32, i32, vp],
+    "etg_sim_rasterize_cb": [vp, f64, f64, f64, f64, f64, f64, f64, i32, vp],
+    "etg_sim_get_cb": [vp, i32, vp],
     "etg_sim_add_monitor": [vp, i32, i32, i32, i32, i32, i32, i64, i64, vp, C.POINTER(i32)],
     "etg_sim_set_phasors": [vp, i32, i64, i64, vp],
     "etg_sim_set_deltas": [vp, i32, i64, i64, vp],

@@ -7,7 +7,10 @@
 C-ABI call per method. Device arrays are ``DeviceArray``: HBM buffers owned through
 the C-ABI allocator (no CuPy, no PyTorch), supporting exactly what the solver does to
 them — row views of phasor tables and ``field[i, j] -= delta`` for injection
-(etalon/fdtd/solver.py:83-110).
+(etalon/fdtd/solver.py:83-110) — and what Etalon Studio's live view does
+(etalon/studio/runner.py:258-291): ``astype``, ``v * v / c`` and ``xp.sum`` for the field
+energy, ``field[:a, :b].reshape(mx, sx, my, sy).mean(axis=(1, 3))`` for the snapshot. Those
+build deferred expressions that run as one fused device reduction when summed or averaged.
 """
 
 from __future__ import annotations
@@ -97,7 +100,13 @@ class DeviceArray:
     def __len__(self) -> int:
         return self.shape[0]
 
+    def astype(self, dtype, copy=True) -> "_Cast":
+        """Deferred conversion (evaluated by the expression that uses it)."""
+        return _Cast(self, np.dtype(dtype))
+
     def __getitem__(self, key):
+        if isinstance(key, tuple) and len(key) == 2 and all(isinstance(k, slice) for k in key) and self.ndim == 2:
+            return _Window(self, key)
         if isinstance(key, (int, np.integer)) and self.ndim >= 1:
             k = int(key) + (self.shape[0] if key < 0 else 0)
             if not 0 <= k < self.shape[0]:
@@ -146,10 +155,100 @@ class _Indexed:
         return self
 
 
+class _Cast:
+    """``a.astype(dtype)``: squared, divided and summed without a converted copy; evaluated
+    on the device (etg_cast) when anything else needs it."""
+
+    def __init__(self, src: DeviceArray, dtype: np.dtype):
+        self.src, self.dtype, self.shape = src, dtype, src.shape
+
+    def __mul__(self, other):
+        if isinstance(other, _Cast) and other.src is self.src:
+            return _Square(self.src, self.dtype)
+        raise TypeError("device arrays support v * v of one converted field")
+
+    def value(self) -> DeviceArray:
+        out = DeviceArray(self.src.shape, self.dtype)
+        call("etg_cast", _lib.dtype_code(self.src.dtype), _lib.dtype_code(self.dtype), self.src.size, self.src.ptr,
+             out.ptr)  # fmt: skip
+        return out
+
+    def astype(self, dtype, copy=True) -> "_Cast":
+        return _Cast(self.src, np.dtype(dtype))
+
+    def get(self) -> np.ndarray:
+        return self.value().get()
+
+    def __array__(self, dtype=None, copy=None):
+        a = self.get()
+        return a if dtype is None else a.astype(dtype)
+
+
+class _Square:
+    """``v * v`` of a converted field, optionally ``/ c``; summed by ``xp.sum`` in float64."""
+
+    def __init__(self, src: DeviceArray, dtype: np.dtype, coeff: DeviceArray | None = None):
+        self.src, self.dtype, self.coeff = src, dtype, coeff
+
+    def __truediv__(self, c):
+        if self.coeff is None and isinstance(c, DeviceArray) and c.shape == self.src.shape and c.dtype == self.src.dtype:
+            return _Square(self.src, self.dtype, c)
+        raise TypeError("device arrays support (v * v) / c with c a device array of the field's shape and dtype")
+
+    def sum(self) -> np.float64:
+        out = C.c_double()
+        rows, cols = (self.src.shape[0], int(np.prod(self.src.shape[1:]))) if self.src.ndim > 1 else (1, self.src.size)
+        call("etg_sum_sq", _lib.dtype_code(self.src.dtype), rows, cols, cols, self.src.ptr,
+             None if self.coeff is None else self.coeff.ptr, C.byref(out))  # fmt: skip
+        return np.float64(out.value)
+
+
+class _Window:
+    """``field[:a, :b]`` of a 2D device array (a leading block of rows and columns)."""
+
+    def __init__(self, src: DeviceArray, key: tuple[slice, slice]):
+        bounds = []
+        for sl, n in zip(key, src.shape):
+            start, stop, step = sl.indices(n)
+            if start != 0 or step != 1:
+                raise TypeError("device arrays support leading windows field[:a, :b] only")
+            bounds.append(stop)
+        self.src, self.rows, self.cols = src, bounds[0], bounds[1]
+
+    def reshape(self, *shape):
+        shape = shape[0] if len(shape) == 1 and isinstance(shape[0], tuple) else shape
+        if len(shape) != 4 or shape[0] * shape[1] != self.rows or shape[2] * shape[3] != self.cols:
+            raise TypeError("device windows reshape to (mx, sx, my, sy) blocks only")
+        return _Blocks(self, *(int(v) for v in shape))
+
+
+class _Blocks:
+    """``window.reshape(mx, sx, my, sy)``, for ``.mean(axis=(1, 3))``: block means."""
+
+    def __init__(self, window: _Window, mx: int, sx: int, my: int, sy: int):
+        self.window, self.mx, self.sx, self.my, self.sy = window, mx, sx, my, sy
+
+    def mean(self, axis=None) -> DeviceArray:
+        if tuple(axis or ()) != (1, 3):
+            raise TypeError("device blocks support mean(axis=(1, 3)) only")
+        src = self.window.src
+        out = DeviceArray((self.mx, self.my), src.dtype)
+        code = _lib.dtype_code(src.dtype)
+        call("etg_block_mean", code, self.window.rows, self.window.cols, src.shape[1], src.ptr, self.sx, self.sy,
+             code, out.ptr)  # fmt: skip
+        return out
+
+
 class _ArrayModule:
-    """The ``xp`` of this backend: array creation and host conversion."""
+    """The ``xp`` of this backend: array creation, host conversion, and the sums of the live view."""
 
     float32, float64, complex64, complex128 = np.float32, np.float64, np.complex64, np.complex128
+
+    @staticmethod
+    def sum(a) -> np.float64:
+        if isinstance(a, _Square):
+            return a.sum()
+        raise TypeError(f"xp.sum of {type(a).__name__} is not supported on device arrays")
 
     @staticmethod
     def asarray(a, dtype=None) -> DeviceArray:
@@ -165,7 +264,7 @@ class _ArrayModule:
 
     @staticmethod
     def asnumpy(a) -> np.ndarray:
-        return a.get() if isinstance(a, DeviceArray) else np.asarray(a)
+        return a.get() if isinstance(a, (DeviceArray, _Cast)) else np.asarray(a)
 
 
 xp = _ArrayModule()
@@ -193,7 +292,7 @@ class Gb300Backend:
         return DeviceArray.from_host(np.asarray(a))
 
     def to_host(self, a: Any) -> np.ndarray:
-        return a.get() if isinstance(a, DeviceArray) else np.asarray(a)
+        return a.get() if isinstance(a, (DeviceArray, _Cast)) else np.asarray(a)
 
     def synchronize(self) -> None:
         call("etg_synchronize")

@@ -17,7 +17,8 @@ import numpy as np
 
 from . import _lib
 from ._lib import call
-from .physics import ComponentSampling, PointInjection, TEProblem, cast_coefficients, phasor_table
+from .physics import (_BOX_TOL, EPSILON_0, ComponentSampling, PointInjection, TEProblem, cast_coefficients,
+                      phasor_table)
 
 # Etalon's phasor-table bound (etalon/fdtd/solver.py:32): rows × frequencies per upload.
 PHASOR_TABLE_ENTRIES = 1 << 22
@@ -92,6 +93,28 @@ class TEEngine:
         self._coeff_arrays = arrays
         call("etg_sim_set_coefficients", self._h, *[_ptr(a) for a in arrays],
              float(c.db), float(c.inv_dx), float(c.inv_dy))  # fmt: skip
+
+    def rasterize(self, boxes, background_eps: float) -> None:
+        """Replace cb_ex and cb_ey by the staircase of ``boxes`` rasterised on the device.
+
+        Same result, bit for bit, as ``permittivity_on_nodes`` then ``cast_coefficients`` on
+        the host (etalon/grid/materials.py:12-35, etalon/fdtd/state.py:80-81): boxes that miss
+        the plane z = grid.z are left out here with the host's test, the rest become rows of
+        (cx, cy, sx/2 + tol, sy/2 + tol, eps) in their order (the last box wins).
+        """
+        g = self.problem.grid
+        rows = [(b.center[0], b.center[1], b.size[0] / 2.0 + _BOX_TOL, b.size[1] / 2.0 + _BOX_TOL, b.eps)
+                for b in boxes if not abs(g.z - b.center[2]) > b.size[2] / 2.0 + _BOX_TOL]  # fmt: skip
+        table = np.ascontiguousarray(np.asarray(rows, dtype=np.float64).reshape(-1, 5))
+        call("etg_sim_rasterize_cb", self._h, float(g.x_min), float(g.y_min), float(g.dx), float(g.dy),
+             float(g.dt), float(EPSILON_0), float(background_eps), len(rows), _ptr(table))  # fmt: skip
+
+    def cb(self, which: str) -> np.ndarray:
+        """The device copy of cb_ex (``"ex"``) or cb_ey (``"ey"``)."""
+        k = {"ex": 0, "ey": 1}[which]
+        out = np.empty((self.nx, self.ny + 1) if k == 0 else (self.nx + 1, self.ny), self.real)
+        call("etg_sim_get_cb", self._h, k, _ptr(out))
+        return out
 
     def _delta_rows(self, inj: PointInjection, n0: int, rows: int) -> np.ndarray:
         return np.ascontiguousarray(inj.delta_table(n0, rows, self.dt, self.real))

@@ -96,6 +96,18 @@ int etg_accumulate_dft(int dtype, int n_f, int n_nodes, void* acc, const void* f
 int etg_scatter_sub(int dtype, int64_t n_cols, int n, void* field, const int64_t* i,
                     const int64_t* j, const void* delta);
 
+/* ---------------------------------------------------------------- reductions for the live view
+ * Etalon Studio's progress energy and snapshot (etalon/studio/runner.py:258-291) on device
+ * arrays, on the default stream like the per-step protocol. Rows of `pitch` elements. */
+/* *out = sum over the rows x cols elements of f*f/c in float64 (c == NULL: f*f). */
+int etg_sum_sq(int dtype, int64_t rows, int64_t cols, int64_t pitch, const void* field, const void* coeff,
+               double* out);
+/* out[(rows/sx) x (cols/sy)] (out_dtype, contiguous) = means of the sx x sy blocks, in float64. */
+int etg_block_mean(int dtype, int64_t rows, int64_t cols, int64_t pitch, const void* field, int sx, int sy,
+                   int out_dtype, void* out);
+/* out[n] = in[n] converted between float32 and float64. */
+int etg_cast(int from_dtype, int to_dtype, int64_t n, const void* in, void* out);
+
 /* ---------------------------------------------------------------- fused simulation
  * A resident 2D TE run: fields, CPML strips, coefficients, per-step source deltas
  * and phasor tables all in HBM; etg_sim_advance runs whole steps (H, inject M,
@@ -116,6 +128,17 @@ int etg_sim_set_coefficients(etg_sim* sim, const void* cb_ex, const void* cb_ey,
 /* Replace a window of cb_ex (which = 0, array (nx, ny+1)) or cb_ey (which = 1, (nx+1, ny)):
  * rows [i0, i0+rows) x columns [j0, j0+cols) from a host array (rows, cols) in dtype. */
 int etg_sim_set_cb_window(etg_sim* sim, int which, int i0, int rows, int j0, int cols, const void* host);
+/* cb_ex and cb_ey rasterised on the device from a staircase of boxes (etalon/grid/materials.py:12-35
+ * with the cast of etalon/fdtd/state.py:80-81): node (i, j) of Ex sits at x = x_min + (i + 0.5) dx,
+ * y = y_min + j dy, of Ey at x = x_min + i dx, y = y_min + (j + 0.5) dy; it takes eps of the last
+ * box b with |x - cx| <= hx and |y - cy| <= hy (float64), else `background`; cb = dt / (eps0 eps)
+ * in float64, cast to dtype. boxes: n_boxes rows of (cx, cy, hx, hy, eps), hx = sx/2 + tolerance
+ * already added, boxes that miss the simulated plane already left out. Bit-identical to the host
+ * rasterisation and cast; set the coefficients once first (the CPML profiles stay). */
+int etg_sim_rasterize_cb(etg_sim* sim, double x_min, double y_min, double dx, double dy, double dt,
+                         double eps0, double background, int n_boxes, const double* boxes);
+/* Copy cb_ex (which = 0, (nx, ny+1)) or cb_ey (which = 1, (nx+1, ny)) to a host array in dtype. */
+int etg_sim_get_cb(etg_sim* sim, int which, void* host);
 /* A point source on `component` (ETG_EX/EY/HZ) over n_nodes nodes (i, j) with its
  * per-step deltas for steps n0 .. n0+rows-1: table (rows, n_nodes) in dtype, the
  * values subtracted (etalon/fdtd/sources.py:54-56 cast to dtype). Sources apply in

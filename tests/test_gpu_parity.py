@@ -587,3 +587,28 @@ def test_sixteen_warp_batch_matches_single_runs(gpu):
         for f in FIELDS:
             np.testing.assert_array_equal(e.field(f), ref.field(f), err_msg=f)
     batch.close()
+
+
+@pytest.mark.parametrize("kernel", ["tb", "plain"])
+def test_large_plane_monitor_many_wavelengths(gpu, kernel):
+    """A 150x120-node plane monitor at 32 wavelengths (575 k complex accumulators per
+    component) through the blocked kernels' per-block DFT, against the live oracle bitwise."""
+    n = 70
+    p = ph.te_problem(
+        size=(6.0, 6.0), dl=0.02, background_eps=2.085,
+        boxes=[ph.Box((0.0, 0.0, 0.0), (8.0, 0.5, 1.0), 12.11)], pml=ph.PMLSpec(layers=12),
+        sources=[ph.PointSource((-2.0, 0.0, 0.0), "Hz", ph.GaussianPulse(1.55, 0.5))],
+        monitors=[ph.DFTMonitor("plane", list(np.linspace(1.4, 1.7, 32)), center=(0.5, 0.1, 0.0),
+                                size=(3.0, 2.4, 0.0), components=("Hz", "Ex"))],
+        n_steps=n, precision="single",
+    )  # fmt: skip
+    e = TEEngine(p, kernel=kernel, graph_steps=32)
+    for k in (5, 33, 32):
+        e.advance(k)
+    o = _oracle_for(p)
+    o.run(n)
+    assert sum(s.flat_index.size for s in p.samplings) > 30000
+    for k, acc in enumerate(o.acc):
+        np.testing.assert_array_equal(e.dft(k), acc)
+    for f in FIELDS:
+        np.testing.assert_array_equal(e.field(f), getattr(o, f), err_msg=f)

@@ -289,7 +289,25 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
       kxe[t] = a.ikx_e[ie];
     }
   }
-  __syncthreads();
+  // Interior tiles drop the "+ psi" of each curl term (psi = +0 there, and x + 0 only turns
+  // -0 into +0) when no Ex, Ey or Hz value of the extended tile is -0. That is exact: a sum
+  // is -0 only when both terms are and a difference x - y only when x is -0 and y is +0, so
+  // a field that is not -0 never becomes -0 (updates, sources), and with the curl terms taken
+  // as they are, results differ from the "+ 0" form only in the sign of a zero increment,
+  // which leaves a field that is not -0 unchanged. Tiles that load a -0 (uploaded state) keep
+  // the adds.
+  bool keep0 = true;
+  if (!PML) {
+    bool nz = false;
+#pragma unroll
+    for (int t = 0; t < RPT; ++t)
+#pragma unroll
+      for (int e = 0; e < W; ++e)
+        nz |= is_neg_zero(ex[t].v[e]) | is_neg_zero(ey[t].v[e]) | is_neg_zero(hz[t].v[e]);
+    keep0 = __syncthreads_or(nz) != 0;
+  } else {
+    __syncthreads();
+  }
   after_load();
   const uint32_t relSrcH = s_rel[0], relSrcE = s_rel[1], relMonH = s_rel[2], relMonE = s_rel[3];
   const int64_t n_base = *a.step + step_off;
@@ -300,167 +318,183 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
   const bool traced = ph.trace.buf && ph.trace.ti0 < tile.x + S::OR && ph.trace.ti0 + ph.trace.tnx > tile.x &&
                       ph.trace.tj0 < tile.y + S::OC && ph.trace.tj0 + ph.trace.tny > tile.y;
 
-  for (int s = 0; s < K; ++s) {
-    const int64_t n = n_base + s;
-    // ---------------------------------------------------------------- H half step
-    {
-      Vw eyb;
-      eyb.ld(sEyX + (ty + 1) * EC + lj0);  // Ey of the row below this warp
-#pragma unroll
-      for (int t = 0; t < RPT; ++t) {
-        T exr = __shfl_down_sync(0xffffffffu, ex[t].v[0], 1);
-        if (lane == 31) exr = zero<T>();
-        // CPML tiles: this row's psi as one 16-byte vector per lane. Outside the strips psi
-        // is +0 and its update b*0 + 0*d is +0 again, so whole vectors go back unchanged there.
-        const int ir = i0 + t;
-        const bool xrow = KIND == KIND_XY || ir < a.xs_lo || ir >= a.xs_hi;
-        Vw pyv, pxv;
-        if (PY) pyv.ld(sPsiY + (lr0 + t) * EC + lj0);
-        if (PX && xrow) pxv.ld(sPsiX + (lr0 + t) * EC + lj0);
-#pragma unroll
-        for (int e = 0; e < W; ++e) {
-          const T exn = e < W - 1 ? ex[t].v[e + 1] : exr;
-          const T eyn = t < RPT - 1 ? ey[t + 1].v[e] : eyb.v[e];
-          const T dex_dy = mul(sub(exn, ex[t].v[e]), idy);
-          const T dey_dx = mul(sub(eyn, ey[t].v[e]), idx);
-          if (!PML) {
-            hz[t].v[e] = add(hz[t].v[e], mul(db, sub(add(dex_dy, zero<T>()), add(dey_dx, zero<T>()))));
-          } else {
-            // computed for every cell and kept only inside the domain: selects, not branches,
-            // so the cells of a row stay independent instructions
-            const int i = ir, j = j0 + e;
-            const bool in = (!PX || (i >= 0 && i < nx)) && (!PY || (j >= 0 && j < ny));
-            T ty_ = add(dex_dy, zero<T>()), tx_ = add(dey_dx, zero<T>());
-            if (PY) {  // every column alike: no divergence between strip and other lanes
-              const T py = add(mul(byh[e], pyv.v[e]), mul(cyh[e], dex_dy));
-              pyv.v[e] = in ? py : pyv.v[e];
-              ty_ = add(mul(dex_dy, kyh[e]), py);
-            }
-            if (PX) {
-              if (xrow) {
-                const T px = add(mul(bxh[t], pxv.v[e]), mul(cxh[t], dey_dx));
-                pxv.v[e] = in ? px : pxv.v[e];
-                tx_ = add(mul(dey_dx, kxh[t]), px);
-              } else {
-                tx_ = add(mul(dey_dx, kxh[t]), zero<T>());
-              }
-            }
-            const T h1 = add(hz[t].v[e], mul(db, sub(ty_, tx_)));
-            hz[t].v[e] = in ? h1 : hz[t].v[e];
-          }
-        }
-        if (PY) pyv.st(sPsiY + (lr0 + t) * EC + lj0);
-        if (PX && xrow) pxv.st(sPsiX + (lr0 + t) * EC + lj0);
-      }
-    }
-    if (relSrcH) tb_inject<T, RPT, W>(ph, relSrcH, ex, ey, hz, i0, j0, n, a.flag);
-    if (relMonH) {  // DFT of H at (n + 1/2) dt, owned nodes only (or their samples)
-      for (uint32_t m = relMonH; m; m &= m - 1) {
-        const MonDesc<T>& d = ph.mon[__ffs(m) - 1];
-        const int64_t r = n - d.n0;
-        if (d.samp) tb_sample<T, RPT, W>(d, hz, i0, j0, t_lo, t_hi, e_lo, e_hi, step_off + s);
-        else if (r < 0 || r >= d.rows) atomicOr(a.flag, ERRBIT_TABLE);
-        else tb_dft<T, RPT, W>(d, hz, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
-      }
-    }
-    if (traced) {
-      const TraceDesc<T>& tr = ph.trace;
-      const int64_t r = n - tr.n0;
-      if (r < 0 || r >= tr.rows) {
-        atomicOr(a.flag, ERRBIT_TABLE);
-      } else {
+  auto steps = [&](auto keep_tag) {
+    constexpr bool KEEP0 = decltype(keep_tag)::value;
+    for (int s = 0; s < K; ++s) {
+      const int64_t n = n_base + s;
+      // ---------------------------------------------------------------- H half step
+      {
+        Vw eyb;
+        eyb.ld(sEyX + (ty + 1) * EC + lj0);  // Ey of the row below this warp
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
-          const unsigned di = (unsigned)(i0 + t - tr.ti0);
-          if (t < t_lo || t >= t_hi || di >= (unsigned)tr.tnx) continue;
+          T exr = __shfl_down_sync(0xffffffffu, ex[t].v[0], 1);
+          if (lane == 31) exr = zero<T>();
+          // CPML tiles: this row's psi as one 16-byte vector per lane. Outside the strips psi
+          // is +0 and its update b*0 + 0*d is +0 again, so whole vectors go back unchanged there.
+          const int ir = i0 + t;
+          const bool xrow = KIND == KIND_XY || ir < a.xs_lo || ir >= a.xs_hi;
+          Vw pyv, pxv;
+          if (PY) pyv.ld(sPsiY + (lr0 + t) * EC + lj0);
+          if (PX && xrow) pxv.ld(sPsiX + (lr0 + t) * EC + lj0);
 #pragma unroll
           for (int e = 0; e < W; ++e) {
-            const unsigned dj = (unsigned)(j0 + e - tr.tj0);
-            if (e >= e_lo && e < e_hi && dj < (unsigned)tr.tny) tr.buf[(r * tr.tnx + di) * tr.tny + dj] = hz[t].v[e];
-          }
-        }
-      }
-    }
-    hz[RPT - 1].st(sHzX + (ty + 1) * EC + lj0);
-    __syncthreads();
-    // ---------------------------------------------------------------- E half step
-    {
-      Vw hza;
-      hza.ld(sHzX + ty * EC + lj0);  // Hz of the row above this warp
-#pragma unroll
-      for (int t = 0; t < RPT; ++t) {
-        T hzl = __shfl_up_sync(0xffffffffu, hz[t].v[W - 1], 1);
-        if (lane == 0) hzl = zero<T>();
-        Vw cx, cy;
-        cx.ld(sCbx + (lr0 + t) * EC + lj0);
-        cy.ld(sCby + (lr0 + t) * EC + lj0);
-        const int ir = i0 + t;
-        const bool xrow = KIND == KIND_XY || ir < a.xs_lo || ir >= a.xs_hi;
-        Vw pyv, pxv;  // psi_ex_y, psi_ey_x of this row (CPML tiles)
-        if (PY) pyv.ld(sPsiY + PL + (lr0 + t) * EC + lj0);
-        if (PX && xrow) pxv.ld(sPsiX + PL + (lr0 + t) * EC + lj0);
-#pragma unroll
-        for (int e = 0; e < W; ++e) {
-          const T hzp = e > 0 ? hz[t].v[e - 1] : hzl;
-          const T hzu = t > 0 ? hz[t - 1].v[e] : hza.v[e];
-          const T dy = mul(sub(hz[t].v[e], hzp), idy);
-          const T dx = mul(sub(hz[t].v[e], hzu), idx);
-          if (!PML) {
-            ex[t].v[e] = add(ex[t].v[e], mul(cx.v[e], add(dy, zero<T>())));
-            ey[t].v[e] = sub(ey[t].v[e], mul(cy.v[e], add(dx, zero<T>())));
-          } else {  // as in the H half step: every cell computed, kept inside the domain
-            const int i = ir, j = j0 + e;
-            const bool in_x = (!PX || (i >= 0 && i < nx)) && (!PY || (j >= 1 && j <= ny - 1));
-            const bool in_y = (!PX || (i >= 1 && i <= nx - 1)) && (!PY || (j >= 0 && j < ny));
-            {
-              T term = add(dy, zero<T>());
-              if (PY) {  // every column alike
-                const T p = add(mul(bye[e], pyv.v[e]), mul(cye[e], dy));
-                pyv.v[e] = in_x ? p : pyv.v[e];
-                term = add(mul(dy, kye[e]), p);
+            const T exn = e < W - 1 ? ex[t].v[e + 1] : exr;
+            const T eyn = t < RPT - 1 ? ey[t + 1].v[e] : eyb.v[e];
+            const T dex_dy = mul(sub(exn, ex[t].v[e]), idy);
+            const T dey_dx = mul(sub(eyn, ey[t].v[e]), idx);
+            if (!PML) {
+              if (KEEP0) hz[t].v[e] = add(hz[t].v[e], mul(db, sub(add(dex_dy, zero<T>()), add(dey_dx, zero<T>()))));
+              else hz[t].v[e] = add(hz[t].v[e], mul(db, sub(dex_dy, dey_dx)));
+            } else {
+              // computed for every cell and kept only inside the domain: selects, not branches,
+              // so the cells of a row stay independent instructions
+              const int i = ir, j = j0 + e;
+              const bool in = (!PX || (i >= 0 && i < nx)) && (!PY || (j >= 0 && j < ny));
+              T ty_ = add(dex_dy, zero<T>()), tx_ = add(dey_dx, zero<T>());
+              if (PY) {  // every column alike: no divergence between strip and other lanes
+                const T py = add(mul(byh[e], pyv.v[e]), mul(cyh[e], dex_dy));
+                pyv.v[e] = in ? py : pyv.v[e];
+                ty_ = add(mul(dex_dy, kyh[e]), py);
               }
-              const T e1 = add(ex[t].v[e], mul(cx.v[e], term));
-              ex[t].v[e] = in_x ? e1 : ex[t].v[e];
-            }
-            {
-              T term = add(dx, zero<T>());
               if (PX) {
                 if (xrow) {
-                  const T p = add(mul(bxe[t], pxv.v[e]), mul(cxe[t], dx));
-                  pxv.v[e] = in_y ? p : pxv.v[e];
-                  term = add(mul(dx, kxe[t]), p);
+                  const T px = add(mul(bxh[t], pxv.v[e]), mul(cxh[t], dey_dx));
+                  pxv.v[e] = in ? px : pxv.v[e];
+                  tx_ = add(mul(dey_dx, kxh[t]), px);
                 } else {
-                  term = add(mul(dx, kxe[t]), zero<T>());
+                  tx_ = add(mul(dey_dx, kxh[t]), zero<T>());
                 }
               }
-              const T e1 = sub(ey[t].v[e], mul(cy.v[e], term));
-              ey[t].v[e] = in_y ? e1 : ey[t].v[e];
+              const T h1 = add(hz[t].v[e], mul(db, sub(ty_, tx_)));
+              hz[t].v[e] = in ? h1 : hz[t].v[e];
+            }
+          }
+          if (PY) pyv.st(sPsiY + (lr0 + t) * EC + lj0);
+          if (PX && xrow) pxv.st(sPsiX + (lr0 + t) * EC + lj0);
+        }
+      }
+      if (relSrcH) tb_inject<T, RPT, W>(ph, relSrcH, ex, ey, hz, i0, j0, n, a.flag);
+      if (relMonH) {  // DFT of H at (n + 1/2) dt, owned nodes only (or their samples)
+        for (uint32_t m = relMonH; m; m &= m - 1) {
+          const MonDesc<T>& d = ph.mon[__ffs(m) - 1];
+          const int64_t r = n - d.n0;
+          if (d.samp) tb_sample<T, RPT, W>(d, hz, i0, j0, t_lo, t_hi, e_lo, e_hi, step_off + s);
+          else if (r < 0 || r >= d.rows) atomicOr(a.flag, ERRBIT_TABLE);
+          else tb_dft<T, RPT, W>(d, hz, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
+        }
+      }
+      if (traced) {
+        const TraceDesc<T>& tr = ph.trace;
+        const int64_t r = n - tr.n0;
+        if (r < 0 || r >= tr.rows) {
+          atomicOr(a.flag, ERRBIT_TABLE);
+        } else {
+#pragma unroll
+          for (int t = 0; t < RPT; ++t) {
+            const unsigned di = (unsigned)(i0 + t - tr.ti0);
+            if (t < t_lo || t >= t_hi || di >= (unsigned)tr.tnx) continue;
+#pragma unroll
+            for (int e = 0; e < W; ++e) {
+              const unsigned dj = (unsigned)(j0 + e - tr.tj0);
+              if (e >= e_lo && e < e_hi && dj < (unsigned)tr.tny) tr.buf[(r * tr.tnx + di) * tr.tny + dj] = hz[t].v[e];
             }
           }
         }
-        if (PY) pyv.st(sPsiY + PL + (lr0 + t) * EC + lj0);
-        if (PX && xrow) pxv.st(sPsiX + PL + (lr0 + t) * EC + lj0);
       }
-    }
-    if (relSrcE) tb_inject<T, RPT, W>(pe, relSrcE, ex, ey, hz, i0, j0, n, a.flag);
-    if (relMonE) {  // DFT of E at (n + 1) dt (or the samples)
-      for (uint32_t m = relMonE; m; m &= m - 1) {
-        const MonDesc<T>& d = pe.mon[__ffs(m) - 1];
-        const int64_t r = n - d.n0;
-        if (d.samp) {
-          if (d.comp == ETG_EX) tb_sample<T, RPT, W>(d, ex, i0, j0, t_lo, t_hi, e_lo, e_hi, step_off + s);
-          else tb_sample<T, RPT, W>(d, ey, i0, j0, t_lo, t_hi, e_lo, e_hi, step_off + s);
-        } else if (r < 0 || r >= d.rows) {
-          atomicOr(a.flag, ERRBIT_TABLE);
-        } else if (d.comp == ETG_EX) {
-          tb_dft<T, RPT, W>(d, ex, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
-        } else {
-          tb_dft<T, RPT, W>(d, ey, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
+      hz[RPT - 1].st(sHzX + (ty + 1) * EC + lj0);
+      __syncthreads();
+      // ---------------------------------------------------------------- E half step
+      {
+        Vw hza;
+        hza.ld(sHzX + ty * EC + lj0);  // Hz of the row above this warp
+#pragma unroll
+        for (int t = 0; t < RPT; ++t) {
+          T hzl = __shfl_up_sync(0xffffffffu, hz[t].v[W - 1], 1);
+          if (lane == 0) hzl = zero<T>();
+          Vw cx, cy;
+          cx.ld(sCbx + (lr0 + t) * EC + lj0);
+          cy.ld(sCby + (lr0 + t) * EC + lj0);
+          const int ir = i0 + t;
+          const bool xrow = KIND == KIND_XY || ir < a.xs_lo || ir >= a.xs_hi;
+          Vw pyv, pxv;  // psi_ex_y, psi_ey_x of this row (CPML tiles)
+          if (PY) pyv.ld(sPsiY + PL + (lr0 + t) * EC + lj0);
+          if (PX && xrow) pxv.ld(sPsiX + PL + (lr0 + t) * EC + lj0);
+#pragma unroll
+          for (int e = 0; e < W; ++e) {
+            const T hzp = e > 0 ? hz[t].v[e - 1] : hzl;
+            const T hzu = t > 0 ? hz[t - 1].v[e] : hza.v[e];
+            const T dy = mul(sub(hz[t].v[e], hzp), idy);
+            const T dx = mul(sub(hz[t].v[e], hzu), idx);
+            if (!PML) {
+              if (KEEP0) {
+                ex[t].v[e] = add(ex[t].v[e], mul(cx.v[e], add(dy, zero<T>())));
+                ey[t].v[e] = sub(ey[t].v[e], mul(cy.v[e], add(dx, zero<T>())));
+              } else {
+                ex[t].v[e] = add(ex[t].v[e], mul(cx.v[e], dy));
+                ey[t].v[e] = sub(ey[t].v[e], mul(cy.v[e], dx));
+              }
+            } else {  // as in the H half step: every cell computed, kept inside the domain
+              const int i = ir, j = j0 + e;
+              const bool in_x = (!PX || (i >= 0 && i < nx)) && (!PY || (j >= 1 && j <= ny - 1));
+              const bool in_y = (!PX || (i >= 1 && i <= nx - 1)) && (!PY || (j >= 0 && j < ny));
+              {
+                T term = add(dy, zero<T>());
+                if (PY) {  // every column alike
+                  const T p = add(mul(bye[e], pyv.v[e]), mul(cye[e], dy));
+                  pyv.v[e] = in_x ? p : pyv.v[e];
+                  term = add(mul(dy, kye[e]), p);
+                }
+                const T e1 = add(ex[t].v[e], mul(cx.v[e], term));
+                ex[t].v[e] = in_x ? e1 : ex[t].v[e];
+              }
+              {
+                T term = add(dx, zero<T>());
+                if (PX) {
+                  if (xrow) {
+                    const T p = add(mul(bxe[t], pxv.v[e]), mul(cxe[t], dx));
+                    pxv.v[e] = in_y ? p : pxv.v[e];
+                    term = add(mul(dx, kxe[t]), p);
+                  } else {
+                    term = add(mul(dx, kxe[t]), zero<T>());
+                  }
+                }
+                const T e1 = sub(ey[t].v[e], mul(cy.v[e], term));
+                ey[t].v[e] = in_y ? e1 : ey[t].v[e];
+              }
+            }
+          }
+          if (PY) pyv.st(sPsiY + PL + (lr0 + t) * EC + lj0);
+          if (PX && xrow) pxv.st(sPsiX + PL + (lr0 + t) * EC + lj0);
         }
       }
+      if (relSrcE) tb_inject<T, RPT, W>(pe, relSrcE, ex, ey, hz, i0, j0, n, a.flag);
+      if (relMonE) {  // DFT of E at (n + 1) dt (or the samples)
+        for (uint32_t m = relMonE; m; m &= m - 1) {
+          const MonDesc<T>& d = pe.mon[__ffs(m) - 1];
+          const int64_t r = n - d.n0;
+          if (d.samp) {
+            if (d.comp == ETG_EX) tb_sample<T, RPT, W>(d, ex, i0, j0, t_lo, t_hi, e_lo, e_hi, step_off + s);
+            else tb_sample<T, RPT, W>(d, ey, i0, j0, t_lo, t_hi, e_lo, e_hi, step_off + s);
+          } else if (r < 0 || r >= d.rows) {
+            atomicOr(a.flag, ERRBIT_TABLE);
+          } else if (d.comp == ETG_EX) {
+            tb_dft<T, RPT, W>(d, ex, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
+          } else {
+            tb_dft<T, RPT, W>(d, ey, i0, j0, t_lo, t_hi, e_lo, e_hi, r);
+          }
+        }
+      }
+      ey[0].st(sEyX + ty * EC + lj0);
+      __syncthreads();
     }
-    ey[0].st(sEyX + ty * EC + lj0);
-    __syncthreads();
+  };
+  if constexpr (PML) {
+    steps(BoolTag<true>{});
+  } else if (keep0) {
+    steps(BoolTag<true>{});
+  } else {
+    steps(BoolTag<false>{});
   }
 
   // write the output tile (vectors lie wholly inside or outside it: K, OC are multiples of W)

@@ -39,4 +39,16 @@ struct TBVec<double> {
 template <typename T>
 __device__ __forceinline__ T zero() { return T(0); }
 
+// x is -0 (sign bit set, every other bit clear)
+__device__ __forceinline__ bool is_neg_zero(float x) { return __float_as_uint(x) == 0x80000000u; }
+__device__ __forceinline__ bool is_neg_zero(double x) {
+  return __double_as_longlong(x) == (long long)0x8000000000000000ull;
+}
+
+// a compile-time bool carried as a value (for generic lambdas)
+template <bool B>
+struct BoolTag {
+  static constexpr bool value = B;
+};
+
 }  // namespace etg

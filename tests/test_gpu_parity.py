@@ -336,7 +336,8 @@ def test_config2_full_length_matches_reference(gpu, precision):
 
 @pytest.mark.parametrize("precision", PRECISIONS)
 def test_config2_prefix_vs_live_oracle(gpu, precision):
-    """The headline grid for 120 steps against the oracle run on this host's cores."""
+    """The headline grid for 120 steps against the oracle run on this host's cores, in raw
+    bits (signs of zeros included)."""
     n = 120
     p = cases.config2(precision, n_steps=n)
     e = TEEngine(p)
@@ -346,9 +347,9 @@ def test_config2_prefix_vs_live_oracle(gpu, precision):
     with ThreadPoolExecutor(workers) as pool:
         o.run(n, pool=pool, bands=workers)
     for f in FIELDS:
-        np.testing.assert_array_equal(e.field(f), getattr(o, f), err_msg=f)
+        assert np.array_equal(_bits(e.field(f)), _bits(getattr(o, f))), f
     for k, acc in enumerate(o.acc):
-        np.testing.assert_array_equal(e.dft(k), acc)
+        assert np.array_equal(e.dft(k).view(np.uint8), acc.view(np.uint8))
 
 
 def _oracle_for(p):
@@ -612,3 +613,68 @@ def test_large_plane_monitor_many_wavelengths(gpu, kernel):
         np.testing.assert_array_equal(e.dft(k), acc)
     for f in FIELDS:
         np.testing.assert_array_equal(e.field(f), getattr(o, f), err_msg=f)
+
+
+def _plant_negative_zeros(fields, rng, frac=0.2):
+    """-0 at a random fraction of the Ex, Ey, Hz nodes of the first half of the rows of an
+    all-zero state (in place): tiles there keep the "+ psi" adds, the others drop them."""
+    for f in ("ex", "ey", "hz"):
+        a = fields[f]
+        half = a[: a.shape[0] // 2]
+        half[rng.random(half.shape) < frac] = -0.0
+
+
+def _bits(a):
+    return a.view(np.uint32 if a.dtype == np.float32 else np.uint64)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("mode", ["single", "batch"])
+def test_interior_tiles_with_uploaded_negative_zeros_bitwise(gpu, precision, mode):
+    """Interior tiles drop NumPy's "+ psi" (psi = +0) only when no loaded Ex, Ey, Hz value is
+    -0; an uploaded state full of -0 must still match the oracle bit for bit, signs of zeros
+    included (np.array_equal does not see them, so raw bits are compared)."""
+    from etalon_gb300.batch import Batch
+
+    n = 12
+    problems = [cases.synthetic_device(s, precision, n_steps=n, min_cells=260, max_cells=300) for s in (3, 4)]
+    rng = np.random.default_rng(11)
+    states = []
+    for p in problems:
+        g = p.grid
+        st = {"ex": np.zeros((g.nx, g.ny + 1), p.real), "ey": np.zeros((g.nx + 1, g.ny), p.real),
+              "hz": np.zeros((g.nx, g.ny), p.real)}  # fmt: skip
+        _plant_negative_zeros(st, rng)
+        states.append(st)
+    if mode == "batch":
+        batch = Batch(problems)
+        engines = batch.engines
+    else:
+        engines = [TEEngine(problems[0], kernel="tb")]
+    try:
+        for e, st in zip(engines, states):
+            for f, v in st.items():
+                e.set_field(f, v)
+        if mode == "batch":
+            batch.advance(5)
+            batch.advance(n - 5)
+            batch.synchronize()
+        else:
+            engines[0].advance(5)
+            engines[0].advance(n - 5)
+        for p, e, st in zip(problems, engines, states):
+            o = _oracle_for(p)
+            for f, v in st.items():
+                getattr(o, f)[...] = v
+            o.run(n)
+            assert any(np.any((getattr(o, f) == 0) & np.signbit(getattr(o, f))) for f in ("ex", "ey", "hz"))
+            for f in FIELDS:
+                assert np.array_equal(_bits(e.field(f)), _bits(getattr(o, f))), f
+            for k, acc in enumerate(o.acc):
+                assert np.array_equal(e.dft(k).view(np.uint8), acc.view(np.uint8))
+    finally:
+        if mode == "batch":
+            batch.close()
+        else:
+            engines[0].close()
+

@@ -340,8 +340,11 @@ def run_ours(args, world, rank, local) -> None:
         if world == 1:  # one grid: replicas would only repeat it
             out["adjoint"] = adjoint_line(args)
         out["batched_adjoint"] = batched_adjoint_line(args, world, rank)
-    if args.fp64:
+    if not args.no_fp64:
         out["fp64"] = fp64_line(args, local)
+    if rank == 0 and not args.no_studio:
+        out["studio"] = studio_line(e, p)
+        out["rasterize"] = rasterize_line(e, p)
     if rank == 0:
         print(json.dumps(out))
     e.close()
@@ -599,6 +602,120 @@ def fp64_line(args, local) -> dict:
     return {"value": p.grid.n_cells * p.n_steps / (t / 1e3), "unit": UNIT, "ms_per_step": t}
 
 
+# ----------------------------------------------------------------------------- next rows
+
+
+def _studio_energy(state, xp, dt, db, cell_area):
+    """Etalon Studio's progress energy (etalon/studio/runner.py:258-281) on any array module."""
+
+    def weighted(field, coefficient):
+        values = field.astype(xp.float64)
+        return float(xp.sum(values * values / coefficient))
+
+    hz = state["hz"].astype(xp.float64)
+    electric = dt * (weighted(state["ex"], state["cb_ex"]) + weighted(state["ey"], state["cb_ey"]))
+    magnetic = dt / float(db) * float(xp.sum(hz * hz))
+    return float(0.5 * cell_area * (electric + magnetic))
+
+
+def _studio_downsample(field, xp, max_nodes=256):
+    """Etalon Studio's snapshot of a field (etalon/studio/runner.py:284-291)."""
+    n_x, n_y = field.shape
+    sx = max(1, -(-n_x // max_nodes))
+    sy = max(1, -(-n_y // max_nodes))
+    mx, my = n_x // sx, n_y // sy
+    return field[: mx * sx, : my * sy].reshape(mx, sx, my, sy).mean(axis=(1, 3)).astype(xp.float32)
+
+
+def studio_line(e, p, frames: int = 20) -> dict:
+    """One Studio progress frame (energy + 256-node Hz snapshot) on the final state of the
+    headline run: on device arrays through the backend's ``xp`` (a few numbers and a small
+    image cross the link) against NumPy after copying the fields and cb to the host."""
+    import torch
+
+    from etalon_gb300 import physics as ph
+    from etalon_gb300.backend import Gb300Backend
+
+    backend = Gb300Backend(p.precision)
+    c = ph.cast_coefficients(p)
+    host = {f: e.field(f) for f in ("ex", "ey", "hz")}
+    host["cb_ex"], host["cb_ey"] = c.cb_ex, c.cb_ey
+    dev = {k: backend.to_device(v) for k, v in host.items()}
+    g = p.grid
+    args = (g.dt, c.db, g.dx * g.dy * ph.UM**2)
+
+    def device_frame():
+        energy = _studio_energy(dev, backend.xp, *args)
+        image = backend.to_host(_studio_downsample(dev["hz"], backend.xp))
+        return energy, image
+
+    def host_frame():
+        state = {k: backend.to_host(v) for k, v in dev.items()}
+        return _studio_energy(state, np, *args), _studio_downsample(state["hz"], np)
+
+    out = {}
+    for name, fn in (("device", device_frame), ("host_copy", host_frame)):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(frames):
+            res = fn()
+        out[f"{name}_ms_per_frame"] = 1e3 * (time.perf_counter() - t0) / frames
+        out[name] = res
+    (ed, imd), (eh, imh) = out.pop("device"), out.pop("host_copy")
+    out.update({
+        "frames": frames, "grid": [g.nx, g.ny], "snapshot": list(imd.shape),
+        "energy_rel_diff": abs(ed - eh) / abs(eh) if eh else abs(ed - eh),
+        "snapshot_max_rel_diff": float(np.max(np.abs(imd.astype(np.float64) - imh.astype(np.float64)))
+                                       / max(float(np.max(np.abs(imh))), 1e-300)),
+        "speedup": out["host_copy_ms_per_frame"] / out["device_ms_per_frame"],
+        "what": "etalon/studio/runner.py:258-291 expressions; device: float64 sums and block means on the GPU",
+    })  # fmt: skip
+    return out
+
+
+def rasterize_line(e, p, reps: int = 5) -> dict:
+    """ε staircase + cb of the headline grid for 64 boxes (a design sweep's geometry): on the
+    device (etg_sim_rasterize_cb) against the host path (permittivity_on_nodes, the float64 cb
+    and cast, the upload), and whether the two give the same bits."""
+    from etalon_gb300 import physics as ph
+
+    g = p.grid
+    rng = np.random.default_rng(7)
+    lx, ly = g.nx * g.dx, g.ny * g.dy
+    boxes = [ph.Box((g.x_min + float(rng.uniform(0, lx)), g.y_min + float(rng.uniform(0, ly)), 0.0),
+                    (float(rng.uniform(0.5, 8.0)), float(rng.uniform(0.2, 8.0)), 0.22),
+                    float(rng.choice([2.085, 12.11]))) for _ in range(64)]  # fmt: skip
+    c = ph.cast_coefficients(p)
+
+    def host():
+        eps = ph.permittivity_on_nodes(g, p.background_eps, boxes)
+        cb_ex = np.ascontiguousarray(g.dt / (ph.EPSILON_0 * eps["Ex"]), dtype=p.real)
+        cb_ey = np.ascontiguousarray(g.dt / (ph.EPSILON_0 * eps["Ey"]), dtype=p.real)
+        c.cb_ex, c.cb_ey = cb_ex, cb_ey
+        e.set_coefficients(c)
+        return cb_ex, cb_ey
+
+    def device():
+        e.rasterize(boxes, p.background_eps)
+        e.synchronize()
+
+    out = {}
+    for name, fn in (("host", host), ("device", device)):
+        res = fn()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        out[f"{name}_ms"] = 1e3 * (time.perf_counter() - t0) / reps
+        if name == "host":
+            want = res
+    same = all(np.array_equal(e.cb(w).view(np.uint8), r.view(np.uint8)) for w, r in zip(("ex", "ey"), want))
+    out.update({"boxes": len(boxes), "grid": [g.nx, g.ny], "bit_identical": bool(same),
+                "speedup": out["host_ms"] / out["device_ms"],
+                "host_path": "permittivity_on_nodes + dt/(eps0 eps) + cast + upload of the coefficients"})  # fmt: skip
+    return out
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -615,7 +732,8 @@ def main() -> None:
     ap.add_argument("--no-adjoint", action="store_true", help="skip the gradient lines")
     ap.add_argument("--adjoint-time-steps", type=int, default=20000)
     ap.add_argument("--batch-adjoint-time-steps", type=int, default=10000)
-    ap.add_argument("--fp64", action="store_true", help="add a float64 line of the same workload")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the float64 line of the same workload")
+    ap.add_argument("--no-studio", action="store_true", help="skip the live-view and rasterisation lines")
     args = ap.parse_args()
     os.environ["ETG_BENCH_IMPL"] = args.impl
     world, rank, local = dist_setup(args.gpus)

@@ -81,7 +81,10 @@ class AdjointRunner:
 
     @staticmethod
     def sqrt_stride(n_steps: int) -> int:
-        return max(1, int(round(np.sqrt(n_steps))))
+        """√N rounded up to a multiple of 8: a segment is then whole launch pairs of the 4-step
+        tiles, with no one-step remainder."""
+        s = max(1, int(round(np.sqrt(n_steps))))
+        return (s + 7) // 8 * 8
 
     def set_eps(self, eps_ex: np.ndarray, eps_ey: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
         """Upload cb = Δt/(ε0 ε) of the window nodes (float64, then one cast); returns cb64."""

@@ -667,6 +667,25 @@ int adj_begin(etg_adj* A, AdjPlan<T>* ph, AdjPlan<T>* pe) {
   return ETG_OK;
 }
 
+// While segments of S steps are recomputed, only the light cone of the window's trace box is
+// stepped: a value moves at most one cell per time step, so the trace box stays exact for S
+// steps when every cell within S cells of it is, and the tiles beyond (their halos read cells
+// that are not updated) only spoil cells farther out. The margin adds room for two launches
+// of the deepest tiles.
+void set_cone(etg_adj* A, int64_t S) {
+  etg_sim* s = A->sim;
+  const int64_t m = S + 2 * 8 + 2;
+  s->act_i0 = (int)std::max<int64_t>(0, A->ti0 - m);
+  s->act_i1 = (int)std::min<int64_t>(1 << 30, A->ti0 + A->tnx + m);
+  s->act_j0 = (int)std::max<int64_t>(0, A->tj0 - m);
+  s->act_j1 = (int)std::min<int64_t>(1 << 30, A->tj0 + A->tny + m);
+}
+
+void clear_cone(etg_sim* s) {
+  s->act_i0 = s->act_j0 = 0;
+  s->act_i1 = s->act_j1 = 1 << 30;
+}
+
 // Restore checkpoint k into the simulation and set it up to re-record the trace of [lo, hi).
 int adj_restore_segment(etg_adj* A, int64_t k, int64_t lo, int64_t hi) {
   etg_sim* s = A->sim;
@@ -698,6 +717,7 @@ int adj_backward(etg_adj* A) {
     // the blocked path recomputes through a one-simulation batch, whose plans live in device
     // memory: moving the trace origin per segment then needs no new graphs
     if (A->tiles && !A->fwd1) rc = etg_batch_create(&A->fwd1, 1, &s);
+    set_cone(A, S);
     for (int64_t k = nseg - 1; k >= 0 && rc == ETG_OK; --k) {
       const int64_t lo = k * S, hi = std::min(A->n_steps, lo + S);
       rc = adj_restore_segment(A, k, lo, hi);
@@ -712,6 +732,7 @@ int adj_backward(etg_adj* A) {
       clear_trace(s);
       if (rc == ETG_OK) rc = backward_sweep<T>(A, hi, lo, lo, &par_e, &par_h, ph, pe);
     }
+    clear_cone(s);
     s->monitors_on = true;
     sim_invalidate(s);
   }
@@ -918,6 +939,7 @@ int batch_backward(etg_adj_batch* B) {
   const int64_t nseg = (B->n_steps + S - 1) / S;
   for (etg_adj* A : B->adjs) {
     A->sim->monitors_on = false;
+    set_cone(A, S);
     sim_invalidate(A->sim);
   }
   int rc = ETG_OK;
@@ -931,6 +953,7 @@ int batch_backward(etg_adj_batch* B) {
     if (rc == ETG_OK) rc = batch_sweep<T>(B, hi, lo, lo, par_e, par_h, ph, pe);
   }
   for (etg_adj* A : B->adjs) {
+    clear_cone(A->sim);
     A->sim->monitors_on = true;
     sim_invalidate(A->sim);
   }

@@ -111,9 +111,14 @@ int refresh(etg_batch* b, int ER, int K, bool* changed) {
       }
       std::vector<int2> t;
       int ni = 0;
-      tb_split_tiles(s->nx, s->ny, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi, ER, 32 * (sizeof(T) == 4 ? 4 : 2), K, hot, &t, &ni);
-      for (int q = 0; q < (int)t.size(); ++q)
-        (q < ni ? inner : pml).push_back(make_int4(k, tb_tile_row(t[q]), t[q].y, tb_tile_kind(t[q])));
+      const int EC = 32 * (sizeof(T) == 4 ? 4 : 2);
+      tb_split_tiles(s->nx, s->ny, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi, ER, EC, K, hot, &t, &ni);
+      for (int q = 0; q < (int)t.size(); ++q) {
+        const int r0 = tb_tile_row(t[q]), c0 = t[q].y;  // output rows [r0, r0+ER-2K), columns [c0, c0+EC-2K)
+        if (r0 >= s->act_i1 || r0 + ER - 2 * K <= s->act_i0 || c0 >= s->act_j1 || c0 + EC - 2 * K <= s->act_j0)
+          continue;
+        (q < ni ? inner : pml).push_back(make_int4(k, r0, c0, tb_tile_kind(t[q])));
+      }
     }
     // CPML tiles grouped by kind over every simulation (one kernel per kind)
     std::stable_sort(pml.begin(), pml.end(), [](const int4& p, const int4& q) { return p.w < q.w; });

@@ -209,6 +209,10 @@ struct etg_sim {
   int64_t trace_n0 = 0, trace_rows = 0;
   int trace_ti0 = 0, trace_tnx = 0, trace_tj0 = 0, trace_tny = 0;
   bool monitors_on = true;
+  // Output cells a batch steps: tiles whose output misses [act_i0, act_i1) x [act_j0, act_j1)
+  // are left out. The adjoint narrows it to the light cone of its window while it recomputes
+  // a segment; everything else runs with the whole grid.
+  int act_i0 = 0, act_i1 = 1 << 30, act_j0 = 0, act_j1 = 1 << 30;
 
   size_t esize() const { return (size_t)dtype; }
   int64_t field_rows(int f) const { return (f == ETG_EY || f == ETG_PSI_EY_X) ? nx + 1 : nx; }

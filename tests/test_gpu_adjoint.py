@@ -249,3 +249,37 @@ def test_single_design_workload_gradient_vs_central_differences(gpu):
     point_power(simulate(eps, r32)[0], p32.samplings[0]).backward()
     r32.close()
     assert _rel(eps.grad.numpy(), g64) < 1e-3
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_segment_recompute_in_the_window_light_cone_keeps_the_bits(gpu, precision):
+    """On a grid much larger than the window's light cone over one segment, the checkpointed
+    gradient (segments recomputed only within the cone) equals the full-trace gradient bit for
+    bit, for one design and inside a batch."""
+    from etalon_gb300.adjoint import AdjointBatch, simulate_batch
+    from tests import cases
+
+    n = 1500
+    p, win = cases.adjoint_device(precision, n_steps=n, region=500, design=40, n_wavelengths=2)
+    d = DesignRegion.from_box(p, win[:2], win[2:])
+    stride = AdjointRunner.sqrt_stride(n)
+    assert d.nx + 2 * (stride + 18) < p.grid.nx // 2  # the cone is a small part of the grid
+    eps0 = torch.as_tensor(cases.smooth_design(d.nx, d.ny, 3))
+    grads = []
+    for s in (0, stride):
+        r = AdjointRunner(p, d, stride=s)
+        eps = eps0.clone().requires_grad_(True)
+        point_power(simulate(eps, r)[0], p.samplings[0]).backward()
+        grads.append(eps.grad.numpy().copy())
+        r.close()
+    assert np.abs(grads[0]).max() > 0
+    np.testing.assert_array_equal(grads[1], grads[0])
+    runners = [AdjointRunner(p, d, stride=stride), AdjointRunner(p, d, stride=stride)]
+    batch = AdjointBatch(runners)
+    eps = [eps0.clone().requires_grad_(True), (eps0 + 0.5).requires_grad_(True)]
+    outs = simulate_batch(eps, batch)
+    point_power(outs[0][0], p.samplings[0]).backward()
+    np.testing.assert_array_equal(eps[0].grad.numpy(), grads[0])
+    batch.close()
+    for r in runners:
+        r.close()

@@ -195,6 +195,8 @@ __global__ void k_adj_esrc(AdjArgs<T> a, AdjPlan<T> pe, int64_t n) {
 
 // Per-node tables of the adjoint sources: tables[q * n_steps + n] = adj_source(plan, node q, n),
 // the exact sum the one-step kernels add at that node and step.
+__global__ void k_set_step(int64_t* step, int64_t value) { *step = value; }
+
 template <typename T>
 __global__ void k_adj_tables(AdjPlan<T> plan, const int4* __restrict__ nodes, int n_nodes, int64_t n_steps,
                              T* __restrict__ tables) {
@@ -687,14 +689,24 @@ void clear_cone(etg_sim* s) {
 }
 
 // Restore checkpoint k into the simulation and set it up to re-record the trace of [lo, hi).
+// Only the rows and columns of the light cone (the simulation's active rectangle) are
+// copied: cells beyond it cannot reach the trace box within the segment. Everything is
+// queued on the simulation's stream; nothing waits on the host.
 int adj_restore_segment(etg_adj* A, int64_t k, int64_t lo, int64_t hi) {
   etg_sim* s = A->sim;
-  void* from[7];
-  for (int f = 0; f < 7; ++f) from[f] = (char*)A->ckpt[k] + f * plane_bytes(s);
-  int rc = copy_state(s, s->field, from);
-  if (rc) return rc;
-  ETG_TRY_CUDA(cudaMemcpyAsync(s->d_step, &lo, sizeof lo, cudaMemcpyHostToDevice, s->stream));
-  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  const int64_t r0 = std::max(0, s->act_i0 - 1), r1 = std::min<int64_t>(s->rows, (int64_t)s->act_i1 + 1);
+  const int64_t c0 = std::max(0, s->act_j0 - 1) / 4 * 4, c1 = std::min<int64_t>(s->P, (int64_t)s->act_j1 + 1);
+  const size_t es = s->esize();
+  for (int f = 0; f < 7; ++f) {
+    const char* from = (const char*)A->ckpt[k] + f * plane_bytes(s);
+    if (r1 > r0 && c1 > c0)
+      ETG_TRY_CUDA(cudaMemcpy2DAsync((char*)s->field[f] + (r0 * s->P + c0) * es, s->P * es,
+                                     from + (r0 * s->P + c0) * es, s->P * es, (c1 - c0) * es, r1 - r0,
+                                     cudaMemcpyDeviceToDevice, s->stream));
+  }
+  k_set_step<<<1, 1, 0, s->stream>>>(s->d_step, lo);
+  g_launches += 1;
+  ETG_LAUNCH_CHECK();
   s->h_step = lo;
   set_trace(s, A->trace, lo, hi - lo, A);
   return ETG_OK;
@@ -801,6 +813,7 @@ struct etg_adj_batch {
   int n_inner = 0, n_pml = 0;
   cudaStream_t stream = nullptr, side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+  cudaEvent_t seg_done = nullptr;  // a segment's recompute is done
   cudaStream_t sides[3] = {};  // one branch per CPML kind
   cudaEvent_t joins[3] = {};
   int n_kind[3] = {};
@@ -948,7 +961,11 @@ int batch_backward(etg_adj_batch* B) {
     for (etg_adj* A : B->adjs)
       if (rc == ETG_OK) rc = adj_restore_segment(A, k, lo, hi);
     if (rc == ETG_OK) rc = etg_batch_advance(B->fwd, hi - lo);
-    if (rc == ETG_OK) rc = etg_batch_synchronize(B->fwd);
+    if (rc == ETG_OK) {  // the sweep's stream waits for the recompute (the simulations' streams wait for it)
+      cudaError_t e = cudaEventRecord(B->seg_done, B->adjs[0]->sim->stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(B->stream, B->seg_done, 0);
+      ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "adjoint batch: %s", cudaGetErrorString(e));
+    }
     for (etg_adj* A : B->adjs) clear_trace(A->sim);
     if (rc == ETG_OK) rc = batch_sweep<T>(B, hi, lo, lo, par_e, par_h, ph, pe);
   }
@@ -957,6 +974,7 @@ int batch_backward(etg_adj_batch* B) {
     A->sim->monitors_on = true;
     sim_invalidate(A->sim);
   }
+  if (rc == ETG_OK) rc = etg_batch_synchronize(B->fwd);  // device flags of the recomputes
   return rc;
 }
 
@@ -1082,6 +1100,7 @@ int etg_adj_batch_create(etg_adj_batch** out, int n, etg_adj* const* adjs) {
        cudaStreamCreateWithFlags(&B->side, cudaStreamNonBlocking) != cudaSuccess ||
        cudaEventCreateWithFlags(&B->fork, cudaEventDisableTiming) != cudaSuccess ||
        cudaEventCreateWithFlags(&B->join, cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&B->seg_done, cudaEventDisableTiming) != cudaSuccess ||
        cudaStreamCreateWithFlags(&B->sides[0], cudaStreamNonBlocking) != cudaSuccess ||
        cudaStreamCreateWithFlags(&B->sides[1], cudaStreamNonBlocking) != cudaSuccess ||
        cudaStreamCreateWithFlags(&B->sides[2], cudaStreamNonBlocking) != cudaSuccess ||
@@ -1109,6 +1128,7 @@ int etg_adj_batch_destroy(etg_adj_batch* B) {
   cudaFree(B->d_tiles);
   if (B->fork) cudaEventDestroy(B->fork);
   if (B->join) cudaEventDestroy(B->join);
+  if (B->seg_done) cudaEventDestroy(B->seg_done);
   if (B->side) cudaStreamDestroy(B->side);
   for (int k = 0; k < 3; ++k) {
     if (B->sides[k]) cudaStreamDestroy(B->sides[k]);

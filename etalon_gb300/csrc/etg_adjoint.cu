@@ -193,10 +193,10 @@ __global__ void k_adj_esrc(AdjArgs<T> a, AdjPlan<T> pe, int64_t n) {
   if (j < s.ny) a.ley[g] = a.ley[g] + adj_source(pe, ETG_EY, i, j, n);
 }
 
-// Per-node tables of the adjoint sources: tables[q * n_steps + n] = adj_source(plan, node q, n),
-// the exact sum the one-step kernels add at that node and step.
 __global__ void k_set_step(int64_t* step, int64_t value) { *step = value; }
 
+// Per-node tables of the adjoint sources: tables[q * n_steps + n] = adj_source(plan, node q, n),
+// the exact sum the one-step kernels add at that node and step.
 template <typename T>
 __global__ void k_adj_tables(AdjPlan<T> plan, const int4* __restrict__ nodes, int n_nodes, int64_t n_steps,
                              T* __restrict__ tables) {

@@ -1199,11 +1199,12 @@ void tb_invalidate(TBState* tb) {
   tb->tiles_valid = false;
 }
 
-// Chosen by "auto": float32 grids of at least 64 x 64 cells. In float64, GB300's FP64 rate
-// rather than HBM bounds the step, and the halo recomputation would cost more than it saves.
+// Chosen by "auto": grids of at least 64 x 64 cells, in both precisions. In float64 GB300's
+// FP64 pipe rather than HBM bounds the step; the blocked kernels still beat one step per
+// launch there, halo recomputation included.
 template <typename T>
 bool tb_supported(int nx, int ny) {
-  return nx >= 64 && ny >= 64;  // both precisions: blocked beats one step per launch from here up
+  return nx >= 64 && ny >= 64;
 }
 
 template <typename T, int RPT, int K, bool PML, int NW = 8>

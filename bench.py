@@ -453,7 +453,7 @@ def batched_line(args, local, world=1, rank=0) -> dict:
             "value": cells * args.batch_time_steps / (t / 1e3), "unit": UNIT, "ms_per_run": t,
             "sims": len(every), "cells": cells, "time_steps": args.batch_time_steps,
             "sharding": f"{world} rank(s), devices balanced by cells, no exchange",
-            "tile_rows_depth": list(choice), "gpu_launches_per_run": launches // len(ms),
+            "tile_rows_depth_warps": list(choice), "gpu_launches_per_run": launches // len(ms),
             "runs_timed": len(ms), "l2": "flushed before each run"}  # fmt: skip
 
 

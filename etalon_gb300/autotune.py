@@ -1,4 +1,5 @@
-"""Autotuner of the stepping kernel: kernel family, tile rows and steps per launch per grid.
+"""Autotuner of the stepping kernel: kernel family, tile rows, steps per launch and warps per
+tile, per grid.
 
 The fastest choice depends on how the tiles of a grid fill the SMs: the number of tiles in
 the last wave, the share of CPML tiles, and whether the grid is large enough for the
@@ -18,10 +19,11 @@ from pathlib import Path
 
 from . import _lib
 
-# (kernel, tile rows, steps per launch); tile columns follow from the precision
+# (kernel, tile rows, steps per launch, warps per tile); tile columns follow from the precision
 CANDIDATES = {
-    "single": [("tb", 48, 4), ("tb", 64, 4), ("tb", 40, 4), ("tma", 40, 4), ("plain", 0, 0)],
-    "double": [("tb", 40, 2), ("tb", 32, 2), ("tma", 40, 2), ("plain", 0, 0)],
+    "single": [("tb", 48, 4, 8), ("tb", 64, 4, 8), ("tb", 40, 4, 8), ("tb", 48, 4, 16), ("tma", 40, 4, 8),
+               ("pipe", 48, 4, 8), ("plain", 0, 0, 8)],
+    "double": [("tb", 40, 2, 8), ("tb", 32, 2, 8), ("tma", 40, 2, 8), ("pipe", 40, 2, 8), ("plain", 0, 0, 8)],
 }  # fmt: skip
 
 
@@ -48,11 +50,13 @@ def _store(table: dict) -> None:
         pass  # a read-only home only costs re-tuning
 
 
-def apply(engine, choice: tuple[str, int, int]) -> None:
-    kernel, rows, depth = choice
+def apply(engine, choice: tuple) -> None:
+    """Set a candidate on an engine; a cached choice without warps per tile means 8."""
+    kernel, rows, depth = choice[:3]
     engine.set_kernel(kernel)
     engine.set_option(_lib.OPT_TILE_ROWS, rows)
     engine.set_option(_lib.OPT_TB_DEPTH, depth)
+    engine.set_option(_lib.OPT_TB_WARPS, choice[3] if len(choice) > 3 else 8)
 
 
 def key_of(engine) -> str:
@@ -60,7 +64,7 @@ def key_of(engine) -> str:
     return f"{engine.nx}x{engine.ny}:{engine.problem.precision}:{name}:{sms}"
 
 
-def tune(engine, *, steps: int = 96, reps: int = 3, use_cache: bool = True) -> tuple[str, int, int]:
+def tune(engine, *, steps: int = 96, reps: int = 3, use_cache: bool = True) -> tuple:
     """Pick and apply the fastest candidate for this engine's grid; returns it."""
     key = key_of(engine)
     table = _load() if use_cache else {}
@@ -86,7 +90,7 @@ def tune(engine, *, steps: int = 96, reps: int = 3, use_cache: bool = True) -> t
     engine.reset()
     choice = min(results, key=results.get)
     apply(engine, choice)
-    table[key] = {"choice": list(choice), "ms": {f"{k}/{r}/{d}": v for (k, r, d), v in results.items()}}
+    table[key] = {"choice": list(choice), "ms": {"/".join(map(str, c)): v for c, v in results.items()}}
     _store(table)
     return choice
 
@@ -99,28 +103,37 @@ def _get(engine, option: int) -> int:
     return v.value
 
 
-BATCH_CANDIDATES = {"single": [(48, 4), (40, 4), (64, 4)], "double": [(40, 2), (32, 2)]}
+# (tile rows, steps per launch, warps per tile)
+BATCH_CANDIDATES = {
+    "single": [(48, 4, 8), (40, 4, 8), (64, 4, 8), (48, 4, 16)],
+    "double": [(40, 2, 8), (32, 2, 8)],
+}  # fmt: skip
 
 
-def tune_batch(batch, *, steps: int = 64, reps: int = 2) -> tuple[int, int]:
-    """Pick and apply the fastest (tile rows, steps per launch) for a Batch; leaves it at step 0."""
+def _apply_batch(batch, choice: tuple[int, int, int]) -> None:
+    batch.set_option(_lib.OPT_TILE_ROWS, choice[0])
+    batch.set_option(_lib.OPT_TB_DEPTH, choice[1])
+    batch.set_option(_lib.OPT_TB_WARPS, choice[2])
+
+
+def tune_batch(batch, *, steps: int = 64, reps: int = 2) -> tuple[int, int, int]:
+    """Pick and apply the fastest (tile rows, steps per launch, warps per tile) for a Batch;
+    leaves it at step 0."""
     precision = batch.engines[0].problem.precision
     batch.set_option(_lib.OPT_TIMING, 1)
     results = {}
-    for rows, depth in BATCH_CANDIDATES[precision]:
+    for cand in BATCH_CANDIDATES[precision]:
         try:
-            batch.set_option(_lib.OPT_TILE_ROWS, rows)
-            batch.set_option(_lib.OPT_TB_DEPTH, depth)
+            _apply_batch(batch, cand)
             best = float("inf")
             for _ in range(reps):
                 batch.reset()
                 batch.advance(steps)
                 best = min(best, batch.last_timing()[0])
-            results[(rows, depth)] = best
+            results[cand] = best
         except (ValueError, _lib.EtgError):
             continue
     batch.reset()
     choice = min(results, key=results.get)
-    batch.set_option(_lib.OPT_TILE_ROWS, choice[0])
-    batch.set_option(_lib.OPT_TB_DEPTH, choice[1])
+    _apply_batch(batch, choice)
     return choice

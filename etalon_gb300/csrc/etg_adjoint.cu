@@ -728,7 +728,15 @@ int adj_backward(etg_adj* A) {
     sim_invalidate(s);
     // the blocked path recomputes through a one-simulation batch, whose plans live in device
     // memory: moving the trace origin per segment then needs no new graphs
-    if (A->tiles && !A->fwd1) rc = etg_batch_create(&A->fwd1, 1, &s);
+    if (A->tiles && !A->fwd1) {
+      rc = etg_batch_create(&A->fwd1, 1, &s);
+      // the light cone is a few dozen tiles, one wave on a fraction of the SMs: there a tile's
+      // latency sets the time, and 16 warps of 3 rows hide it better than 8 of 6 (float32)
+      if (rc == ETG_OK && s->dtype == ETG_F32 && s->opt[ETG_OPT_TB_WARPS] == 0 && s->opt[ETG_OPT_TILE_ROWS] == 0) {
+        etg_batch_set_option(A->fwd1, ETG_OPT_TILE_ROWS, 48);
+        etg_batch_set_option(A->fwd1, ETG_OPT_TB_WARPS, 16);
+      }
+    }
     set_cone(A, S);
     for (int64_t k = nseg - 1; k >= 0 && rc == ETG_OK; --k) {
       const int64_t lo = k * S, hi = std::min(A->n_steps, lo + S);

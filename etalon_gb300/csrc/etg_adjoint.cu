@@ -193,7 +193,28 @@ __global__ void k_adj_esrc(AdjArgs<T> a, AdjPlan<T> pe, int64_t n) {
   if (j < s.ny) a.ley[g] = a.ley[g] + adj_source(pe, ETG_EY, i, j, n);
 }
 
-__global__ void k_set_step(int64_t* step, int64_t value) { *step = value; }
+// One rectangle of one plane, in 32-bit words: dst[r * dst_pitch + w] = src[r * src_pitch + w]
+// for r < rows, w < words, with src and dst advanced by src_k and dst_k words per checkpoint
+// index k. `step`, when set, receives the launch's step value (a restored simulation).
+struct RectCopy {
+  const uint32_t* src;
+  uint32_t* dst;
+  int64_t src_pitch, dst_pitch, src_k, dst_k;
+  int64_t* step;
+  int rows, words;
+};
+
+__global__ void k_copy_rects(const RectCopy* __restrict__ copies, int64_t k, int64_t step_value) {
+  const RectCopy c = copies[blockIdx.y];
+  const uint32_t* src = c.src + k * c.src_k;
+  uint32_t* dst = c.dst + k * c.dst_k;
+  const int64_t n = (int64_t)c.rows * c.words;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = q / c.words, w = q % c.words;
+    dst[r * c.dst_pitch + w] = src[r * c.src_pitch + w];
+  }
+  if (c.step && blockIdx.x == 0 && threadIdx.x == 0) *c.step = step_value;
+}
 
 // Per-node tables of the adjoint sources: tables[q * n_steps + n] = adj_source(plan, node q, n),
 // the exact sum the one-step kernels add at that node and step.
@@ -222,7 +243,13 @@ struct etg_adj {
   int64_t n_steps = 0, stride = 0;  // stride 0: trace of every step
   void* trace = nullptr;
   size_t trace_cap = 0;
-  std::vector<void*> ckpt;  // each 7 planes
+  // checkpoints: nseg x 7 planes of the light-cone rectangle [ck_r0, ck_r1) x [ck_c0, ck_c1)
+  // (elements of the pitched planes), stored compactly one after the other
+  void* ckpt = nullptr;
+  size_t ckpt_cap = 0;
+  int64_t ck_r0 = 0, ck_r1 = 0, ck_c0 = 0, ck_c1 = 0;
+  void* d_copies = nullptr;  // the RectCopy list of the current save or restore
+  size_t copies_cap = 0;
   void* lam[3] = {};        // lambda Ex, Ey, Hz
   void* lpsi[2][4] = {};    // double-buffered lambda psi
   double* grad = nullptr;   // gx then gy
@@ -326,12 +353,6 @@ void set_trace(etg_sim* s, void* buf, int64_t n0, int64_t rows, const etg_adj* A
 void clear_trace(etg_sim* s) {
   s->trace_buf = nullptr;
   sim_invalidate(s);
-}
-
-int copy_state(etg_sim* s, void* const* to, void* const* from) {
-  for (int f = 0; f < 7; ++f)
-    ETG_TRY_CUDA(cudaMemcpyAsync(to[f], from[f], plane_bytes(s), cudaMemcpyDeviceToDevice, s->stream));
-  return ETG_OK;
 }
 
 // Arguments of one temporally blocked launch; `to_alt` reads the primary lambda buffers
@@ -673,14 +694,19 @@ int adj_begin(etg_adj* A, AdjPlan<T>* ph, AdjPlan<T>* pe) {
 // stepped: a value moves at most one cell per time step, so the trace box stays exact for S
 // steps when every cell within S cells of it is, and the tiles beyond (their halos read cells
 // that are not updated) only spoil cells farther out. The margin adds room for two launches
-// of the deepest tiles.
+// of the deepest tiles. Checkpoints keep only that rectangle of the planes (one more row and
+// column on each side, columns from a multiple of 4): nothing else is ever restored.
+void cone_of(const etg_adj* A, int64_t S, int* i0, int* i1, int* j0, int* j1) {
+  const int64_t m = S + 2 * 8 + 2;
+  *i0 = (int)std::max<int64_t>(0, A->ti0 - m);
+  *i1 = (int)std::min<int64_t>(1 << 30, A->ti0 + A->tnx + m);
+  *j0 = (int)std::max<int64_t>(0, A->tj0 - m);
+  *j1 = (int)std::min<int64_t>(1 << 30, A->tj0 + A->tny + m);
+}
+
 void set_cone(etg_adj* A, int64_t S) {
   etg_sim* s = A->sim;
-  const int64_t m = S + 2 * 8 + 2;
-  s->act_i0 = (int)std::max<int64_t>(0, A->ti0 - m);
-  s->act_i1 = (int)std::min<int64_t>(1 << 30, A->ti0 + A->tnx + m);
-  s->act_j0 = (int)std::max<int64_t>(0, A->tj0 - m);
-  s->act_j1 = (int)std::min<int64_t>(1 << 30, A->tj0 + A->tny + m);
+  cone_of(A, S, &s->act_i0, &s->act_i1, &s->act_j0, &s->act_j1);
 }
 
 void clear_cone(etg_sim* s) {
@@ -688,28 +714,72 @@ void clear_cone(etg_sim* s) {
   s->act_i1 = s->act_j1 = 1 << 30;
 }
 
-// Restore checkpoint k into the simulation and set it up to re-record the trace of [lo, hi).
-// Only the rows and columns of the light cone (the simulation's active rectangle) are
-// copied: cells beyond it cannot reach the trace box within the segment. Everything is
-// queued on the simulation's stream; nothing waits on the host.
-int adj_restore_segment(etg_adj* A, int64_t k, int64_t lo, int64_t hi) {
-  etg_sim* s = A->sim;
-  const int64_t r0 = std::max(0, s->act_i0 - 1), r1 = std::min<int64_t>(s->rows, (int64_t)s->act_i1 + 1);
-  const int64_t c0 = std::max(0, s->act_j0 - 1) / 4 * 4, c1 = std::min<int64_t>(s->P, (int64_t)s->act_j1 + 1);
-  const size_t es = s->esize();
+// The checkpoint rectangle of A for segments of S steps.
+void set_ckpt_rect(etg_adj* A, int64_t S) {
+  const etg_sim* s = A->sim;
+  int i0, i1, j0, j1;
+  cone_of(A, S, &i0, &i1, &j0, &j1);
+  A->ck_r0 = std::max(0, i0 - 1);
+  A->ck_r1 = std::min<int64_t>(s->rows, (int64_t)i1 + 1);
+  A->ck_c0 = std::max(0, j0 - 1) / 4 * 4;
+  A->ck_c1 = std::min<int64_t>(s->P, (int64_t)j1 + 1);
+}
+
+size_t ckpt_bytes(const etg_adj* A) {
+  return 7 * (size_t)std::max<int64_t>(0, A->ck_r1 - A->ck_r0) * std::max<int64_t>(0, A->ck_c1 - A->ck_c0) *
+         A->sim->esize();
+}
+
+// The 7 plane copies of design A: fields -> checkpoint k (save) or checkpoint k -> fields,
+// which also sets the step counter (restore).
+void ckpt_copies(const etg_adj* A, bool save, std::vector<RectCopy>* out) {
+  const etg_sim* s = A->sim;
+  const int64_t es = (int64_t)s->esize(), rows = std::max<int64_t>(0, A->ck_r1 - A->ck_r0);
+  const int64_t words = std::max<int64_t>(0, A->ck_c1 - A->ck_c0) * es / 4, plane = rows * words;
   for (int f = 0; f < 7; ++f) {
-    const char* from = (const char*)A->ckpt[k] + f * plane_bytes(s);
-    if (r1 > r0 && c1 > c0)
-      ETG_TRY_CUDA(cudaMemcpy2DAsync((char*)s->field[f] + (r0 * s->P + c0) * es, s->P * es,
-                                     from + (r0 * s->P + c0) * es, s->P * es, (c1 - c0) * es, r1 - r0,
-                                     cudaMemcpyDeviceToDevice, s->stream));
+    uint32_t* field = (uint32_t*)((char*)s->field[f] + (A->ck_r0 * s->P + A->ck_c0) * es);
+    uint32_t* ck = (uint32_t*)A->ckpt + f * plane;
+    RectCopy c;
+    c.src = save ? field : ck;
+    c.dst = save ? ck : field;
+    c.src_pitch = save ? s->P * es / 4 : words;
+    c.dst_pitch = save ? words : s->P * es / 4;
+    c.src_k = save ? 0 : 7 * plane;
+    c.dst_k = save ? 7 * plane : 0;
+    c.step = !save && f == 0 ? s->d_step : nullptr;
+    c.rows = (int)rows;
+    c.words = (int)words;
+    out->push_back(c);
   }
-  k_set_step<<<1, 1, 0, s->stream>>>(s->d_step, lo);
+}
+
+// Upload a copy list (once per pass) and run it for checkpoint k in one launch.
+int upload_copies(void** buf, size_t* cap, const std::vector<RectCopy>& copies, cudaStream_t st) {
+  const size_t bytes = copies.size() * sizeof(RectCopy);
+  if (*cap < bytes) {
+    cudaFree(*buf);
+    *buf = nullptr;
+    *cap = 0;
+    int rc = etg_malloc(buf, bytes);
+    if (rc) return rc;
+    *cap = bytes;
+  }
+  ETG_TRY_CUDA(cudaMemcpyAsync(*buf, copies.data(), bytes, cudaMemcpyHostToDevice, st));
+  return ETG_OK;
+}
+
+int run_copies(const void* buf, int n, int64_t k, int64_t step_value, cudaStream_t st) {
+  k_copy_rects<<<dim3(64, (unsigned)n), 256, 0, st>>>((const RectCopy*)buf, k, step_value);
   g_launches += 1;
   ETG_LAUNCH_CHECK();
-  s->h_step = lo;
-  set_trace(s, A->trace, lo, hi - lo, A);
   return ETG_OK;
+}
+
+// Host side of restoring segment [lo, hi) of design A (the copies run separately): step
+// index, and the trace it re-records.
+void begin_segment(etg_adj* A, int64_t lo, int64_t hi) {
+  A->sim->h_step = lo;
+  set_trace(A->sim, A->trace, lo, hi - lo, A);
 }
 
 template <typename T>
@@ -738,9 +808,13 @@ int adj_backward(etg_adj* A) {
       }
     }
     set_cone(A, S);
+    std::vector<RectCopy> copies;
+    ckpt_copies(A, false, &copies);
+    if (rc == ETG_OK) rc = upload_copies(&A->d_copies, &A->copies_cap, copies, s->stream);
     for (int64_t k = nseg - 1; k >= 0 && rc == ETG_OK; --k) {
       const int64_t lo = k * S, hi = std::min(A->n_steps, lo + S);
-      rc = adj_restore_segment(A, k, lo, hi);
+      rc = run_copies(A->d_copies, (int)copies.size(), k, lo, s->stream);
+      begin_segment(A, lo, hi);
       if (rc == ETG_OK) {
         if (A->tiles) {
           rc = etg_batch_advance(A->fwd1, hi - lo);
@@ -788,24 +862,18 @@ int adj_forward_setup(etg_adj* A, int64_t n_steps, int64_t stride) {
   }
   if (stride > 0) {
     const int64_t nseg = (n_steps + stride - 1) / stride;
-    if ((int64_t)A->ckpt.size() != nseg) {
-      for (void* p : A->ckpt) cudaFree(p);
-      A->ckpt.assign(nseg, nullptr);
-    }
-    for (void*& p : A->ckpt) {
-      if (p) continue;
-      rc = etg_malloc(&p, 7 * plane_bytes(s));
+    set_ckpt_rect(A, stride);
+    const size_t bytes = std::max<size_t>(1, (size_t)nseg * ckpt_bytes(A));
+    if (A->ckpt_cap < bytes) {
+      cudaFree(A->ckpt);
+      A->ckpt = nullptr;
+      A->ckpt_cap = 0;
+      rc = etg_malloc(&A->ckpt, bytes);
       if (rc) return rc;
+      A->ckpt_cap = bytes;
     }
   }
   return ETG_OK;
-}
-
-int adj_save_checkpoint(etg_adj* A, int64_t k) {
-  etg_sim* s = A->sim;
-  void* to[7];
-  for (int f = 0; f < 7; ++f) to[f] = (char*)A->ckpt[k] + f * plane_bytes(s);
-  return copy_state(s, to, s->field);
 }
 
 // ------------------------------------------------------------------ many designs at once
@@ -822,6 +890,8 @@ struct etg_adj_batch {
   cudaStream_t stream = nullptr, side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
   cudaEvent_t seg_done = nullptr;  // a segment's recompute is done
+  void* d_copies = nullptr;        // RectCopy list of every design's checkpoint save or restore
+  size_t copies_cap = 0;
   cudaStream_t sides[3] = {};  // one branch per CPML kind
   cudaEvent_t joins[3] = {};
   int n_kind[3] = {};
@@ -963,11 +1033,16 @@ int batch_backward(etg_adj_batch* B) {
     set_cone(A, S);
     sim_invalidate(A->sim);
   }
-  int rc = ETG_OK;
+  // one launch restores every design's light cone and step counter; the batch then waits for
+  // it (it synchronises the simulations' streams first)
+  std::vector<RectCopy> copies;
+  for (etg_adj* A : B->adjs) ckpt_copies(A, false, &copies);
+  cudaStream_t cs = B->adjs[0]->sim->stream;
+  int rc = upload_copies(&B->d_copies, &B->copies_cap, copies, cs);
   for (int64_t k = nseg - 1; k >= 0 && rc == ETG_OK; --k) {
     const int64_t lo = k * S, hi = std::min(B->n_steps, lo + S);
-    for (etg_adj* A : B->adjs)
-      if (rc == ETG_OK) rc = adj_restore_segment(A, k, lo, hi);
+    rc = run_copies(B->d_copies, (int)copies.size(), k, lo, cs);
+    for (etg_adj* A : B->adjs) begin_segment(A, lo, hi);
     if (rc == ETG_OK) rc = etg_batch_advance(B->fwd, hi - lo);
     if (rc == ETG_OK) {  // the sweep's stream waits for the recompute (the simulations' streams wait for it)
       cudaError_t e = cudaEventRecord(B->seg_done, B->adjs[0]->sim->stream);
@@ -1024,7 +1099,8 @@ int etg_adj_destroy(etg_adj* A) {
   if (!A) return ETG_OK;
   if (A->sim && A->sim->trace_buf == A->trace) clear_trace(A->sim);
   cudaFree(A->trace);
-  for (void* p : A->ckpt) cudaFree(p);
+  cudaFree(A->ckpt);
+  cudaFree(A->d_copies);
   for (void* p : A->lam) cudaFree(p);
   for (auto& b : A->lpsi)
     for (void* p : b) cudaFree(p);
@@ -1058,11 +1134,15 @@ int etg_adj_forward(etg_adj* A, int64_t n_steps, int64_t stride) {
     clear_trace(s);
     if (rc) return rc;
   } else {
-    for (int64_t k = 0; k < (int64_t)A->ckpt.size(); ++k) {
-      rc = adj_save_checkpoint(A, k);
+    std::vector<RectCopy> copies;
+    ckpt_copies(A, true, &copies);
+    rc = upload_copies(&A->d_copies, &A->copies_cap, copies, s->stream);
+    const int64_t nseg = (n_steps + stride - 1) / stride;
+    for (int64_t k = 0; k < nseg && rc == ETG_OK; ++k) {
+      rc = run_copies(A->d_copies, (int)copies.size(), k, -1, s->stream);
       if (rc == ETG_OK) rc = sim_advance_internal(s, std::min(stride, n_steps - k * stride));
-      if (rc) return rc;
     }
+    if (rc) return rc;
   }
   return etg_sim_synchronize(s);
 }
@@ -1137,6 +1217,7 @@ int etg_adj_batch_destroy(etg_adj_batch* B) {
   if (B->fork) cudaEventDestroy(B->fork);
   if (B->join) cudaEventDestroy(B->join);
   if (B->seg_done) cudaEventDestroy(B->seg_done);
+  cudaFree(B->d_copies);
   if (B->side) cudaStreamDestroy(B->side);
   for (int k = 0; k < 3; ++k) {
     if (B->sides[k]) cudaStreamDestroy(B->sides[k]);
@@ -1168,10 +1249,15 @@ int etg_adj_batch_forward(etg_adj_batch* B, int64_t n_steps, int64_t stride) {
     for (etg_adj* A : B->adjs) clear_trace(A->sim);
     return rc;
   }
+  // one launch saves every design's checkpoint k (the batch makes every simulation's stream
+  // wait for its steps, and synchronises them before the next ones)
+  std::vector<RectCopy> copies;
+  for (etg_adj* A : B->adjs) ckpt_copies(A, true, &copies);
+  cudaStream_t cs = B->adjs[0]->sim->stream;
+  rc = upload_copies(&B->d_copies, &B->copies_cap, copies, cs);
   const int64_t nseg = (n_steps + stride - 1) / stride;
   for (int64_t k = 0; k < nseg && rc == ETG_OK; ++k) {
-    for (etg_adj* A : B->adjs)
-      if (rc == ETG_OK) rc = adj_save_checkpoint(A, k);
+    rc = run_copies(B->d_copies, (int)copies.size(), k, -1, cs);
     if (rc == ETG_OK) rc = etg_batch_advance(B->fwd, std::min(stride, n_steps - k * stride));
   }
   if (rc == ETG_OK) rc = etg_batch_synchronize(B->fwd);

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
@@ -45,8 +46,9 @@ __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, 
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
 
-// Counts kernel launches issued by the library (reported by the bench).
-extern int64_t g_launches;
+// Counts kernel launches issued by the library (reported by the bench); engines on several
+// host threads add to it concurrently.
+extern std::atomic<int64_t> g_launches;
 
 template <typename T>
 struct Vec4;  // four consecutive elements, 16-byte (f32) or 2x16-byte (f64) accesses

@@ -14,7 +14,7 @@
 namespace etg {
 
 static thread_local std::string t_error;
-int64_t g_launches = 0;
+std::atomic<int64_t> g_launches{0};
 
 void set_error(const char* fmt, ...) {
   char buf[1024];

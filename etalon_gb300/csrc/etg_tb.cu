@@ -320,7 +320,7 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
 
   auto steps = [&](auto keep_tag) {
     constexpr bool KEEP0 = decltype(keep_tag)::value;
-    for (int s = 0; s < K; ++s) {
+    auto body = [&](const int s) {
       const int64_t n = n_base + s;
       // ---------------------------------------------------------------- H half step
       {
@@ -487,6 +487,12 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
       }
       ey[0].st(sEyX + ty * EC + lj0);
       __syncthreads();
+    };
+    if constexpr (KEEP0 && !PML) {  // the rare path (a -0 was loaded) stays small in the instruction cache
+#pragma unroll 1
+      for (int s = 0; s < K; ++s) body(s);
+    } else {
+      for (int s = 0; s < K; ++s) body(s);
     }
   };
   if constexpr (PML) {

@@ -221,6 +221,42 @@ class TEEngine:
         call("etg_sim_get_dft", self._h, self.monitors[k].id, _ptr(out))
         return out
 
+    def set_dft(self, k: int, value: np.ndarray) -> None:
+        m = self.monitors[k].sampling
+        a = np.ascontiguousarray(value, dtype=self.complex)
+        if a.shape != (m.wavelengths.size, m.flat_index.size):
+            raise ValueError(f"monitor {k}: shape {a.shape}, expected {(m.wavelengths.size, m.flat_index.size)}")
+        call("etg_sim_set_dft", self._h, self.monitors[k].id, _ptr(a))
+
+    # ------------------------------------------------------------------ checkpoint / resume
+    STATE_FIELDS = ("ex", "ey", "hz", "psi_ex_y", "psi_ey_x", "psi_hz_x", "psi_hz_y")
+
+    def save_state(self, path=None) -> dict[str, np.ndarray]:
+        """Everything a run needs to continue: the seven field and ψ arrays, every DFT
+        accumulator and the step index (host copies; also written to ``path`` as .npz)."""
+        state = {f: self.field(f) for f in self.STATE_FIELDS}
+        for k in range(len(self.monitors)):
+            state[f"dft{k}"] = self.dft(k)
+        state["step"] = np.array(self.n, dtype=np.int64)
+        if path is not None:
+            np.savez(path, **state)
+        return state
+
+    def load_state(self, state) -> None:
+        """Resume from ``save_state`` output (a dict or an .npz path) of a run of the same
+        problem; the continued run gives the uninterrupted run's bits."""
+        if not isinstance(state, dict):
+            with np.load(state, allow_pickle=False) as z:
+                state = {k: z[k] for k in z.files}
+        n_mon = sum(1 for k in state if k.startswith("dft"))
+        if n_mon != len(self.monitors):
+            raise ValueError(f"state holds {n_mon} monitor accumulators, the engine has {len(self.monitors)}")
+        for f in self.STATE_FIELDS:
+            self.set_field(f, state[f])
+        for k in range(len(self.monitors)):
+            self.set_dft(k, state[f"dft{k}"])
+        call("etg_sim_set_step_index", self._h, int(state["step"]))
+
     def set_option(self, option: int, value: int) -> None:
         call("etg_sim_set_option", self._h, option, int(value))
 

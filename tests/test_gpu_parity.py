@@ -678,3 +678,30 @@ def test_interior_tiles_with_uploaded_negative_zeros_bitwise(gpu, precision, mod
         else:
             engines[0].close()
 
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("kernel", ["auto", "plain"])
+def test_checkpoint_resume_in_a_new_engine_keeps_the_bits(gpu, precision, kernel, tmp_path):
+    """Save the state half way (fields, ψ, accumulators, step index) to .npz, resume it in a
+    fresh engine: the continued run equals the uninterrupted one bit for bit."""
+    n = 300
+    p = cases.g4_full(precision, n_steps=n)
+    whole = TEEngine(p, kernel=kernel)
+    whole.advance(n)
+    first = TEEngine(p, kernel=kernel)
+    first.advance(137)
+    first.save_state(tmp_path / "half.npz")
+    first.close()
+    second = TEEngine(p, kernel=kernel)
+    second.load_state(tmp_path / "half.npz")
+    assert second.n == 137
+    second.advance(n - 137)
+    try:
+        for f in FIELDS:
+            assert np.array_equal(_bits(second.field(f)), _bits(whole.field(f))), f
+        for k in range(len(whole.monitors)):
+            assert np.array_equal(second.dft(k).view(np.uint8), whole.dft(k).view(np.uint8))
+    finally:
+        whole.close()
+        second.close()

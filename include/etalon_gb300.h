@@ -206,8 +206,9 @@ typedef struct etg_adj etg_adj;
 int etg_adj_create(etg_adj** out, etg_sim* sim, int i0, int nxd, int j0, int nyd);
 int etg_adj_destroy(etg_adj* adj);
 /* Forward run of n_steps from zero fields (monitors accumulate as in etg_sim_advance).
- * stride 0 records Hz on the window at every step; stride S > 0 keeps full-state
- * checkpoints every S steps instead and recomputes each segment in the backward pass. */
+ * stride 0 records Hz on the window at every step; stride S > 0 keeps a checkpoint every S
+ * steps instead (fields and psi over the window's light cone for S steps) and recomputes each
+ * segment, within that cone, in the backward pass. */
 int etg_adj_forward(etg_adj* adj, int64_t n_steps, int64_t stride);
 /* Reverse sweep: grad_acc[m] is dJ/d(accumulator m), (n_f, nodes) complex in dtype, or NULL
  * for monitors J does not use (one entry per monitor, in order of addition). Writes

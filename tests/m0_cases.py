@@ -1,0 +1,75 @@
+"""Setups and analytic references of Etalon's M0 physics validations (tests/validation/test_m0.py,
+etalon/validation/m0.py), shared by the oracle's CPU run and the GPU engine's run."""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from etalon_gb300 import physics as ph
+
+GREEN_WAVELENGTHS = np.linspace(1.3, 1.8, 11)
+
+
+def centred_size(half_width: float, dl: float) -> float:
+    """A region with an odd number of cells, so the origin is an Hz node."""
+    return (2 * math.ceil(half_width / dl) + 1) * dl
+
+
+def late_time_problem(precision: str = "single") -> ph.TEProblem:
+    """V5: a Gaussian Hz pulse at the centre of a 2 µm vacuum box, 12-layer CPML, 30 000 steps."""
+    dl = 0.05
+    size = centred_size(1.0, dl)
+    return ph.te_problem(size=(size, size), dl=dl, pml=ph.PMLSpec(layers=12),
+                         sources=[ph.PointSource((0.0, 0.0, 0.0), "Hz", ph.GaussianPulse(1.55, 0.5))],
+                         n_steps=30_000, precision=precision)  # fmt: skip
+
+
+def late_time_energy(p: ph.TEProblem, advance, fields) -> np.ndarray:
+    """Total field energy per unit length after steps 1, 51, 101, … (``advance(k)`` runs k
+    steps, ``fields()`` returns Ex, Ey, Hz), normalised to its peak."""
+    area = (p.grid.dx * ph.UM) * (p.grid.dy * ph.UM)
+    energy = []
+    for k in range(p.n_steps // 50):
+        advance(1 if k == 0 else 50)
+        ex, ey, hz = fields()
+        w = 0.5 * ph.EPSILON_0 * (np.sum(ex.astype(float) ** 2) + np.sum(ey.astype(float) ** 2))
+        w += 0.5 * ph.MU_0 * np.sum(hz.astype(float) ** 2)
+        energy.append(w * area)
+    energy = np.asarray(energy)
+    return energy / energy.max()
+
+
+def green_problem(precision: str = "single", dl: float = 0.05, radius: float = 3.0):
+    """V6: Hz line source at the origin, point monitor at (r, 0) with r = round(3/dl)·dl."""
+    pulse = ph.GaussianPulse(1.55, 0.5, amplitude=1.0)
+    size = centred_size(radius + 1.5, dl)
+    m = round(radius / dl)
+    p = ph.te_problem(size=(size, size), dl=dl, pml=ph.PMLSpec(layers=12),
+                      sources=[ph.PointSource((0.0, 0.0, 0.0), "Hz", pulse)],
+                      monitors=[ph.DFTMonitor("probe", list(GREEN_WAVELENGTHS), center=(m * dl, 0.0, 0.0),
+                                              components=("Hz",))],
+                      run_time=250e-15, precision=precision)  # fmt: skip
+    return p, pulse, m * dl
+
+
+def yee_wavenumber_along_x(wavelengths_um, grid) -> np.ndarray:
+    """k̃ (1/m) of the 2D Yee scheme in vacuum along x: sin(k̃Δx/2)/Δx = sin(ωΔt/2)/(cΔt)
+    (Taflove & Hagness, ch. 4), solved in closed form."""
+    omega = 2.0 * np.pi * ph.C_0_SI / (np.asarray(wavelengths_um, dtype=np.float64) * ph.UM)
+    dx, dt = grid.dx * ph.UM, grid.dt
+    return 2.0 / dx * np.arcsin(dx * np.sin(omega * dt / 2.0) / (ph.C_0_SI * dt))
+
+
+def green_analytic(p: ph.TEProblem, pulse: ph.GaussianPulse, r_um: float) -> np.ndarray:
+    """−(ωε0/4) K̂(ω) H0⁽¹⁾(k̃ r) for M_z = K(t) δ²(r), time convention e^(−iωt); K̂ is the DFT of
+    the injected samples K(nΔt) with the monitor's Δt."""
+    from scipy.special import hankel1
+
+    g = p.grid
+    t = np.arange(p.n_steps) * g.dt
+    omega = 2.0 * np.pi * ph.C_0 / GREEN_WAVELENGTHS
+    k_hat = (ph.pulse_signal(pulse, t)[None, :] * np.exp(1j * omega[:, None] * t[None, :])).sum(1) * g.dt
+    k_yee = yee_wavenumber_along_x(GREEN_WAVELENGTHS, g)
+    return -(omega * ph.EPSILON_0 / 4.0) * k_hat * hankel1(0, k_yee * r_um * ph.UM)

@@ -1,0 +1,44 @@
+"""Etalon's M0 physics validations on this backend's resident engine (needs a GPU).
+
+Etalon checks its 2D TE solver against analytic results in tests/validation/test_m0.py; V5
+(late-time stability) and V6 (2D Green's function) are restated on TEEngine at their full
+lengths with the same thresholds (setups in tests/m0_cases.py). The oracle passes the same
+checks on the CPU (tests/test_oracle_physics.py).
+"""
+
+import numpy as np
+import pytest
+
+from etalon_gb300.engine import TEEngine
+from etalon_gb300.solver import interpolate_monitor
+from tests import m0_cases
+
+pytestmark = pytest.mark.gpu
+
+
+def test_v5_late_time_energy_decays_and_never_grows(gpu):
+    """30 000 steps: the energy ends below 1e-8 of its peak and never grows after it."""
+    p = m0_cases.late_time_problem()
+    e = TEEngine(p)
+    try:
+        energy = m0_cases.late_time_energy(p, e.advance, lambda: (e.field("ex"), e.field("ey"), e.field("hz")))
+    finally:
+        e.close()
+    peak = int(np.argmax(energy))
+    assert energy[-1] < 1e-8
+    assert np.all(np.diff(energy[peak:]) <= 1e-12)
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_v6_field_matches_2d_greens_function(gpu, precision):
+    """Hz at r = 3 µm within 1 % of the analytic line-source field at 11 wavelengths."""
+    pytest.importorskip("scipy.special")
+    p, pulse, r = m0_cases.green_problem(precision)
+    e = TEEngine(p)
+    try:
+        e.advance(p.n_steps)
+        measured = interpolate_monitor(p.samplings[0], e.dft(0)).reshape(-1).astype(np.complex128)
+    finally:
+        e.close()
+    ratio = measured / m0_cases.green_analytic(p, pulse, r)
+    assert np.all(np.abs(ratio - 1.0) < 1e-2), ratio

@@ -1,0 +1,38 @@
+"""The oracle passes Etalon's M0 physics validations V5 and V6 (tests/validation/test_m0.py)
+with Etalon's thresholds, on the CPU (a few seconds each)."""
+
+import numpy as np
+import pytest
+
+from etalon_gb300 import physics as ph
+from etalon_gb300.solver import interpolate_monitor
+from oracle.te_numpy import OracleMonitor, OracleSource, OracleTE
+from tests import m0_cases
+
+
+def _oracle(p):
+    return OracleTE(
+        p.grid.nx, p.grid.ny, p.grid.dt, vars(ph.cast_coefficients(p)), p.real,
+        [OracleSource(i.component, i.i, i.j, i.coefficient, (i.pulse.wavelength, i.pulse.bandwidth, i.pulse.amplitude))
+         for i in p.injections],
+        [OracleMonitor(s.component, s.flat_index, s.frequencies) for s in p.samplings],
+    )  # fmt: skip
+
+
+def test_v5_oracle_late_time_energy_decays():
+    p = m0_cases.late_time_problem()
+    o = _oracle(p)
+    energy = m0_cases.late_time_energy(p, o.run, lambda: (o.ex, o.ey, o.hz))
+    peak = int(np.argmax(energy))
+    assert energy[-1] < 1e-8
+    assert np.all(np.diff(energy[peak:]) <= 1e-12)
+
+
+def test_v6_oracle_matches_2d_greens_function():
+    pytest.importorskip("scipy.special")
+    p, pulse, r = m0_cases.green_problem("single")
+    o = _oracle(p)
+    o.run(p.n_steps)
+    measured = interpolate_monitor(p.samplings[0], o.acc[0]).reshape(-1).astype(np.complex128)
+    ratio = measured / m0_cases.green_analytic(p, pulse, r)
+    assert np.all(np.abs(ratio - 1.0) < 1e-2), ratio

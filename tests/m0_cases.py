@@ -73,3 +73,37 @@ def green_analytic(p: ph.TEProblem, pulse: ph.GaussianPulse, r_um: float) -> np.
     k_hat = (ph.pulse_signal(pulse, t)[None, :] * np.exp(1j * omega[:, None] * t[None, :])).sum(1) * g.dt
     k_yee = yee_wavenumber_along_x(GREEN_WAVELENGTHS, g)
     return -(omega * ph.EPSILON_0 / 4.0) * k_hat * hankel1(0, k_yee * r_um * ph.UM)
+
+
+def reflection_problems(layers: int = 12, run_time: float = 100e-15, precision: str = "single"):
+    """V4 (Taflove & Hagness, ch. 7): Hz at probes 2 cells inside the region, next to the side
+    and the corner of a 3.05 µm box, against a box large enough that its boundary reflections
+    arrive after the run. Returns [(problem, [(i, j) per probe])] for the small and the large box."""
+    dl = 0.05
+    size = centred_size(1.5, dl)
+    edge = size / 2.0
+    probes = [(edge - 2.5 * dl, 0.0), (edge - 2.5 * dl, edge - 2.5 * dl)]  # side, corner
+    margin = ph.C_0 * run_time / 2.0
+    src = [ph.PointSource((0.0, 0.0, 0.0), "Hz", ph.GaussianPulse(1.55, 0.5))]
+    out = []
+    for region in (size, centred_size(1.5 + margin, dl)):
+        p = ph.te_problem(size=(region, region), dl=dl, pml=ph.PMLSpec(layers=layers), sources=src,
+                          run_time=run_time, precision=precision)  # fmt: skip
+        x, y = p.grid.coords("Hz")
+        out.append((p, [(int(np.argmin(np.abs(x - px))), int(np.argmin(np.abs(y - py)))) for px, py in probes]))
+    return out
+
+
+def hz_traces(p: ph.TEProblem, idx, advance, hz) -> np.ndarray:
+    """Hz at the probe nodes after every step, (n_steps, n_probes)."""
+    trace = np.empty((p.n_steps, len(idx)))
+    for n in range(p.n_steps):
+        advance(1)
+        h = hz()
+        trace[n] = [float(h[i, j]) for i, j in idx]
+    return trace
+
+
+def reflection_error(small: np.ndarray, reference: np.ndarray) -> np.ndarray:
+    """max_t |Hz − Hz_ref| / max_t |Hz_ref| per probe."""
+    return np.abs(small - reference).max(0) / np.abs(reference).max(0)

@@ -42,3 +42,18 @@ def test_v6_field_matches_2d_greens_function(gpu, precision):
         e.close()
     ratio = measured / m0_cases.green_analytic(p, pulse, r)
     assert np.all(np.abs(ratio - 1.0) < 1e-2), ratio
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_v4_cpml_reflection_below_minus_80_db(gpu, precision):
+    """Hz next to the CPML side and corner against a reflection-free larger box: within 1e-4
+    of the reference's peak (Etalon's −80 dB guard; it measures about −91 dB)."""
+    traces = []
+    for p, idx in m0_cases.reflection_problems(precision=precision):
+        e = TEEngine(p)
+        try:
+            traces.append(m0_cases.hz_traces(p, idx, e.advance, lambda: e.field("hz")))
+        finally:
+            e.close()
+    assert np.abs(traces[1]).max() > 0
+    assert np.all(m0_cases.reflection_error(*traces) < 1e-4)

@@ -36,3 +36,12 @@ def test_v6_oracle_matches_2d_greens_function():
     measured = interpolate_monitor(p.samplings[0], o.acc[0]).reshape(-1).astype(np.complex128)
     ratio = measured / m0_cases.green_analytic(p, pulse, r)
     assert np.all(np.abs(ratio - 1.0) < 1e-2), ratio
+
+
+def test_v4_oracle_cpml_reflection_below_minus_80_db():
+    traces = []
+    for p, idx in m0_cases.reflection_problems():
+        o = _oracle(p)
+        traces.append(m0_cases.hz_traces(p, idx, o.run, lambda: o.hz))
+    assert np.abs(traces[1]).max() > 0
+    assert np.all(m0_cases.reflection_error(*traces) < 1e-4)

@@ -352,6 +352,7 @@ void set_trace(etg_sim* s, void* buf, int64_t n0, int64_t rows, const etg_adj* A
 
 void clear_trace(etg_sim* s) {
   s->trace_buf = nullptr;
+  s->trace_cone = false;
   sim_invalidate(s);
 }
 
@@ -779,6 +780,7 @@ int run_copies(const void* buf, int n, int64_t k, int64_t step_value, cudaStream
 // index, and the trace it re-records.
 void begin_segment(etg_adj* A, int64_t lo, int64_t hi) {
   A->sim->h_step = lo;
+  A->sim->trace_cone = true;
   set_trace(A->sim, A->trace, lo, hi - lo, A);
 }
 

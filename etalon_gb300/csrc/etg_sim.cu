@@ -125,6 +125,7 @@ int build_plans(etg_sim* s, PhasePlan<T>* ph, PhasePlan<T>* pe, int64_t sample_s
     ph->trace.tnx = s->trace_tnx;
     ph->trace.tj0 = s->trace_tj0;
     ph->trace.tny = s->trace_tny;
+    ph->trace.cone = s->trace_cone ? 1 : 0;
   }
   for (Monitor& m : s->monitors) {
     if (!s->monitors_on) break;

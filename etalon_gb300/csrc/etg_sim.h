@@ -37,6 +37,9 @@ struct TraceDesc {
   T* buf;  // nullptr: no trace
   int64_t n0, rows;
   int ti0, tnx, tj0, tny;
+  // Recompute of an adjoint segment [n0, n0 + rows): only the trace box is wanted, so a tile
+  // farther from it (in cells) than the steps left in the segment does nothing.
+  int cone;
 };
 
 // Sources and monitors of one half step (H or E), passed by value as a kernel parameter.
@@ -209,6 +212,7 @@ struct etg_sim {
   int64_t trace_n0 = 0, trace_rows = 0;
   int trace_ti0 = 0, trace_tnx = 0, trace_tj0 = 0, trace_tny = 0;
   bool monitors_on = true;
+  bool trace_cone = false;  // the trace is a segment recompute (TraceDesc::cone)
   // Output cells a batch steps: tiles whose output misses [act_i0, act_i1) x [act_j0, act_j1)
   // are left out. The adjoint narrows it to the light cone of its window while it recomputes
   // a segment; everything else runs with the whole grid.

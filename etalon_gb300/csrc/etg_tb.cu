@@ -161,6 +161,20 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
   T* const sEyX = sHzX + S::XCH;                 // [k = ty]: first-row Ey of warp ty; [NW] = zeros
   __shared__ uint32_t s_rel[4];  // relevant plan entries: H sources, E sources, H monitors, E monitors
 
+  if constexpr (!STAGED) {
+    // recompute of an adjoint segment: a tile whose output lies farther (in cells) from the
+    // trace box than the steps left in the segment cannot change the trace and does nothing
+    // (the whole CTA leaves before its first barrier). Values move one cell per step, so the
+    // tiles still stepped read exact halos: each of their cells was within the cone one launch
+    // earlier. 2K + 2 cells of margin.
+    const TraceDesc<T>& tr = ph.trace;
+    if (tr.buf && tr.cone) {
+      const int di = max(0, max(tr.ti0 - (tile.x + S::OR - 1), tile.x - (tr.ti0 + tr.tnx - 1)));
+      const int dj = max(0, max(tr.tj0 - (tile.y + S::OC - 1), tile.y - (tr.tj0 + tr.tny - 1)));
+      const int64_t left = tr.n0 + tr.rows - (*a.step + step_off);
+      if ((int64_t)max(di, dj) > left + 2 * K + 2) return;
+    }
+  }
   const int lane = threadIdx.x, ty = threadIdx.y;
   const int R0 = tile.x - K, C0 = tile.y - K;  // global cell of local (0, 0); C0 % W == 0
   const int nx = a.nx, ny = a.ny;

@@ -107,3 +107,74 @@ def hz_traces(p: ph.TEProblem, idx, advance, hz) -> np.ndarray:
 def reflection_error(small: np.ndarray, reference: np.ndarray) -> np.ndarray:
     """max_t |Hz − Hz_ref| / max_t |Hz_ref| per probe."""
     return np.abs(small - reference).max(0) / np.abs(reference).max(0)
+
+
+BROADBAND = ph.GaussianPulse(1.35, 0.9)
+BROADBAND_WAVELENGTHS = np.linspace(0.9, 1.8, 19)
+
+
+def dispersion_problem(dl: float, n: float = 1.0, run_time: float = 200e-15, r_near: float = 1.5,
+                       r_far: float = 4.5, precision: str = "single"):
+    """V1–V3: broadband Hz point source at an Hz node in a medium of index n; Hz point monitors
+    on Hz nodes at two distances along 0° and along 45°. Returns the problem and, per angle,
+    the monitor indices and the two distances (µm)."""
+    m_axis = (round(r_near / dl), round(r_far / dl))
+    m_diag = (round(r_near / (math.sqrt(2) * dl)), round(r_far / (math.sqrt(2) * dl)))
+    points = {0.0: [(m * dl, 0.0, m * dl) for m in m_axis],
+              45.0: [(m * dl, m * dl, math.sqrt(2) * m * dl) for m in m_diag]}  # fmt: skip
+    monitors, probes = [], {}
+    for angle, pts in points.items():
+        probes[angle] = []
+        for x, y, r in pts:
+            probes[angle].append((len(monitors), r))
+            monitors.append(ph.DFTMonitor(f"{angle:g}-{len(monitors)}", list(BROADBAND_WAVELENGTHS),
+                                          center=(x, y, 0.0), components=("Hz",)))  # fmt: skip
+    size = centred_size(r_far + 1.0, dl)
+    p = ph.te_problem(size=(size, size), dl=dl, background_eps=n * n, pml=ph.PMLSpec(layers=12),
+                      sources=[ph.PointSource((0.0, 0.0, 0.0), "Hz", BROADBAND)], monitors=monitors,
+                      run_time=run_time, precision=precision)  # fmt: skip
+    return p, probes
+
+
+def yee_phase_velocity(wavelengths_um, grid, angle: float, n: float = 1.0) -> np.ndarray:
+    """ṽp / (c/n) of the 2D Yee scheme along 0° or 45° on square cells (Taflove & Hagness,
+    ch. 4), from the closed forms sin(k̃Δ/2) = Δ sin(ωΔt/2)/(vΔt) and, on the diagonal,
+    sin(k̃Δ/(2√2)) = Δ sin(ωΔt/2)/(√2 vΔt)."""
+    v = ph.C_0_SI / n
+    omega = 2.0 * np.pi * ph.C_0_SI / (np.asarray(wavelengths_um, dtype=np.float64) * ph.UM)
+    d, dt = grid.dx * ph.UM, grid.dt
+    s = d * np.sin(omega * dt / 2.0) / (v * dt)
+    k = 2.0 / d * np.arcsin(s) if angle == 0.0 else 2.0 * math.sqrt(2.0) / d * np.arcsin(s / math.sqrt(2.0))
+    return omega / (k * v)
+
+
+def measured_phase_velocity(near: np.ndarray, far: np.ndarray, r_near: float, r_far: float,
+                            n: float = 1.0) -> np.ndarray:
+    """ṽp / (c/n) from the phase of far/near (which cancels the source spectrum) matched to the
+    outgoing cylindrical wave arg H0⁽¹⁾(k̃ r_far) − arg H0⁽¹⁾(k̃ r_near); the 2π ambiguity is
+    resolved against the exact k = 2πn/λ and k̃ found by bracketed root finding."""
+    from scipy.optimize import brentq
+    from scipy.special import hankel1
+
+    def model(k: float) -> float:
+        corr = np.angle(hankel1(0, np.array([k * r_far, k * r_near])) * np.exp(-1j * np.array([k * r_far, k * r_near])))
+        return k * (r_far - r_near) + float(corr[0] - corr[1])
+
+    phase = np.angle(far / near)
+    k_exact = 2.0 * np.pi * n / BROADBAND_WAVELENGTHS
+    k_meas = np.empty_like(k_exact)
+    for q, (k0, phi) in enumerate(zip(k_exact, phase)):
+        target = phi + 2.0 * np.pi * round((model(k0) - phi) / (2.0 * np.pi))
+        k_meas[q] = brentq(lambda k, t=target: model(k) - t, 0.7 * k0, 1.3 * k0, xtol=1e-14)
+    return k_exact / k_meas
+
+
+def dispersion_velocities(p: ph.TEProblem, probes: dict, point_values, n: float = 1.0) -> dict:
+    """{angle: (cells per wavelength, measured ṽp, Yee ṽp)}; ``point_values(k)`` returns the
+    interpolated DFT of monitor k (one complex value per wavelength)."""
+    out = {}
+    for angle, ((k_near, r_near), (k_far, r_far)) in probes.items():
+        v = measured_phase_velocity(point_values(k_near), point_values(k_far), r_near, r_far, n)
+        out[angle] = (BROADBAND_WAVELENGTHS / (n * p.grid.dx), v,
+                      yee_phase_velocity(BROADBAND_WAVELENGTHS, p.grid, angle, n))  # fmt: skip
+    return out

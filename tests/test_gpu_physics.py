@@ -57,3 +57,39 @@ def test_v4_cpml_reflection_below_minus_80_db(gpu, precision):
             e.close()
     assert np.abs(traces[1]).max() > 0
     assert np.all(m0_cases.reflection_error(*traces) < 1e-4)
+
+
+def _gpu_dispersion(dl, n=1.0, precision="single"):
+    p, probes = m0_cases.dispersion_problem(dl, n=n, precision=precision)
+    e = TEEngine(p)
+    try:
+        e.advance(p.n_steps)
+        accs = [e.dft(k) for k in range(len(p.samplings))]
+    finally:
+        e.close()
+
+    def values(k):
+        return interpolate_monitor(p.samplings[k], accs[k]).reshape(-1).astype(np.complex128)
+
+    return m0_cases.dispersion_velocities(p, probes, values, n)
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_v1_v2_dispersion_and_phase_velocity(gpu, precision):
+    """V1 (ṽp within 1e-3 of the Yee relation along 0° and 45°, anisotropy visible at 9 cells
+    per wavelength) and V2 (resolved raw ṽp within 0.5 % of c), at Δ = 0.1 and 0.05 µm."""
+    pytest.importorskip("scipy.optimize")
+    cases = {dl: _gpu_dispersion(dl, precision=precision) for dl in (0.1, 0.05)}
+    for dl, by_angle in cases.items():
+        for angle, (cpw, v, v_yee) in by_angle.items():
+            assert np.abs(v / v_yee - 1).max() < 1e-3, (dl, angle)
+            assert np.all(np.abs(v[cpw >= 20] - 1) < 5e-3), (dl, angle)
+    (cpw, axis, _), (_, diagonal, _) = cases[0.1][0.0], cases[0.1][45.0]
+    coarsest = int(np.argmin(cpw))
+    assert axis[coarsest] < 0.99 and diagonal[coarsest] - axis[coarsest] > 0.01
+
+
+def test_v3_uniform_dielectric(gpu):
+    pytest.importorskip("scipy.optimize")
+    for angle, (_, v, v_yee) in _gpu_dispersion(0.05, n=1.5).items():
+        assert np.abs(v / v_yee - 1).max() < 1e-3, angle

@@ -818,9 +818,8 @@ int adj_backward(etg_adj* A) {
       rc = run_copies(A->d_copies, (int)copies.size(), k, lo, s->stream);
       begin_segment(A, lo, hi);
       if (rc == ETG_OK) {
-        if (A->tiles) {
+        if (A->tiles) {  // the simulation's stream (the sweep's) waits for the recompute
           rc = etg_batch_advance(A->fwd1, hi - lo);
-          if (rc == ETG_OK) rc = etg_batch_synchronize(A->fwd1);
         } else {
           rc = sim_advance_internal(s, hi - lo);
         }
@@ -831,6 +830,7 @@ int adj_backward(etg_adj* A) {
     clear_cone(s);
     s->monitors_on = true;
     sim_invalidate(s);
+    if (rc == ETG_OK && A->fwd1) rc = etg_batch_synchronize(A->fwd1);  // device flags of the recomputes
   }
   ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
   return rc;

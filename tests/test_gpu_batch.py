@@ -84,3 +84,28 @@ def test_batch_of_synthetic_devices_vs_live_oracle(gpu, precision):
         for k, acc in enumerate(o.acc):
             np.testing.assert_array_equal(e.dft(k), acc)
     batch.close()
+
+
+def test_config3_full_batch_equals_single_runs(gpu):
+    """The 64-device, 5000-step batch of the batched throughput line, at full size: every
+    device's fields, ψ and accumulators equal its own run bit for bit (the oracle cannot run
+    this size; the single runs are pinned to it by the parity tests)."""
+    from etalon_gb300 import autotune
+
+    problems = cases.synthetic_batch(64, n_steps=5000)
+    batch = Batch(problems)
+    try:
+        autotune.tune_batch(batch, steps=32, reps=1)
+        batch.advance(5000)
+        batch.synchronize()
+        for p, eb in zip(problems, batch.engines):
+            e = TEEngine(p)
+            e.advance(5000)
+            for f in FIELDS:
+                a, b = eb.field(f), e.field(f)
+                assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), f
+            for k in range(len(e.monitors)):
+                assert np.array_equal(eb.dft(k).view(np.uint8), e.dft(k).view(np.uint8))
+            e.close()
+    finally:
+        batch.close()

@@ -50,9 +50,14 @@ int etg_sim_rasterize_cb(etg_sim* s, double x_min, double y_min, double dx, doub
   if (n_boxes) {
     int rc = etg_malloc((void**)&dev, n_boxes * sizeof(RasterBox));
     if (rc) return rc;
-    ETG_TRY_CUDA(cudaMemcpy(dev, host.data(), n_boxes * sizeof(RasterBox), cudaMemcpyHostToDevice));
   }
-  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));  // nothing still reads cb
+  cudaError_t e = n_boxes ? cudaMemcpy(dev, host.data(), n_boxes * sizeof(RasterBox), cudaMemcpyHostToDevice)
+                          : cudaSuccess;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);  // nothing still reads cb
+  if (e != cudaSuccess) {
+    cudaFree(dev);
+    ETG_REQUIRE(false, ETG_ERR_CUDA, "etg_sim_rasterize_cb: %s", cudaGetErrorString(e));
+  }
   const dim3 block(256);
   // Ex nodes: (nx, ny+1), half-cell in x; Ey nodes: (nx+1, ny), half-cell in y
   const int shapes[2][2] = {{s->nx, s->ny + 1}, {s->nx + 1, s->ny}};
@@ -67,7 +72,7 @@ int etg_sim_rasterize_cb(etg_sim* s, double x_min, double y_min, double dx, doub
                                                          (double*)s->cb[c]);
     g_launches += 1;
   }
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   cudaFree(dev);
   ETG_REQUIRE(e == cudaSuccess, ETG_ERR_CUDA, "etg_sim_rasterize_cb: %s", cudaGetErrorString(e));

@@ -237,7 +237,14 @@ def run_ours(args, world, rank, local) -> None:
     _lib.call("etg_set_device", local)
     p = workload(args.precision, args.time_steps)
     e = TEEngine(p, kernel="auto" if args.kernel == "tuned" else args.kernel)
-    choice = list(autotune.tune(e)) if args.kernel == "tuned" else [args.kernel]
+    if args.kernel == "tuned":
+        choice = list(autotune.tune(e))
+    else:
+        if args.tile_rows:
+            e.set_option(_lib.OPT_TILE_ROWS, args.tile_rows)
+        if args.warps:
+            e.set_option(_lib.OPT_TB_WARPS, args.warps)
+        choice = [args.kernel, args.tile_rows, args.warps]
     e.set_option(_lib.OPT_TIMING, 1)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -364,7 +371,8 @@ def kernel_roofline(e, p) -> dict:
 
     peak, peak_kind = hbm_peak()
     s = np.dtype(p.real).itemsize
-    kind, rows, depth = (get_option(e, o) for o in (_lib.OPT_KERNEL, _lib.OPT_TILE_ROWS, _lib.OPT_TB_DEPTH))
+    kind, rows, depth, warps = (get_option(e, o) for o in (_lib.OPT_KERNEL, _lib.OPT_TILE_ROWS, _lib.OPT_TB_DEPTH,
+                                                          _lib.OPT_TB_WARPS))
     e.set_option(_lib.OPT_TIMING, 2)
     e.reset()
     e.advance(p.n_steps)
@@ -374,7 +382,7 @@ def kernel_roofline(e, p) -> dict:
     ms, launches, cells = kt["interior"]
     if launches:
         dt = "float" if s == 4 else "double"
-        name = f"k_tb_step<{dt},{rows // 8},{depth},false>"
+        name = f"k_tb_step<{dt},{rows // warps},{depth},false,{warps}>"
         launch_ms = ms / launches
         bytes_launch = 8 * s * cells * depth
         cp_ms, cp_launches, cp_cells = kt["cpml"]
@@ -382,7 +390,7 @@ def kernel_roofline(e, p) -> dict:
                  "output_cells_per_launch": cells, "launch_ms": launch_ms, "launches_timed": launches,
                  "cpml_kernel": {"launch_ms": cp_ms / max(cp_launches, 1), "output_cells_per_launch": cp_cells},
                  "timing": "CUDA events around each launch, one extra run of the workload, kernels serialised"}
-        tag = f"k_tb_step_interior_{rows}x{128 if s == 4 else 64}"
+        tag = f"k_tb_step_interior_{rows}x{128 if s == 4 else 64}" + ("" if warps == 8 else f"_{warps}w")
     elif kind in (3, 4):  # persistent kernels: the run's device time over its launches
         e.reset()
         e.advance(p.n_steps)
@@ -724,7 +732,10 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="single", choices=["single", "double"])
     ap.add_argument("--time-steps", type=int, default=10000)
-    ap.add_argument("--kernel", default="auto", choices=["auto", "tuned", "plain", "tb", "pipe"])
+    ap.add_argument("--kernel", default="tuned", choices=["auto", "tuned", "plain", "tb", "pipe"],
+                    help="tuned: the autotuner picks kernel, tile rows, depth and warps (before timing)")
+    ap.add_argument("--tile-rows", type=int, default=0, help="with a fixed --kernel: tile rows (0: its default)")
+    ap.add_argument("--warps", type=int, default=0, help="with a fixed --kernel: warps per tile (0: 8)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-device batched line")

@@ -1155,7 +1155,9 @@ struct TBConfig {
   int dtype, RPT, K, NW;  // tile rows NW * RPT, columns 32 * W (128 for f32, 64 for f64), depth K, NW warps
 };
 
-static constexpr TBConfig kDefault32 = {ETG_F32, 6, 4, 8};
+// 40 x 128 tiles of 8 warps of 5 rows: 128 registers, two CTAs per SM, so one CTA's tile load
+// overlaps the other's steps (9 % shorter launches than 48 x 128 tiles at one CTA per SM)
+static constexpr TBConfig kDefault32 = {ETG_F32, 5, 4, 8};
 static constexpr TBConfig kDefault64 = {ETG_F64, 5, 2, 8};
 static constexpr TBConfig kTmaDefault32 = {ETG_F32, 5, 4, 8};
 static constexpr TBConfig kTmaDefault64 = {ETG_F64, 5, 2, 8};
@@ -1588,15 +1590,21 @@ static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt, cons
   TBConfig want = mode == 1 ? (dt == 4 ? kTmaDefault32 : kTmaDefault64) : (dt == 4 ? kDefault32 : kDefault64);
   if (opt[ETG_OPT_TB_DEPTH] > 0) want.K = (int)opt[ETG_OPT_TB_DEPTH];
   if (opt[ETG_OPT_TB_WARPS] > 0 && opt[ETG_OPT_TB_WARPS] != want.NW) {  // same rows, other split
-    want.RPT = want.RPT * want.NW / (int)opt[ETG_OPT_TB_WARPS];
-    want.NW = (int)opt[ETG_OPT_TB_WARPS];
+    const int rows = want.RPT * want.NW, nw = (int)opt[ETG_OPT_TB_WARPS];
+    if (opt[ETG_OPT_TILE_ROWS] == 0 && rows % nw != 0) {
+      set_error("the default tile of %d rows does not split over %d warps: set ETG_OPT_TILE_ROWS too (have:%s)",
+                rows, nw, shapes_text(dt, mode).c_str());
+      return ETG_ERR_ARGUMENT;
+    }
+    want.RPT = rows / nw;
+    want.NW = nw;
   }
   if (opt[ETG_OPT_TILE_ROWS] > 0) want.RPT = (int)(opt[ETG_OPT_TILE_ROWS] / want.NW);
   const bool cols_ok = opt[ETG_OPT_TILE_COLS] == 0 || opt[ETG_OPT_TILE_COLS] == EC;
   if (!cols_ok || opt[ETG_OPT_TILE_ROWS] % want.NW != 0 || !pick<T>(want, mode).two) {
     set_error("no compiled %s kernel with tile %lldx%lld and depth %d (have:%s)",
               mode == 1 ? "persistent TMA" : mode == 2 ? "persistent pipelined" : "temporally blocked",
-              (long long)(opt[ETG_OPT_TILE_ROWS] ? opt[ETG_OPT_TILE_ROWS] : 8 * want.RPT),
+              (long long)(opt[ETG_OPT_TILE_ROWS] ? opt[ETG_OPT_TILE_ROWS] : want.NW * want.RPT),
               (long long)(opt[ETG_OPT_TILE_COLS] ? opt[ETG_OPT_TILE_COLS] : EC), want.K,
               shapes_text(dt, mode).c_str());
     return ETG_ERR_ARGUMENT;

@@ -561,6 +561,7 @@ def test_sixteen_warp_tiles_on_headline_grid(gpu, precision):
     n = 40
     p = cases.config2(precision, n_steps=n)
     e = TEEngine(p, kernel="tb", graph_steps=16)
+    e.set_option(_lib.OPT_TILE_ROWS, 48)
     e.set_option(_lib.OPT_TB_WARPS, 16)
     for k in (3, 8, 29):
         e.advance(k)
@@ -579,6 +580,7 @@ def test_sixteen_warp_batch_matches_single_runs(gpu):
 
     problems = [cases.synthetic_device(s, "single", n_steps=90, min_cells=60, max_cells=400) for s in range(4)]
     batch = Batch(problems)
+    batch.set_option(_lib.OPT_TILE_ROWS, 48)
     batch.set_option(_lib.OPT_TB_WARPS, 16)
     batch.advance(90)
     batch.synchronize()

@@ -478,14 +478,14 @@ __device__ __forceinline__ void adj_dispatch(const TBAdjArgs<T>& a, int r0, int 
 }
 
 template <typename T, int RPT, int K, bool PML>
-__global__ void __launch_bounds__(TB_THREADS, 1)
+__global__ void __launch_bounds__(TB_THREADS, PML ? 1 : 2)
 k_tb_adj(const __grid_constant__ TBAdjArgs<T> a, const int2* __restrict__ tiles, int step_off) {
   const int2 t = tiles[blockIdx.x];
   adj_dispatch<T, RPT, K, PML>(a, t.x & ((1 << AKIND_SHIFT) - 1), t.y, t.x >> AKIND_SHIFT, step_off);
 }
 
 template <typename T, int RPT, int K, bool PML>
-__global__ void __launch_bounds__(TB_THREADS, 1)
+__global__ void __launch_bounds__(TB_THREADS, PML ? 1 : 2)
 k_tb_adj_batch(const TBAdjArgs<T>* __restrict__ args, const int4* __restrict__ tiles, int parity, int step_off) {
   const int4 t = tiles[blockIdx.x];  // simulation, r0, c0, kind
   adj_dispatch<T, RPT, K, PML>(args[2 * t.x + parity], t.y, t.z, t.w, step_off);
@@ -562,7 +562,7 @@ template <typename T>
 struct AdjCfg;
 template <>
 struct AdjCfg<float> {
-  static constexpr int RPT = 6, K = 4;
+  static constexpr int RPT = 5, K = 4;
 };
 template <>
 struct AdjCfg<double> {

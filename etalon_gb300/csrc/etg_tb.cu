@@ -1158,7 +1158,9 @@ struct TBConfig {
 // 40 x 128 tiles of 8 warps of 5 rows: 128 registers, two CTAs per SM, so one CTA's tile load
 // overlaps the other's steps (9 % shorter launches than 48 x 128 tiles at one CTA per SM)
 static constexpr TBConfig kDefault32 = {ETG_F32, 5, 4, 8};
-static constexpr TBConfig kDefault64 = {ETG_F64, 5, 2, 8};
+// float64: 32 x 64 tiles (8 warps of 4 rows, two CTAs per SM) spill less under the 128-register
+// cap than 40-row tiles and measured 4 % faster at 2024² (the FP64 pipe binds either way)
+static constexpr TBConfig kDefault64 = {ETG_F64, 4, 2, 8};
 static constexpr TBConfig kTmaDefault32 = {ETG_F32, 5, 4, 8};
 static constexpr TBConfig kTmaDefault64 = {ETG_F64, 5, 2, 8};
 

@@ -22,7 +22,7 @@ from etalon_gb300 import _lib
 from etalon_gb300 import physics as ph
 from etalon_gb300.engine import TEEngine
 from tests import cases
-from tests.golden_io import COEFFS, FIELDS, GOLDEN, compare_outputs, count, load, oracle_from_golden, sha
+from tests.golden_io import COEFFS, FIELDS, GOLDEN, compare_outputs, count, load, sha
 
 pytestmark = pytest.mark.gpu
 PRECISIONS = ["single", "double"]

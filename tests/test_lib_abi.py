@@ -62,3 +62,28 @@ def test_injected_fault_is_reported(monkeypatch):
     with pytest.raises(_lib.EtgError, match="fault injected") as err:
         _lib.call("etg_sim_create", C.byref(C.c_void_p()), 4, 10, 10)
     assert err.value.code == _lib.ERR_INJECTED
+
+
+@pytest.mark.parametrize(
+    "name,args,words",
+    [
+        ("etg_sum_sq", (3, 4, 4, 4, 1, None, "OUT"), "dtype"),      # dtype must be 4 or 8
+        ("etg_sum_sq", (4, 4, 4, 4, None, None, None), "bad arguments"),
+        ("etg_block_mean", (4, 8, 8, 8, 1, 0, 2, 4, 1), "bad arguments"),  # block of 0 rows
+        ("etg_block_mean", (4, 8, 8, 8, 1, 2, 2, 2, 1), "dtypes"),
+        ("etg_cast", (4, 2, 8, 1, 1), "dtypes"),
+        ("etg_sim_rasterize_cb", (None, 0.0, 0.0, 0.02, 0.02, 1e-16, 8.85e-12, 1.0, 0, None), "bad arguments"),
+        ("etg_sim_get_cb", (None, 0, None), "bad arguments"),
+        ("etg_sim_set_cb_window", (None, 0, 0, 1, 0, 1, None), "bad arguments"),
+    ],
+)  # fmt: skip
+def test_entry_points_reject_bad_arguments_before_touching_the_gpu(name, args, words):
+    """Argument checks come first, so they hold (ValueError with the reason) on any machine."""
+    import ctypes as C
+
+    from etalon_gb300 import _lib
+
+    out = C.c_double()
+    args = tuple(C.byref(out) if a == "OUT" else a for a in args)
+    with pytest.raises(ValueError, match=words):
+        _lib.call(name, *args)

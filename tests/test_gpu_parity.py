@@ -320,15 +320,24 @@ def test_config2_full_length_matches_reference(gpu, precision):
     g = load("config2", precision)
     n = int(g["n_steps"])
     p = cases.config2(precision, n_steps=n)
-    if not _config2_fixture_usable(g, p):
-        pytest.skip("this platform's float64 libm gives other host tables than the fixture's; "
-                    "parity at this size is then pinned by test_config2_prefix_vs_live_oracle")
+    replay = not _config2_fixture_usable(g, p)
+    if replay and "src0_table" not in g:
+        pytest.skip("this platform's float64 libm gives other host tables than the fixture's, which "
+                    "holds only their hashes; parity at this size is then pinned by "
+                    "test_config2_prefix_vs_live_oracle")
     c = ph.cast_coefficients(p)
     assert sha(c.cb_ex) == str(g["in_cb_ex_sha"]) and sha(c.cb_ey) == str(g["in_cb_ey_sha"])
     for k in COEFFS[2:]:
         setattr(c, k, g[f"in_{k}"])
     e = TEEngine(p)
     e.set_coefficients(c)
+    if replay:  # feed Etalon's own per-step deltas and phasor rows (this host's libm differs)
+        for k in range(len(e.sources)):
+            assert sha(g[f"src{k}_table"]) == str(g[f"src{k}_table_sha"])
+            e.set_source_table(k, 0, g[f"src{k}_table"])
+        for k in range(len(e.monitors)):
+            assert sha(g[f"mon{k}_table"]) == str(g[f"mon{k}_table_sha"])
+            e.set_phasor_table(k, 0, g[f"mon{k}_table"])
     e.advance(n)
     e.synchronize()
     assert compare_outputs(g, *engine_outputs(e)) == []

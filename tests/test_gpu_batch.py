@@ -109,3 +109,30 @@ def test_config3_full_batch_equals_single_runs(gpu):
             e.close()
     finally:
         batch.close()
+
+
+def test_config3_every_device_vs_live_oracle(gpu):
+    """All 64 devices of the batched workload (bends, rings, MMIs, 256²–1536²), 120 steps as
+    one batch, each bit-identical to the oracle run on the host's cores."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+
+    from tests.test_gpu_parity import _oracle_for
+
+    n = 120
+    problems = cases.synthetic_batch(64, n_steps=n)
+    batch = Batch(problems)
+    try:
+        batch.advance(n)
+        batch.synchronize()
+        workers = min(16, os.cpu_count() or 1)
+        with ThreadPoolExecutor(workers) as pool:
+            for p, e in zip(problems, batch.engines):
+                o = _oracle_for(p)
+                o.run(n, pool=pool, bands=workers)
+                for f in FIELDS:
+                    assert np.array_equal(e.field(f).view(np.uint8), getattr(o, f).view(np.uint8)), f
+                for k, acc in enumerate(o.acc):
+                    assert np.array_equal(e.dft(k).view(np.uint8), acc.view(np.uint8))
+    finally:
+        batch.close()

@@ -70,3 +70,35 @@ def test_every_candidate_names_a_known_kernel():
         for kernel, rows, depth, warps in cands:
             assert kernel in ("tb", "tma", "pipe", "plain") and warps in (8, 16)
             assert kernel == "plain" or depth == (4 if precision == "single" else 2)
+
+
+class FakeBatch:
+    """A batch of fake engines whose 'time' depends on (rows, depth, warps)."""
+
+    def __init__(self, times, fail=()):
+        self.engines = [FakeEngine("single", {})]
+        self.times, self.fail = times, set(fail)
+        self.opts, self.resets = {}, 0
+
+    def set_option(self, option, value):
+        self.opts[option] = value
+
+    def reset(self):
+        self.resets += 1
+
+    def advance(self, steps):
+        cand = (self.opts[_lib.OPT_TILE_ROWS], self.opts[_lib.OPT_TB_DEPTH], self.opts[_lib.OPT_TB_WARPS])
+        if cand in self.fail:
+            raise _lib.EtgError(1, "no compiled batched kernel")
+        self.last = self.times.get(cand, 50.0)
+
+    def last_timing(self):
+        return self.last, 1
+
+
+def test_batch_tuner_applies_the_fastest_shape_and_skips_missing_ones():
+    b = FakeBatch({(40, 4, 8): 3.0, (48, 4, 16): 2.5}, fail={(48, 4, 16)})
+    choice = autotune.tune_batch(b, steps=8, reps=1)
+    assert choice == (40, 4, 8)
+    assert (b.opts[_lib.OPT_TILE_ROWS], b.opts[_lib.OPT_TB_DEPTH], b.opts[_lib.OPT_TB_WARPS]) == (40, 4, 8)
+    assert b.resets >= len(autotune.BATCH_CANDIDATES["single"])  # left at step 0

@@ -803,7 +803,7 @@ int adj_backward(etg_adj* A) {
     if (A->tiles && !A->fwd1) {
       rc = etg_batch_create(&A->fwd1, 1, &s);
       // the light cone is a few dozen tiles, one wave on a fraction of the SMs: there a tile's
-      // latency sets the time, and 16 warps of 3 rows hide it better than 8 of 6 (float32)
+      // latency sets the time, and 16 warps of 3 rows hide it better than 8 warps (float32)
       if (rc == ETG_OK && s->dtype == ETG_F32 && s->opt[ETG_OPT_TB_WARPS] == 0 && s->opt[ETG_OPT_TILE_ROWS] == 0) {
         etg_batch_set_option(A->fwd1, ETG_OPT_TILE_ROWS, 48);
         etg_batch_set_option(A->fwd1, ETG_OPT_TB_WARPS, 16);

@@ -52,4 +52,4 @@ def test_torch_gradient_matches_central_differences():
             with torch.no_grad():
                 vals.append(float((te.run(x, cby)[1][2] ** 2).sum()))
         fd = (vals[0] - vals[1]) / (2 * h)
-        assert float(cbx.grad[i, k]) == pytest.approx(fd, rel=1e-5, abs=1e-12 * abs(float(j)) / abs(h))
+        assert float(cbx.grad[i, k]) == pytest.approx(fd, rel=1e-5, abs=1e-12 * abs(float(j.detach())) / abs(h))

@@ -136,7 +136,11 @@ int advance_static(int nx, int ny, int64_t pitch, void* const f[7], const void* 
   int rc = scratch_address((void**)&base);
   if (rc) return rc;
   const cudaStream_t s = 0;  // the default stream: calls return when their work is done
-  ETG_TRY_CUDA(cudaMemsetAsync(base + counters, 0, 256, s));  // step counter and error flag
+  // The seven planes of the second buffer, the step counter and the error flag start at zero,
+  // as the allocating engine's second buffer does: corner tiles read psi over their whole
+  // extended tile, so halo cells that no launch writes must not keep an earlier call's bytes
+  // (another grid, pitch or precision).
+  ETG_TRY_CUDA(cudaMemsetAsync(base, 0, counters + 256, s));
   ETG_TRY_CUDA(cudaMemcpyAsync(base + tiles_at, tiles.data(), tiles.size() * sizeof(int2),
                                cudaMemcpyHostToDevice, s));
 
@@ -162,16 +166,23 @@ int advance_static(int nx, int ny, int64_t pitch, void* const f[7], const void* 
   for (int k = 0; k < 7; ++k) *bp[k] = (T*)(base + k * plane);
   const int2* d_tiles = (const int2*)(base + tiles_at);
 
+  // Launch offsets are relative to the device step counter and fit an int: the counter is
+  // advanced every kPairsPerAdd pairs, so any 64-bit step count is covered.
+  constexpr int64_t kPairsPerAdd = 1 << 20;
   const int64_t pairs = n_steps / (2 * K);
-  for (int64_t p = 0; p < pairs; ++p) {
-    ETG_TRY_CUDA(tb_default_launch<T>(a, b, d_tiles, n_inner, n_pml, (int)(2 * K * p), s));
-    ETG_TRY_CUDA(tb_default_launch<T>(b, a, d_tiles, n_inner, n_pml, (int)(2 * K * p + K), s));
+  for (int64_t p0 = 0; p0 < pairs; p0 += kPairsPerAdd) {
+    const int64_t np = std::min(kPairsPerAdd, pairs - p0);
+    for (int64_t p = 0; p < np; ++p) {
+      ETG_TRY_CUDA(tb_default_launch<T>(a, b, d_tiles, n_inner, n_pml, (int)(2 * K * p), s));
+      ETG_TRY_CUDA(tb_default_launch<T>(b, a, d_tiles, n_inner, n_pml, (int)(2 * K * p + K), s));
+    }
+    launch_step_add<T>(a, 2 * K * np, s);
   }
-  if (pairs) launch_step_add<T>(a, 2 * K * pairs, s);
   PhasePlan<T> none;
   memset(&none, 0, sizeof none);
   const int64_t rem = n_steps - 2 * K * pairs;
   for (int64_t k = 0; k < rem; ++k) launch_step_plain<T>(a, none, none, (int)k, s);
+  if (rem) launch_step_add<T>(a, rem, s);
   ETG_LAUNCH_CHECK();
   ETG_TRY_CUDA(cudaStreamSynchronize(s));
   int flag = 0;

@@ -60,50 +60,84 @@ def _problem(precision):
     return p
 
 
+def _other_problem(precision):
+    """A larger vacuum grid (300 x 260 cells, 12-layer CPML): its scratch planes cover every
+    byte the 184² grid's planes use, at another pitch."""
+    return ph.te_problem(size=(13.8, 11.8), dl=0.05, sources=[], pml=ph.PMLSpec(layers=12),
+                         precision=precision)  # fmt: skip
+
+
+class StaticRun:
+    """One grid stepped twice: by the resident engine and by etg_tb_advance_static on
+    device arrays the test allocates and owns."""
+
+    SHAPES = lambda nx, ny: {"ex": (nx, ny + 1), "ey": (nx + 1, ny), "hz": (nx, ny),  # noqa: E731
+                             "psi_ex_y": (nx, ny + 1), "psi_ey_x": (nx + 1, ny),
+                             "psi_hz_x": (nx, ny), "psi_hz_y": (nx, ny)}  # fmt: skip
+
+    def __init__(self, p, seed):
+        self.p = p
+        nx, ny, real = p.grid.nx, p.grid.ny, p.real
+        shapes = StaticRun.SHAPES(nx, ny)
+        rng = np.random.default_rng(seed)
+        start = {f: np.zeros(shapes[f], real) for f in FIELDS}  # psi starts at +0
+        for f in ("ex", "ey", "hz"):
+            start[f][...] = rng.standard_normal(shapes[f])
+        start["hz"] *= 1 / 377.0
+        self.engine = TEEngine(p, kernel="tb")
+        for f in ("ex", "ey", "hz"):
+            self.engine.set_field(f, start[f])
+        self.buf = Pitched(nx, ny, real)
+        c = ph.cast_coefficients(p)
+        self.c = c
+        self.fields = {f: self.buf.alloc(start[f]) for f in FIELDS}
+        self.cb_ex, self.cb_ey = self.buf.alloc(c.cb_ex), self.buf.alloc(c.cb_ey)
+        self.coef = {}
+        for k in COEFFS:
+            a = np.ascontiguousarray(getattr(c, k))
+            q = C.c_void_p()
+            _lib.call("etg_malloc", C.byref(q), a.nbytes)
+            _lib.call("etg_memcpy_h2d", q.value, a.ctypes.data, a.nbytes)
+            self.coef[k] = q.value
+            self.buf.ptrs.append(q.value)
+
+    def step_and_check(self, steps):
+        nx, ny, c = self.p.grid.nx, self.p.grid.ny, self.c
+        self.engine.advance(steps)
+        self.engine.synchronize()
+        _lib.call("etg_tb_advance_static", _lib.dtype_code(self.p.real), nx, ny, self.buf.pitch,
+                  *[self.fields[f] for f in FIELDS], self.cb_ex, self.cb_ey,
+                  *[self.coef[k] for k in COEFFS], float(c.db), float(c.inv_dx), float(c.inv_dy),
+                  steps)  # fmt: skip
+        for f in FIELDS:
+            want = self.engine.field(f)
+            got = self.buf.read(self.fields[f], want.shape)
+            # raw bits, so that the sign of a zero counts too
+            assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), (
+                f"{f} differs from the engine after {steps} more steps ({nx} x {ny}, {self.p.precision})")
+        assert np.abs(self.engine.field("hz")).max() > 0
+
+    def close(self):
+        self.buf.free()
+        self.engine.close()
+
+
 @pytest.mark.parametrize("precision", ["single", "double"])
 def test_static_advance_matches_engine_on_two_calls(gpu, precision):
-    p = _problem(precision)
-    nx, ny, real = p.grid.nx, p.grid.ny, p.real
-    rng = np.random.default_rng(7)
-    shapes = {"ex": (nx, ny + 1), "ey": (nx + 1, ny), "hz": (nx, ny), "psi_ex_y": (nx, ny + 1),
-              "psi_ey_x": (nx + 1, ny), "psi_hz_x": (nx, ny), "psi_hz_y": (nx, ny)}  # fmt: skip
-    start = {f: np.zeros(shapes[f], real) for f in FIELDS}  # psi starts at +0
-    for f in ("ex", "ey", "hz"):
-        start[f][...] = rng.standard_normal(shapes[f])
-    start["hz"] *= 1 / 377.0
-
-    engine = TEEngine(p, kernel="tb")
-    for f in ("ex", "ey", "hz"):
-        engine.set_field(f, start[f])
-
-    buf = Pitched(nx, ny, real)
-    c = ph.cast_coefficients(p)
-    fields = {f: buf.alloc(start[f]) for f in FIELDS}
-    cb_ex, cb_ey = buf.alloc(c.cb_ex), buf.alloc(c.cb_ey)
-    coef = {}
-    for k in COEFFS:
-        a = np.ascontiguousarray(getattr(c, k))
-        q = C.c_void_p()
-        _lib.call("etg_malloc", C.byref(q), a.nbytes)
-        _lib.call("etg_memcpy_h2d", q.value, a.ctypes.data, a.nbytes)
-        coef[k] = q.value
-        buf.ptrs.append(q.value)
-    code = _lib.dtype_code(real)
+    """Two calls on the 184² grid, with a call on a larger grid of the other precision (live
+    psi in its strips, another pitch) in between: whatever that call leaves in the shared
+    scratch must not reach the second result."""
+    main = StaticRun(_problem(precision), seed=7)
+    other = StaticRun(_other_problem("double" if precision == "single" else "single"), seed=11)
     try:
-        for steps in (21, 30):  # two calls in a row: TB pairs plus a one-step remainder each
-            engine.advance(steps)
-            engine.synchronize()
-            _lib.call("etg_tb_advance_static", code, nx, ny, buf.pitch,
-                      *[fields[f] for f in FIELDS], cb_ex, cb_ey, *[coef[k] for k in COEFFS],
-                      float(c.db), float(c.inv_dx), float(c.inv_dy), steps)  # fmt: skip
-            for f in FIELDS:
-                want = engine.field(f)
-                got = buf.read(fields[f], want.shape)
-                np.testing.assert_array_equal(got, want, err_msg=f"{f} after {steps} more steps")
-            assert np.abs(engine.field("hz")).max() > 0
+        main.step_and_check(21)  # TB pairs plus a one-step remainder
+        other.step_and_check(40)
+        assert np.abs(other.engine.field("psi_hz_x")).max() > 0  # the strips hold live psi
+        main.step_and_check(30)
+        main.step_and_check(16)  # whole pairs only
     finally:
-        buf.free()
-        engine.close()
+        main.close()
+        other.close()
 
 
 def test_static_advance_rejects_grids_beyond_its_scratch(gpu):

@@ -249,11 +249,26 @@ def simulate(eps_cells: torch.Tensor, runner: AdjointRunner) -> tuple[torch.Tens
     return _Simulate.apply(eps_ex, eps_ey, runner)
 
 
+def point_value(acc: torch.Tensor, sampling: ComponentSampling) -> tuple[torch.Tensor, torch.Tensor]:
+    """The monitor value F as (real, imaginary) float64 tensors of shape (n_f, raw axes...).
+
+    ``acc`` is an accumulator as ``simulate`` returns it, (n_f, nodes, 2). The nodes are
+    contracted with the bilinear weights of each interpolated axis, x first and then y, as
+    etalon/io/result.py:60-79 does in float64; an interpolated axis holds at most two nodes,
+    so every sum has at most two terms and F equals Etalon's value bit for bit."""
+    n_f = sampling.wavelengths.size
+    shape = (n_f, sampling.x.index.size, sampling.y.index.size)
+    re, im = acc[..., 0].reshape(shape), acc[..., 1].reshape(shape)
+    if sampling.x.weights is not None:
+        wx = torch.as_tensor(sampling.x.weights, dtype=torch.float64)
+        re, im = torch.einsum("fab,a->fb", re, wx), torch.einsum("fab,a->fb", im, wx)
+    if sampling.y.weights is not None:
+        wy = torch.as_tensor(sampling.y.weights, dtype=torch.float64)
+        re, im = re @ wy, im @ wy
+    return re, im
+
+
 def point_power(acc: torch.Tensor, sampling: ComponentSampling) -> torch.Tensor:
-    """Σ_f |F(f)|² of a point monitor, F the bilinear interpolation of its nodes (io/result.py:54-91)."""
-    wx = torch.as_tensor(sampling.x.weights if sampling.x.weights is not None else np.ones(sampling.x.index.size))
-    wy = torch.as_tensor(sampling.y.weights if sampling.y.weights is not None else np.ones(sampling.y.index.size))
-    w = (wx[:, None] * wy[None, :]).reshape(-1)
-    re = (acc[..., 0] * w[None, :]).sum(-1)
-    im = (acc[..., 1] * w[None, :]).sum(-1)
+    """Σ_f |F(f)|² of a monitor component, F its interpolated value (``point_value``)."""
+    re, im = point_value(acc, sampling)
     return (re**2 + im**2).sum()

@@ -134,39 +134,52 @@ def gpu_available() -> bool:
         return False
 
 
+def select_backend(name: str, precision: str, numpy_backend):
+    """Etalon's backend selection (etalon/fdtd/backends/__init__.py:16-43) with "cuda" meaning
+    this backend: "numpy" → ``numpy_backend()``; "cuda" → ``Gb300Backend`` or a RuntimeError
+    (never a silent fallback); "auto" → ``Gb300Backend`` when a GPU is usable, else NumPy, with
+    a warning when a device is present but the backend fails to start."""
+    import warnings
+
+    from .backend import Gb300Backend
+
+    if name == "numpy":
+        return numpy_backend()
+    if name == "cuda":
+        return Gb300Backend(precision)
+    if name == "auto":
+        if not gpu_available():
+            return numpy_backend()
+        try:
+            return Gb300Backend(precision)
+        except RuntimeError as error:
+            warnings.warn(f"{error}\nFalling back to the NumPy backend.", stacklevel=3)
+            return numpy_backend()
+    raise ValueError(f"unknown backend {name!r}; use 'auto', 'numpy' or 'cuda'")
+
+
+def uses_gpu(backend_name: str) -> bool:
+    """Whether ``Simulation.run`` goes to the fused engine for this ``Simulation.backend``."""
+    return backend_name == "cuda" or (backend_name == "auto" and gpu_available())
+
+
 def install() -> None:
     """Route Etalon's "cuda" backend (and "auto" on a GPU machine) to this backend.
 
     Explicit "cuda" without a usable GPU raises (never a silent fallback); "auto" falls
     back to NumPy with a warning, as etalon/fdtd/backends/__init__.py:16-43 does.
     """
-    import warnings
-
     import etalon.fdtd.backends as backends
     import etalon.fdtd.solver as solver_module
     from etalon.fdtd.backends.numpy_backend import NumpyBackend
 
-    from .backend import Gb300Backend
-
     def get_backend(name: str, precision: str):
-        if name == "numpy":
-            return NumpyBackend()
-        if name == "cuda":
-            return Gb300Backend(precision)
-        if name == "auto":
-            if not gpu_available():
-                return NumpyBackend()
-            try:
-                return Gb300Backend(precision)
-            except RuntimeError as error:
-                warnings.warn(f"{error}\nFalling back to the NumPy backend.", stacklevel=3)
-                return NumpyBackend()
-        raise ValueError(f"unknown backend {name!r}; use 'auto', 'numpy' or 'cuda'")
+        return select_backend(name, precision, NumpyBackend)
 
     plain_run = solver_module.run
 
     def run(sim):
-        if sim.backend == "cuda" or (sim.backend == "auto" and gpu_available()):
+        if uses_gpu(sim.backend):
             return GB300FDTDSolver(sim).run()
         return plain_run(sim)
 

@@ -1,11 +1,14 @@
 """Generate golden vectors by running Etalon's own NumPy reference (not the oracle).
 
-Run in a checkout where Etalon's source tree is available (default /root/reference):
+Run where Etalon's source tree is available, naming it with ``--ref`` or ``ETALON_SRC``:
 
-    python tests/golden/make_golden.py [--cases config1,g4_full,...] [--ref PATH]
+    python tests/golden/make_golden.py --ref PATH [--cases config1,g4_full,...]
+    python tests/golden/make_golden.py --ref PATH --augment config2   # monitor values only
 
 Etalon's ``io/result.py`` imports xarray at module level; xarray is only needed to
-label results, so a stub module stands in for it. Each case is built through Etalon's
+label results, so a stub module stands in for it. Its ``DataArray`` keeps the data and
+dimension names it is given, so the fixtures also record the monitor values Etalon's own
+``monitor_dataarray`` (io/result.py:54-91) reports for each accumulator. Each case is built through Etalon's
 public API (``etalon.Simulation`` …) with the same parameters as tests/cases.py and is
 stepped by ``etalon.fdtd.solver.FDTDSolver`` on ``NumpyBackend``. Per case and precision
 the fixture holds:
@@ -15,8 +18,9 @@ the fixture holds:
 * the host values the solver consumed — per-step source deltas and phasor rows, already
   cast — so the GPU path can be fed Etalon's exact inputs on any platform (config2 keeps
   only their hashes in float32, 10 000 steps, and the tables themselves in float64);
-* outputs after the run — SHA-256, sum and max|.| of the seven field/ψ arrays, and the
-  DFT accumulators in full.
+* outputs after the run — SHA-256, sum and max|.| of the seven field/ψ arrays, the
+  DFT accumulators in full, and the interpolated monitor values ``monitor_dataarray``
+  returns for them (with their dimension names).
 
 Kernel-level cases (Etalon tests/gpu/test_cupy_equality.py:36-110, seeds 1 and 2) store
 input and output hashes of one ``update_h_te`` / ``update_e_te`` / ``accumulate_dft`` call.
@@ -44,14 +48,42 @@ def sha(a) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
+class RecordedDataArray:
+    """Stands in for ``xarray.DataArray``: keeps the data and dimension names."""
+
+    def __init__(self, data, dims=(), coords=None, name=None, attrs=None):
+        self.data = np.asarray(data)
+        self.dims = tuple(dims)
+        self.coords, self.name, self.attrs = coords, name, attrs
+
+
 def import_etalon(ref: str):
     sys.path.insert(0, ref)
     stub = types.ModuleType("xarray")
-    stub.DataArray = object
+    stub.DataArray = RecordedDataArray
     sys.modules.setdefault("xarray", stub)
     import etalon
 
     return etalon
+
+
+def monitor_values(solver, accs) -> dict:
+    """Etalon's own interpolated monitor values (io/result.py:54-91) for the given accumulators."""
+    from etalon.io.result import monitor_dataarray
+
+    out = {}
+    for k, (mon, acc) in enumerate(zip(solver.monitors, accs)):
+        s = mon.sampling
+        da = monitor_dataarray(s, np.asarray(acc), solver.grid.z)
+        v = np.asarray(da.data)
+        out[f"out_value{k}_sha"] = np.array(sha(v))
+        out[f"out_value{k}_dims"] = np.array(",".join(da.dims))
+        if v.size <= 4096:
+            out[f"out_value{k}"] = v
+        for axis, a in (("x", s.x), ("y", s.y)):
+            if a.weights is not None:
+                out[f"mon{k}_{axis}w"] = a.weights
+    return out
 
 
 def reference_sims(et, precision):
@@ -209,6 +241,7 @@ def run_case(et, name, precision, steps_override=None):
             out[f"out_acc{k}"] = acc
         else:  # large plane monitors: hash plus a strided sample
             out[f"out_acc{k}_sample"] = acc.ravel()[::97]
+    out.update(monitor_values(solver, [m.acc for m in solver.monitors]))
     for f in FIELDS:
         a = np.asarray(getattr(s, f))
         out[f"out_{f}_sha"] = np.array(sha(a))
@@ -272,14 +305,194 @@ def kernel_cases(et, precision):
     print(f"wrote {path.name}")
 
 
+# ----------------------------------------------------------------- protocol traces
+# Opcodes of a recorded protocol trace (tests/test_gpu_etalon_trace.py replays them).
+OP_TO_DEVICE, OP_UPDATE_H, OP_UPDATE_E, OP_ISUB, OP_ACCUMULATE, OP_TO_HOST, OP_SYNC = range(7)
+STATE_ARRAYS = FIELDS + COEFFS
+
+
+class _Tracked(np.ndarray):
+    """A NumPy array the recording backend handed out: knows its handle, or the (handle, row)
+    it is a row view of."""
+
+    def __array_finalize__(self, obj):
+        self._h = None
+        self._row = None
+
+    def __getitem__(self, key):
+        if isinstance(key, (int, np.integer)) and self._h is not None:
+            v = np.ndarray.__getitem__(self.view(np.ndarray), key).view(_Tracked)
+            v._row = (self._h, int(key))
+            return v
+        if isinstance(key, tuple) and len(key) == 2 and all(isinstance(k, _Tracked) for k in key):
+            return _TrackedIndexed(self, key[0], key[1])
+        return np.ndarray.__getitem__(self.view(np.ndarray), key)
+
+    def __setitem__(self, key, value):
+        if isinstance(value, _TrackedIndexed) and value.target is self and value.applied:
+            return
+        np.ndarray.__setitem__(self.view(np.ndarray), key, value)
+
+
+class _TrackedIndexed:
+    """``field[i, j]`` for ``field[i, j] -= delta`` (etalon/fdtd/solver.py:89): recorded, then
+    applied with NumPy's own fancy-index semantics."""
+
+    def __init__(self, target, i, j):
+        self.target, self.i, self.j, self.applied = target, i, j, False
+
+    def __isub__(self, delta):
+        rec = _TraceBackend.active
+        rec.events.append((OP_ISUB, self.target._h, self.i._h, self.j._h, delta._h, 0))
+        plain = self.target.view(np.ndarray)
+        plain[self.i.view(np.ndarray), self.j.view(np.ndarray)] -= delta.view(np.ndarray)
+        self.applied = True
+        return self
+
+
+class _TraceBackend:
+    """Etalon's NumpyBackend, recording every protocol call Etalon's FDTDSolver makes and every
+    array it moves to the device."""
+
+    active = None
+
+    def __init__(self, inner):
+        self.inner, self.events, self.payloads = inner, [], []
+        self.name, self.device, self.xp = inner.name, inner.device, inner.xp
+        _TraceBackend.active = self
+
+    def to_device(self, a):
+        a = self.inner.to_device(a)
+        h = len(self.payloads)
+        self.payloads.append(np.array(a, copy=True))
+        self.events.append((OP_TO_DEVICE, h, 0, 0, 0, 0))
+        t = a.view(_Tracked)
+        t._h = h
+        return t
+
+    def to_host(self, a):
+        self.events.append((OP_TO_HOST, a._h, 0, 0, 0, 0))
+        return np.array(a.view(np.ndarray), copy=True)
+
+    def synchronize(self):
+        self.events.append((OP_SYNC, 0, 0, 0, 0, 0))
+
+    @staticmethod
+    def _plain_state(s):
+        import copy
+
+        p = copy.copy(s)
+        for k in STATE_ARRAYS:
+            setattr(p, k, getattr(s, k).view(np.ndarray))
+        return p
+
+    def update_h_te(self, s):
+        self.events.append((OP_UPDATE_H, 0, 0, 0, 0, 0))
+        self.inner.update_h_te(self._plain_state(s))
+
+    def update_e_te(self, s):
+        self.events.append((OP_UPDATE_E, 0, 0, 0, 0, 0))
+        self.inner.update_e_te(self._plain_state(s))
+
+    def accumulate_dft(self, acc, field, index, phasors):
+        table, row = phasors._row if phasors._row is not None else (phasors._h, -1)
+        self.events.append((OP_ACCUMULATE, acc._h, field._h, index._h, table, row))
+        self.inner.accumulate_dft(acc.view(np.ndarray), field.view(np.ndarray), index.view(np.ndarray),
+                                  phasors.view(np.ndarray))  # fmt: skip
+
+
+def trace_case(et, name, precision, steps=None):
+    """Record the protocol calls of Etalon's FDTDSolver on a case: ``steps`` solver.step()
+    calls then fields(), or solver.run() to its end when ``steps`` is None."""
+    import etalon.fdtd.solver as solver_module
+    from etalon.fdtd.backends.numpy_backend import NumpyBackend
+
+    sim, _ = reference_sims(et, precision)[name]
+    plain_get = solver_module.get_backend
+    solver_module.get_backend = lambda n, p: _TraceBackend(NumpyBackend())
+    try:
+        solver = solver_module.FDTDSolver(sim)
+    finally:
+        solver_module.get_backend = plain_get
+    if steps is not None:
+        solver.n_steps = steps  # phasor tables of the steps run, not of run_time's millions
+    rec = solver.backend
+    s = solver.state
+    state_handles = np.array([getattr(s, k)._h for k in STATE_ARRAYS], np.int64)
+    scalars = np.array([s.db, s.inv_dx, s.inv_dy])
+    if steps is None:
+        solver.run()
+    else:
+        for _ in range(steps):
+            solver.step()
+    fields = solver.fields()
+    out = {"events": np.array(rec.events, np.int64), "state_handles": state_handles,
+           "state_scalars": scalars.astype(solver.real), "grid": np.array([s.nx, s.ny], np.int64),
+           "n_steps": np.array(solver.n), "mon_handles": np.array([m.acc._h for m in solver.monitors], np.int64)}  # fmt: skip
+    # payloads: one byte buffer, with per-handle offset, shape and dtype
+    offs, shapes, dtypes, chunks, off = [], [], [], [], 0
+    for a in rec.payloads:
+        b = np.ascontiguousarray(a).view(np.uint8).ravel()
+        offs.append(off)
+        shapes.append(list(a.shape) + [-1] * (3 - a.ndim))
+        dtypes.append(a.dtype.str)
+        chunks.append(b)
+        off += b.size
+    out["payload"] = np.concatenate(chunks)
+    out["p_off"], out["p_shape"], out["p_dtype"] = np.array(offs, np.int64), np.array(shapes, np.int64), np.array(dtypes)
+    # what Etalon's run ended with: every state array, every accumulator, the host fields
+    for k in STATE_ARRAYS:
+        out[f"out_{k}_sha"] = np.array(sha(getattr(s, k).view(np.ndarray)))
+    for k, m in enumerate(solver.monitors):
+        out[f"out_acc{k}_sha"] = np.array(sha(m.acc.view(np.ndarray)))
+    for c, a in fields.items():
+        out[f"out_host_{c}_sha"] = np.array(sha(a))
+    path = HERE / f"trace_{name}_{precision}.npz"
+    np.savez_compressed(path, **out)
+    print(f"wrote {path.name}: {len(rec.events)} protocol calls, {len(rec.payloads)} uploads, "
+          f"{solver.n} steps, {path.stat().st_size} bytes")
+
+
+def augment_case(et, name, precision):
+    """Add Etalon's monitor values to an existing fixture from the accumulators it holds
+    (for the long config2 runs, which are not stepped again)."""
+    from etalon.fdtd.solver import FDTDSolver
+
+    path = HERE / f"{name}_{precision}.npz"
+    with np.load(path, allow_pickle=False) as z:
+        out = {k: z[k] for k in z.files}
+    sim, _ = reference_sims(et, precision)[name]
+    solver = FDTDSolver(sim)  # setup only: samplings and grid
+    accs = [out[f"out_acc{k}"] for k in range(len(solver.monitors))]
+    out.update(monitor_values(solver, accs))
+    np.savez_compressed(path, **out)
+    print(f"added monitor values to {path.name}")
+
+
 def main():
+    import os
+
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("ETALON_SRC"),
+                    help="Etalon's source tree (default: $ETALON_SRC)")
     ap.add_argument("--cases", default="kernels,config1,g4_full,small")
+    ap.add_argument("--augment", default="", help="cases whose existing fixtures get monitor values only")
+    ap.add_argument("--trace", default="", help="cases whose protocol calls are recorded (g4_full: 600 "
+                    "steps then fields(); small: run() to its end)")
     ap.add_argument("--precisions", default="single,double")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("name Etalon's source tree with --ref or ETALON_SRC")
     et = import_etalon(args.ref)
     for precision in args.precisions.split(","):
+        if args.augment:
+            for name in args.augment.split(","):
+                augment_case(et, name, precision)
+            continue
+        if args.trace:
+            for name in args.trace.split(","):
+                trace_case(et, name, precision, steps=600 if name == "g4_full" else None)
+            continue
         for name in args.cases.split(","):
             if name == "kernels":
                 kernel_cases(et, precision)

@@ -66,13 +66,19 @@ def hbm_peak() -> tuple[float, str]:
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic(kernel_tag: str):
-    """Per-launch DRAM bytes of the dominant kernel from its committed ncu summary, if any."""
+def profile_entry(key: str, kernel_tag: str):
+    """The text of a ``key[kernel_tag]: ...`` line of a committed ncu summary, and its file."""
     for f in sorted((ROOT / "profiles").glob("*.md")):
         for line in f.read_text().splitlines():
-            if line.startswith(f"traffic_bytes_per_launch[{kernel_tag}]:"):
-                return float(line.split(":", 1)[1].split()[0]), f.name
+            if line.startswith(f"{key}[{kernel_tag}]:"):
+                return line.split(":", 1)[1].strip(), f.name
     return None, None
+
+
+def ncu_traffic(kernel_tag: str):
+    """Per-launch DRAM bytes of the dominant kernel from its committed ncu summary, if any."""
+    text, src = profile_entry("traffic_bytes_per_launch", kernel_tag)
+    return (float(text.split()[0]), src) if text else (None, None)
 
 
 class ClockSampler:
@@ -320,6 +326,7 @@ def run_ours(args, world, rank, local) -> None:
 
     # roofline of the dominant kernel: algorithmic bytes per launch / its average launch time
     roofline = kernel_roofline(e, p)
+    ref_kernels = None if args.no_ref_kernels or rank != 0 else reference_kernels_line(e, p, args.ref_kernel_steps)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -333,6 +340,9 @@ def run_ours(args, world, rank, local) -> None:
         "clocks": clocks.summary(),
         "wall_ms_per_step": 1e3 * wall / args.steps,
     }  # fmt: skip
+    if ref_kernels is not None:
+        ref_kernels["ours_over_reference_kernels"] = value / world / ref_kernels["value"] if "value" in ref_kernels else None
+        out["reference_kernels"] = ref_kernels
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         rate, steps, cwall, _ = cpu_oracle_rate(args.precision, args.cpu_seconds, threads)
@@ -360,11 +370,12 @@ def run_ours(args, world, rank, local) -> None:
 def kernel_roofline(e, p) -> dict:
     """Roofline of the dominant kernel, timed live with CUDA events on its launching stream.
 
-    Temporally blocked path: one more run of the workload with every interior-tile and
-    CPML-tile launch timed on its own (option TIMING = 2: the two kernels one after the
-    other, an event pair around each, no graphs). The interior kernel advances its output
-    cells K steps per launch; its algorithmic bytes are those of K single-pass steps over
-    them, 8 values per cell-step (Ex, Ey, Hz read and write, cb_ex and cb_ey read).
+    Temporally blocked path: one more run of the workload with every kernel launch timed on
+    its own (option TIMING = 2: the kernels one after the other, an event pair around each, no
+    graphs). The dominant kernel is the lean interior kernel (interior tiles without a source,
+    monitor or trace node); it advances its output cells K steps per launch, and its algorithmic
+    bytes are those of K single-pass steps over them, 8 values per cell-step (Ex, Ey, Hz read
+    and write, cb_ex and cb_ey read).
     One-step path: the run's own time per step against the algorithmic bytes of a step.
     """
     from etalon_gb300 import _lib
@@ -382,7 +393,7 @@ def kernel_roofline(e, p) -> dict:
     ms, launches, cells = kt["interior"]
     if launches:
         dt = "float" if s == 4 else "double"
-        name = f"k_tb_step<{dt},{rows // warps},{depth},false,{warps}>"
+        name = f"k_tb_step<{dt},{rows // warps},{depth},false,{warps},false>"  # the lean interior kernel
         launch_ms = ms / launches
         bytes_launch = 8 * s * cells * depth
         cp_ms, cp_launches, cp_cells = kt["cpml"]
@@ -413,9 +424,57 @@ def kernel_roofline(e, p) -> dict:
         tag = "k_fused"
     achieved = bytes_launch / (launch_ms / 1e3) / 1e9
     traffic, traffic_src = ncu_traffic(tag)
+    # "bound" names the roofline the fraction is taken against (HBM: the stencil is no
+    # contraction). Temporal blocking moves a cell through HBM once per K steps, so the
+    # algorithmic fraction can pass 1; "dram_frac" is the DRAM traffic ncu measured per launch
+    # over the same launch time, and "limiter" what ncu shows actually limits the kernel.
+    limiter, _ = profile_entry("limiter", tag)
+    dram_frac = traffic / (launch_ms / 1e3) / 1e9 / peak if traffic else None
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_source": f"{peak_kind} (hbm_gbs)", "traffic": traffic, "traffic_source": traffic_src,
+            "dram_frac": dram_frac, "limiter": limiter,
             "algorithmic_bytes_per_launch": bytes_launch, **extra}  # fmt: skip
+
+
+def reference_kernels_line(e, p, steps: int, warmup: int = 20) -> dict:
+    """Etalon's own CUDA kernels (update_te.cu, dft.cu: compiled unchanged by
+    oracle/build_ref.py, launched with its CuPy backend's shapes by oracle/ref_kernels.py) on
+    the same workload and GPU, one step at a time as Etalon's FDTDSolver steps them: cell-updates
+    per second over ``steps`` steps timed with events on their stream after ``warmup`` steps,
+    and the fields and accumulators after them against this package's engine, bit for bit."""
+    from etalon_gb300 import _lib
+    from oracle import ref_kernels
+    from tests.ref_kernel_run import RefRun
+
+    if not ref_kernels.available(p.precision):
+        return {"unavailable": "reference kernel images missing (oracle/build_ref.py needs Etalon's tree)"}
+    k = ref_kernels.RefKernels(p.precision)
+    run = RefRun(k, p, warmup + steps)
+    for _ in range(warmup):
+        run.step()
+    a, b = k.event(), k.event()
+    _lib.call("etg_synchronize")
+    launches0 = k.launches
+    k.record(a)
+    for _ in range(steps):
+        run.step()
+    k.record(b)
+    ms = k.elapsed_ms(a, b)
+    e.reset()
+    e.advance(warmup + steps)
+    e.synchronize()
+    same = all(np.array_equal(run.field(f).view(np.uint8), e.field(f).view(np.uint8))
+               for f in ("ex", "ey", "hz", "psi_ex_y", "psi_ey_x", "psi_hz_x", "psi_hz_y"))  # fmt: skip
+    same = same and all(np.array_equal(run.acc(m), e.dft(m)) for m in range(len(p.samplings)))
+    out = {"value": p.grid.n_cells * steps / (ms / 1e3), "unit": UNIT, "time_steps": steps,
+           "ms_per_time_step": ms / steps, "kernel_launches_per_time_step": (k.launches - launches0) / steps,
+           "bit_identical_to_ours": bool(same),
+           "what": "Etalon's update_h_te/update_e_te/accumulate_dft, nvcc -fmad=false for sm_103a, CuPy's launch "
+                   "shapes, legacy default stream, one launch per kernel per step (+ one injection scatter per "
+                   "source); device time from events around the steps"}  # fmt: skip
+    run.close()
+    k.close()
+    return out
 
 
 def get_option(e, option: int) -> int:
@@ -519,9 +578,11 @@ def adjoint_line(args) -> dict:
 
 def batched_adjoint_line(args, world=1, rank=0) -> dict:
     """32 seeded design variants (regions 512-1024 cells per side + CPML, design windows 50-150
-    cells, 8 λ, 10 000 steps): all forward and reverse passes run as one batch; gradients per
-    second against the same 32 designs run one at a time on the one-step kernels with √N
-    checkpoints (the single-design workload's plain path)."""
+    cells, 8 λ, 10 000 steps): all forward and reverse passes run as one batch with √N
+    checkpoints (the headline) and with the full trace; gradients per second against the same
+    32 designs run one at a time on the single-design default path (temporally blocked kernels,
+    √N checkpoints: the single-design workload's own path), and every design's float32
+    gradient against its float64 gradient."""
     import torch
 
     from etalon_gb300 import _lib
@@ -539,14 +600,15 @@ def batched_adjoint_line(args, world=1, rank=0) -> dict:
         items.append((p, d, torch.as_tensor(cases.smooth_design(d.nx, d.ny, seed))))
         designs.append(design)
     S = AdjointRunner.sqrt_stride(n)
-    out = {"metric": "gradient evaluations/s (32 designs 512^2-1024^2, 50^2-150^2 windows, 8 wavelengths, fp32)",
-           "unit": "gradients/s", "time_steps": n}  # fmt: skip
-    grads = {}
-    for name, stride in (("trace", 0), ("checkpoints", S)):
+    out = {"metric": "gradient evaluations/s (32 designs 512^2-1024^2, 50^2-150^2 windows, 8 wavelengths, fp32, "
+                     "sqrt-N checkpoints)",
+           "unit": "gradients/s", "time_steps": n, "checkpoint_stride": S}  # fmt: skip
+
+    def batched(items, stride, reps):
         runners = [AdjointRunner(p, d, stride=stride) for p, d, _ in items]
         b = AdjointBatch(runners)
         ts = []
-        for _ in range(3):
+        for _ in range(reps):
             eps = [e.clone().requires_grad_(True) for _, _, e in items]
             _lib.call("etg_synchronize")
             t = time.perf_counter()
@@ -554,37 +616,50 @@ def batched_adjoint_line(args, world=1, rank=0) -> dict:
             sum(point_power(o[0], it[0].samplings[0]) for o, it in zip(outs, items)).backward()
             _lib.call("etg_synchronize")
             ts.append(time.perf_counter() - t)
-        grads[name] = [e.grad.numpy().copy() for e in eps]
+        grads = [e.grad.numpy().copy() for e in eps]
         b.close()
         for r in runners:
             r.close()
-        out[f"batched_{name}_s"] = reduce_max(world, min(ts[1:]))
+        return min(ts[1:]) if reps > 1 else ts[0], grads
+
+    grads = {}
+    for name, stride in (("checkpoints", S), ("trace", 0)):
+        t, grads[name] = batched(items, stride, 3)
+        out[f"batched_{name}_s"] = reduce_max(world, t)
+    # the baseline: one design at a time on the single-design default path, one untimed
+    # gradient per design first (graph capture, tuning), then one timed gradient
     total, one = 0.0, []
-    for p, d, e0 in items:  # the baseline: one design at a time, one-step kernels, √N checkpoints
-        r = AdjointRunner(p, d, stride=S, kernel="plain")
+    for p, d, e0 in items:
+        r = AdjointRunner(p, d, stride=S)
+        _gradient_once(r, p, e0)
         t, g = _gradient_once(r, p, e0)
         total += t
         one.append(g)
         r.close()
     total = reduce_max(world, total)
-    out["one_at_a_time_one_step_s"] = total
+    out["one_at_a_time_s"] = total
+    out["one_at_a_time_path"] = "single-design default (temporally blocked kernels, sqrt-N checkpoints)"
     out["designs"] = 32
     out["sharding"] = f"{world} rank(s), designs balanced by cells, no exchange"
-    out["value"] = 32 / out["batched_trace_s"]
-    out["checkpoints_value"] = 32 / out["batched_checkpoints_s"]
+    out["value"] = 32 / out["batched_checkpoints_s"]
+    out["trace_value"] = 32 / out["batched_trace_s"]
     out["one_at_a_time_value"] = 32 / total
-    out["speedup_vs_one_at_a_time"] = total / out["batched_trace_s"]
-    out["checkpoints_speedup_vs_one_at_a_time"] = total / out["batched_checkpoints_s"]
-    out["batched_equals_one_at_a_time_bits"] = bool(all(np.array_equal(a, b) for a, b in zip(grads["trace"], one)))
-    errs = []
-    for (p, d, e0), g32, design in list(zip(items, grads["trace"], designs))[:2]:  # float64, two designs
+    out["speedup_vs_one_at_a_time"] = total / out["batched_checkpoints_s"]
+    out["trace_speedup_vs_one_at_a_time"] = total / out["batched_trace_s"]
+    out["batched_equals_one_at_a_time_bits"] = bool(
+        all(np.array_equal(a, b) and np.array_equal(a, c) for a, b, c in zip(grads["checkpoints"], grads["trace"], one)))
+    # float64 gradients of every design, as one float64 batch with the same checkpoints
+    items64 = []
+    for (p, d, e0), design in zip(items, designs):
         p64, win = cases.adjoint_device("double", n_steps=n, region=p.grid.nx - 24, design=design, n_wavelengths=8)
-        r = AdjointRunner(p64, DesignRegion.from_box(p64, win[:2], win[2:]), stride=S)
-        _, g64 = _gradient_once(r, p64, e0)
-        r.close()
-        if np.abs(g64).max() > 0:  # a run too short for the pulse to reach the objective has none
-            errs.append(float(np.abs(g32 - g64).max() / np.abs(g64).max()))
+        items64.append((p64, DesignRegion.from_box(p64, win[:2], win[2:]), e0))
+    t64, g64s = batched(items64, S, 1)
+    out["fp64_batched_s"] = t64
+    errs = [float(np.abs(g32 - g64).max() / np.abs(g64).max())
+            for g32, g64 in zip(grads["checkpoints"], g64s) if np.abs(g64).max() > 0]  # fmt: skip
+    # (a run too short for the pulse to reach the objective has no gradient to compare)
     out["rel_err_vs_fp64"] = max(errs) if errs else None
+    out["rel_err_vs_fp64_median"] = float(np.median(errs)) if errs else None
     out["rel_err_designs"] = len(errs)
     return out
 
@@ -748,6 +823,8 @@ def main() -> None:
     ap.add_argument("--batch-adjoint-time-steps", type=int, default=10000)
     ap.add_argument("--no-fp64", action="store_true", help="skip the float64 line of the same workload")
     ap.add_argument("--no-studio", action="store_true", help="skip the live-view and rasterisation lines")
+    ap.add_argument("--no-ref-kernels", action="store_true", help="skip timing Etalon's own CUDA kernels")
+    ap.add_argument("--ref-kernel-steps", type=int, default=1000)
     args = ap.parse_args()
     os.environ["ETG_BENCH_IMPL"] = args.impl
     world, rank, local = dist_setup(args.gpus)

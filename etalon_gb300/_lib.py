@@ -85,6 +85,8 @@ SIGNATURES: dict[str, list] = {
     "etg_adj_batch_forward": [vp, i64, i64],
     "etg_adj_batch_backward": [vp],
     "etg_tb_advance_static": [i32, i32, i32, i64] + [vp] * 21 + [f64, f64, f64, i64],
+    "etg_debug_set_wait_tries": [i64],
+    "etg_sim_device_array": [vp, i32, vp, vp],
 }
 
 

@@ -254,8 +254,10 @@ def point_value(acc: torch.Tensor, sampling: ComponentSampling) -> tuple[torch.T
 
     ``acc`` is an accumulator as ``simulate`` returns it, (n_f, nodes, 2). The nodes are
     contracted with the bilinear weights of each interpolated axis, x first and then y, as
-    etalon/io/result.py:60-79 does in float64; an interpolated axis holds at most two nodes,
-    so every sum has at most two terms and F equals Etalon's value bit for bit."""
+    etalon/io/result.py:60-79 does in float64 (an interpolated axis holds at most two nodes).
+    F equals Etalon's value bit for bit where torch and NumPy round these two-term sums alike
+    (tested against Etalon's own values on the machine that made the fixtures); elsewhere it
+    can differ in the last bit, as Etalon's own value does between x86 and Arm."""
     n_f = sampling.wavelengths.size
     shape = (n_f, sampling.x.index.size, sampling.y.index.size)
     re, im = acc[..., 0].reshape(shape), acc[..., 1].reshape(shape)

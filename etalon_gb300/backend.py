@@ -59,18 +59,31 @@ POOL = _Pool()
 
 
 class DeviceArray:
-    """A C-contiguous array in device memory."""
+    """An array in device memory: C-contiguous, or (2D views of a resident simulation's arrays)
+    rows of ``pitch`` elements, of which the first ``shape[1]`` belong to the array."""
 
     __array_priority__ = 1000
 
-    def __init__(self, shape, dtype, ptr: int | None = None, base: "DeviceArray | None" = None):
+    def __init__(self, shape, dtype, ptr: int | None = None, base=None, pitch: int | None = None):
         self.shape = tuple(int(s) for s in shape)
         self.dtype = np.dtype(dtype)
         self.size = int(np.prod(self.shape, dtype=np.int64))
         self.nbytes = self.size * self.dtype.itemsize
         self.base = base
+        self.pitch = self.shape[-1] if pitch is None or len(self.shape) != 2 else int(pitch)
+        if self.pitch != self.shape[-1] and (ptr is None or self.pitch < self.shape[-1]):
+            raise ValueError("a pitched device array is a view of memory it does not own")
         self._owner = ptr is None
         self.ptr = POOL.get(self.nbytes) if ptr is None else int(ptr)
+
+    @property
+    def contiguous(self) -> bool:
+        return self.pitch == self.shape[-1] or len(self.shape) != 2
+
+    @property
+    def span(self) -> int:
+        """Elements from the first to one past the last of the array (rows × pitch when pitched)."""
+        return self.shape[0] * self.pitch if not self.contiguous else self.size
 
     @property
     def ndim(self) -> int:
@@ -84,6 +97,10 @@ class DeviceArray:
         return out
 
     def get(self) -> np.ndarray:
+        if not self.contiguous:
+            rows = np.empty((self.shape[0], self.pitch), self.dtype)
+            call("etg_memcpy_d2h", rows.ctypes.data, self.ptr, rows.nbytes)
+            return np.ascontiguousarray(rows[:, : self.shape[1]])
         out = np.empty(self.shape, self.dtype)
         call("etg_memcpy_d2h", out.ctypes.data, self.ptr, self.nbytes)
         return out
@@ -93,6 +110,8 @@ class DeviceArray:
         return a if dtype is None else a.astype(dtype)
 
     def copy(self) -> "DeviceArray":
+        if not self.contiguous:
+            return DeviceArray.from_host(self.get())
         out = DeviceArray(self.shape, self.dtype)
         call("etg_memcpy_d2d", out.ptr, self.ptr, self.nbytes)
         return out
@@ -111,9 +130,11 @@ class DeviceArray:
             k = int(key) + (self.shape[0] if key < 0 else 0)
             if not 0 <= k < self.shape[0]:
                 raise IndexError(f"index {key} out of range for axis 0 of size {self.shape[0]}")
-            row = self.nbytes // self.shape[0]
+            row = self.nbytes // self.shape[0] if self.contiguous else self.pitch * self.dtype.itemsize
             return DeviceArray(self.shape[1:], self.dtype, self.ptr + k * row, base=self)
         if isinstance(key, tuple) and len(key) == 2 and all(isinstance(k, DeviceArray) for k in key):
+            if not self.contiguous:
+                raise TypeError("field[i, j] -= delta needs a contiguous device array")
             return _Indexed(self, key[0], key[1])
         raise TypeError(f"DeviceArray supports a row index or two index arrays, not {key!r}")
 
@@ -168,9 +189,13 @@ class _Cast:
         raise TypeError("device arrays support v * v of one converted field")
 
     def value(self) -> DeviceArray:
-        out = DeviceArray(self.src.shape, self.dtype)
-        call("etg_cast", _lib.dtype_code(self.src.dtype), _lib.dtype_code(self.dtype), self.src.size, self.src.ptr,
-             out.ptr)  # fmt: skip
+        src = self.src
+        if not src.contiguous:  # cast the pitched rows whole, then read the array's columns
+            out = DeviceArray((src.shape[0] * src.pitch,), self.dtype)
+            call("etg_cast", _lib.dtype_code(src.dtype), _lib.dtype_code(self.dtype), src.span, src.ptr, out.ptr)
+            return DeviceArray(src.shape, self.dtype, out.ptr, base=out, pitch=src.pitch)
+        out = DeviceArray(src.shape, self.dtype)
+        call("etg_cast", _lib.dtype_code(src.dtype), _lib.dtype_code(self.dtype), src.size, src.ptr, out.ptr)
         return out
 
     def astype(self, dtype, copy=True) -> "_Cast":
@@ -191,14 +216,17 @@ class _Square:
         self.src, self.dtype, self.coeff = src, dtype, coeff
 
     def __truediv__(self, c):
-        if self.coeff is None and isinstance(c, DeviceArray) and c.shape == self.src.shape and c.dtype == self.src.dtype:
+        if (self.coeff is None and isinstance(c, DeviceArray) and c.shape == self.src.shape
+                and c.dtype == self.src.dtype and c.pitch == self.src.pitch):  # fmt: skip
             return _Square(self.src, self.dtype, c)
         raise TypeError("device arrays support (v * v) / c with c a device array of the field's shape and dtype")
 
     def sum(self) -> np.float64:
         out = C.c_double()
-        rows, cols = (self.src.shape[0], int(np.prod(self.src.shape[1:]))) if self.src.ndim > 1 else (1, self.src.size)
-        call("etg_sum_sq", _lib.dtype_code(self.src.dtype), rows, cols, cols, self.src.ptr,
+        src = self.src
+        rows, cols = (src.shape[0], int(np.prod(src.shape[1:]))) if src.ndim > 1 else (1, src.size)
+        pitch = cols if src.contiguous else src.pitch
+        call("etg_sum_sq", _lib.dtype_code(src.dtype), rows, cols, pitch, src.ptr,
              None if self.coeff is None else self.coeff.ptr, C.byref(out))  # fmt: skip
         return np.float64(out.value)
 
@@ -234,7 +262,7 @@ class _Blocks:
         src = self.window.src
         out = DeviceArray((self.mx, self.my), src.dtype)
         code = _lib.dtype_code(src.dtype)
-        call("etg_block_mean", code, self.window.rows, self.window.cols, src.shape[1], src.ptr, self.sx, self.sy,
+        call("etg_block_mean", code, self.window.rows, self.window.cols, src.pitch, src.ptr, self.sx, self.sy,
              code, out.ptr)  # fmt: skip
         return out
 

@@ -77,6 +77,11 @@ class GB300FDTDSolver:
     def n(self) -> int:
         return self._solver.n
 
+    @property
+    def state(self):
+        """Device views of the fields and coefficients (what Etalon Studio's live view reads)."""
+        return self._solver.state
+
     def step(self) -> None:
         self._solver.step()
 
@@ -163,11 +168,17 @@ def uses_gpu(backend_name: str) -> bool:
     return backend_name == "cuda" or (backend_name == "auto" and gpu_available())
 
 
-def install() -> None:
+def install(fused_solver: bool = False) -> None:
     """Route Etalon's "cuda" backend (and "auto" on a GPU machine) to this backend.
 
     Explicit "cuda" without a usable GPU raises (never a silent fallback); "auto" falls
     back to NumPy with a warning, as etalon/fdtd/backends/__init__.py:16-43 does.
+    ``Simulation.run`` goes through the fused engine (``GB300FDTDSolver``). Code that builds
+    ``FDTDSolver(sim)`` itself and steps it — Etalon Studio's runner
+    (etalon/studio/runner.py:463) — gets Etalon's own solver on the per-step protocol, or, with
+    ``fused_solver=True``, ``GB300FDTDSolver`` for GPU backends: the same ``step``, ``n``,
+    ``n_steps``, ``grid``, ``backend``, ``state`` (device views), ``fields`` and ``result``,
+    on the fused engine.
     """
     import etalon.fdtd.backends as backends
     import etalon.fdtd.solver as solver_module
@@ -186,3 +197,11 @@ def install() -> None:
     backends.get_backend = get_backend
     solver_module.get_backend = get_backend
     solver_module.run = run
+    if fused_solver:
+        plain_solver = getattr(solver_module.FDTDSolver, "etalon_solver", solver_module.FDTDSolver)
+
+        def FDTDSolver(sim):  # noqa: N802 - stands in for Etalon's class
+            return GB300FDTDSolver(sim) if uses_gpu(sim.backend) else plain_solver(sim)
+
+        FDTDSolver.etalon_solver = plain_solver
+        solver_module.FDTDSolver = FDTDSolver

@@ -22,13 +22,14 @@ struct etg_batch {
   std::vector<int4> h_tiles;
   int4* d_tiles = nullptr;
   int n_inner = 0, n_pml = 0, tiles_er = 0, tiles_k = 0;
+  int n_hot = 0;  // leading interior tiles with a source, monitor or trace node (the others: lean kernel)
   int64_t dft_work = 0;  // largest sampled monitor (frequencies x nodes) of any simulation
   int dft_mon = 0;       // most monitor components of any simulation
   int64_t** d_steps = nullptr;     // each simulation's step counter
   cudaStream_t stream = nullptr, side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, ev0 = nullptr, ev1 = nullptr, done = nullptr;
-  cudaStream_t sides[3] = {};  // one branch per CPML kind
-  cudaEvent_t joins[3] = {};
+  cudaStream_t sides[4] = {};  // one branch per CPML kind, one for the interior tiles with a plan
+  cudaEvent_t joins[4] = {};
   int n_kind[3] = {};
   int64_t opt[8] = {0, 0, 32, 0, 0, 0, 0, 0};
   std::map<int64_t, cudaGraphExec_t> graphs;
@@ -98,7 +99,9 @@ int refresh(etg_batch* b, int ER, int K, bool* changed) {
     b->h_sims.swap(host);
   }
   {
-    std::vector<int4> inner, pml;
+    // interior tiles holding a source, monitor or trace node (every simulation's) lead the
+    // interior list and run the kernel with the per-step plan code; the rest run the lean one
+    std::vector<int4> inner, cold, pml;
     for (int k = 0; k < n; ++k) {
       etg_sim* s = b->sims[k];
       PhasePlan<T> ph, pe;
@@ -109,28 +112,34 @@ int refresh(etg_batch* b, int ER, int K, bool* changed) {
         for (int q = 0; q < p->n_mon; ++q)
           hot.push_back(make_int4(p->mon[q].ix0, p->mon[q].jy0, p->mon[q].ix0 + p->mon[q].nxm, p->mon[q].jy0 + p->mon[q].nym));
       }
+      if (ph.trace.buf)
+        hot.push_back(make_int4(ph.trace.ti0, ph.trace.tj0, ph.trace.ti0 + ph.trace.tnx, ph.trace.tj0 + ph.trace.tny));
       std::vector<int2> t;
-      int ni = 0;
+      int ni = 0, nh = 0;
       const int EC = 32 * (sizeof(T) == 4 ? 4 : 2);
-      tb_split_tiles(s->nx, s->ny, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi, ER, EC, K, hot, &t, &ni);
+      tb_split_tiles(s->nx, s->ny, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi, ER, EC, K, hot, &t, &ni, &nh);
       for (int q = 0; q < (int)t.size(); ++q) {
         const int r0 = tb_tile_row(t[q]), c0 = t[q].y;  // output rows [r0, r0+ER-2K), columns [c0, c0+EC-2K)
         if (r0 >= s->act_i1 || r0 + ER - 2 * K <= s->act_i0 || c0 >= s->act_j1 || c0 + EC - 2 * K <= s->act_j0)
           continue;
-        (q < ni ? inner : pml).push_back(make_int4(k, r0, c0, tb_tile_kind(t[q])));
+        (q < nh ? inner : q < ni ? cold : pml).push_back(make_int4(k, r0, c0, tb_tile_kind(t[q])));
       }
     }
+    const int n_hot = (int)inner.size();
+    inner.insert(inner.end(), cold.begin(), cold.end());
     // CPML tiles grouped by kind over every simulation (one kernel per kind)
     std::stable_sort(pml.begin(), pml.end(), [](const int4& p, const int4& q) { return p.w < q.w; });
     int n_kind[3] = {0, 0, 0};
     for (const int4& q : pml) n_kind[q.w - 1] += 1;
     const int n_inner = (int)inner.size(), n_pml = (int)pml.size();
     inner.insert(inner.end(), pml.begin(), pml.end());
-    const bool same = b->d_tiles && n_inner == b->n_inner && n_pml == b->n_pml && inner.size() == b->h_tiles.size() &&
+    const bool same = b->d_tiles && n_inner == b->n_inner && n_pml == b->n_pml && n_hot == b->n_hot &&
+                      inner.size() == b->h_tiles.size() &&
                       memcmp(inner.data(), b->h_tiles.data(), inner.size() * sizeof(int4)) == 0;
     if (!same) {
       b->n_inner = n_inner;
       b->n_pml = n_pml;
+      b->n_hot = n_hot;
       for (int k = 0; k < 3; ++k) b->n_kind[k] = n_kind[k];
       cudaFree(b->d_tiles);
       b->d_tiles = nullptr;
@@ -163,10 +172,10 @@ int batch_advance(etg_batch* b, int64_t n_steps) {
   const int64_t pairs = n_steps / (2 * K);
   const int64_t per_graph = std::max<int64_t>(1, b->opt[ETG_OPT_GRAPH_STEPS] / (2 * K));
   auto pair = [&](int64_t p) -> int {
-    int r = tb_batch_pair<T>(ER, K, NW, b->d_sims, b->d_tiles, b->n_inner, b->n_kind, 0, (int)(2 * K * p),
+    int r = tb_batch_pair<T>(ER, K, NW, b->d_sims, b->d_tiles, b->n_inner, b->n_hot, b->n_kind, 0, (int)(2 * K * p),
                              b->stream, b->sides, b->fork, b->joins);
     if (r == ETG_OK)
-      r = tb_batch_pair<T>(ER, K, NW, b->d_sims, b->d_tiles, b->n_inner, b->n_kind, 1, (int)(2 * K * p + K),
+      r = tb_batch_pair<T>(ER, K, NW, b->d_sims, b->d_tiles, b->n_inner, b->n_hot, b->n_kind, 1, (int)(2 * K * p + K),
                            b->stream, b->sides, b->fork, b->joins);
     return r;
   };
@@ -255,9 +264,11 @@ int etg_batch_create(etg_batch** out, int n_sims, etg_sim* const* sims) {
        cudaStreamCreateWithFlags(&b->sides[0], cudaStreamNonBlocking) != cudaSuccess ||
        cudaStreamCreateWithFlags(&b->sides[1], cudaStreamNonBlocking) != cudaSuccess ||
        cudaStreamCreateWithFlags(&b->sides[2], cudaStreamNonBlocking) != cudaSuccess ||
+       cudaStreamCreateWithFlags(&b->sides[3], cudaStreamNonBlocking) != cudaSuccess ||
        cudaEventCreateWithFlags(&b->joins[0], cudaEventDisableTiming) != cudaSuccess ||
        cudaEventCreateWithFlags(&b->joins[1], cudaEventDisableTiming) != cudaSuccess ||
        cudaEventCreateWithFlags(&b->joins[2], cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&b->joins[3], cudaEventDisableTiming) != cudaSuccess ||
        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)) {
     set_error("etg_batch_create: %s", cudaGetErrorString(cudaGetLastError()));
     rc = ETG_ERR_CUDA;
@@ -281,7 +292,7 @@ int etg_batch_destroy(etg_batch* b) {
   for (cudaEvent_t e : {b->fork, b->join, b->ev0, b->ev1, b->done})
     if (e) cudaEventDestroy(e);
   if (b->side) cudaStreamDestroy(b->side);
-  for (int k = 0; k < 3; ++k) {
+  for (int k = 0; k < 4; ++k) {
     if (b->sides[k]) cudaStreamDestroy(b->sides[k]);
     if (b->joins[k]) cudaEventDestroy(b->joins[k]);
   }

@@ -574,6 +574,14 @@ int etg_sim_get_field(etg_sim* s, int f, void* host) {
   return ETG_OK;
 }
 
+int etg_sim_device_array(etg_sim* s, int array, void** ptr, int64_t* pitch) {
+  ETG_REQUIRE(s && ptr && pitch && array >= 0 && array < 9, ETG_ERR_ARGUMENT,
+              "etg_sim_device_array: bad array %d", array);
+  *ptr = array < 7 ? (void*)s->field[array] : (void*)s->cb[array - 7];
+  *pitch = s->P;
+  return ETG_OK;
+}
+
 int etg_sim_get_dft(etg_sim* s, int monitor, void* host) {
   ETG_REQUIRE(s && host && monitor >= 0 && monitor < (int)s->monitors.size(), ETG_ERR_ARGUMENT,
               "etg_sim_get_dft: bad monitor %d", monitor);

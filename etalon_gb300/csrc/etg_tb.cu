@@ -141,7 +141,12 @@ struct TBNoHook {
 // already in shared memory at `stage` (three planes) and cb at `cb_s` (two planes), placed
 // there by TMA; the exchange rows live at `xch_s`. `after_load` runs on every thread right
 // after the barrier that ends the load phase, when the stage is free again.
-template <typename T, int RPT, int K, int KIND, bool STAGED = false, typename Hook = TBNoHook, int NW = 8>
+// PLAN false (interior tiles that hold no source node, no monitor node and no trace cell):
+// the tile skips the per-step source, monitor and trace code altogether. Without it the
+// interior kernel fits 128 registers with no spills, which makes its launches about 15 %
+// shorter; the tile lists put such tiles after the others, so each part is its own launch.
+template <typename T, int RPT, int K, int KIND, bool STAGED = false, typename Hook = TBNoHook, int NW = 8,
+          bool PLAN = true>
 __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst, const int2 tile,
                                         const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                         const T* stage = nullptr, T* cb_s = nullptr, T* xch_s = nullptr,
@@ -183,7 +188,7 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
   const int lr0 = RPT * ty, i0 = R0 + lr0;     // this warp's first row, local and global
   const bool lane_in = j0 >= 0 && j0 + W <= P;
 
-  if (ty == 0) {  // which plan entries touch this tile (sources: extended region; monitors: output)
+  if (PLAN && ty == 0) {  // which plan entries touch this tile (sources: extended region; monitors: output)
     auto src_hits = [&](const PhasePlan<T>& p) {
       bool hit = false;
       if (lane < p.n_src) {
@@ -208,6 +213,8 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
       s_rel[2] = r2;
       s_rel[3] = r3;
     }
+  }
+  if (ty == 0) {
     Vw z;
     z.zero();
     z.st(sHzX + lj0);  // the row above the tile
@@ -323,13 +330,14 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
     __syncthreads();
   }
   after_load();
-  const uint32_t relSrcH = s_rel[0], relSrcE = s_rel[1], relMonH = s_rel[2], relMonE = s_rel[3];
+  const uint32_t relSrcH = PLAN ? s_rel[0] : 0u, relSrcE = PLAN ? s_rel[1] : 0u;
+  const uint32_t relMonH = PLAN ? s_rel[2] : 0u, relMonE = PLAN ? s_rel[3] : 0u;
   const int64_t n_base = *a.step + step_off;
   const T db = a.db, idx = a.inv_dx, idy = a.inv_dy;
   // owned output cells of this thread: rows t in [t_lo, t_hi), columns e in [e_lo, e_hi)
   const int t_lo = max(0, K - lr0), t_hi = min(RPT, ER - K - lr0);
   const int e_lo = lj0 >= K ? 0 : W, e_hi = lj0 + W <= EC - K ? W : 0;
-  const bool traced = ph.trace.buf && ph.trace.ti0 < tile.x + S::OR && ph.trace.ti0 + ph.trace.tnx > tile.x &&
+  const bool traced = PLAN && ph.trace.buf && ph.trace.ti0 < tile.x + S::OR && ph.trace.ti0 + ph.trace.tnx > tile.x &&
                       ph.trace.tj0 < tile.y + S::OC && ph.trace.tj0 + ph.trace.tny > tile.y;
 
   auto steps = [&](auto keep_tag) {
@@ -554,20 +562,20 @@ constexpr size_t tb_smem() {
   return TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER, NW>::SMEM;
 }
 
-template <typename T, int RPT, int K, int KIND, int NW>
+template <typename T, int RPT, int K, int KIND, int NW, bool PLAN = true>
 __device__ __forceinline__ void tb_tile_nw(const SimArgs<T>& a, const TBDst<T>& dst, const int2 tile,
                                            const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off) {
-  tb_tile<T, RPT, K, KIND, false, TBNoHook, NW>(a, dst, tile, ph, pe, step_off);
+  tb_tile<T, RPT, K, KIND, false, TBNoHook, NW, PLAN>(a, dst, tile, ph, pe, step_off);
 }
 
-template <typename T, int RPT, int K, bool PML, int NW = 8>
+template <typename T, int RPT, int K, bool PML, int NW = 8, bool PLAN = true>
 __global__ void __launch_bounds__(32 * NW, TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER, NW>::MIN_BLOCKS)
 k_tb_step(const __grid_constant__ SimArgs<T> a, const __grid_constant__ TBDst<T> dst,
           const int2* __restrict__ tiles, const __grid_constant__ PhasePlan<T> ph,
           const __grid_constant__ PhasePlan<T> pe, int step_off) {
   const int2 t = tiles[blockIdx.x];
   if (!PML) {
-    tb_tile_nw<T, RPT, K, KIND_INNER, NW>(a, dst, t, ph, pe, step_off);
+    tb_tile_nw<T, RPT, K, KIND_INNER, NW, PLAN>(a, dst, t, ph, pe, step_off);
     return;
   }
   const int2 u = make_int2(t.x & ((1 << KIND_SHIFT) - 1), t.y);
@@ -599,14 +607,14 @@ k_tb_batch_kind(const BatchSim<T>* __restrict__ sims, const int4* __restrict__ t
 
 // Batched form: every tile names its simulation (and, for CPML tiles, its kind in .w); all
 // simulations advance the same K steps.
-template <typename T, int RPT, int K, bool PML, int NW = 8>
+template <typename T, int RPT, int K, bool PML, int NW = 8, bool PLAN = true>
 __global__ void __launch_bounds__(32 * NW, TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER, NW>::MIN_BLOCKS)
 k_tb_batch(const BatchSim<T>* __restrict__ sims, const int4* __restrict__ tiles, int parity, int step_off) {
   const int4 t = tiles[blockIdx.x];  // simulation, r0, c0, kind
   const BatchSim<T>& b = sims[t.x];
   const int2 u = make_int2(t.y, t.z);
   if (!PML) {
-    tb_tile_nw<T, RPT, K, KIND_INNER, NW>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off);
+    tb_tile_nw<T, RPT, K, KIND_INNER, NW, PLAN>(b.src[parity], b.dst[parity], u, b.ph, b.pe, step_off);
     return;
   }
   switch (t.w) {
@@ -651,10 +659,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+// Iteration limit of the first attempt of every bounded stage wait. Tests lower it (see
+// etg_debug_set_wait_tries) to make the wait give up on a real, completing copy.
+constexpr uint32_t kWaitTries = 1u << 20;
+__device__ uint32_t g_wait_tries = kWaitTries;
+
 // Wait for the stage with an iteration limit; on time-out flag the error, wait once more
 // (bounded) for the copy still in flight, and report failure so the CTA can return.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* flag) {
-  for (uint32_t it = 0; it < (1u << 20); ++it) {
+  const uint32_t tries = *(volatile uint32_t*)&g_wait_tries;
+  for (uint32_t it = 0; it < tries; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if (it > 32) __nanosleep(128);
   }
@@ -765,8 +779,10 @@ k_tb_tma(const __grid_constant__ TMAMaps maps, const __grid_constant__ SimArgs<T
         s_rel[3] = r3;
       }
     }
-    if (!mbar_wait_bounded(mbar, parity, a.flag)) return;
+    const bool landed = mbar_wait_bounded(mbar, parity, a.flag);
     parity ^= 1;
+    // leave together: a thread that gave up has also waited (bounded) for the copy in flight
+    if (!__syncthreads_and(landed)) return;
     Vw ex[RPT], ey[RPT], hz[RPT], cbx[RPT], cby[RPT];
 #pragma unroll
     for (int t = 0; t < RPT; ++t) {
@@ -1171,23 +1187,26 @@ struct TBState {
   int mode = -1;            // 0: interior + CPML kernels per launch, 1: persistent TMA kernel
   void* alt[7] = {};  // second buffer of each field / psi plane, same pitch
   size_t alt_bytes = 0;
-  int2* tiles = nullptr;  // interior tiles first, then CPML tiles
+  int2* tiles = nullptr;  // interior tiles first (those with sources, monitors or traces leading), then CPML tiles
   int n_inner = 0, n_pml = 0;
+  int n_hot = 0;                 // leading interior tiles that hold a source, monitor or trace node
+  std::vector<int4> hot_key;     // the rectangles n_hot was counted for
   TBConfig cfg = {0, 0, 0, 0};
   int nx = -1, ny = -1;
   bool tiles_valid = false;
   std::map<int64_t, cudaGraphExec_t> graphs;
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
-  cudaStream_t sides[3] = {};    // one branch per CPML kind
-  cudaEvent_t joins[3] = {};
+  cudaStream_t sides[4] = {};    // one branch per CPML kind, one for the interior tiles with a plan
+  cudaEvent_t joins[4] = {};
   // per-kernel timing (ETG_OPT_TIMING 2): launches serialised on the main stream, no graphs
   bool profile = false;
   cudaEvent_t pev[7] = {};
   double prof_ms[2] = {};        // interior, CPML
   double prof_kind_ms[3] = {};   // CPML tiles of each kind launched alone: X, Y, XY
   int64_t prof_launches[2] = {};
-  int64_t owned_cells[5] = {};   // output cells of one launch: interior, CPML, and per CPML kind
+  int64_t owned_cells[5] = {};   // output cells of one launch: lean interior tiles, every other tile
+                                 // (CPML, interior with a plan), and per CPML kind
   int n_kind[3] = {};            // CPML tiles of each kind (the CPML list is sorted by kind)
   unsigned* ctr = nullptr;       // persistent pipelined kernel: claim counters of the two launches
 };
@@ -1208,7 +1227,7 @@ void tb_destroy(TBState* tb) {
   for (cudaEvent_t e : tb->pev)
     if (e) cudaEventDestroy(e);
   if (tb->side) cudaStreamDestroy(tb->side);
-  for (int k = 0; k < 3; ++k) {
+  for (int k = 0; k < 4; ++k) {
     if (tb->sides[k]) cudaStreamDestroy(tb->sides[k]);
     if (tb->joins[k]) cudaEventDestroy(tb->joins[k]);
   }
@@ -1231,12 +1250,13 @@ bool tb_supported(int nx, int ny) {
   return nx >= 64 && ny >= 64;
 }
 
-template <typename T, int RPT, int K, bool PML, int NW = 8>
+template <typename T, int RPT, int K, bool PML, int NW = 8, bool PLAN = true>
 static cudaError_t tb_launch_one(const SimArgs<T>& a, const TBDst<T>& d, const int2* tiles, int n,
                                  const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                  cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  k_tb_step<T, RPT, K, PML, NW><<<n, dim3(32, NW), tb_smem<T, RPT, K, PML, NW>(), s>>>(a, d, tiles, ph, pe, step_off);
+  k_tb_step<T, RPT, K, PML, NW, PLAN><<<n, dim3(32, NW), tb_smem<T, RPT, K, PML, NW>(), s>>>(a, d, tiles, ph, pe,
+                                                                                           step_off);
   g_launches += 1;
   return cudaGetLastError();
 }
@@ -1276,10 +1296,12 @@ static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<
                                   const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                   cudaStream_t s) {
   constexpr int RP = RPT * NW / 8;  // CPML tiles: 8 warps over the same rows
-  // interior tiles on the main stream, CPML tiles on a side branch (parallel graph nodes)
+  const int2* hot = tb->tiles;                 // interior tiles with sources, monitors or traces
+  const int2* cold = tb->tiles + tb->n_hot;    // the other interior tiles: the lean kernel
+  const int n_cold = tb->n_inner - tb->n_hot;
   if (tb->profile) {  // one after the other on s, an event pair around each kernel
     cudaError_t e = cudaEventRecord(tb->pev[0], s);
-    if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW>(a, d, tb->tiles, tb->n_inner, ph, pe, step_off, s);
+    if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW, false>(a, d, cold, n_cold, ph, pe, step_off, s);
     const int2* t = tb->tiles + tb->n_inner;
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
       int only[3] = {0, 0, 0};
@@ -1292,23 +1314,28 @@ static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<
       t += tb->n_kind[k];
     }
     if (e == cudaSuccess) e = cudaEventRecord(tb->pev[4], s);
-    if (e == cudaSuccess) e = cudaEventSynchronize(tb->pev[4]);
-    float m[4] = {};
-    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventElapsedTime(&m[k], tb->pev[k], tb->pev[k + 1]);
+    if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW, true>(a, d, hot, tb->n_hot, ph, pe, step_off, s);
+    if (e == cudaSuccess) e = cudaEventRecord(tb->pev[5], s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(tb->pev[5]);
+    float m[5] = {};
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k) e = cudaEventElapsedTime(&m[k], tb->pev[k], tb->pev[k + 1]);
     tb->prof_ms[0] += m[0];
-    tb->prof_ms[1] += m[1] + m[2] + m[3];
+    tb->prof_ms[1] += m[1] + m[2] + m[3] + m[4];
     for (int k = 0; k < 3; ++k) tb->prof_kind_ms[k] += m[1 + k];
-    tb->prof_launches[0] += tb->n_inner > 0;
-    tb->prof_launches[1] += tb->n_pml > 0;
+    tb->prof_launches[0] += n_cold > 0;
+    tb->prof_launches[1] += tb->n_pml + tb->n_hot > 0;
     return e;
   }
-  // CPML kinds on three side branches, interior tiles on the main stream (parallel graph nodes)
+  // CPML kinds and the interior tiles with a plan on four side branches, the other interior
+  // tiles on the main stream (parallel graph nodes)
   cudaError_t e = cudaEventRecord(tb->fork, s);
-  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(tb->sides[k], tb->fork, 0);
+  for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(tb->sides[k], tb->fork, 0);
   if (e == cudaSuccess)
     e = tb_launch_kinds<T, RP, K>(a, d, tb->tiles + tb->n_inner, tb->n_kind, ph, pe, step_off, tb->sides);
-  if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW>(a, d, tb->tiles, tb->n_inner, ph, pe, step_off, s);
-  for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+  if (e == cudaSuccess)
+    e = tb_launch_one<T, RPT, K, false, NW, true>(a, d, hot, tb->n_hot, ph, pe, step_off, tb->sides[3]);
+  if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW, false>(a, d, cold, n_cold, ph, pe, step_off, s);
+  for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
     e = cudaEventRecord(tb->joins[k], tb->sides[k]);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, tb->joins[k], 0);
   }
@@ -1346,8 +1373,11 @@ static cudaError_t tb_two(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& 
 // Dynamic shared memory above 48 KB must be allowed per kernel, before any launch or capture.
 template <typename T, int RPT, int K, int NW = 8>
 static cudaError_t tb_attrs() {
-  cudaError_t e = cudaFuncSetAttribute(k_tb_step<T, RPT, K, false, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)tb_smem<T, RPT, K, false, NW>());
+  cudaError_t e = cudaFuncSetAttribute(k_tb_step<T, RPT, K, false, NW, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<T, RPT, K, false, NW>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_tb_step<T, RPT, K, false, NW, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tb_smem<T, RPT, K, false, NW>());
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_tb_step<T, RPT * NW / 8, K, true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)tb_smem<T, RPT * NW / 8, K, true, 8>());
@@ -1538,8 +1568,12 @@ struct Hot {
   }
 };
 
+// With `hot`, the interior tiles whose extended region meets a hot rectangle lead the interior
+// list and *n_hot counts them (the rest run the lean kernel, which has no source, monitor or
+// trace code).
 static void split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_hi, int ER, int EC,
-                        int K, std::vector<int2>* tiles, int* n_inner, const Hot* hot = nullptr) {
+                        int K, std::vector<int2>* tiles, int* n_inner, const Hot* hot = nullptr,
+                        int* n_hot = nullptr) {
   const int OR = ER - 2 * K, OC = EC - 2 * K;
   const int rlo = std::max(ux_lo, 1), rhi = std::min(ux_hi, nx), clo = std::max(uy_lo, 1), chi = std::min(uy_hi, ny);
   std::vector<int2> inner, pml;
@@ -1555,11 +1589,14 @@ static void split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_
     }
   // CPML tiles grouped by kind (X, Y, XY), so that each kind is one contiguous range
   std::stable_sort(pml.begin(), pml.end(), [](int2 p, int2 q) { return (p.x >> KIND_SHIFT) < (q.x >> KIND_SHIFT); });
+  if (n_hot) *n_hot = 0;
   if (hot) {
     auto first = [&](std::vector<int2>::iterator b, std::vector<int2>::iterator e) {
-      std::stable_partition(b, e, [&](int2 t) { return hot->hits((t.x & ((1 << KIND_SHIFT) - 1)) - K, t.y - K, ER, EC); });
+      return std::stable_partition(
+          b, e, [&](int2 t) { return hot->hits((t.x & ((1 << KIND_SHIFT) - 1)) - K, t.y - K, ER, EC); });
     };
-    first(inner.begin(), inner.end());
+    const auto split = first(inner.begin(), inner.end());
+    if (n_hot) *n_hot = (int)(split - inner.begin());
     for (int kind = KIND_X; kind <= KIND_XY; ++kind) {
       auto b = std::find_if(pml.begin(), pml.end(), [&](int2 t) { return (t.x >> KIND_SHIFT) == kind; });
       auto e = std::find_if(b, pml.end(), [&](int2 t) { return (t.x >> KIND_SHIFT) != kind; });
@@ -1571,6 +1608,8 @@ static void split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_
   *tiles = inner;
 }
 
+// Everything a tile must hold to need the per-step plan code: source nodes, monitor nodes and
+// the trace box of an adjoint run.
 template <typename T>
 static Hot hot_of(const PhasePlan<T>& ph, const PhasePlan<T>& pe) {
   Hot h;
@@ -1581,7 +1620,13 @@ static Hot hot_of(const PhasePlan<T>& ph, const PhasePlan<T>& pe) {
       h.rects.push_back(make_int4(m.ix0, m.jy0, m.ix0 + m.nxm, m.jy0 + m.nym));
     }
   }
+  const TraceDesc<T>& tr = ph.trace;
+  if (tr.buf) h.rects.push_back(make_int4(tr.ti0, tr.tj0, tr.ti0 + tr.tnx, tr.tj0 + tr.tny));
   return h;
+}
+
+static bool same_rects(const std::vector<int4>& a, const std::vector<int4>& b) {
+  return a.size() == b.size() && (a.empty() || memcmp(a.data(), b.data(), a.size() * sizeof(int4)) == 0);
 }
 
 template <typename T>
@@ -1640,15 +1685,18 @@ static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt, cons
     ETG_TRY_CUDA(cudaStreamCreateWithFlags(&tb->side, cudaStreamNonBlocking));
     ETG_TRY_CUDA(cudaEventCreateWithFlags(&tb->fork, cudaEventDisableTiming));
     ETG_TRY_CUDA(cudaEventCreateWithFlags(&tb->join, cudaEventDisableTiming));
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 4; ++k) {
       ETG_TRY_CUDA(cudaStreamCreateWithFlags(&tb->sides[k], cudaStreamNonBlocking));
       ETG_TRY_CUDA(cudaEventCreateWithFlags(&tb->joins[k], cudaEventDisableTiming));
     }
   }
-  if (!tb->tiles_valid || tb->nx != a.nx || tb->ny != a.ny) {
+  // the tiles holding sources, monitors or the trace decide which kernel runs a tile: split
+  // again whenever they change
+  if (!tb->tiles_valid || tb->nx != a.nx || tb->ny != a.ny || !same_rects(tb->hot_key, hot.rects)) {
     std::vector<int2> inner;
     split_tiles(a.nx, a.ny, a.ux_lo, a.ux_hi, a.uy_lo, a.uy_hi, tb->cfg.NW * tb->cfg.RPT, EC, tb->cfg.K, &inner,
-                &tb->n_inner, &hot);
+                &tb->n_inner, &hot, &tb->n_hot);
+    tb->hot_key = hot.rects;
     tb->n_pml = (int)inner.size() - tb->n_inner;
     const int OR = tb->cfg.NW * tb->cfg.RPT - 2 * tb->cfg.K, OC = EC - 2 * tb->cfg.K;
     for (int64_t& c : tb->owned_cells) c = 0;
@@ -1656,7 +1704,7 @@ static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt, cons
     for (int q = 0; q < (int)inner.size(); ++q) {
       const int64_t r = std::max(0, std::min(OR, a.nx - tb_tile_row(inner[q]))),
                     c = std::max(0, std::min(OC, a.ny - inner[q].y));
-      tb->owned_cells[q < tb->n_inner ? 0 : 1] += r * c;
+      tb->owned_cells[q >= tb->n_hot && q < tb->n_inner ? 0 : 1] += r * c;
       if (q >= tb->n_inner) {
         const int kind = tb_tile_kind(inner[q]);
         tb->owned_cells[1 + kind] += r * c;
@@ -1804,8 +1852,8 @@ cudaError_t tb_default_launch(const SimArgs<T>& src, const SimArgs<T>& dst, cons
   PhasePlan<T> none;
   memset(&none, 0, sizeof none);
   cudaError_t e = tb_attrs<T, RPT, K>();
-  if (e == cudaSuccess)
-    e = tb_launch_one<T, RPT, K, false>(src, as_dst(dst), tiles, n_inner, none, none, step_off, s);
+  if (e == cudaSuccess)  // no sources, monitors or traces: every interior tile takes the lean kernel
+    e = tb_launch_one<T, RPT, K, false, 8, false>(src, as_dst(dst), tiles, n_inner, none, none, step_off, s);
   if (e == cudaSuccess)
     e = tb_launch_one<T, RPT, K, true>(src, as_dst(dst), tiles + n_inner, n_pml, none, none, step_off, s);
   return e;
@@ -1828,26 +1876,32 @@ static cudaError_t batch_kind(const BatchSim<T>* b, const int4* tiles, int n, in
 }
 
 template <typename T, int RPT, int K, int NW>
-static cudaError_t batch_pair(const void* sims, const int4* tiles, int n_inner, const int* n_kind, int parity,
-                              int step_off, cudaStream_t main, const cudaStream_t* sides, cudaEvent_t fork,
-                              const cudaEvent_t* joins) {
+static cudaError_t batch_pair(const void* sims, const int4* tiles, int n_inner, int n_hot, const int* n_kind,
+                              int parity, int step_off, cudaStream_t main, const cudaStream_t* sides,
+                              cudaEvent_t fork, const cudaEvent_t* joins) {
   constexpr int RP = RPT * NW / 8;  // CPML tiles: 8 warps over the same rows, one kernel per kind
   const BatchSim<T>* b = (const BatchSim<T>*)sims;
   cudaError_t e = cudaEventRecord(fork, main);
-  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(sides[k], fork, 0);
+  for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(sides[k], fork, 0);
   const int4* t = tiles + n_inner;
   if (e == cudaSuccess) e = batch_kind<T, RP, K, KIND_X>(b, t, n_kind[0], parity, step_off, sides[0]);
   t += n_kind[0];
   if (e == cudaSuccess) e = batch_kind<T, RP, K, KIND_Y>(b, t, n_kind[1], parity, step_off, sides[1]);
   t += n_kind[1];
   if (e == cudaSuccess) e = batch_kind<T, RP, K, KIND_XY>(b, t, n_kind[2], parity, step_off, sides[2]);
-  if (e == cudaSuccess && n_inner) {
-    k_tb_batch<T, RPT, K, false, NW><<<n_inner, dim3(32, NW), tb_smem<T, RPT, K, false, NW>(), main>>>(
+  if (e == cudaSuccess && n_hot) {
+    k_tb_batch<T, RPT, K, false, NW, true><<<n_hot, dim3(32, NW), tb_smem<T, RPT, K, false, NW>(), sides[3]>>>(
         b, tiles, parity, step_off);
     g_launches += 1;
     e = cudaGetLastError();
   }
-  for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+  if (e == cudaSuccess && n_inner > n_hot) {
+    k_tb_batch<T, RPT, K, false, NW, false><<<n_inner - n_hot, dim3(32, NW), tb_smem<T, RPT, K, false, NW>(), main>>>(
+        b, tiles + n_hot, parity, step_off);
+    g_launches += 1;
+    e = cudaGetLastError();
+  }
+  for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
     e = cudaEventRecord(joins[k], sides[k]);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(main, joins[k], 0);
   }
@@ -1857,8 +1911,11 @@ static cudaError_t batch_pair(const void* sims, const int4* tiles, int n_inner, 
 template <typename T, int RPT, int K, int NW>
 static cudaError_t batch_attrs() {
   constexpr int RP = RPT * NW / 8;
-  cudaError_t e = cudaFuncSetAttribute(k_tb_batch<T, RPT, K, false, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)tb_smem<T, RPT, K, false, NW>());
+  cudaError_t e = cudaFuncSetAttribute(k_tb_batch<T, RPT, K, false, NW, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<T, RPT, K, false, NW>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_tb_batch<T, RPT, K, false, NW, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tb_smem<T, RPT, K, false, NW>());
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_tb_batch_kind<T, RP, K, KIND_X>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)TBShape<T, RP, K, KIND_X>::SMEM);
@@ -1872,14 +1929,14 @@ static cudaError_t batch_attrs() {
 }
 
 template <typename T>
-int tb_batch_pair(int ER, int K, int NW, const void* sims, const int4* tiles, int n_inner, const int* n_kind,
-                  int parity, int step_off, cudaStream_t main, const cudaStream_t* sides, cudaEvent_t fork,
-                  const cudaEvent_t* joins) {
-#define ETG_BATCH_CASE(DT, R, KK, NWW)                                                                           \
-  if ((int)sizeof(T) == DT && ER == NWW * R && K == KK && NW == NWW) {                                           \
-    ETG_TRY_CUDA(                                                                                                \
-        (batch_pair<T, R, KK, NWW>(sims, tiles, n_inner, n_kind, parity, step_off, main, sides, fork, joins))); \
-    return ETG_OK;                                                                                               \
+int tb_batch_pair(int ER, int K, int NW, const void* sims, const int4* tiles, int n_inner, int n_hot,
+                  const int* n_kind, int parity, int step_off, cudaStream_t main, const cudaStream_t* sides,
+                  cudaEvent_t fork, const cudaEvent_t* joins) {
+#define ETG_BATCH_CASE(DT, R, KK, NWW)                                                                        \
+  if ((int)sizeof(T) == DT && ER == NWW * R && K == KK && NW == NWW) {                                        \
+    ETG_TRY_CUDA((batch_pair<T, R, KK, NWW>(sims, tiles, n_inner, n_hot, n_kind, parity, step_off, main, sides, \
+                                            fork, joins)));                                                    \
+    return ETG_OK;                                                                                            \
   }
   if constexpr (sizeof(T) == 4) {
     ETG_TB_SHAPES_F32(ETG_BATCH_CASE)
@@ -1909,17 +1966,25 @@ int tb_batch_attrs(int ER, int K, int NW) {
 }
 
 void tb_split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_hi, int ER, int EC, int K,
-                    const std::vector<int4>& hot, std::vector<int2>* tiles, int* n_inner) {
+                    const std::vector<int4>& hot, std::vector<int2>* tiles, int* n_inner, int* n_hot) {
   Hot h;
   h.rects = hot;
-  split_tiles(nx, ny, ux_lo, ux_hi, uy_lo, uy_hi, ER, EC, K, tiles, n_inner, &h);
+  split_tiles(nx, ny, ux_lo, ux_hi, uy_lo, uy_hi, ER, EC, K, tiles, n_inner, &h, n_hot);
 }
 
-template int tb_batch_pair<float>(int, int, int, const void*, const int4*, int, const int*, int, int, cudaStream_t,
-                                  const cudaStream_t*, cudaEvent_t, const cudaEvent_t*);
-template int tb_batch_pair<double>(int, int, int, const void*, const int4*, int, const int*, int, int, cudaStream_t,
-                                   const cudaStream_t*, cudaEvent_t, const cudaEvent_t*);
+template int tb_batch_pair<float>(int, int, int, const void*, const int4*, int, int, const int*, int, int,
+                                  cudaStream_t, const cudaStream_t*, cudaEvent_t, const cudaEvent_t*);
+template int tb_batch_pair<double>(int, int, int, const void*, const int4*, int, int, const int*, int, int,
+                                   cudaStream_t, const cudaStream_t*, cudaEvent_t, const cudaEvent_t*);
 template int tb_batch_attrs<float>(int, int, int);
 template int tb_batch_attrs<double>(int, int, int);
 
 }  // namespace etg
+
+extern "C" int etg_debug_set_wait_tries(int64_t tries) {
+  ETG_REQUIRE(tries <= (int64_t)etg::kWaitTries, ETG_ERR_ARGUMENT,
+              "etg_debug_set_wait_tries: at most %u tries", etg::kWaitTries);
+  const uint32_t v = tries < 0 ? etg::kWaitTries : (uint32_t)tries;
+  ETG_TRY_CUDA(cudaMemcpyToSymbol(etg::g_wait_tries, &v, sizeof v));
+  return ETG_OK;
+}

@@ -23,14 +23,15 @@ struct BatchSim {
   PhasePlan<T> ph, pe;
 };
 
-// Batched launch pair (interior tiles on `main`, the CPML tiles of each kind on its side
-// stream) of the compiled shape with ER rows, depth K and NW warps; `sims` is a device array of
-// BatchSim<T>, `tiles` (sim, r0, c0, kind): interior tiles first, then n_kind[0..2] tiles of
-// kinds X, Y, XY.
+// Batched launch pair (interior tiles without a plan on `main`; the CPML tiles of each kind
+// and the interior tiles with a source, monitor or trace node each on a side stream, sides[0..3])
+// of the compiled shape with ER rows, depth K and NW warps; `sims` is a device array of
+// BatchSim<T>, `tiles` (sim, r0, c0, kind): interior tiles first (the n_hot with a plan
+// leading), then n_kind[0..2] tiles of kinds X, Y, XY.
 template <typename T>
-int tb_batch_pair(int ER, int K, int NW, const void* sims, const int4* tiles, int n_inner, const int* n_kind,
-                  int parity, int step_off, cudaStream_t main, const cudaStream_t* sides, cudaEvent_t fork,
-                  const cudaEvent_t* joins);
+int tb_batch_pair(int ER, int K, int NW, const void* sims, const int4* tiles, int n_inner, int n_hot,
+                  const int* n_kind, int parity, int step_off, cudaStream_t main, const cudaStream_t* sides,
+                  cudaEvent_t fork, const cudaEvent_t* joins);
 template <typename T>
 int tb_batch_attrs(int ER, int K, int NW);
 // Block DFT of a batch: every simulation's sampled monitors (at most max_mon per simulation,
@@ -40,8 +41,9 @@ void tb_batch_dft(const void* sims, int n_sims, int64_t max_work, int max_mon, i
 // Output tiles of one grid, interior tiles first; tiles meeting a `hot` rectangle lead each kind.
 // A CPML tile carries its kind (1: CPML across rows, 2: across columns, 3: both) in bits
 // 28-29 of .x (tb_tile_row and tb_tile_kind take it apart).
+// *n_hot (if given): the leading interior tiles that meet a `hot` rectangle.
 void tb_split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_hi, int ER, int EC, int K,
-                    const std::vector<int4>& hot, std::vector<int2>* tiles, int* n_inner);
+                    const std::vector<int4>& hot, std::vector<int2>* tiles, int* n_inner, int* n_hot = nullptr);
 
 inline int tb_tile_row(int2 t) { return t.x & ((1 << 28) - 1); }
 inline int tb_tile_kind(int2 t) { return t.x >> 28; }
@@ -49,7 +51,9 @@ inline int tb_tile_kind(int2 t) { return t.x >> 28; }
 TBState* tb_create();
 void tb_destroy(TBState* tb);
 // Kernel time (ms), launches and output cells per launch of the last advance run with
-// ETG_OPT_TIMING 2, for [interior, CPML, CPML X tiles alone, Y alone, XY alone] (zeros
+// ETG_OPT_TIMING 2, for [interior tiles without a plan (the lean kernel), every other tile
+// (CPML and interior tiles with sources, monitors or traces), CPML X tiles alone, Y alone,
+// XY alone] (zeros
 // otherwise or before any temporally blocked advance).
 void tb_kernel_timing(const TBState* tb, double* ms, int64_t* launches, int64_t* cells);
 void tb_invalidate(TBState* tb);  // drop cached graphs and plans (pointers changed)

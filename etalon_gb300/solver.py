@@ -66,6 +66,41 @@ def interpolate_monitor(sampling: ComponentSampling, acc: np.ndarray) -> np.ndar
     return np.moveaxis(data, 0, -1).astype(acc.dtype)
 
 
+class EngineState:
+    """Etalon's ``TEState`` (etalon/fdtd/state.py:15-49) as device views of a resident engine.
+
+    ``ex``, ``ey``, ``hz``, the four ψ arrays, ``cb_ex`` and ``cb_ey`` are ``DeviceArray`` views
+    of the engine's own pitched arrays (no copy); reading an attribute first waits for the
+    engine's queued steps. ``db``, ``inv_dx``, ``inv_dy`` are the cast scalars and ``nx``, ``ny``
+    the grid. This is what Etalon Studio's live view reads (etalon/studio/runner.py:258-310:
+    ``field_energy`` and ``snapshot_frame``), through ``Gb300Backend.xp``."""
+
+    _ARRAYS = {"ex": 0, "ey": 1, "hz": 2, "psi_ex_y": 3, "psi_ey_x": 4, "psi_hz_x": 5, "psi_hz_y": 6,
+               "cb_ex": 7, "cb_ey": 8}  # fmt: skip
+
+    def __init__(self, engine: TEEngine):
+        self._engine = engine
+        c = engine._coeffs
+        real = engine.real
+        self.db, self.inv_dx, self.inv_dy = real(c.db), real(c.inv_dx), real(c.inv_dy)
+        self.nx, self.ny = engine.nx, engine.ny
+
+    def __getattr__(self, name: str):
+        if name not in EngineState._ARRAYS:
+            raise AttributeError(name)
+        import ctypes as C
+
+        from . import _lib
+        from .backend import DeviceArray
+
+        e = self._engine
+        e.synchronize()
+        ptr, pitch = C.c_void_p(), C.c_int64()
+        _lib.call("etg_sim_device_array", e._h, EngineState._ARRAYS[name], C.byref(ptr), C.byref(pitch))
+        shape = e.field_shape(name) if not name.startswith("cb") else e.field_shape("ex" if name == "cb_ex" else "ey")
+        return DeviceArray(shape, e.real, ptr.value, base=e, pitch=pitch.value)
+
+
 class GB300Solver:
     """Builds the device state of a problem and advances it."""
 
@@ -82,6 +117,11 @@ class GB300Solver:
     @property
     def n(self) -> int:
         return self.engine.n
+
+    @property
+    def state(self) -> EngineState:
+        """Device views of the fields and coefficients, as Etalon's ``FDTDSolver.state``."""
+        return EngineState(self.engine)
 
     def step(self) -> None:
         """One time step (H, inject M, DFT H, E, inject J, DFT E)."""

@@ -157,6 +157,12 @@ int etg_sim_set_deltas(etg_sim* sim, int source, int64_t n0, int64_t rows, const
 /* Host <-> device copies of one field in TEState shape. */
 int etg_sim_set_field(etg_sim* sim, int field, const void* host);
 int etg_sim_get_field(etg_sim* sim, int field, void* host);
+/* Device address and row pitch (elements) of one array of the simulation, for reading it in
+ * place on the device (Etalon Studio's live view: etalon/studio/runner.py:258-291 reads
+ * state.ex, ey, hz, cb_ex, cb_ey). array: 0-6 as the field ids, 7 = cb_ex, 8 = cb_ey. Element
+ * (i, j) is at ptr + i * pitch + j; the address stays valid until the simulation is destroyed.
+ * Reads must come after etg_sim_synchronize. */
+int etg_sim_device_array(etg_sim* sim, int array, void** ptr, int64_t* pitch);
 /* Accumulator of a monitor: (n_f, nxm*nym) complex. */
 int etg_sim_get_dft(etg_sim* sim, int monitor, void* host);
 int etg_sim_set_dft(etg_sim* sim, int monitor, const void* host);
@@ -178,8 +184,9 @@ int etg_sim_last_timing(etg_sim* sim, double* ms, int64_t* launches);
  * interior-tile and CPML-tile kernels of the temporally blocked path one after the other on
  * the simulation's stream, without graphs, with a CUDA-event pair around each launch, then
  * each kind of CPML tile once more on its own (same inputs, same outputs). Arrays of 5
- * (interior, CPML, CPML tiles across rows, across columns, corners): total ms, launches,
- * output cells inside the grid per launch. */
+ * (interior tiles without sources, monitors or traces; every other tile: CPML tiles and the
+ * interior tiles with a source, monitor or trace node; CPML tiles across rows, across columns,
+ * corners): total ms, launches, output cells inside the grid per launch. */
 int etg_sim_kernel_timing(etg_sim* sim, double* ms, int64_t* launches, int64_t* cells);
 
 /* ---------------------------------------------------------------- batch
@@ -264,6 +271,14 @@ int etg_tb_advance_static(int dtype, int nx, int ny, int64_t pitch, void* ex, vo
                           const void* iky_e, const void* by_h, const void* cy_h,
                           const void* iky_h, double db, double inv_dx, double inv_dy,
                           int64_t n_steps);
+
+/* Test hook of the failure detection (no counterpart in Etalon): the iteration limit of the
+ * first attempt of every bounded wait of the TMA-fed kernels (ETG_OPT_KERNEL 3 and 4) for
+ * their shared-memory stage, on the current device. tries < 0 restores the default (2^20);
+ * 0 gives up at once. A wait that runs out flags ETG_ERR_TIMEOUT (reported by the next
+ * etg_sim_synchronize), waits once more, bounded, for the copy still in flight, and its CTA
+ * returns. A limit of 0 makes real, completing copies time out, with no fault and no hang. */
+int etg_debug_set_wait_tries(int64_t tries);
 
 #define ETG_OPT_KERNEL 0        /* 0 = auto, 1 = one step per launch, 2 = temporal blocking,
                                    3 = temporal blocking, persistent CTAs fed by TMA (two per SM),

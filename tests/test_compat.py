@@ -92,3 +92,32 @@ def test_install_routes_backends(et, monkeypatch):
         backends.get_backend("cuda", "single")
     with pytest.raises(ValueError, match="unknown backend"):
         backends.get_backend("metal", "single")
+
+
+def test_install_fused_solver_routes_stepped_solvers(et, monkeypatch):
+    """install(fused_solver=True): FDTDSolver(sim) — what Studio's runner builds — is the fused
+    engine's solver for GPU backends and Etalon's own for NumPy."""
+    import etalon.fdtd.backends as backends
+    import etalon.fdtd.solver as solver_module
+
+    from etalon_gb300 import compat
+
+    for name in ("get_backend", "run", "FDTDSolver"):
+        monkeypatch.setattr(solver_module, name, getattr(solver_module, name))
+    monkeypatch.setattr(backends, "get_backend", backends.get_backend)
+    plain = solver_module.FDTDSolver
+    built = []
+
+    class FakeFused:
+        def __init__(self, sim):
+            built.append(sim.backend)
+
+    monkeypatch.setattr(compat, "GB300FDTDSolver", FakeFused)
+    monkeypatch.setattr(compat, "gpu_available", lambda: True)
+    compat.install(fused_solver=True)
+    compat.install(fused_solver=True)  # twice: still wraps Etalon's own class
+    sims = _sims(et)
+    assert isinstance(solver_module.FDTDSolver(sims["config1"].model_copy(update={"backend": "cuda"})), FakeFused)
+    assert isinstance(solver_module.FDTDSolver(sims["config1"].model_copy(update={"backend": "auto"})), FakeFused)
+    assert built == ["cuda", "auto"]
+    assert isinstance(solver_module.FDTDSolver(sims["config1"]), plain)

@@ -76,3 +76,49 @@ def test_unsupported_device_expressions_fail_loudly(gpu):
         backend.xp.sum(a)
     with pytest.raises(TypeError):
         a[1:, :]
+
+
+def _studio_progress_loop(solver, every, frames, cell_area):
+    """Studio's stepping loop (etalon/studio/runner.py:525-545): step(), then every few steps a
+    progress frame (field_energy, runner.py:258-281) and a snapshot (snapshot_frame's
+    downsample, runner.py:284-297), read from ``solver.state`` through ``solver.backend.xp``."""
+    out = []
+    xp = solver.backend.xp
+    for _ in range(frames):
+        for _ in range(every):
+            solver.step()
+        state = solver.state
+        s = {k: getattr(state, k) for k in ("ex", "ey", "hz", "cb_ex", "cb_ey")}
+        energy = _energy(s, xp, solver.grid.dt, state.db, cell_area)
+        blocks, sx, sy = _downsample(state.hz, xp, 64)
+        out.append((solver.n, energy, np.asarray(solver.backend.to_host(blocks), dtype=np.float32), sx, sy))
+    return out
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_studio_loop_on_the_resident_solver(gpu, precision):
+    """Studio's live view on the fused engine: GB300Solver.state exposes the engine's own
+    (pitched) arrays to the same expressions; each frame equals NumPy on host copies of the
+    same fields (energy to float64 summation order, snapshot to float32 rounding)."""
+    from etalon_gb300 import physics as ph
+    from etalon_gb300.solver import GB300Solver
+    from tests import cases
+
+    p = cases.config1(precision, n_steps=600)
+    solver = GB300Solver(p)
+    c = ph.cast_coefficients(p)
+    cell_area = p.grid.dx * 1e-6 * p.grid.dy * 1e-6
+    frames = _studio_progress_loop(solver, every=97, frames=6, cell_area=cell_area)
+    ref = GB300Solver(p)
+    for n, energy, snap, sx, sy in frames:
+        ref.advance(n - ref.n)
+        host = {k: ref.engine.field(k) for k in ("ex", "ey", "hz")}
+        host.update(cb_ex=c.cb_ex, cb_ey=c.cb_ey)
+        want = _energy(host, np, p.grid.dt, c.db, cell_area)
+        assert energy == pytest.approx(want, rel=1e-12) and want > 0
+        blocks, rx, ry = _downsample(host["hz"], np, 64)
+        assert (sx, sy) == (rx, ry) and snap.shape == blocks.shape
+        np.testing.assert_allclose(snap, blocks, rtol=2e-6, atol=1e-7 * np.abs(blocks).max())
+    assert frames[-1][0] == 6 * 97
+    solver.close()
+    ref.close()

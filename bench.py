@@ -243,14 +243,18 @@ def run_ours(args, world, rank, local) -> None:
     _lib.call("etg_set_device", local)
     p = workload(args.precision, args.time_steps)
     e = TEEngine(p, kernel="auto" if args.kernel == "tuned" else args.kernel)
+    tuned_ms = None
     if args.kernel == "tuned":
         choice = list(autotune.tune(e))
+        tuned_ms = autotune.timings(e)
     else:
         if args.tile_rows:
             e.set_option(_lib.OPT_TILE_ROWS, args.tile_rows)
         if args.warps:
             e.set_option(_lib.OPT_TB_WARPS, args.warps)
-        choice = [args.kernel, args.tile_rows, args.warps]
+        if args.depth:
+            e.set_option(_lib.OPT_TB_DEPTH, args.depth)
+        choice = [args.kernel, args.tile_rows, args.depth, args.warps]
     e.set_option(_lib.OPT_TIMING, 1)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -337,6 +341,7 @@ def run_ours(args, world, rank, local) -> None:
         "gpu_launches": int(launches),
         "roofline": roofline,
         "kernel_choice": choice,
+        "autotune_ms": tuned_ms,
         "clocks": clocks.summary(),
         "wall_ms_per_step": 1e3 * wall / args.steps,
     }  # fmt: skip
@@ -401,7 +406,8 @@ def kernel_roofline(e, p) -> dict:
                  "output_cells_per_launch": cells, "launch_ms": launch_ms, "launches_timed": launches,
                  "cpml_kernel": {"launch_ms": cp_ms / max(cp_launches, 1), "output_cells_per_launch": cp_cells},
                  "timing": "CUDA events around each launch, one extra run of the workload, kernels serialised"}
-        tag = f"k_tb_step_interior_{rows}x{128 if s == 4 else 64}" + ("" if warps == 8 else f"_{warps}w")
+        tag = (f"k_tb_step_interior_{rows}x{128 if s == 4 else 64}" + ("" if warps == 8 else f"_{warps}w")
+               + ("" if depth == (4 if s == 4 else 2) else f"_k{depth}"))
     elif kind in (3, 4):  # persistent kernels: the run's device time over its launches
         e.reset()
         e.advance(p.n_steps)
@@ -814,6 +820,7 @@ def main() -> None:
                     help="tuned: the autotuner picks kernel, tile rows, depth and warps (before timing)")
     ap.add_argument("--tile-rows", type=int, default=0, help="with a fixed --kernel: tile rows (0: its default)")
     ap.add_argument("--warps", type=int, default=0, help="with a fixed --kernel: warps per tile (0: 8)")
+    ap.add_argument("--depth", type=int, default=0, help="with a fixed --kernel: steps per launch (0: its default)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-device batched line")

@@ -87,6 +87,7 @@ SIGNATURES: dict[str, list] = {
     "etg_tb_advance_static": [i32, i32, i32, i64] + [vp] * 21 + [f64, f64, f64, i64],
     "etg_debug_set_wait_tries": [i64],
     "etg_sim_device_array": [vp, i32, vp, vp],
+    "etg_sim_set_db_nodes": [vp, vp],
 }
 
 

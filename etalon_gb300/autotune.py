@@ -21,9 +21,10 @@ from . import _lib
 
 # (kernel, tile rows, steps per launch, warps per tile); tile columns follow from the precision
 CANDIDATES = {
-    "single": [("tb", 48, 4, 8), ("tb", 64, 4, 8), ("tb", 40, 4, 8), ("tb", 48, 4, 16), ("tma", 40, 4, 8),
-               ("pipe", 48, 4, 8), ("plain", 0, 0, 8)],
-    "double": [("tb", 40, 2, 8), ("tb", 32, 2, 8), ("tma", 40, 2, 8), ("pipe", 40, 2, 8), ("plain", 0, 0, 8)],
+    "single": [("tb", 48, 4, 8), ("tb", 64, 4, 8), ("tb", 40, 4, 8), ("tb", 40, 8, 8), ("tb", 48, 4, 16),
+               ("tma", 40, 4, 8), ("pipe", 48, 4, 8), ("plain", 0, 0, 8)],
+    "double": [("tb", 40, 2, 8), ("tb", 32, 2, 8), ("tb", 32, 4, 8), ("tma", 40, 2, 8), ("pipe", 40, 2, 8),
+               ("plain", 0, 0, 8)],
 }  # fmt: skip
 
 
@@ -95,6 +96,12 @@ def tune(engine, *, steps: int = 96, reps: int = 3, use_cache: bool = True) -> t
     return choice
 
 
+def timings(engine) -> dict | None:
+    """The cached time (ms) of every candidate for this engine's grid, as ``tune`` measured them."""
+    entry = _load().get(key_of(engine))
+    return entry.get("ms") if entry else None
+
+
 def _get(engine, option: int) -> int:
     import ctypes as C
 
@@ -105,8 +112,8 @@ def _get(engine, option: int) -> int:
 
 # (tile rows, steps per launch, warps per tile)
 BATCH_CANDIDATES = {
-    "single": [(48, 4, 8), (40, 4, 8), (64, 4, 8), (48, 4, 16)],
-    "double": [(40, 2, 8), (32, 2, 8)],
+    "single": [(48, 4, 8), (40, 4, 8), (64, 4, 8), (48, 4, 16), (40, 8, 8)],
+    "double": [(40, 2, 8), (32, 2, 8), (32, 4, 8)],
 }  # fmt: skip
 
 

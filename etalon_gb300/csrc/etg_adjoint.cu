@@ -1070,6 +1070,8 @@ extern "C" {
 int etg_adj_create(etg_adj** out, etg_sim* sim, int i0, int nxd, int j0, int nyd) {
   ETG_REQUIRE(out && sim, ETG_ERR_ARGUMENT, "etg_adj_create: null argument");
   ETG_REQUIRE(nxd > 0 && nyd > 0, ETG_ERR_ARGUMENT, "etg_adj_create: empty design window");
+  ETG_REQUIRE(!sim->db_node, ETG_ERR_ARGUMENT,
+              "etg_adj_create: the adjoint is for TE runs; this simulation has per-node Hz coefficients (TM mode)");
   // the window with one cell of halo must lie in the unit rectangle, off the PEC edges
   const int rlo = std::max(sim->ux_lo, 1), rhi = std::min(sim->ux_hi, sim->nx);
   const int clo = std::max(sim->uy_lo, 1), chi = std::min(sim->uy_hi, sim->ny);

@@ -23,6 +23,7 @@ struct etg_batch {
   int4* d_tiles = nullptr;
   int n_inner = 0, n_pml = 0, tiles_er = 0, tiles_k = 0;
   int n_hot = 0;  // leading interior tiles with a source, monitor or trace node (the others: lean kernel)
+  std::vector<std::vector<int4>> hot_seen;  // per simulation: every such rectangle seen so far
   int64_t dft_work = 0;  // largest sampled monitor (frequencies x nodes) of any simulation
   int dft_mon = 0;       // most monitor components of any simulation
   int64_t** d_steps = nullptr;     // each simulation's step counter
@@ -30,7 +31,7 @@ struct etg_batch {
   cudaEvent_t fork = nullptr, join = nullptr, ev0 = nullptr, ev1 = nullptr, done = nullptr;
   cudaStream_t sides[4] = {};  // one branch per CPML kind, one for the interior tiles with a plan
   cudaEvent_t joins[4] = {};
-  int n_kind[3] = {};
+  int n_kind[6] = {};  // CPML tiles of each kind, then the leading ones of each with a plan
   int64_t opt[8] = {0, 0, 32, 0, 0, 0, 0, 0};
   std::map<int64_t, cudaGraphExec_t> graphs;
   double last_ms = 0;
@@ -101,7 +102,8 @@ int refresh(etg_batch* b, int ER, int K, bool* changed) {
   {
     // interior tiles holding a source, monitor or trace node (every simulation's) lead the
     // interior list and run the kernel with the per-step plan code; the rest run the lean one
-    std::vector<int4> inner, cold, pml;
+    std::vector<int4> inner, cold;
+    std::vector<std::pair<int4, bool>> pml;  // CPML tiles and whether they hold a plan node
     for (int k = 0; k < n; ++k) {
       etg_sim* s = b->sims[k];
       PhasePlan<T> ph, pe;
@@ -114,33 +116,49 @@ int refresh(etg_batch* b, int ER, int K, bool* changed) {
       }
       if (ph.trace.buf)
         hot.push_back(make_int4(ph.trace.ti0, ph.trace.tj0, ph.trace.ti0 + ph.trace.tnx, ph.trace.tj0 + ph.trace.tny));
+      // the union of those seen so far: runs with and without monitors or traces keep one list
+      if ((int)b->hot_seen.size() != n) b->hot_seen.assign(n, {});
+      tb_hot_union(&b->hot_seen[k], hot, 1024);
+      hot = b->hot_seen[k];
       std::vector<int2> t;
-      int ni = 0, nh = 0;
+      int ni = 0, nh = 0, kh[3] = {0, 0, 0};
       const int EC = 32 * (sizeof(T) == 4 ? 4 : 2);
-      tb_split_tiles(s->nx, s->ny, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi, ER, EC, K, hot, &t, &ni, &nh);
+      tb_split_tiles(s->nx, s->ny, s->ux_lo, s->ux_hi, s->uy_lo, s->uy_hi, ER, EC, K, hot, &t, &ni, &nh, kh);
+      int seen_of_kind[3] = {0, 0, 0};  // this simulation's CPML tiles come grouped by kind, plan tiles first
       for (int q = 0; q < (int)t.size(); ++q) {
         const int r0 = tb_tile_row(t[q]), c0 = t[q].y;  // output rows [r0, r0+ER-2K), columns [c0, c0+EC-2K)
+        const int kind = tb_tile_kind(t[q]);
+        const bool planned = q >= ni && seen_of_kind[kind - 1]++ < kh[kind - 1];
         if (r0 >= s->act_i1 || r0 + ER - 2 * K <= s->act_i0 || c0 >= s->act_j1 || c0 + EC - 2 * K <= s->act_j0)
           continue;
-        (q < nh ? inner : q < ni ? cold : pml).push_back(make_int4(k, r0, c0, tb_tile_kind(t[q])));
+        const int4 tile = make_int4(k, r0, c0, kind);
+        if (q < nh) inner.push_back(tile);
+        else if (q < ni) cold.push_back(tile);
+        else pml.emplace_back(tile, planned);
       }
     }
     const int n_hot = (int)inner.size();
     inner.insert(inner.end(), cold.begin(), cold.end());
-    // CPML tiles grouped by kind over every simulation (one kernel per kind)
-    std::stable_sort(pml.begin(), pml.end(), [](const int4& p, const int4& q) { return p.w < q.w; });
-    int n_kind[3] = {0, 0, 0};
-    for (const int4& q : pml) n_kind[q.w - 1] += 1;
+    // CPML tiles grouped by kind over every simulation (one kernel per kind), those with a plan
+    // leading their kind
+    std::stable_sort(pml.begin(), pml.end(), [](const std::pair<int4, bool>& p, const std::pair<int4, bool>& q) {
+      return p.first.w != q.first.w ? p.first.w < q.first.w : p.second > q.second;
+    });
+    int n_kind[6] = {0, 0, 0, 0, 0, 0};
+    for (const auto& q : pml) {
+      n_kind[q.first.w - 1] += 1;
+      n_kind[q.first.w + 2] += q.second;
+    }
     const int n_inner = (int)inner.size(), n_pml = (int)pml.size();
-    inner.insert(inner.end(), pml.begin(), pml.end());
+    for (const auto& q : pml) inner.push_back(q.first);
     const bool same = b->d_tiles && n_inner == b->n_inner && n_pml == b->n_pml && n_hot == b->n_hot &&
-                      inner.size() == b->h_tiles.size() &&
+                      memcmp(n_kind, b->n_kind, sizeof n_kind) == 0 && inner.size() == b->h_tiles.size() &&
                       memcmp(inner.data(), b->h_tiles.data(), inner.size() * sizeof(int4)) == 0;
     if (!same) {
       b->n_inner = n_inner;
       b->n_pml = n_pml;
       b->n_hot = n_hot;
-      for (int k = 0; k < 3; ++k) b->n_kind[k] = n_kind[k];
+      for (int k = 0; k < 6; ++k) b->n_kind[k] = n_kind[k];
       cudaFree(b->d_tiles);
       b->d_tiles = nullptr;
       int rc = etg_malloc((void**)&b->d_tiles, std::max<size_t>(1, inner.size()) * sizeof(int4));
@@ -245,6 +263,9 @@ int etg_batch_create(etg_batch** out, int n_sims, etg_sim* const* sims) {
     ETG_REQUIRE(sims[k], ETG_ERR_ARGUMENT, "etg_batch_create: simulation %d is null", k);
     ETG_REQUIRE(sims[k]->dtype == sims[0]->dtype, ETG_ERR_ARGUMENT, "etg_batch_create: mixed precisions");
     ETG_REQUIRE(sims[k]->have_coeffs, ETG_ERR_STATE, "etg_batch_create: simulation %d has no coefficients", k);
+    ETG_REQUIRE(!sims[k]->db_node, ETG_ERR_ARGUMENT,
+                "etg_batch_create: simulation %d has per-node Hz coefficients (TM mode), which only the "
+                "one-step kernels take; advance it on its own", k);
   }
   etg_batch* b = new etg_batch;
   b->sims.assign(sims, sims + n_sims);

@@ -104,7 +104,8 @@ __global__ void __launch_bounds__(128) k_fused_h(SimArgs<T> a, PhasePlan<T> plan
     const T px = add(mul(bx, psx), mul(cx, dey_dx));
     if (sy) a.psi_hz_y[row + j] = py;
     if (sx) a.psi_hz_x[row + j] = px;
-    hz.v[v] = add(hz.v[v], mul(a.db, sub(add(mul(dex_dy, a.iky_h[j]), py), add(mul(dey_dx, ikx), px))));
+    const T db = a.db_node ? a.db_node[row + j] : a.db;  // per node in TM mode
+    hz.v[v] = add(hz.v[v], mul(db, sub(add(mul(dex_dy, a.iky_h[j]), py), add(mul(dey_dx, ikx), px))));
   }
   const int64_t n = *a.step + step_off;
   apply_sources(plan, ETG_HZ, i, j0, n, hz.v, a.flag);

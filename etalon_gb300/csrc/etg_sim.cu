@@ -77,6 +77,7 @@ SimArgs<T> sim_args(etg_sim* s) {
   a.psi_hz_y = (T*)s->field[ETG_PSI_HZ_Y];
   a.cb_ex = (const T*)s->cb[0];
   a.cb_ey = (const T*)s->cb[1];
+  a.db_node = (const T*)s->db_node;
   const T** c[12] = {&a.bx_e, &a.cx_e, &a.ikx_e, &a.bx_h, &a.cx_h, &a.ikx_h,
                      &a.by_e, &a.cy_e, &a.iky_e, &a.by_h, &a.cy_h, &a.iky_h};
   for (int k = 0; k < 12; ++k) *c[k] = (const T*)s->c1d[k];
@@ -211,6 +212,7 @@ int advance_plain(etg_sim* s, int64_t n_steps) {
 template <typename T>
 int advance_dispatch(etg_sim* s, int64_t n_steps) {
   const int64_t kernel = s->opt[ETG_OPT_KERNEL];
+  if (s->db_node) return advance_plain<T>(s, n_steps);  // per-node db (TM mode): one-step kernels
   if (kernel == 2 || kernel == 3 || kernel == 4 || (kernel == 0 && tb_supported<T>(s->nx, s->ny))) {
     PhasePlan<T> ph, pe;  // the TMA kernel accumulates in place; the others sample per block
     int rc = build_plans<T>(s, &ph, &pe, kernel == 3 ? 0 : sim_sample_slots(s));
@@ -352,6 +354,7 @@ int etg_sim_destroy(etg_sim* s) {
   if (s->tb) tb_destroy(s->tb);
   for (void* p : s->field) cudaFree(p);
   for (void* p : s->cb) cudaFree(p);
+  cudaFree(s->db_node);
   for (void* p : s->c1d) cudaFree(p);
   for (Source& src : s->sources) cudaFree(src.table);
   for (Monitor& m : s->monitors) {
@@ -443,6 +446,18 @@ int etg_sim_set_cb_window(etg_sim* s, int which, int i0, int rows, int j0, int c
                                  cudaMemcpyHostToDevice, s->stream));
   ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
   return ETG_OK;
+}
+
+int etg_sim_set_db_nodes(etg_sim* s, const void* host) {
+  ETG_REQUIRE(s && host, ETG_ERR_ARGUMENT, "etg_sim_set_db_nodes: bad arguments");
+  if (!s->db_node) {
+    const size_t bytes = (size_t)s->rows * s->P * s->esize();
+    ETG_TRY_CUDA(cudaMalloc(&s->db_node, bytes));
+    ETG_TRY_CUDA(cudaMemset(s->db_node, 0, bytes));
+    invalidate_graphs(s);  // the pointer is a captured kernel parameter
+    if (s->tb) tb_invalidate(s->tb);
+  }
+  return copy_field_in(s, s->db_node, host, s->nx, s->ny);
 }
 
 int etg_sim_add_source(etg_sim* s, int component, int n_nodes, const int64_t* i, const int64_t* j,

@@ -61,6 +61,10 @@ struct SimArgs {
   const T *cb_ex, *cb_ey;
   const T *bx_e, *cx_e, *ikx_e, *bx_h, *cx_h, *ikx_h, *by_e, *cy_e, *iky_e, *by_h, *cy_h, *iky_h;
   T db, inv_dx, inv_dy;
+  // Per-node coefficient of the Hz-position update (pitched, nx rows of ny), replacing the
+  // scalar db where set: the 2D TM mode runs its Ez update there (dt / (eps0 eps_r) per node).
+  // nullptr for TE. Only the one-step kernels read it.
+  const T* db_node;
   // CPML strips: rows i < xs_lo or i >= xs_hi, columns j < ys_lo or j >= ys_hi carry psi;
   // everywhere else psi is exactly +0 and is neither read nor written.
   int xs_lo, xs_hi, ys_lo, ys_hi;
@@ -186,6 +190,7 @@ struct etg_sim {
   int64_t P = 0, rows = 0;
   void* field[7] = {};  // ETG_EX .. ETG_PSI_HZ_Y, pitched
   void* cb[2] = {};     // cb_ex, cb_ey, pitched
+  void* db_node = nullptr;  // per-node Hz-position coefficient (TM mode), pitched; nullptr for TE
   void* c1d[12] = {};   // bx_e cx_e ikx_e bx_h cx_h ikx_h by_e cy_e iky_e by_h cy_h iky_h
   double db = 0, inv_dx = 0, inv_dy = 0;
   bool have_coeffs = false;

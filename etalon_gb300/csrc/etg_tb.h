@@ -27,7 +27,8 @@ struct BatchSim {
 // and the interior tiles with a source, monitor or trace node each on a side stream, sides[0..3])
 // of the compiled shape with ER rows, depth K and NW warps; `sims` is a device array of
 // BatchSim<T>, `tiles` (sim, r0, c0, kind): interior tiles first (the n_hot with a plan
-// leading), then n_kind[0..2] tiles of kinds X, Y, XY.
+// leading), then n_kind[0..2] tiles of kinds X, Y, XY, of which the leading n_kind[3..5] have
+// a source, monitor or trace node (they run with the plan code on sides[3]).
 template <typename T>
 int tb_batch_pair(int ER, int K, int NW, const void* sims, const int4* tiles, int n_inner, int n_hot,
                   const int* n_kind, int parity, int step_off, cudaStream_t main, const cudaStream_t* sides,
@@ -41,9 +42,15 @@ void tb_batch_dft(const void* sims, int n_sims, int64_t max_work, int max_mon, i
 // Output tiles of one grid, interior tiles first; tiles meeting a `hot` rectangle lead each kind.
 // A CPML tile carries its kind (1: CPML across rows, 2: across columns, 3: both) in bits
 // 28-29 of .x (tb_tile_row and tb_tile_kind take it apart).
+// Adds to `into` the rectangles of `add` it lacks (restarting from `add` past `cap`); true if
+// any was new. Tile lists split on such a union keep a tile's kernel across runs with and
+// without monitors or traces.
+bool tb_hot_union(std::vector<int4>* into, const std::vector<int4>& add, size_t cap);
 // *n_hot (if given): the leading interior tiles that meet a `hot` rectangle.
+// *kind_hot (if given, three counts): the leading CPML tiles of each kind that meet one.
 void tb_split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_hi, int ER, int EC, int K,
-                    const std::vector<int4>& hot, std::vector<int2>* tiles, int* n_inner, int* n_hot = nullptr);
+                    const std::vector<int4>& hot, std::vector<int2>* tiles, int* n_inner, int* n_hot = nullptr,
+                    int* kind_hot = nullptr);
 
 inline int tb_tile_row(int2 t) { return t.x & ((1 << 28) - 1); }
 inline int tb_tile_kind(int2 t) { return t.x >> 28; }

@@ -128,6 +128,12 @@ int etg_sim_set_coefficients(etg_sim* sim, const void* cb_ex, const void* cb_ey,
 /* Replace a window of cb_ex (which = 0, array (nx, ny+1)) or cb_ey (which = 1, (nx+1, ny)):
  * rows [i0, i0+rows) x columns [j0, j0+cols) from a host array (rows, cols) in dtype. */
 int etg_sim_set_cb_window(etg_sim* sim, int which, int i0, int rows, int j0, int cols, const void* host);
+/* 2D TM mode (no counterpart in Etalon, which refuses TM: fdtd/capabilities.py:7-24). A TM run
+ * (Ez, Hx, Hy) is stepped as its dual TE run: Ez in the Hz array, -Hx in Ex, -Hy in Ey, with
+ * dt/mu0 as cb and dt/(eps0 eps_r) per Ez node in place of the scalar db. This uploads that
+ * per-node coefficient, (nx, ny) in TEState Hz layout; from then on the simulation advances
+ * with the one-step kernels, and batches and the adjoint refuse it. */
+int etg_sim_set_db_nodes(etg_sim* sim, const void* host);
 /* cb_ex and cb_ey rasterised on the device from a staircase of boxes (etalon/grid/materials.py:12-35
  * with the cast of etalon/fdtd/state.py:80-81): node (i, j) of Ex sits at x = x_min + (i + 0.5) dx,
  * y = y_min + j dy, of Ey at x = x_min + i dx, y = y_min + (j + 0.5) dy; it takes eps of the last

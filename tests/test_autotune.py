@@ -69,7 +69,9 @@ def test_every_candidate_names_a_known_kernel():
     for precision, cands in autotune.CANDIDATES.items():
         for kernel, rows, depth, warps in cands:
             assert kernel in ("tb", "tma", "pipe", "plain") and warps in (8, 16)
-            assert kernel == "plain" or depth == (4 if precision == "single" else 2)
+            # the depths compiled: 4 and 8 steps per launch (float32), 2 and 4 (float64)
+            assert kernel == "plain" or depth in ((4, 8) if precision == "single" else (2, 4))
+            assert kernel != "tb" or depth == (4 if precision == "single" else 2) or rows in (40, 32)
 
 
 class FakeBatch:

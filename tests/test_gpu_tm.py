@@ -1,0 +1,49 @@
+"""2D TM mode on the GPU against the direct TM oracle, bit for bit (needs a GPU).
+
+The engine steps a TM run as its dual TE run (etalon_gb300/tm.py) on the one-step kernels
+with a per-node Ez coefficient (etg_sim_set_db_nodes); oracle/tm_numpy.py writes the TM
+update directly and is pinned to the TE oracle by tests/test_tm_oracle.py.
+"""
+
+import numpy as np
+import pytest
+
+from etalon_gb300 import physics as ph
+from etalon_gb300 import tm
+from tests.test_tm_oracle import oracle_tm, raw, tm_case
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+@pytest.mark.parametrize("steps", [160, 37])
+def test_tm_engine_matches_tm_oracle(gpu, precision, steps):
+    boxes = [ph.Box((0.1, -0.05, 0.0), (0.7, 0.35, 0.22), 11.7)]
+    p = tm_case(precision, boxes=boxes, background_eps=2.085, n_steps=160)
+    o = oracle_tm(p)
+    o.run(steps)
+    with tm.TMEngine(p) as e:
+        e.advance(steps)
+        e.synchronize()
+        for name in o.FIELDS:
+            assert np.array_equal(raw(e.field(name)), raw(getattr(o, name))), name
+        for k in range(len(p.components)):
+            assert np.array_equal(raw(e.dft(k)), raw(o.acc[k])), f"accumulator {k} ({p.components[k]})"
+        res = e.result()
+        assert set(res) == {"point", "plane"} and set(res["plane"]) == {"Ez", "Hy"}
+        assert res["point"]["Ez"].shape == (2,)
+    assert np.abs(o.ez).max() > 0 and np.abs(o.hx).max() > 0
+
+
+def test_tm_runs_are_refused_by_batches_and_the_adjoint(gpu):
+    import ctypes as C
+
+    from etalon_gb300 import _lib
+
+    p = tm_case("single", n_steps=8)
+    with tm.TMEngine(p) as e:
+        h = C.c_void_p()
+        with pytest.raises(ValueError, match="TM mode"):
+            _lib.call("etg_batch_create", C.byref(h), 1, (C.c_void_p * 1)(e.te._h.value))
+        with pytest.raises(ValueError, match="TM mode"):
+            _lib.call("etg_adj_create", C.byref(h), e.te._h, 20, 4, 20, 4)

@@ -19,9 +19,14 @@ def _problems(precision):
 
 @pytest.mark.parametrize("precision", ["single", "double"])
 @pytest.mark.parametrize("steps", [(600,), (1, 7, 8, 9, 63, 64, 65, 383)])
-def test_batch_equals_individual_runs(gpu, precision, steps):
+@pytest.mark.parametrize("deep", [False, True])
+def test_batch_equals_individual_runs(gpu, precision, steps, deep):
+    """Deep: K = 8 (float32) or 4 (float64) steps per launch instead of the default 4 or 2."""
     problems = _problems(precision)
     batch = Batch(problems)
+    if deep:
+        batch.set_option(_lib.OPT_TB_DEPTH, 8 if precision == "single" else 4)
+        batch.set_option(_lib.OPT_TILE_ROWS, 40 if precision == "single" else 32)
     for k in steps:
         batch.advance(k)
     batch.synchronize()

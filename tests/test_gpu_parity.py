@@ -343,13 +343,15 @@ def test_config2_full_length_matches_reference(gpu, precision):
     assert compare_outputs(g, *engine_outputs(e)) == []
 
 
-@pytest.mark.parametrize("precision", PRECISIONS)
-def test_config2_prefix_vs_live_oracle(gpu, precision):
+@pytest.mark.parametrize(("precision", "depth"), [("single", 0), ("single", 8), ("double", 0), ("double", 4)])
+def test_config2_prefix_vs_live_oracle(gpu, precision, depth):
     """The headline grid for 120 steps against the oracle run on this host's cores, in raw
-    bits (signs of zeros included)."""
+    bits (signs of zeros included), with the default depth and with the deeper one."""
     n = 120
     p = cases.config2(precision, n_steps=n)
     e = TEEngine(p)
+    if depth:
+        e.set_option(_lib.OPT_TB_DEPTH, depth)
     e.advance(n)
     o = _oracle_for(p)
     workers = min(16, os.cpu_count() or 1)
@@ -374,8 +376,8 @@ def _oracle_for(p):
 
 # ----------------------------------------------------------------- temporal blocking
 
-TB_SHAPES_F32 = [(40, 128, 4), (48, 128, 4), (64, 128, 4), (48, 128, 4, 16)]  # (rows, cols, K[, warps])
-TB_SHAPES_F64 = [(32, 64, 2), (40, 64, 2)]
+TB_SHAPES_F32 = [(40, 128, 4), (48, 128, 4), (64, 128, 4), (48, 128, 4, 16), (40, 128, 8)]  # (rows, cols, K[, warps])
+TB_SHAPES_F64 = [(32, 64, 2), (40, 64, 2), (32, 64, 4)]
 
 
 def _tb_engine(name, precision, g, shape, kernel="tb", **kw):
@@ -433,11 +435,11 @@ def test_tma_seams_and_config2_prefix(gpu, precision):
         np.testing.assert_array_equal(e.dft(k), acc)
 
 
-@pytest.mark.parametrize("precision", PRECISIONS)
-def test_tb_seams_and_remainders(gpu, precision):
+@pytest.mark.parametrize(("precision", "shape"), [("single", (40, 128, 4)), ("single", (40, 128, 8)),
+                                                  ("double", (40, 64, 2)), ("double", (32, 64, 4))])
+def test_tb_seams_and_remainders(gpu, precision, shape):
     """Blocks of 1, 2K−1, 2K, 2K+1 … steps (TB pairs, graph replays, one-step remainders) agree."""
     g = load("g4_full", precision)
-    shape = (40, 128, 4) if precision == "single" else (40, 64, 2)
     a, n = _tb_engine("g4_full", precision, g, shape)
     a.advance(n)
     b, _ = _tb_engine("g4_full", precision, g, shape, graph_steps=16)

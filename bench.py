@@ -365,6 +365,8 @@ def run_ours(args, world, rank, local) -> None:
     if not args.no_fp64:
         out["fp64"] = fp64_line(args, local)
     if rank == 0 and not args.no_studio:
+        out["tm"] = tm_line(args)
+    if rank == 0 and not args.no_studio:
         out["studio"] = studio_line(e, p)
         out["rasterize"] = rasterize_line(e, p)
     if rank == 0:
@@ -681,6 +683,7 @@ def fp64_line(args, local) -> dict:
     p = workload("double", args.time_steps)
     e = TEEngine(p, kernel="auto" if args.kernel == "tuned" else args.kernel)
     choice = list(autotune.tune(e)) if args.kernel == "tuned" else [args.kernel]
+    tuned_ms = autotune.timings(e) if args.kernel == "tuned" else None
     e.set_option(_lib.OPT_TIMING, 1)
     e.advance(p.n_steps)
     ms = []
@@ -691,7 +694,43 @@ def fp64_line(args, local) -> dict:
         ms.append(e.last_timing()[0])
     e.close()
     t = sum(ms) / len(ms)
-    return {"value": p.grid.n_cells * p.n_steps / (t / 1e3), "unit": UNIT, "ms_per_step": t, "kernel_choice": choice}
+    return {"value": p.grid.n_cells * p.n_steps / (t / 1e3), "unit": UNIT, "ms_per_step": t, "kernel_choice": choice,
+            "autotune_ms": tuned_ms}
+
+
+def tm_line(args) -> dict:
+    """The 2D TM mode on the headline grid: 2000² + 12-layer CPML, the Si strip along x in oxide,
+    an Ez point current in the core, 3 point monitors × 16 wavelengths, fp32, 2000 steps; the
+    dual TE run on the one-step kernels, device time per step."""
+    import torch
+
+    from etalon_gb300 import _lib
+    from etalon_gb300 import physics as ph
+    from etalon_gb300 import tm
+    from tests import cases
+
+    steps = 2000
+    wl = list(np.linspace(1.5, 1.6, 16))
+    p = tm.tm_problem(
+        size=(40.0, 40.0), dl=0.02, background_eps=cases.EPS_OXIDE,
+        boxes=[ph.Box((0.0, 0.0, 0.0), (42.0, 0.5, 0.22), cases.EPS_SILICON)], pml=ph.PMLSpec(layers=12),
+        sources=[tm.TMPointSource((-15.0, 0.0, 0.0), ph.GaussianPulse(1.55, 0.5))],
+        monitors=[ph.DFTMonitor(f"m{k}", wl, center=(x, 0.0, 0.0)) for k, x in enumerate((-5.0, 5.0, 15.0))],
+        n_steps=steps, precision="single",
+    )  # fmt: skip
+    e = tm.TMEngine(p)
+    e.te.set_option(_lib.OPT_TIMING, 1)
+    e.advance(200)
+    ms = []
+    for _ in range(2):
+        e.reset()
+        torch.cuda.synchronize()
+        e.advance(steps)
+        ms.append(e.te.last_timing()[0])
+    e.close()
+    t = min(ms)
+    return {"value": p.grid.n_cells * steps / (t / 1e3), "unit": UNIT, "time_steps": steps,
+            "grid": [p.grid.nx, p.grid.ny], "path": "dual TE run, one-step fused kernels, per-node Ez coefficient"}  # fmt: skip
 
 
 # ----------------------------------------------------------------------------- next rows

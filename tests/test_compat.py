@@ -15,7 +15,14 @@ import pytest
 from etalon_gb300 import physics as ph
 from tests import cases
 
-REF = os.environ.get("ETALON_SRC", "/root/reference")
+def _etalon_tree() -> str:
+    """Etalon's source tree: $ETALON_SRC, else the checkout the oracle's build recipe reads."""
+    from oracle import build_ref
+
+    return os.environ.get("ETALON_SRC") or str(build_ref.DEFAULT_TREE)
+
+
+REF = _etalon_tree()
 
 
 @pytest.fixture(scope="module")

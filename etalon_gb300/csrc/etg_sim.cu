@@ -211,14 +211,18 @@ int advance_plain(etg_sim* s, int64_t n_steps) {
 
 template <typename T>
 int advance_dispatch(etg_sim* s, int64_t n_steps) {
-  const int64_t kernel = s->opt[ETG_OPT_KERNEL];
-  if (s->db_node) return advance_plain<T>(s, n_steps);  // per-node db (TM mode): one-step kernels
+  int64_t opt[8];
+  memcpy(opt, s->opt, sizeof opt);
+  // per-node db (TM mode): the TMA-fed kernels stage cb themselves and do not take it, so such a
+  // simulation runs the plain temporally blocked kernel instead
+  if (s->db_node && (opt[ETG_OPT_KERNEL] == 3 || opt[ETG_OPT_KERNEL] == 4)) opt[ETG_OPT_KERNEL] = 2;
+  const int64_t kernel = opt[ETG_OPT_KERNEL];
   if (kernel == 2 || kernel == 3 || kernel == 4 || (kernel == 0 && tb_supported<T>(s->nx, s->ny))) {
     PhasePlan<T> ph, pe;  // the TMA kernel accumulates in place; the others sample per block
     int rc = build_plans<T>(s, &ph, &pe, kernel == 3 ? 0 : sim_sample_slots(s));
     if (rc) return rc;
     if (!s->tb) s->tb = tb_create();
-    return tb_advance<T>(s->tb, sim_args<T>(s), ph, pe, n_steps, s->opt, s->stream);
+    return tb_advance<T>(s->tb, sim_args<T>(s), ph, pe, n_steps, opt, s->stream);
   }
   return advance_plain<T>(s, n_steps);
 }

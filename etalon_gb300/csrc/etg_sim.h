@@ -63,7 +63,7 @@ struct SimArgs {
   T db, inv_dx, inv_dy;
   // Per-node coefficient of the Hz-position update (pitched, nx rows of ny), replacing the
   // scalar db where set: the 2D TM mode runs its Ez update there (dt / (eps0 eps_r) per node).
-  // nullptr for TE. Only the one-step kernels read it.
+  // nullptr for TE. The one-step and the temporally blocked kernels read it (not the TMA-fed).
   const T* db_node;
   // CPML strips: rows i < xs_lo or i >= xs_hi, columns j < ys_lo or j >= ys_hi carry psi;
   // everywhere else psi is exactly +0 and is neither read nor written.

@@ -557,12 +557,13 @@ void tb_adj_ctl_add(int64_t* ctl, int64_t delta, cudaStream_t s) {
 
 // ------------------------------------------------------------------------ host side
 
-// Compiled shapes: the forward's default tile of each dtype.
+// Compiled shapes: 40-row tiles of 8 steps (float32: the forward's deep tile, which also
+// shortened the reverse sweep, config-5 batch 1.87 s to 1.78 s) and of 2 steps (float64).
 template <typename T>
 struct AdjCfg;
 template <>
 struct AdjCfg<float> {
-  static constexpr int RPT = 5, K = 4;
+  static constexpr int RPT = 5, K = 8;
 };
 template <>
 struct AdjCfg<double> {

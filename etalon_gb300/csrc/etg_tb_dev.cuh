@@ -21,6 +21,7 @@ struct TBVec<float> {
     *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
   }
   __device__ __forceinline__ void zero() { v[0] = v[1] = v[2] = v[3] = 0.f; }
+  __device__ __forceinline__ void fill(float x) { v[0] = v[1] = v[2] = v[3] = x; }
 };
 template <>
 struct TBVec<double> {
@@ -34,6 +35,7 @@ struct TBVec<double> {
     *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
   }
   __device__ __forceinline__ void zero() { v[0] = v[1] = 0.0; }
+  __device__ __forceinline__ void fill(double x) { v[0] = v[1] = x; }
 };
 
 template <typename T>

@@ -198,6 +198,9 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
     z.st(sEyX + NW * EC + lj0);  // the row below the tile
   }
 
+  // TM mode (the dual TE run of a TM run): cb_ex and cb_ey both hold dt/mu0, so the cb_ey plane
+  // carries the per-node Hz-position coefficient instead, and the Ey update reads cb_ex's plane
+  const bool tm = !STAGED && a.db_node != nullptr;
   // load the extended tile: fields to registers, cb (and psi) to shared memory
   Vw ex[RPT], ey[RPT], hz[RPT];
 #pragma unroll
@@ -218,7 +221,7 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
       ey[t].ld(a.ey + g);
       hz[t].ld(a.hz + g);
       cx.ld(a.cb_ex + g);
-      cy.ld(a.cb_ey + g);
+      cy.ld((tm ? a.db_node : a.cb_ey) + g);
     } else {
       ex[t].zero();
       ey[t].zero();
@@ -325,6 +328,9 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
         for (int t = 0; t < RPT; ++t) {
           T exr = __shfl_down_sync(0xffffffffu, ex[t].v[0], 1);
           if (lane == 31) exr = zero<T>();
+          Vw dbr;  // this row's Hz-position coefficients: the scalar db, or per node in TM mode
+          if (tm) dbr.ld(sCby + (lr0 + t) * EC + lj0);
+          else dbr.fill(db);
           // CPML tiles: this row's psi as one 16-byte vector per lane. Outside the strips psi
           // is +0 and its update b*0 + 0*d is +0 again, so whole vectors go back unchanged there.
           const int ir = i0 + t;
@@ -339,8 +345,8 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
             const T dex_dy = mul(sub(exn, ex[t].v[e]), idy);
             const T dey_dx = mul(sub(eyn, ey[t].v[e]), idx);
             if (!PML) {
-              if (KEEP0) hz[t].v[e] = add(hz[t].v[e], mul(db, sub(add(dex_dy, zero<T>()), add(dey_dx, zero<T>()))));
-              else hz[t].v[e] = add(hz[t].v[e], mul(db, sub(dex_dy, dey_dx)));
+              if (KEEP0) hz[t].v[e] = add(hz[t].v[e], mul(dbr.v[e], sub(add(dex_dy, zero<T>()), add(dey_dx, zero<T>()))));
+              else hz[t].v[e] = add(hz[t].v[e], mul(dbr.v[e], sub(dex_dy, dey_dx)));
             } else {
               // computed for every cell and kept only inside the domain: selects, not branches,
               // so the cells of a row stay independent instructions
@@ -361,7 +367,7 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
                   tx_ = add(mul(dey_dx, kxh[t]), zero<T>());
                 }
               }
-              const T h1 = add(hz[t].v[e], mul(db, sub(ty_, tx_)));
+              const T h1 = add(hz[t].v[e], mul(dbr.v[e], sub(ty_, tx_)));
               hz[t].v[e] = in ? h1 : hz[t].v[e];
             }
           }
@@ -409,7 +415,7 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
           if (lane == 0) hzl = zero<T>();
           Vw cx, cy;
           cx.ld(sCbx + (lr0 + t) * EC + lj0);
-          cy.ld(sCby + (lr0 + t) * EC + lj0);
+          cy.ld((tm ? sCbx : sCby) + (lr0 + t) * EC + lj0);
           const int ir = i0 + t;
           const bool xrow = KIND == KIND_XY || ir < a.xs_lo || ir >= a.xs_hi;
           Vw pyv, pxv;  // psi_ex_y, psi_ey_x of this row (CPML tiles)

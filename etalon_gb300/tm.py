@@ -19,7 +19,8 @@ right after the Ez update, with Etalon's bilinear weights (etalon/fdtd/sources.p
 coefficient dt/(eps0 eps_r) w/(dx dy). Monitors of Ez are Fourier sums at (n+1/2) dt, of Hx, Hy
 at (n+1) dt, as Etalon's H and E monitors of the dual run.
 
-The dual run takes the one-step kernels (the per-node Ez coefficient is read there only);
+The dual run takes the temporally blocked kernels (in their tiles the cb_ey plane, which in
+TM mode would only repeat dt/mu0, carries the per-node Ez coefficient) or the one-step ones;
 batches and the adjoint are for TE.
 """
 

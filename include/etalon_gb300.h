@@ -132,7 +132,8 @@ int etg_sim_set_cb_window(etg_sim* sim, int which, int i0, int rows, int j0, int
  * (Ez, Hx, Hy) is stepped as its dual TE run: Ez in the Hz array, -Hx in Ex, -Hy in Ey, with
  * dt/mu0 as cb and dt/(eps0 eps_r) per Ez node in place of the scalar db. This uploads that
  * per-node coefficient, (nx, ny) in TEState Hz layout; from then on the simulation advances
- * with the one-step kernels, and batches and the adjoint refuse it. */
+ * with the one-step or the temporally blocked kernels (a TMA-fed kernel choice falls back to
+ * the plain blocked one), and batches and the adjoint refuse it. */
 int etg_sim_set_db_nodes(etg_sim* sim, const void* host);
 /* cb_ex and cb_ey rasterised on the device from a staircase of boxes (etalon/grid/materials.py:12-35
  * with the cast of etalon/fdtd/state.py:80-81): node (i, j) of Ex sits at x = x_min + (i + 0.5) dx,

@@ -141,3 +141,38 @@ def test_config3_every_device_vs_live_oracle(gpu):
                     assert np.array_equal(e.dft(k).view(np.uint8), acc.view(np.uint8))
     finally:
         batch.close()
+
+
+def test_config3_devices_full_length_vs_live_oracle(gpu):
+    """Three devices of the batched workload — the smallest, one of middle size and the largest
+    — at the full 5000 steps inside the 64-device batch (the batch tuner's shape), each
+    bit-identical to the oracle run on the host's cores for all 5000 steps."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+
+    from etalon_gb300 import autotune
+    from tests.test_gpu_parity import _oracle_for
+
+    n = 5000
+    problems = cases.synthetic_batch(64, n_steps=n)
+    sizes = [p.grid.n_cells for p in problems]
+    order = sorted(range(len(problems)), key=sizes.__getitem__)
+    picked = [order[0], order[len(order) // 2], order[-1]]
+    batch = Batch(problems)
+    try:
+        autotune.tune_batch(batch, steps=32, reps=1)
+        batch.advance(n)
+        batch.synchronize()
+        workers = min(16, os.cpu_count() or 1)
+        with ThreadPoolExecutor(workers) as pool:
+            for q in picked:
+                p, e = problems[q], batch.engines[q]
+                o = _oracle_for(p)
+                o.run(n, pool=pool, bands=workers)
+                for f in FIELDS:
+                    assert np.array_equal(e.field(f).view(np.uint8), getattr(o, f).view(np.uint8)), (q, f)
+                for k, acc in enumerate(o.acc):
+                    assert np.array_equal(e.dft(k).view(np.uint8), acc.view(np.uint8)), (q, k)
+                assert np.abs(o.hz).max() > 0
+    finally:
+        batch.close()

@@ -17,12 +17,19 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("precision", ["single", "double"])
 @pytest.mark.parametrize("steps", [160, 37])
-def test_tm_engine_matches_tm_oracle(gpu, precision, steps):
+@pytest.mark.parametrize(("kernel", "deep"), [("plain", False), ("tb", False), ("tb", True), ("tma", False)])
+def test_tm_engine_matches_tm_oracle(gpu, precision, steps, kernel, deep):
+    """One-step and temporally blocked kernels (default and deep tiles; a TMA-fed choice runs
+    the plain blocked kernel), 37 steps ending in one-step remainders."""
+    from etalon_gb300 import _lib
+
     boxes = [ph.Box((0.1, -0.05, 0.0), (0.7, 0.35, 0.22), 11.7)]
     p = tm_case(precision, boxes=boxes, background_eps=2.085, n_steps=160)
     o = oracle_tm(p)
     o.run(steps)
-    with tm.TMEngine(p) as e:
+    with tm.TMEngine(p, kernel=kernel) as e:
+        if deep:
+            e.te.set_option(_lib.OPT_TB_DEPTH, 8 if precision == "single" else 4)
         e.advance(steps)
         e.synchronize()
         for name in o.FIELDS:

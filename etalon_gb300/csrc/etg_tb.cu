@@ -663,32 +663,33 @@ bool tb_supported(int nx, int ny) {
   return nx >= 64 && ny >= 64;
 }
 
-template <typename T, int RPT, int K, bool PML, int NW = 8, bool PLAN = true>
+template <typename T, int RPT, int K, bool PML, int NW = 8, bool PLAN = true, bool TMM = false>
 static cudaError_t tb_launch_one(const SimArgs<T>& a, const TBDst<T>& d, const int2* tiles, int n,
                                  const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                  cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  k_tb_step<T, RPT, K, PML, NW, PLAN><<<n, dim3(32, NW), tb_smem<T, RPT, K, PML, NW>(), s>>>(a, d, tiles, ph, pe,
-                                                                                           step_off);
+  k_tb_step<T, RPT, K, PML, NW, PLAN, TMM><<<n, dim3(32, NW), tb_smem<T, RPT, K, PML, NW>(), s>>>(a, d, tiles, ph,
+                                                                                                pe, step_off);
   g_launches += 1;
   return cudaGetLastError();
 }
 
 // CPML tiles of one kind: the leading n_hot (sources, monitors, traces) with the plan code on
 // `hot_stream`, the rest with the lean body on `stream`.
-template <typename T, int RP, int K, int KIND>
+template <typename T, int RP, int K, int KIND, bool TMM = false>
 static cudaError_t tb_launch_kind(const SimArgs<T>& a, const TBDst<T>& d, const int2* t, int n, int n_hot,
                                   const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off, cudaStream_t stream,
                                   cudaStream_t hot_stream) {
   constexpr size_t SMEM = TBShape<T, RP, K, KIND>::SMEM;
   if (n_hot) {
-    k_tb_kind<T, RP, K, KIND, 8, true><<<n_hot, dim3(32, 8), SMEM, hot_stream>>>(a, d, t, ph, pe, step_off);
+    k_tb_kind<T, RP, K, KIND, 8, true, TMM><<<n_hot, dim3(32, 8), SMEM, hot_stream>>>(a, d, t, ph, pe, step_off);
     g_launches += 1;
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   if (n > n_hot) {
-    k_tb_kind<T, RP, K, KIND, 8, false><<<n - n_hot, dim3(32, 8), SMEM, stream>>>(a, d, t + n_hot, ph, pe, step_off);
+    k_tb_kind<T, RP, K, KIND, 8, false, TMM><<<n - n_hot, dim3(32, 8), SMEM, stream>>>(a, d, t + n_hot, ph, pe,
+                                                                                      step_off);
     g_launches += 1;
     return cudaGetLastError();
   }
@@ -697,22 +698,24 @@ static cudaError_t tb_launch_kind(const SimArgs<T>& a, const TBDst<T>& d, const 
 
 // CPML tiles, one kernel per kind on its own side stream side[0..2], the tiles of each kind with
 // a plan on side[3] (tiles sorted X, Y, XY from `tiles`; n_kind: three counts, three hot counts).
-template <typename T, int RP, int K>
+template <typename T, int RP, int K, bool TMM = false>
 static cudaError_t tb_launch_kinds(const SimArgs<T>& a, const TBDst<T>& d, const int2* tiles, const int* n_kind,
                                    const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                    cudaStream_t const* side) {
-  cudaError_t e = tb_launch_kind<T, RP, K, KIND_X>(a, d, tiles, n_kind[0], n_kind[3], ph, pe, step_off, side[0],
-                                                   side[3]);
+  cudaError_t e = tb_launch_kind<T, RP, K, KIND_X, TMM>(a, d, tiles, n_kind[0], n_kind[3], ph, pe, step_off,
+                                                        side[0], side[3]);
   tiles += n_kind[0];
   if (e == cudaSuccess)
-    e = tb_launch_kind<T, RP, K, KIND_Y>(a, d, tiles, n_kind[1], n_kind[4], ph, pe, step_off, side[1], side[3]);
+    e = tb_launch_kind<T, RP, K, KIND_Y, TMM>(a, d, tiles, n_kind[1], n_kind[4], ph, pe, step_off, side[1],
+                                              side[3]);
   tiles += n_kind[1];
   if (e == cudaSuccess)
-    e = tb_launch_kind<T, RP, K, KIND_XY>(a, d, tiles, n_kind[2], n_kind[5], ph, pe, step_off, side[2], side[3]);
+    e = tb_launch_kind<T, RP, K, KIND_XY, TMM>(a, d, tiles, n_kind[2], n_kind[5], ph, pe, step_off, side[2],
+                                               side[3]);
   return e;
 }
 
-template <typename T, int RPT, int K, int NW = 8>
+template <typename T, int RPT, int K, int NW = 8, bool TMM = false>
 static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<T>& d,
                                   const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                   cudaStream_t s) {
@@ -722,7 +725,7 @@ static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<
   const int n_cold = tb->n_inner - tb->n_hot;
   if (tb->profile) {  // one after the other on s, an event pair around each kernel
     cudaError_t e = cudaEventRecord(tb->pev[0], s);
-    if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW, false>(a, d, cold, n_cold, ph, pe, step_off, s);
+    if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW, false, TMM>(a, d, cold, n_cold, ph, pe, step_off, s);
     const int2* t = tb->tiles + tb->n_inner;
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
       int only[6] = {0, 0, 0, 0, 0, 0};
@@ -731,12 +734,12 @@ static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<
       e = cudaEventRecord(tb->pev[1 + k], s);
       if (e == cudaSuccess) {
         cudaStream_t ss[4] = {s, s, s, s};
-        e = tb_launch_kinds<T, RP, K>(a, d, t, only, ph, pe, step_off, ss);
+        e = tb_launch_kinds<T, RP, K, TMM>(a, d, t, only, ph, pe, step_off, ss);
       }
       t += tb->n_kind[k];
     }
     if (e == cudaSuccess) e = cudaEventRecord(tb->pev[4], s);
-    if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW, true>(a, d, hot, tb->n_hot, ph, pe, step_off, s);
+    if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW, true, TMM>(a, d, hot, tb->n_hot, ph, pe, step_off, s);
     if (e == cudaSuccess) e = cudaEventRecord(tb->pev[5], s);
     if (e == cudaSuccess) e = cudaEventSynchronize(tb->pev[5]);
     float m[5] = {};
@@ -753,10 +756,10 @@ static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<
   cudaError_t e = cudaEventRecord(tb->fork, s);
   for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(tb->sides[k], tb->fork, 0);
   if (e == cudaSuccess)
-    e = tb_launch_kinds<T, RP, K>(a, d, tb->tiles + tb->n_inner, tb->n_kind, ph, pe, step_off, tb->sides);
+    e = tb_launch_kinds<T, RP, K, TMM>(a, d, tb->tiles + tb->n_inner, tb->n_kind, ph, pe, step_off, tb->sides);
   if (e == cudaSuccess)
-    e = tb_launch_one<T, RPT, K, false, NW, true>(a, d, hot, tb->n_hot, ph, pe, step_off, tb->sides[3]);
-  if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW, false>(a, d, cold, n_cold, ph, pe, step_off, s);
+    e = tb_launch_one<T, RPT, K, false, NW, true, TMM>(a, d, hot, tb->n_hot, ph, pe, step_off, tb->sides[3]);
+  if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW, false, TMM>(a, d, cold, n_cold, ph, pe, step_off, s);
   for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
     e = cudaEventRecord(tb->joins[k], tb->sides[k]);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, tb->joins[k], 0);
@@ -787,6 +790,11 @@ template <typename T, int RPT, int K, int NW = 8>
 static cudaError_t tb_two(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& ph,
                           const PhasePlan<T>& pe, int step_off, cudaStream_t s) {
   const SimArgs<T> b = swap_args(a, tb);
+  if (a.db_node) {  // TM mode: the kernels that read the per-node coefficient
+    cudaError_t e = tb_launch_pair<T, RPT, K, NW, true>(tb, a, as_dst(b), ph, pe, step_off, s);
+    if (e == cudaSuccess) e = tb_launch_pair<T, RPT, K, NW, true>(tb, b, as_dst(a), ph, pe, step_off + K, s);
+    return e;
+  }
   cudaError_t e = tb_launch_pair<T, RPT, K, NW>(tb, a, as_dst(b), ph, pe, step_off, s);
   if (e == cudaSuccess) e = tb_launch_pair<T, RPT, K, NW>(tb, b, as_dst(a), ph, pe, step_off + K, s);
   return e;
@@ -795,26 +803,43 @@ static cudaError_t tb_two(TBState* tb, const SimArgs<T>& a, const PhasePlan<T>& 
 // Dynamic shared memory above 48 KB must be allowed per kernel, before any launch or capture.
 template <typename T, int RPT, int K, int NW = 8>
 static cudaError_t tb_attrs() {
-  cudaError_t e = cudaFuncSetAttribute(k_tb_step<T, RPT, K, false, NW, true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb_smem<T, RPT, K, false, NW>());
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_tb_step<T, RPT, K, false, NW, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  constexpr int RP = RPT * NW / 8;
+  cudaError_t e = cudaSuccess;
+#define ETG_STEP_ATTR(PL, TM)                                                                                   \
+  if (e == cudaSuccess)                                                                                        \
+    e = cudaFuncSetAttribute(k_tb_step<T, RPT, K, false, NW, PL, TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                              (int)tb_smem<T, RPT, K, false, NW>());
+#define ETG_KIND_ATTR(KD, PL, TM)                                                                               \
+  if (e == cudaSuccess)                                                                                        \
+    e = cudaFuncSetAttribute(k_tb_kind<T, RP, K, KD, 8, PL, TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             (int)TBShape<T, RP, K, KD>::SMEM);
+  for (const bool tm : {false, true}) {
+    // the TM variants (TMM) are separate kernels; both are allowed their shared memory up front
+    if (tm) {
+      ETG_STEP_ATTR(true, true)
+      ETG_STEP_ATTR(false, true)
+      ETG_KIND_ATTR(KIND_X, true, true)
+      ETG_KIND_ATTR(KIND_X, false, true)
+      ETG_KIND_ATTR(KIND_Y, true, true)
+      ETG_KIND_ATTR(KIND_Y, false, true)
+      ETG_KIND_ATTR(KIND_XY, true, true)
+      ETG_KIND_ATTR(KIND_XY, false, true)
+    } else {
+      ETG_STEP_ATTR(true, false)
+      ETG_STEP_ATTR(false, false)
+      ETG_KIND_ATTR(KIND_X, true, false)
+      ETG_KIND_ATTR(KIND_X, false, false)
+      ETG_KIND_ATTR(KIND_Y, true, false)
+      ETG_KIND_ATTR(KIND_Y, false, false)
+      ETG_KIND_ATTR(KIND_XY, true, false)
+      ETG_KIND_ATTR(KIND_XY, false, false)
+    }
+  }
+#undef ETG_STEP_ATTR
+#undef ETG_KIND_ATTR
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_tb_step<T, RPT * NW / 8, K, true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)tb_smem<T, RPT * NW / 8, K, true, 8>());
-  constexpr int RP = RPT * NW / 8;
-#define ETG_KIND_ATTR(KD, PL)                                                                                   \
-  if (e == cudaSuccess)                                                                                        \
-    e = cudaFuncSetAttribute(k_tb_kind<T, RP, K, KD, 8, PL>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             (int)TBShape<T, RP, K, KD>::SMEM);
-  ETG_KIND_ATTR(KIND_X, true)
-  ETG_KIND_ATTR(KIND_X, false)
-  ETG_KIND_ATTR(KIND_Y, true)
-  ETG_KIND_ATTR(KIND_Y, false)
-  ETG_KIND_ATTR(KIND_XY, true)
-  ETG_KIND_ATTR(KIND_XY, false)
-#undef ETG_KIND_ATTR
   return e;
 }
 

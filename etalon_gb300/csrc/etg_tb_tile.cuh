@@ -118,8 +118,11 @@ struct TBNoHook {
 // the tile skips the per-step source, monitor and trace code altogether. Without it the
 // interior kernel fits 128 registers with no spills, which makes its launches about 15 %
 // shorter; the tile lists put such tiles after the others, so each part is its own launch.
+// TMM (the dual TE run of a TM run, compiled separately so TE kernels carry none of it):
+// cb_ex and cb_ey both hold dt/mu0, so the cb_ey plane of the tile carries the per-node
+// Hz-position coefficient (SimArgs::db_node) and the Ey update reads the cb_ex plane.
 template <typename T, int RPT, int K, int KIND, bool STAGED = false, typename Hook = TBNoHook, int NW = 8,
-          bool PLAN = true>
+          bool PLAN = true, bool TMM = false>
 __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst, const int2 tile,
                                         const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                         const T* stage = nullptr, T* cb_s = nullptr, T* xch_s = nullptr,
@@ -198,9 +201,8 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
     z.st(sEyX + NW * EC + lj0);  // the row below the tile
   }
 
-  // TM mode (the dual TE run of a TM run): cb_ex and cb_ey both hold dt/mu0, so the cb_ey plane
-  // carries the per-node Hz-position coefficient instead, and the Ey update reads cb_ex's plane
-  const bool tm = !STAGED && a.db_node != nullptr;
+  static_assert(!(TMM && STAGED), "the staged kernels take cb by TMA, not the TM coefficient");
+  constexpr bool tm = TMM;
   // load the extended tile: fields to registers, cb (and psi) to shared memory
   Vw ex[RPT], ey[RPT], hz[RPT];
 #pragma unroll
@@ -329,7 +331,7 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
           T exr = __shfl_down_sync(0xffffffffu, ex[t].v[0], 1);
           if (lane == 31) exr = zero<T>();
           Vw dbr;  // this row's Hz-position coefficients: the scalar db, or per node in TM mode
-          if (tm) dbr.ld(sCby + (lr0 + t) * EC + lj0);
+          if constexpr (tm) dbr.ld(sCby + (lr0 + t) * EC + lj0);
           else dbr.fill(db);
           // CPML tiles: this row's psi as one 16-byte vector per lane. Outside the strips psi
           // is +0 and its update b*0 + 0*d is +0 again, so whole vectors go back unchanged there.
@@ -541,20 +543,20 @@ constexpr size_t tb_smem() {
   return TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER, NW>::SMEM;
 }
 
-template <typename T, int RPT, int K, int KIND, int NW, bool PLAN = true>
+template <typename T, int RPT, int K, int KIND, int NW, bool PLAN = true, bool TMM = false>
 __device__ __forceinline__ void tb_tile_nw(const SimArgs<T>& a, const TBDst<T>& dst, const int2 tile,
                                            const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off) {
-  tb_tile<T, RPT, K, KIND, false, TBNoHook, NW, PLAN>(a, dst, tile, ph, pe, step_off);
+  tb_tile<T, RPT, K, KIND, false, TBNoHook, NW, PLAN, TMM>(a, dst, tile, ph, pe, step_off);
 }
 
-template <typename T, int RPT, int K, bool PML, int NW = 8, bool PLAN = true>
+template <typename T, int RPT, int K, bool PML, int NW = 8, bool PLAN = true, bool TMM = false>
 __global__ void __launch_bounds__(32 * NW, TBShape<T, RPT, K, PML ? KIND_XY : KIND_INNER, NW>::MIN_BLOCKS)
 k_tb_step(const __grid_constant__ SimArgs<T> a, const __grid_constant__ TBDst<T> dst,
           const int2* __restrict__ tiles, const __grid_constant__ PhasePlan<T> ph,
           const __grid_constant__ PhasePlan<T> pe, int step_off) {
   const int2 t = tiles[blockIdx.x];
   if (!PML) {
-    tb_tile_nw<T, RPT, K, KIND_INNER, NW, PLAN>(a, dst, t, ph, pe, step_off);
+    tb_tile_nw<T, RPT, K, KIND_INNER, NW, PLAN, TMM>(a, dst, t, ph, pe, step_off);
     return;
   }
   const int2 u = make_int2(t.x & ((1 << KIND_SHIFT) - 1), t.y);
@@ -569,13 +571,14 @@ k_tb_step(const __grid_constant__ SimArgs<T> a, const __grid_constant__ TBDst<T>
 // launch within the instruction cache (the three bodies in one kernel did not fit). As for the
 // interior tiles, the CPML tiles without a source, monitor or trace node take the lean body
 // (PLAN false): fewer registers, and the step is 13 % shorter at 2024² fp32.
-template <typename T, int RPT, int K, int KIND, int NW = 8, bool PLAN = true>
+template <typename T, int RPT, int K, int KIND, int NW = 8, bool PLAN = true, bool TMM = false>
 __global__ void __launch_bounds__(32 * NW, 1)
 k_tb_kind(const __grid_constant__ SimArgs<T> a, const __grid_constant__ TBDst<T> dst,
           const int2* __restrict__ tiles, const __grid_constant__ PhasePlan<T> ph,
           const __grid_constant__ PhasePlan<T> pe, int step_off) {
   const int2 t = tiles[blockIdx.x];
-  tb_tile_nw<T, RPT, K, KIND, NW, PLAN>(a, dst, make_int2(t.x & ((1 << KIND_SHIFT) - 1), t.y), ph, pe, step_off);
+  tb_tile_nw<T, RPT, K, KIND, NW, PLAN, TMM>(a, dst, make_int2(t.x & ((1 << KIND_SHIFT) - 1), t.y), ph, pe,
+                                             step_off);
 }
 
 template <typename T, int RPT, int K, int KIND, int NW = 8, bool PLAN = true>

@@ -366,6 +366,8 @@ def run_ours(args, world, rank, local) -> None:
         out["fp64"] = fp64_line(args, local)
     if rank == 0 and not args.no_studio:
         out["tm"] = tm_line(args)
+    if rank == 0 and not args.no_yee3d:
+        out["yee3d"] = yee3d_line(args)
     if rank == 0 and not args.no_studio:
         out["studio"] = studio_line(e, p)
         out["rasterize"] = rasterize_line(e, p)
@@ -701,7 +703,7 @@ def fp64_line(args, local) -> dict:
 def tm_line(args) -> dict:
     """The 2D TM mode on the headline grid: 2000² + 12-layer CPML, the Si strip along x in oxide,
     an Ez point current in the core, 3 point monitors × 16 wavelengths, fp32, 2000 steps; the
-    dual TE run on the one-step kernels, device time per step."""
+    dual TE run on the temporally blocked kernels (their TM variant), device time per step."""
     import torch
 
     from etalon_gb300 import _lib
@@ -730,7 +732,55 @@ def tm_line(args) -> dict:
     e.close()
     t = min(ms)
     return {"value": p.grid.n_cells * steps / (t / 1e3), "unit": UNIT, "time_steps": steps,
-            "grid": [p.grid.nx, p.grid.ny], "path": "dual TE run, one-step fused kernels, per-node Ez coefficient"}  # fmt: skip
+            "grid": [p.grid.nx, p.grid.ny],
+            "path": "dual TE run, temporally blocked kernels (TM variant: per-node Ez coefficient)"}  # fmt: skip
+
+
+def yee3d_line(args) -> dict:
+    """3D Yee on Etalon's planned 3D performance cell (docs/mvp-spec.md:109): 10 × 10 × 3 µm at
+    20 nm with 12-layer CPML on every face (524 × 524 × 174 cells), a 0.5 × 0.22 µm Si strip
+    along x in oxide, an Ey point current in the core, 3 point monitors × 16 wavelengths on all
+    six components, fp32. Device time of the steps (fields 1.1 GB: past L2, no flush needed);
+    each stencil kernel also timed alone for its roofline: the E kernel reads six fields and
+    three cb and writes three fields (48 algorithmic B per cell), the H kernel 36 B per cell."""
+    from etalon_gb300 import physics as ph
+    from etalon_gb300 import yee3d
+    from tests import cases
+
+    steps, warm, timed = args.yee3d_steps, 20, 10
+    wl = list(np.linspace(1.5, 1.6, 16))
+    p = yee3d.yee3d_problem(
+        (10.0, 10.0, 3.0), 0.02, background_eps=cases.EPS_OXIDE,
+        boxes=[ph.Box((0.0, 0.0, 0.0), (12.0, 0.5, 0.22), cases.EPS_SILICON)], layers=12,
+        sources=[ph.PointSource((-4.0, 0.0, 0.0), "Ey", ph.GaussianPulse(1.55, 0.5))],
+        monitors=[ph.DFTMonitor(f"m{k}", wl, center=(x, 0.0, 0.0)) for k, x in enumerate((-2.0, 0.0, 2.0))],
+        n_steps=warm + 2 * steps + timed, precision="single",
+    )  # fmt: skip
+    g = p.grid
+    e = yee3d.Yee3DEngine(p)
+    e.advance(warm)
+    e.synchronize()
+    ms = []
+    for _ in range(2):
+        e.advance(steps)
+        e.synchronize()
+        ms.append(e.last_timing()[0])
+    launches = e.last_timing()[1]
+    ms_h, ms_e = e.kernel_timing(timed)
+    e.close()
+    t = min(ms)
+    cells = g.n_cells
+    peak, peak_kind = hbm_peak()
+    achieved = 48 * cells / (ms_e / 1e3) / 1e9
+    return {
+        "value": cells * steps / (t / 1e3), "unit": UNIT, "time_steps": steps, "ms_per_step": t / steps,
+        "grid": [g.nx, g.ny, g.nz], "dtype": "f32", "gpu_launches_per_step": launches / steps,
+        "kernels_ms": {"update_h": ms_h, "update_e": ms_e},
+        "roofline": {"kernel": "k3_update_e<float>", "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": 48 * cells,
+                     "h_kernel_frac": 36 * cells / (ms_h / 1e3) / 1e9 / peak},
+    }  # fmt: skip
 
 
 # ----------------------------------------------------------------------------- next rows
@@ -870,6 +920,8 @@ def main() -> None:
     ap.add_argument("--no-fp64", action="store_true", help="skip the float64 line of the same workload")
     ap.add_argument("--no-studio", action="store_true", help="skip the live-view and rasterisation lines")
     ap.add_argument("--no-ref-kernels", action="store_true", help="skip timing Etalon's own CUDA kernels")
+    ap.add_argument("--no-yee3d", action="store_true", help="skip the 3D Yee line")
+    ap.add_argument("--yee3d-steps", type=int, default=200)
     ap.add_argument("--ref-kernel-steps", type=int, default=1000)
     args = ap.parse_args()
     os.environ["ETG_BENCH_IMPL"] = args.impl

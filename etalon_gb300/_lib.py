@@ -85,6 +85,20 @@ SIGNATURES: dict[str, list] = {
     "etg_adj_batch_forward": [vp, i64, i64],
     "etg_adj_batch_backward": [vp],
     "etg_tb_advance_static": [i32, i32, i32, i64] + [vp] * 21 + [f64, f64, f64, i64],
+    "etg_yee3d_create": [C.POINTER(vp), i32, i32, i32, i32, i32],
+    "etg_yee3d_destroy": [vp],
+    "etg_yee3d_set_scalars": [vp, vp],
+    "etg_yee3d_set_profile": [vp, i32, vp, vp, vp, vp, vp, vp],
+    "etg_yee3d_set_field": [vp, i32, vp],
+    "etg_yee3d_get_field": [vp, i32, vp],
+    "etg_yee3d_add_source": [vp, i32, i32, vp, i64, i64, vp],
+    "etg_yee3d_add_monitor": [vp, i32, i32, vp, i32, i64, i64, vp],
+    "etg_yee3d_get_dft": [vp, i32, vp],
+    "etg_yee3d_advance": [vp, i64],
+    "etg_yee3d_synchronize": [vp],
+    "etg_yee3d_step_index": [vp, pi64],
+    "etg_yee3d_last_timing": [vp, C.POINTER(f64), pi64],
+    "etg_yee3d_kernel_timing": [vp, i32, C.POINTER(f64), C.POINTER(f64)],
     "etg_debug_set_wait_tries": [i64],
     "etg_sim_device_array": [vp, i32, vp, vp],
     "etg_sim_set_db_nodes": [vp, vp],

@@ -328,8 +328,10 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
         eyb.ld(sEyX + (ty + 1) * EC + lj0);  // Ey of the row below this warp
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
+          // lane 31 takes its own value in interior tiles: the last column of the extended
+          // tile is K columns from the output and its error moves one column per step
           T exr = __shfl_down_sync(0xffffffffu, ex[t].v[0], 1);
-          if (lane == 31) exr = zero<T>();
+          if (PML && lane == 31) exr = zero<T>();
           Vw dbr;  // this row's Hz-position coefficients: the scalar db, or per node in TM mode
           if constexpr (tm) dbr.ld(sCby + (lr0 + t) * EC + lj0);
           else dbr.fill(db);
@@ -414,7 +416,7 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
 #pragma unroll
         for (int t = 0; t < RPT; ++t) {
           T hzl = __shfl_up_sync(0xffffffffu, hz[t].v[W - 1], 1);
-          if (lane == 0) hzl = zero<T>();
+          if (PML && lane == 0) hzl = zero<T>();  // lane 0 of interior tiles: as lane 31 above
           Vw cx, cy;
           cx.ld(sCbx + (lr0 + t) * EC + lj0);
           cy.ld((tm ? sCbx : sCby) + (lr0 + t) * EC + lj0);

@@ -301,6 +301,69 @@ int etg_debug_set_wait_tries(int64_t tries);
 #define ETG_OPT_TIMING 6        /* 1 = record CUDA-event timing of each advance,
                                    2 = also time each temporally blocked kernel launch */
 
+/* ---------------------------------------------------------------- 3D Yee
+ * Has no counterpart in Etalon: etalon/fdtd/capabilities.py:7-24 refuses 3D. The engine
+ * carries Etalon's 2D TE discretisation to three axes (layout of etalon/grid/yee.py:27-79 with
+ * a z axis, update order of etalon/fdtd/backends/numpy_backend.py:41-61 per component, step
+ * order of etalon/fdtd/solver.py:83-128), so that a run invariant along a one-cell periodic
+ * axis steps the other two exactly as the 2D TE update does.
+ *
+ * Arrays are C-ordered (x slowest, z fastest). Along a PEC axis of n cells a component has
+ * n + 1 integer positions (both walls) or n half positions; along a periodic axis n of
+ * either. Ex: (half, int, int), Ey: (int, half, int), Ez: (int, int, half), Hx: (int, half,
+ * half), Hy: (half, int, half), Hz: (half, half, int). Tangential E on a PEC wall stays 0.
+ *
+ * Hx += db ((dEy/dz / kz + psi_hx_z) - (dEz/dy / ky + psi_hx_y)), Hy and Hz cyclically;
+ * Ex += cb_ex ((dHz/dy / ky + psi_ex_y) - (dHy/dz / kz + psi_ex_z)),
+ * Ey -= cb_ey ((dHz/dx / kx + psi_ey_x) - (dHx/dz / kz + psi_ey_z)),
+ * Ez += cb_ez ((dHy/dx / kx + psi_ez_x) - (dHx/dy / ky + psi_ez_y)),
+ * psi <- b psi + c d before each use; one IEEE rounding per operation, no fused multiply-add.
+ * A step is H, H sources, H monitors, E, E sources, E monitors. */
+#define ETG3_EX 0
+#define ETG3_EY 1
+#define ETG3_EZ 2
+#define ETG3_HX 3
+#define ETG3_HY 4
+#define ETG3_HZ 5
+/* array ids 6..17: psi_hx_y psi_hx_z psi_hy_z psi_hy_x psi_hz_x psi_hz_y psi_ex_y psi_ex_z
+ * psi_ey_z psi_ey_x psi_ez_x psi_ez_y (each shaped as its field); 18..20: cb_ex cb_ey cb_ez */
+#define ETG3_PSI0 6
+#define ETG3_CB0 18
+typedef struct etg_yee3d etg_yee3d;
+/* periodic_mask: bit a set = axis a (0 x, 1 y, 2 z) periodic. Fields, psi and cb start at 0;
+ * profiles start as b = 1, c = 0, 1/kappa = 1 (no CPML). */
+int etg_yee3d_create(etg_yee3d** out, int dtype, int nx, int ny, int nz, int periodic_mask);
+int etg_yee3d_destroy(etg_yee3d* sim);
+/* db, 1/dx, 1/dy, 1/dz (1/m), four values of the run's dtype */
+int etg_yee3d_set_scalars(etg_yee3d* sim, const void* host4);
+/* CPML profile of one axis: b, c, 1/kappa at the integer positions (n + 1 on a PEC axis, n on
+ * a periodic one) and at the n half positions (etalon/fdtd/cpml.py:74-92 per axis). psi is
+ * kept only where b != 1 or c != 0: leading and trailing strips of each profile. */
+int etg_yee3d_set_profile(etg_yee3d* sim, int axis, const void* b_e, const void* c_e, const void* ik_e,
+                          const void* b_h, const void* c_h, const void* ik_h);
+/* whole arrays, C-ordered in the shapes above; psi must be +0 outside the strips, and the
+ * psi of an axis without CPML is not stored (set accepts only zeros, get returns zeros) */
+int etg_yee3d_set_field(etg_yee3d* sim, int array, const void* host);
+int etg_yee3d_get_field(etg_yee3d* sim, int array, void* host);
+/* field[nodes] -= table[n - n0] at step n, nodes as flat C-order indices into the component
+ * (at most 64; etalon/fdtd/solver.py:83-89); table: rows x n_nodes of the dtype */
+int etg_yee3d_add_source(etg_yee3d* sim, int component, int n_nodes, const int64_t* flat, int64_t n0,
+                         int64_t rows, const void* table);
+/* acc[f, node] += field[node] * phasor[n - n0, f] (etalon/fdtd/backends/numpy_backend.py:63-67);
+ * table: rows x n_f complex of the dtype; accumulators start at 0 */
+int etg_yee3d_add_monitor(etg_yee3d* sim, int component, int n_nodes, const int64_t* flat, int n_f,
+                          int64_t n0, int64_t rows, const void* table);
+int etg_yee3d_get_dft(etg_yee3d* sim, int monitor, void* host);
+/* n_steps steps on the engine's stream (asynchronous); ETG_ERR_STATE if a table does not
+ * cover them */
+int etg_yee3d_advance(etg_yee3d* sim, int64_t n_steps);
+int etg_yee3d_synchronize(etg_yee3d* sim);
+int etg_yee3d_step_index(etg_yee3d* sim, int64_t* n);
+/* device time (CUDA events) of the last etg_yee3d_advance and its kernel launches */
+int etg_yee3d_last_timing(etg_yee3d* sim, double* ms, int64_t* launches);
+/* n_steps more steps, each H and E stencil launch timed alone: mean ms per launch */
+int etg_yee3d_kernel_timing(etg_yee3d* sim, int n_steps, double* ms_h, double* ms_e);
+
 #ifdef __cplusplus
 }
 #endif

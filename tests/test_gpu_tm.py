@@ -1,7 +1,8 @@
 """2D TM mode on the GPU against the direct TM oracle, bit for bit (needs a GPU).
 
-The engine steps a TM run as its dual TE run (etalon_gb300/tm.py) on the one-step kernels
-with a per-node Ez coefficient (etg_sim_set_db_nodes); oracle/tm_numpy.py writes the TM
+The engine steps a TM run as its dual TE run (etalon_gb300/tm.py) on the one-step and the
+temporally blocked kernels with a per-node Ez coefficient (etg_sim_set_db_nodes; the blocked
+tiles run their compile-time TM variant); oracle/tm_numpy.py writes the TM
 update directly and is pinned to the TE oracle by tests/test_tm_oracle.py.
 """
 

@@ -739,8 +739,10 @@ def tm_line(args) -> dict:
 def yee3d_line(args) -> dict:
     """3D Yee on Etalon's planned 3D performance cell (docs/mvp-spec.md:109): 10 × 10 × 3 µm at
     20 nm with 12-layer CPML on every face (524 × 524 × 174 cells), a 0.5 × 0.22 µm Si strip
-    along x in oxide, an Ey point current in the core, 3 point monitors × 16 wavelengths on all
-    six components, fp32. Device time of the steps (fields 1.1 GB: past L2, no flush needed);
+    along x in oxide, an Ey point current in the core (x = -4 µm), 3 point monitors × 16
+    wavelengths (x = -2, 0, 2 µm) on all six components, fp32. ``--yee3d-cell`` scales the cell
+    (source and monitors at the same fractions of its length). Device time of the steps (fields
+    1.1 GB: past L2, no flush needed);
     each stencil kernel also timed alone for its roofline: the E kernel reads six fields and
     three cb and writes three fields (48 algorithmic B per cell), the H kernel 36 B per cell."""
     from etalon_gb300 import physics as ph
@@ -749,11 +751,12 @@ def yee3d_line(args) -> dict:
 
     steps, warm, timed = args.yee3d_steps, 20, 10
     wl = list(np.linspace(1.5, 1.6, 16))
+    cell = tuple(float(v) for v in args.yee3d_cell.split(","))
     p = yee3d.yee3d_problem(
-        (10.0, 10.0, 3.0), 0.02, background_eps=cases.EPS_OXIDE,
+        cell, 0.02, background_eps=cases.EPS_OXIDE,
         boxes=[ph.Box((0.0, 0.0, 0.0), (12.0, 0.5, 0.22), cases.EPS_SILICON)], layers=12,
-        sources=[ph.PointSource((-4.0, 0.0, 0.0), "Ey", ph.GaussianPulse(1.55, 0.5))],
-        monitors=[ph.DFTMonitor(f"m{k}", wl, center=(x, 0.0, 0.0)) for k, x in enumerate((-2.0, 0.0, 2.0))],
+        sources=[ph.PointSource((-0.4 * cell[0], 0.0, 0.0), "Ey", ph.GaussianPulse(1.55, 0.5))],
+        monitors=[ph.DFTMonitor(f"m{k}", wl, center=(f * cell[0], 0.0, 0.0)) for k, f in enumerate((-0.2, 0.0, 0.2))],
         n_steps=warm + 2 * steps + timed, precision="single",
     )  # fmt: skip
     g = p.grid
@@ -772,6 +775,9 @@ def yee3d_line(args) -> dict:
     cells = g.n_cells
     peak, peak_kind = hbm_peak()
     achieved = 48 * cells / (ms_e / 1e3) / 1e9
+    per_cell, src = profile_entry("traffic_bytes_per_cell", "k3_update_e_f32")
+    traffic = float(per_cell.split()[0]) * cells if per_cell else None
+    limiter, _ = profile_entry("limiter", "k3_update_e_f32")
     return {
         "value": cells * steps / (t / 1e3), "unit": UNIT, "time_steps": steps, "ms_per_step": t / steps,
         "grid": [g.nx, g.ny, g.nz], "dtype": "f32", "gpu_launches_per_step": launches / steps,
@@ -779,6 +785,8 @@ def yee3d_line(args) -> dict:
         "roofline": {"kernel": "k3_update_e<float>", "bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": 48 * cells,
+                     "traffic": traffic, "traffic_source": f"{src}, DRAM bytes per cell x cells" if src else None,
+                     "dram_frac": traffic / (ms_e / 1e3) / 1e9 / peak if traffic else None, "limiter": limiter,
                      "h_kernel_frac": 36 * cells / (ms_h / 1e3) / 1e9 / peak},
     }  # fmt: skip
 
@@ -922,6 +930,7 @@ def main() -> None:
     ap.add_argument("--no-ref-kernels", action="store_true", help="skip timing Etalon's own CUDA kernels")
     ap.add_argument("--no-yee3d", action="store_true", help="skip the 3D Yee line")
     ap.add_argument("--yee3d-steps", type=int, default=200)
+    ap.add_argument("--yee3d-cell", default="10,10,3", help="3D line: region size in µm (x,y,z), 20 nm cells")
     ap.add_argument("--ref-kernel-steps", type=int, default=1000)
     args = ap.parse_args()
     os.environ["ETG_BENCH_IMPL"] = args.impl

@@ -83,34 +83,27 @@ struct Y3MonPhase {
   Y3Mon<T> m[Y3_MAX_MON];
 };
 
-// CPML term of an H update along `axis` at half position `pos`: psi <- b psi + c d, then
-// d / kappa + psi (numpy_backend.py:41-49 per axis). Outside the strips psi is +0 and stays so.
-template <typename T>
-__device__ __forceinline__ T h_term(const Y3Args<T>& a, int p, int axis, int pos, int64_t idx, T d) {
-  T v = T(0);
-  T* psi = a.psi[p];
-  if (psi != nullptr && (pos < a.lo_h[axis] || pos >= a.hi_h[axis])) {
-    v = add(mul(a.prof[axis][3][pos], psi[idx]), mul(a.prof[axis][4][pos], d));
-    psi[idx] = v;
-  }
-  return add(mul(d, a.prof[axis][5][pos]), v);
-}
-
-// The same for an E update at integer position `pos` (numpy_backend.py:51-61 per axis).
-template <typename T>
-__device__ __forceinline__ T e_term(const Y3Args<T>& a, int p, int axis, int pos, int64_t idx, T d) {
-  T v = T(0);
-  T* psi = a.psi[p];
-  if (psi != nullptr && (pos < a.lo_e[axis] || pos >= a.hi_e[axis])) {
-    v = add(mul(a.prof[axis][0][pos], psi[idx]), mul(a.prof[axis][1][pos], d));
-    psi[idx] = v;
-  }
-  return add(mul(d, a.prof[axis][2][pos]), v);
+// CPML term of an update along `axis` at position `pos` (W = 0: integer positions, E updates;
+// W = 1: half positions, H updates): psi <- b psi + c d, then d / kappa + psi
+// (numpy_backend.py:41-61 per axis). Outside the strips b = 1, c = 0, 1/kappa = 1 and psi is +0,
+// so the term is d + 0 exactly and nothing is loaded. Inside, psi and the profile are read
+// here, after the field loads: strip cells pay the extra round trip, the others keep few
+// registers (many cells in flight per SM).
+template <typename T, int W>
+__device__ __forceinline__ T term(const Y3Args<T>& a, int p, int axis, int pos, int64_t idx, T d) {
+  T* const psi = a.psi[p];
+  const int lo = W ? a.lo_h[axis] : a.lo_e[axis], hi = W ? a.hi_h[axis] : a.hi_e[axis];
+  if (psi == nullptr || (pos >= lo && pos < hi)) return add(d, T(0));
+  const T* const* pr = a.prof[axis] + 3 * W;
+  const T v = add(mul(pr[0][pos], psi[idx]), mul(pr[1][pos], d));
+  psi[idx] = v;
+  return add(mul(d, pr[2][pos]), v);
 }
 
 // H^(n-1/2) -> H^(n+1/2) from E^n: forward differences (the +1 neighbour wraps to 0 on a
 // periodic axis). Hx lives at (integer x, half y, half z), Hy at (half, integer, half), Hz at
-// (half, half, integer).
+// (half, half, integer). One thread per (i, j, k), z across the lanes of a warp; all field
+// loads first, then the three updates.
 template <typename T>
 __global__ void __launch_bounds__(256) k3_update_h(const Y3Args<T> a) {
   const int k = blockIdx.x * 32 + threadIdx.x;
@@ -118,35 +111,38 @@ __global__ void __launch_bounds__(256) k3_update_h(const Y3Args<T> a) {
   const int i = blockIdx.z;
   if (k >= a.m2 || j >= a.m1) return;
   const int64_t idx = i * a.si + j * a.sj + k;
-  const int64_t dk = (a.p2 && k + 1 == a.n2) ? -(int64_t)k : 1;
-  const int64_t dj = (a.p1 && j + 1 == a.n1) ? -(int64_t)j * a.sj : a.sj;
+  const int dk = (a.p2 && k + 1 == a.n2) ? -k : 1;
+  const int dj = (a.p1 && j + 1 == a.n1) ? -j * (int)a.sj : (int)a.sj;
   const int64_t di = (a.p0 && i + 1 == a.n0) ? -(int64_t)i * a.si : a.si;
-  if (i < a.m0 && j < a.n1 && k < a.n2) {
-    const T dey_dz = mul(sub(a.ey[idx + dk], a.ey[idx]), a.inv_dz);
-    const T dez_dy = mul(sub(a.ez[idx + dj], a.ez[idx]), a.inv_dy);
-    const T tz = h_term(a, 1, 2, k, idx, dey_dz);
-    const T ty = h_term(a, 0, 1, j, idx, dez_dy);
-    a.hx[idx] = add(a.hx[idx], mul(a.db, sub(tz, ty)));
+  const bool vx = j < a.n1 && k < a.n2, vy = i < a.n0 && k < a.n2, vz = i < a.n0 && j < a.n1;
+  const T* __restrict__ ex = a.ex + idx;
+  const T* __restrict__ ey = a.ey + idx;
+  const T* __restrict__ ez = a.ez + idx;
+  const T ex0 = ex[0], ey0 = ey[0], ez0 = ez[0];  // every (i, j, k) of the block is in the arrays
+  const T hx0 = a.hx[idx], hy0 = a.hy[idx], hz0 = a.hz[idx];
+  const T ey_k = vx ? ey[dk] : T(0), ez_j = vx ? ez[dj] : T(0);
+  const T ez_i = vy ? ez[di] : T(0), ex_k = vy ? ex[dk] : T(0);
+  const T ex_j = vz ? ex[dj] : T(0), ey_i = vz ? ey[di] : T(0);
+  if (vx) {
+    const T tz = term<T, 1>(a, 1, 2, k, idx, mul(sub(ey_k, ey0), a.inv_dz));
+    const T ty = term<T, 1>(a, 0, 1, j, idx, mul(sub(ez_j, ez0), a.inv_dy));
+    a.hx[idx] = add(hx0, mul(a.db, sub(tz, ty)));
   }
-  if (i < a.n0 && j < a.m1 && k < a.n2) {
-    const T dez_dx = mul(sub(a.ez[idx + di], a.ez[idx]), a.inv_dx);
-    const T dex_dz = mul(sub(a.ex[idx + dk], a.ex[idx]), a.inv_dz);
-    const T tx = h_term(a, 3, 0, i, idx, dez_dx);
-    const T tz = h_term(a, 2, 2, k, idx, dex_dz);
-    a.hy[idx] = add(a.hy[idx], mul(a.db, sub(tx, tz)));
+  if (vy) {
+    const T tx = term<T, 1>(a, 3, 0, i, idx, mul(sub(ez_i, ez0), a.inv_dx));
+    const T tz = term<T, 1>(a, 2, 2, k, idx, mul(sub(ex_k, ex0), a.inv_dz));
+    a.hy[idx] = add(hy0, mul(a.db, sub(tx, tz)));
   }
-  if (i < a.n0 && j < a.n1 && k < a.m2) {
-    const T dex_dy = mul(sub(a.ex[idx + dj], a.ex[idx]), a.inv_dy);
-    const T dey_dx = mul(sub(a.ey[idx + di], a.ey[idx]), a.inv_dx);
-    const T ty = h_term(a, 5, 1, j, idx, dex_dy);
-    const T tx = h_term(a, 4, 0, i, idx, dey_dx);
-    a.hz[idx] = add(a.hz[idx], mul(a.db, sub(ty, tx)));
+  if (vz) {
+    const T ty = term<T, 1>(a, 5, 1, j, idx, mul(sub(ex_j, ex0), a.inv_dy));
+    const T tx = term<T, 1>(a, 4, 0, i, idx, mul(sub(ey_i, ey0), a.inv_dx));
+    a.hz[idx] = add(hz0, mul(a.db, sub(ty, tx)));
   }
 }
 
 // E^n -> E^(n+1) from H^(n+1/2): backward differences at the integer positions off the PEC
 // walls (1 .. n-1), or at all n on a periodic axis (the -1 neighbour of 0 is n-1). Tangential
-// E on a wall is never written and stays 0.
+// E on a wall is never written and stays as it is. All loads first, then the three updates.
 template <typename T>
 __global__ void __launch_bounds__(256) k3_update_e(const Y3Args<T> a) {
   const int k = blockIdx.x * 32 + threadIdx.x;
@@ -157,29 +153,34 @@ __global__ void __launch_bounds__(256) k3_update_e(const Y3Args<T> a) {
   const bool in_i = a.p0 ? i < a.n0 : (i >= 1 && i < a.n0);
   const bool in_j = a.p1 ? j < a.n1 : (j >= 1 && j < a.n1);
   const bool in_k = a.p2 ? k < a.n2 : (k >= 1 && k < a.n2);
-  const int64_t bk = (k == 0) ? (int64_t)(a.n2 - 1) : -1;
-  const int64_t bj = (j == 0) ? (int64_t)(a.n1 - 1) * a.sj : -a.sj;
+  const int bk = (k == 0) ? a.n2 - 1 : -1;
+  const int bj = (j == 0) ? (a.n1 - 1) * (int)a.sj : -(int)a.sj;
   const int64_t bi = (i == 0) ? (int64_t)(a.n0 - 1) * a.si : -a.si;
-  if (i < a.n0 && in_j && in_k) {
-    const T dhz_dy = mul(sub(a.hz[idx], a.hz[idx + bj]), a.inv_dy);
-    const T dhy_dz = mul(sub(a.hy[idx], a.hy[idx + bk]), a.inv_dz);
-    const T ty = e_term(a, 6, 1, j, idx, dhz_dy);
-    const T tz = e_term(a, 7, 2, k, idx, dhy_dz);
-    a.ex[idx] = add(a.ex[idx], mul(a.cb_ex[idx], sub(ty, tz)));
+  const bool vx = i < a.n0 && in_j && in_k, vy = in_i && j < a.n1 && in_k, vz = in_i && in_j && k < a.n2;
+  const T* __restrict__ hx = a.hx + idx;
+  const T* __restrict__ hy = a.hy + idx;
+  const T* __restrict__ hz = a.hz + idx;
+  const T hx0 = hx[0], hy0 = hy[0], hz0 = hz[0];
+  const T hz_j = vx ? hz[bj] : T(0), hy_k = vx ? hy[bk] : T(0);
+  const T hz_i = vy ? hz[bi] : T(0), hx_k = vy ? hx[bk] : T(0);
+  const T hy_i = vz ? hy[bi] : T(0), hx_j = vz ? hx[bj] : T(0);
+  const T ex0 = vx ? a.ex[idx] : T(0), cx = vx ? a.cb_ex[idx] : T(0);
+  const T ey0 = vy ? a.ey[idx] : T(0), cy = vy ? a.cb_ey[idx] : T(0);
+  const T ez0 = vz ? a.ez[idx] : T(0), cz = vz ? a.cb_ez[idx] : T(0);
+  if (vx) {
+    const T ty = term<T, 0>(a, 6, 1, j, idx, mul(sub(hz0, hz_j), a.inv_dy));
+    const T tz = term<T, 0>(a, 7, 2, k, idx, mul(sub(hy0, hy_k), a.inv_dz));
+    a.ex[idx] = add(ex0, mul(cx, sub(ty, tz)));
   }
-  if (in_i && j < a.n1 && in_k) {
-    const T dhz_dx = mul(sub(a.hz[idx], a.hz[idx + bi]), a.inv_dx);
-    const T dhx_dz = mul(sub(a.hx[idx], a.hx[idx + bk]), a.inv_dz);
-    const T tx = e_term(a, 9, 0, i, idx, dhz_dx);
-    const T tz = e_term(a, 8, 2, k, idx, dhx_dz);
-    a.ey[idx] = sub(a.ey[idx], mul(a.cb_ey[idx], sub(tx, tz)));
+  if (vy) {
+    const T tx = term<T, 0>(a, 9, 0, i, idx, mul(sub(hz0, hz_i), a.inv_dx));
+    const T tz = term<T, 0>(a, 8, 2, k, idx, mul(sub(hx0, hx_k), a.inv_dz));
+    a.ey[idx] = sub(ey0, mul(cy, sub(tx, tz)));
   }
-  if (in_i && in_j && k < a.n2) {
-    const T dhy_dx = mul(sub(a.hy[idx], a.hy[idx + bi]), a.inv_dx);
-    const T dhx_dy = mul(sub(a.hx[idx], a.hx[idx + bj]), a.inv_dy);
-    const T tx = e_term(a, 10, 0, i, idx, dhy_dx);
-    const T ty = e_term(a, 11, 1, j, idx, dhx_dy);
-    a.ez[idx] = add(a.ez[idx], mul(a.cb_ez[idx], sub(tx, ty)));
+  if (vz) {
+    const T tx = term<T, 0>(a, 10, 0, i, idx, mul(sub(hy0, hy_i), a.inv_dx));
+    const T ty = term<T, 0>(a, 11, 1, j, idx, mul(sub(hx0, hx_j), a.inv_dy));
+    a.ez[idx] = add(ez0, mul(cz, sub(tx, ty)));
   }
 }
 
@@ -405,10 +406,11 @@ int advance(etg_yee3d* s, int64_t steps) {
   return ETG_OK;
 }
 
-// positions of a profile that carry psi: [0, lo) and [hi, len); the rest must be b = 1, c = 0
+// positions of a profile that carry psi: [0, lo) and [hi, len); the rest must be b = 1, c = 0,
+// 1/kappa = 1
 template <typename T>
-void strips(const T* b, const T* c, int len, int* lo, int* hi) {
-  auto trivial = [&](int p) { return b[p] == T(1) && c[p] == T(0); };
+void strips(const T* b, const T* c, const T* ik, int len, int* lo, int* hi) {
+  auto trivial = [&](int p) { return b[p] == T(1) && c[p] == T(0) && ik[p] == T(1); };
   int l = 0, h = len;
   while (l < len && !trivial(l)) ++l;
   while (h > l && !trivial(h - 1)) --h;
@@ -574,11 +576,13 @@ int etg_yee3d_set_profile(etg_yee3d* s, int axis, const void* b_e, const void* c
   for (int q = 0; q < 6; ++q)
     ETG_TRY_CUDA(cudaMemcpyAsync(s->prof[axis][q], in[q], len[q] * z, cudaMemcpyHostToDevice, s->stream));
   if (s->dtype == ETG_F32) {
-    strips(static_cast<const float*>(b_e), static_cast<const float*>(c_e), len[0], &s->lo_e[axis], &s->hi_e[axis]);
-    strips(static_cast<const float*>(b_h), static_cast<const float*>(c_h), len[3], &s->lo_h[axis], &s->hi_h[axis]);
+    using F = const float*;
+    strips(static_cast<F>(b_e), static_cast<F>(c_e), static_cast<F>(ik_e), len[0], &s->lo_e[axis], &s->hi_e[axis]);
+    strips(static_cast<F>(b_h), static_cast<F>(c_h), static_cast<F>(ik_h), len[3], &s->lo_h[axis], &s->hi_h[axis]);
   } else {
-    strips(static_cast<const double*>(b_e), static_cast<const double*>(c_e), len[0], &s->lo_e[axis], &s->hi_e[axis]);
-    strips(static_cast<const double*>(b_h), static_cast<const double*>(c_h), len[3], &s->lo_h[axis], &s->hi_h[axis]);
+    using D = const double*;
+    strips(static_cast<D>(b_e), static_cast<D>(c_e), static_cast<D>(ik_e), len[0], &s->lo_e[axis], &s->hi_e[axis]);
+    strips(static_cast<D>(b_h), static_cast<D>(c_h), static_cast<D>(ik_h), len[3], &s->lo_h[axis], &s->hi_h[axis]);
   }
   const bool cpml = s->lo_e[axis] > 0 || s->hi_e[axis] < len[0] || s->lo_h[axis] > 0 || s->hi_h[axis] < len[3];
   if (cpml) {

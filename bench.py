@@ -742,9 +742,10 @@ def yee3d_line(args) -> dict:
     along x in oxide, an Ey point current in the core (x = -4 µm), 3 point monitors × 16
     wavelengths (x = -2, 0, 2 µm) on all six components, fp32. ``--yee3d-cell`` scales the cell
     (source and monitors at the same fractions of its length). Device time of the steps (fields
-    1.1 GB: past L2, no flush needed);
-    each stencil kernel also timed alone for its roofline: the E kernel reads six fields and
-    three cb and writes three fields (48 algorithmic B per cell), the H kernel 36 B per cell."""
+    1.1 GB: past L2, no flush needed) with the default step, an H and an E kernel (each timed
+    alone; the E kernel has the roofline entry: it reads six fields and three cb and writes three
+    fields, 48 algorithmic B per cell; the H kernel 36 B); then the same run continued with the
+    fused step (one kernel over two buffer sets, 60 B per cell)."""
     from etalon_gb300 import physics as ph
     from etalon_gb300 import yee3d
     from tests import cases
@@ -757,10 +758,10 @@ def yee3d_line(args) -> dict:
         boxes=[ph.Box((0.0, 0.0, 0.0), (12.0, 0.5, 0.22), cases.EPS_SILICON)], layers=12,
         sources=[ph.PointSource((-0.4 * cell[0], 0.0, 0.0), "Ey", ph.GaussianPulse(1.55, 0.5))],
         monitors=[ph.DFTMonitor(f"m{k}", wl, center=(f * cell[0], 0.0, 0.0)) for k, f in enumerate((-0.2, 0.0, 0.2))],
-        n_steps=warm + 2 * steps + timed, precision="single",
+        n_steps=warm + 3 * steps + 2 * timed, precision="single",
     )  # fmt: skip
     g = p.grid
-    e = yee3d.Yee3DEngine(p)
+    e = yee3d.Yee3DEngine(p)  # the default step: an H and an E kernel per step
     e.advance(warm)
     e.synchronize()
     ms = []
@@ -770,6 +771,11 @@ def yee3d_line(args) -> dict:
         ms.append(e.last_timing()[0])
     launches = e.last_timing()[1]
     ms_h, ms_e = e.kernel_timing(timed)
+    e.set_fused(True)  # the same run continued with the fused step (one kernel, two buffer sets)
+    e.advance(steps)
+    e.synchronize()
+    ms_fused = e.last_timing()[0]
+    ms_f, _ = e.kernel_timing(timed)
     e.close()
     t = min(ms)
     cells = g.n_cells
@@ -782,6 +788,8 @@ def yee3d_line(args) -> dict:
         "value": cells * steps / (t / 1e3), "unit": UNIT, "time_steps": steps, "ms_per_step": t / steps,
         "grid": [g.nx, g.ny, g.nz], "dtype": "f32", "gpu_launches_per_step": launches / steps,
         "kernels_ms": {"update_h": ms_h, "update_e": ms_e},
+        "fused_step": {"value": cells * steps / (ms_fused / 1e3), "ms_per_step": ms_fused / steps,
+                       "kernel_ms": ms_f, "frac": 60 * cells / (ms_f / 1e3) / 1e9 / peak},
         "roofline": {"kernel": "k3_update_e<float>", "bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": 48 * cells,
@@ -789,9 +797,6 @@ def yee3d_line(args) -> dict:
                      "dram_frac": traffic / (ms_e / 1e3) / 1e9 / peak if traffic else None, "limiter": limiter,
                      "h_kernel_frac": 36 * cells / (ms_h / 1e3) / 1e9 / peak},
     }  # fmt: skip
-
-
-# ----------------------------------------------------------------------------- next rows
 
 
 def _studio_energy(state, xp, dt, db, cell_area):

@@ -99,6 +99,7 @@ SIGNATURES: dict[str, list] = {
     "etg_yee3d_step_index": [vp, pi64],
     "etg_yee3d_last_timing": [vp, C.POINTER(f64), pi64],
     "etg_yee3d_kernel_timing": [vp, i32, C.POINTER(f64), C.POINTER(f64)],
+    "etg_yee3d_set_option": [vp, i32, i64],
     "etg_debug_set_wait_tries": [i64],
     "etg_sim_device_array": [vp, i32, vp, vp],
     "etg_sim_set_db_nodes": [vp, vp],

@@ -17,7 +17,8 @@
 // One step is two stencil kernels (H, then E: one thread per (i, j, k), z across the lanes of
 // a warp), each followed by its phase's source injection (one thread, NumPy's gather-subtract-
 // scatter per source) and DFT accumulation (one thread per frequency and node). Steps run in
-// CUDA graphs of up to 32 steps; a device step counter gives every kernel its step n.
+// CUDA graphs of up to 32 steps; a device step counter gives every kernel its step n. A fused
+// step (one kernel for H and E over two buffer sets, below) is an option with the same bits.
 #include <cstring>
 #include <map>
 #include <vector>
@@ -225,6 +226,172 @@ __global__ void k3_dft(const Y3MonPhase<T> p, const int64_t* step, int s_off, in
   }
 }
 
+// ---------------------------------------------------------------------------- fused step
+// One kernel per step, H and E together, from one buffer set (src) into the other (dst): a
+// step reads E, H and cb once and writes E and H once (60 B per cell in fp32, against 84 for
+// the two kernels). A block covers 7 rows (y) x 31 columns (z) of owned cells plus one halo
+// row and column below them, and walks a chunk of x planes: at plane i every thread computes
+// H(i) at its position (halo threads included, on the wrapped position along a periodic axis)
+// from src; rows exchange Hz and Hx through shared memory, columns Hy and Hx by shuffle, Hz and
+// Hy of plane i - 1 stay in registers, and the owning threads then update E(i). Every H
+// position is owned by one block, which writes it; a block's halo and the plane before its
+// chunk are recomputed, not written. psi comes from src and goes to dst the same way. Point
+// sources are applied where their node is computed (H sources by every thread that computes
+// the node, halo included, before E reads it; E sources after the E update), each source as
+// NumPy's gather-subtract-scatter does it (a node listed twice keeps its last delta).
+// Positions no update writes (tangential E on a PEC wall) are equal in both sets.
+// Measured at 524 x 524 x 174 fp32 it is the slower form: 1.52 ms per step against 0.88 ms
+// for the two kernels. DRAM moves 78 B per cell (the halo row and column and the plane before
+// each chunk are read again), the halo recompute adds instructions, and the barrier per plane
+// stalls 8 warps at 5 CTAs per SM (16-row blocks: 1.81 ms). It stays an option, not the default.
+constexpr int Y3F_NODES = 32, Y3F_SRC = 16, Y3F_CH = 16, Y3F_ROWS = 8;
+
+struct Y3FNode {
+  int i, j, k;
+  int8_t comp, slot;
+  int16_t col;
+};
+
+template <typename T>
+struct Y3FSrc {
+  int n;                    // nodes, in the order their deltas are subtracted
+  Y3FNode node[Y3F_NODES];
+  const T* tab[Y3F_SRC];    // (rows, nn) per source
+  int64_t n0[Y3F_SRC], rows[Y3F_SRC];
+  int nn[Y3F_SRC];
+};
+
+template <typename T>
+struct Y3Fused {
+  Y3Args<T> a;                         // src fields and psi, coefficients
+  T *dex, *dey, *dez, *dhx, *dhy, *dhz;  // dst fields
+  T* dpsi[Y3_NPSI];                    // dst psi
+  Y3FSrc<T> hs, es;
+  const int64_t* step;
+  int s_off;
+  int* flag;
+};
+
+// CPML term from src psi; the new psi goes to dst when `keep`.
+template <typename T, int W>
+__device__ __forceinline__ T term2(const Y3Args<T>& a, T* const* dpsi, int p, int axis, int pos, int64_t idx, T d,
+                                   bool keep) {
+  const T* psi = a.psi[p];
+  const int lo = W ? a.lo_h[axis] : a.lo_e[axis], hi = W ? a.hi_h[axis] : a.hi_e[axis];
+  if (psi == nullptr || (pos >= lo && pos < hi)) return add(d, T(0));
+  const T* const* pr = a.prof[axis] + 3 * W;
+  const T v = add(mul(pr[0][pos], psi[idx]), mul(pr[1][pos], d));
+  if (keep) dpsi[p][idx] = v;
+  return add(mul(d, pr[2][pos]), v);
+}
+
+// subtract the deltas of the sources whose node is (i, j, k) of component c (mask: this
+// thread's candidate nodes)
+template <typename T>
+__device__ __forceinline__ T inject(const Y3FSrc<T>& q, uint32_t mask, int i, int c, int64_t n, T v, int* flag) {
+  for (; mask; mask &= mask - 1) {
+    const Y3FNode& d = q.node[__ffs(mask) - 1];
+    if (d.i != i || d.comp != c) continue;
+    const int64_t r = n - q.n0[d.slot];
+    if (r < 0 || r >= q.rows[d.slot]) {
+      atomicOr(flag, ERR_TABLE);
+      continue;
+    }
+    v = sub(v, q.tab[d.slot][r * q.nn[d.slot] + d.col]);
+  }
+  return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * Y3F_ROWS) k3_step_fused(const Y3Fused<T> P) {
+  const Y3Args<T>& a = P.a;
+  __shared__ T sHz[2][Y3F_ROWS][32], sHx[2][Y3F_ROWS][32];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int k = blockIdx.x * 31 - 1 + tx, j = blockIdx.y * (Y3F_ROWS - 1) - 1 + ty;
+  const int ib = blockIdx.z * Y3F_CH, ie = min(ib + Y3F_CH, a.m0);
+  // the position this thread computes H at (wrapped on a periodic axis; -1: none)
+  const int kw = k < 0 ? (a.p2 ? k + a.n2 : -1) : (k < a.m2 ? k : -1);
+  const int jw = j < 0 ? (a.p1 ? j + a.n1 : -1) : (j < a.m1 ? j : -1);
+  const bool live = kw >= 0 && jw >= 0;
+  const bool own = live && tx >= 1 && ty >= 1;
+  const int64_t n = *P.step + P.s_off;
+  uint32_t hmask = 0, emask = 0;
+  for (int q = 0; q < P.hs.n; ++q)
+    if (P.hs.node[q].j == jw && P.hs.node[q].k == kw) hmask |= 1u << q;
+  if (own)
+    for (int q = 0; q < P.es.n; ++q)
+      if (P.es.node[q].j == jw && P.es.node[q].k == kw) emask |= 1u << q;
+  const int dk = (a.p2 && kw + 1 == a.n2) ? -kw : 1;
+  const int dj = (a.p1 && jw + 1 == a.n1) ? -jw * (int)a.sj : (int)a.sj;
+  const int64_t jk = (int64_t)jw * a.sj + kw;
+  const bool in_j = a.p1 ? jw < a.n1 : (jw >= 1 && jw < a.n1);
+  const bool in_k = a.p2 ? kw < a.n2 : (kw >= 1 && kw < a.n2);
+  T hz_p = T(0), hy_p = T(0);
+  int par = 0;
+  for (int i = ib - 1; i < ie; ++i, par ^= 1) {
+    const bool warm = i < ib;  // the plane before the chunk: H only, not written
+    const int iw = i < 0 ? (a.p0 ? i + a.n0 : -1) : i;
+    T hx_c = T(0), hy_c = T(0), hz_c = T(0), ex0 = T(0), ey0 = T(0), ez0 = T(0);
+    if (live && iw >= 0) {
+      const int64_t idx = iw * a.si + jk;
+      const int64_t di = (a.p0 && iw + 1 == a.n0) ? -(int64_t)iw * a.si : a.si;
+      const bool vx = jw < a.n1 && kw < a.n2, vy = iw < a.n0 && kw < a.n2, vz = iw < a.n0 && jw < a.n1;
+      const T* __restrict__ ex = a.ex + idx;
+      const T* __restrict__ ey = a.ey + idx;
+      const T* __restrict__ ez = a.ez + idx;
+      ex0 = ex[0], ey0 = ey[0], ez0 = ez[0];
+      const T hx0 = a.hx[idx], hy0 = a.hy[idx], hz0 = a.hz[idx];
+      const T ey_k = vx ? ey[dk] : T(0), ez_j = vx ? ez[dj] : T(0);
+      const T ez_i = vy ? ez[di] : T(0), ex_k = vy ? ex[dk] : T(0);
+      const T ex_j = vz ? ex[dj] : T(0), ey_i = vz ? ey[di] : T(0);
+      const bool keep = own && !warm;
+      if (vx) {
+        const T tz = term2<T, 1>(a, P.dpsi, 1, 2, kw, idx, mul(sub(ey_k, ey0), a.inv_dz), keep);
+        const T ty_ = term2<T, 1>(a, P.dpsi, 0, 1, jw, idx, mul(sub(ez_j, ez0), a.inv_dy), keep);
+        hx_c = inject(P.hs, hmask, iw, 3, n, add(hx0, mul(a.db, sub(tz, ty_))), P.flag);
+        if (keep) P.dhx[idx] = hx_c;
+      }
+      if (vy) {
+        const T tx_ = term2<T, 1>(a, P.dpsi, 3, 0, iw, idx, mul(sub(ez_i, ez0), a.inv_dx), keep);
+        const T tz = term2<T, 1>(a, P.dpsi, 2, 2, kw, idx, mul(sub(ex_k, ex0), a.inv_dz), keep);
+        hy_c = inject(P.hs, hmask, iw, 4, n, add(hy0, mul(a.db, sub(tx_, tz))), P.flag);
+        if (keep) P.dhy[idx] = hy_c;
+      }
+      if (vz) {
+        const T ty_ = term2<T, 1>(a, P.dpsi, 5, 1, jw, idx, mul(sub(ex_j, ex0), a.inv_dy), keep);
+        const T tx_ = term2<T, 1>(a, P.dpsi, 4, 0, iw, idx, mul(sub(ey_i, ey0), a.inv_dx), keep);
+        hz_c = inject(P.hs, hmask, iw, 5, n, add(hz0, mul(a.db, sub(ty_, tx_))), P.flag);
+        if (keep) P.dhz[idx] = hz_c;
+      }
+    }
+    sHz[par][ty][tx] = hz_c;
+    sHx[par][ty][tx] = hx_c;
+    const T hy_km = __shfl_up_sync(0xffffffffu, hy_c, 1), hx_km = __shfl_up_sync(0xffffffffu, hx_c, 1);
+    __syncthreads();
+    if (!warm && own) {
+      const int64_t idx = (int64_t)i * a.si + jk;
+      const bool in_i = a.p0 ? i < a.n0 : (i >= 1 && i < a.n0);
+      const T hz_jm = sHz[par][ty - 1][tx], hx_jm = sHx[par][ty - 1][tx];
+      if (i < a.n0 && in_j && in_k) {
+        const T ty_ = term2<T, 0>(a, P.dpsi, 6, 1, jw, idx, mul(sub(hz_c, hz_jm), a.inv_dy), true);
+        const T tz = term2<T, 0>(a, P.dpsi, 7, 2, kw, idx, mul(sub(hy_c, hy_km), a.inv_dz), true);
+        P.dex[idx] = inject(P.es, emask, i, 0, n, add(ex0, mul(a.cb_ex[idx], sub(ty_, tz))), P.flag);
+      }
+      if (in_i && jw < a.n1 && in_k) {
+        const T tx_ = term2<T, 0>(a, P.dpsi, 9, 0, i, idx, mul(sub(hz_c, hz_p), a.inv_dx), true);
+        const T tz = term2<T, 0>(a, P.dpsi, 8, 2, kw, idx, mul(sub(hx_c, hx_km), a.inv_dz), true);
+        P.dey[idx] = inject(P.es, emask, i, 1, n, sub(ey0, mul(a.cb_ey[idx], sub(tx_, tz))), P.flag);
+      }
+      if (in_i && in_j && kw < a.n2) {
+        const T tx_ = term2<T, 0>(a, P.dpsi, 10, 0, i, idx, mul(sub(hy_c, hy_p), a.inv_dx), true);
+        const T ty_ = term2<T, 0>(a, P.dpsi, 11, 1, jw, idx, mul(sub(hx_c, hx_jm), a.inv_dy), true);
+        P.dez[idx] = inject(P.es, emask, i, 2, n, add(ez0, mul(a.cb_ez[idx], sub(tx_, ty_))), P.flag);
+      }
+    }
+    hz_p = hz_c, hy_p = hy_c;
+  }
+}
+
 __global__ void k3_step_add(int64_t* step, int g) { *step += g; }
 
 }  // namespace
@@ -237,8 +404,13 @@ struct etg_yee3d {
   int n[3] = {}, m[3] = {}, per[3] = {};
   int64_t pz = 0, sj = 0, si = 0;
   size_t elems = 0;
-  void* f[Y3_NFIELD] = {};
-  void* psi[Y3_NPSI] = {};
+  // two sets of fields and psi: the state is in set `cur`; the fused step writes the other
+  // set and flips `cur` (set 1 is allocated at the first fused step)
+  void* f[2][Y3_NFIELD] = {};
+  void* psi[2][Y3_NPSI] = {};
+  int cur = 0;
+  bool two_sets = false;
+  bool fused = false;  // ETG3_OPT_FUSED
   void* cb[Y3_NCB] = {};
   void* prof[3][6] = {};
   int lo_e[3] = {}, hi_e[3] = {}, lo_h[3] = {}, hi_h[3] = {};
@@ -249,6 +421,7 @@ struct etg_yee3d {
     int64_t* idx;
     void* table;
     int64_t n0, rows;
+    std::vector<int64_t> host_idx;  // the padded node indices, for the fused step's node list
   };
   struct Mon {
     int comp, nn, nf;
@@ -266,7 +439,8 @@ struct etg_yee3d {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0;
   int64_t last_launches = 0;
-  std::map<int, cudaGraphExec_t> graphs;
+  std::map<int, cudaGraphExec_t> graphs;  // keyed by the starting set (+2 for the fused step)
+  std::map<int, int64_t> graph_launches;
 };
 
 namespace {
@@ -281,18 +455,19 @@ void extent(const etg_yee3d* s, int c, int64_t out[3]) {
 void drop_graphs(etg_yee3d* s) {
   for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
   s->graphs.clear();
+  s->graph_launches.clear();
 }
 
 template <typename T>
-Y3Args<T> args_of(const etg_yee3d* s) {
+Y3Args<T> args_of(const etg_yee3d* s, int set) {
   Y3Args<T> a{};
   a.n0 = s->n[0], a.n1 = s->n[1], a.n2 = s->n[2];
   a.m0 = s->m[0], a.m1 = s->m[1], a.m2 = s->m[2];
   a.p0 = s->per[0], a.p1 = s->per[1], a.p2 = s->per[2];
   a.si = s->si, a.sj = s->sj;
-  T* const* f = reinterpret_cast<T* const*>(s->f);
+  T* const* f = reinterpret_cast<T* const*>(s->f[set]);
   a.ex = f[0], a.ey = f[1], a.ez = f[2], a.hx = f[3], a.hy = f[4], a.hz = f[5];
-  for (int p = 0; p < Y3_NPSI; ++p) a.psi[p] = static_cast<T*>(s->psi[p]);
+  for (int p = 0; p < Y3_NPSI; ++p) a.psi[p] = static_cast<T*>(s->psi[set][p]);
   a.cb_ex = static_cast<const T*>(s->cb[0]);
   a.cb_ey = static_cast<const T*>(s->cb[1]);
   a.cb_ez = static_cast<const T*>(s->cb[2]);
@@ -305,13 +480,13 @@ Y3Args<T> args_of(const etg_yee3d* s) {
 }
 
 template <typename T>
-void phases_of(const etg_yee3d* s, bool magnetic, Y3SrcPhase<T>* sp, Y3MonPhase<T>* mp) {
+void phases_of(const etg_yee3d* s, bool magnetic, int set, Y3SrcPhase<T>* sp, Y3MonPhase<T>* mp) {
   std::memset(sp, 0, sizeof(*sp));
   std::memset(mp, 0, sizeof(*mp));
   for (const auto& q : s->src) {
     if ((q.comp >= 3) != magnetic) continue;
     Y3Src<T>& d = sp->s[sp->n++];
-    d.field = static_cast<T*>(s->f[q.comp]);
+    d.field = static_cast<T*>(s->f[set][q.comp]);
     d.idx = q.idx;
     d.table = static_cast<const T*>(q.table);
     d.n0 = q.n0, d.rows = q.rows, d.nn = q.nn;
@@ -320,7 +495,7 @@ void phases_of(const etg_yee3d* s, bool magnetic, Y3SrcPhase<T>* sp, Y3MonPhase<
     if ((q.comp >= 3) != magnetic) continue;
     Y3Mon<T>& d = mp->m[mp->n++];
     d.acc = static_cast<T*>(q.acc);
-    d.field = static_cast<const T*>(s->f[q.comp]);
+    d.field = static_cast<const T*>(s->f[set][q.comp]);
     d.idx = q.idx;
     d.table = static_cast<const T*>(q.table);
     d.n0 = q.n0, d.rows = q.rows, d.nn = q.nn, d.nf = q.nf;
@@ -332,6 +507,78 @@ int mon_blocks(const etg_yee3d* s, bool magnetic) {
   for (const auto& q : s->mon)
     if ((q.comp >= 3) == magnetic) most = std::max(most, q.nn * q.nf);
   return std::max(1, std::min(1024, (most + 255) / 256));
+}
+
+// The sources of one phase as the fused kernel's node list, in subtraction order; false when
+// they do not fit it (the two-kernel step then runs).
+template <typename T>
+bool fused_sources(const etg_yee3d* s, bool magnetic, Y3FSrc<T>* out) {
+  std::memset(out, 0, sizeof(*out));
+  int slot = 0;
+  for (const auto& q : s->src) {
+    if ((q.comp >= 3) != magnetic) continue;
+    if (slot == Y3F_SRC) return false;
+    for (int m = 0; m < q.nn; ++m) {
+      bool later = false;  // NumPy's scatter keeps the last delta of a node listed twice
+      for (int m2 = m + 1; m2 < q.nn; ++m2) later |= q.host_idx[m2] == q.host_idx[m];
+      if (later) continue;
+      if (out->n == Y3F_NODES) return false;
+      const int64_t x = q.host_idx[m];
+      Y3FNode& d = out->node[out->n++];
+      d.i = (int)(x / s->si), d.j = (int)((x % s->si) / s->sj), d.k = (int)(x % s->sj);
+      d.comp = (int8_t)q.comp, d.slot = (int8_t)slot, d.col = (int16_t)m;
+    }
+    out->tab[slot] = static_cast<const T*>(q.table);
+    out->n0[slot] = q.n0, out->rows[slot] = q.rows, out->nn[slot] = q.nn;
+    ++slot;
+  }
+  return true;
+}
+
+// The second set: allocated at the first fused step as a copy of the current one.
+int ensure_two_sets(etg_yee3d* s) {
+  if (s->two_sets) return ETG_OK;
+  const size_t bytes = s->elems * esize(s);
+  const int other = s->cur ^ 1;
+  for (int c = 0; c < Y3_NFIELD; ++c) {
+    ETG_REQUIRE(cudaMalloc(&s->f[other][c], bytes) == cudaSuccess, ETG_ERR_ALLOC,
+                "etg_yee3d: second field set (%zu bytes per array) could not be allocated", bytes);
+    ETG_TRY_CUDA(cudaMemcpyAsync(s->f[other][c], s->f[s->cur][c], bytes, cudaMemcpyDeviceToDevice, s->stream));
+  }
+  for (int p = 0; p < Y3_NPSI; ++p) {
+    if (!s->psi[s->cur][p]) continue;
+    ETG_REQUIRE(cudaMalloc(&s->psi[other][p], bytes) == cudaSuccess, ETG_ERR_ALLOC,
+                "etg_yee3d: second psi set could not be allocated");
+    ETG_TRY_CUDA(cudaMemcpyAsync(s->psi[other][p], s->psi[s->cur][p], bytes, cudaMemcpyDeviceToDevice, s->stream));
+  }
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  s->two_sets = true;
+  return ETG_OK;
+}
+
+// one fused step from set `set` into the other; returns the number of launches
+template <typename T>
+int launch_fused(const etg_yee3d* s, int set, const Y3FSrc<T>& hs, const Y3FSrc<T>& es, int s_off, cudaStream_t st,
+                 cudaEvent_t* ev = nullptr) {
+  Y3Fused<T> P{};
+  P.a = args_of<T>(s, set);
+  T* const* d = reinterpret_cast<T* const*>(s->f[set ^ 1]);
+  P.dex = d[0], P.dey = d[1], P.dez = d[2], P.dhx = d[3], P.dhy = d[4], P.dhz = d[5];
+  for (int p = 0; p < Y3_NPSI; ++p) P.dpsi[p] = static_cast<T*>(s->psi[set ^ 1][p]);
+  P.hs = hs, P.es = es, P.step = s->d_step, P.s_off = s_off, P.flag = s->d_flag;
+  const dim3 block(32, Y3F_ROWS), grid((s->m[2] + 30) / 31, (s->m[1] + Y3F_ROWS - 2) / (Y3F_ROWS - 1),
+                                       (s->m[0] + Y3F_CH - 1) / Y3F_CH);
+  if (ev) cudaEventRecord(ev[0], st);
+  k3_step_fused<T><<<grid, block, 0, st>>>(P);
+  if (ev) cudaEventRecord(ev[1], st);
+  Y3SrcPhase<T> sp;
+  Y3MonPhase<T> mh, me;
+  phases_of<T>(s, true, set ^ 1, &sp, &mh);
+  phases_of<T>(s, false, set ^ 1, &sp, &me);
+  int launches = 1;
+  if (mh.n) k3_dft<T><<<dim3(mon_blocks(s, true), mh.n), 256, 0, st>>>(mh, s->d_step, s_off, s->d_flag), ++launches;
+  if (me.n) k3_dft<T><<<dim3(mon_blocks(s, false), me.n), 256, 0, st>>>(me, s->d_step, s_off, s->d_flag), ++launches;
+  return launches;
 }
 
 // one step (s_off: its offset from the device counter); returns the number of launches
@@ -355,24 +602,53 @@ int launch_step(const etg_yee3d* s, const Y3Args<T>& a, const Y3SrcPhase<T>& sh,
 }
 
 template <typename T>
+bool use_fused(const etg_yee3d* s, Y3FSrc<T>* hs, Y3FSrc<T>* es) {
+  return s->fused && fused_sources<T>(s, true, hs) && fused_sources<T>(s, false, es);
+}
+
+// g steps from set `set` at counter offsets 0 .. g-1, then the counter add; returns the set
+// the state ends in (the two-kernel step works in place)
+template <typename T>
+int steps_from(etg_yee3d* s, bool fused, const Y3FSrc<T>& hs, const Y3FSrc<T>& es, int set, int g,
+               int64_t* launches) {
+  for (int k = 0; k < g; ++k) {
+    if (fused) {
+      *launches += launch_fused<T>(s, set, hs, es, k, s->stream);
+      set ^= 1;
+    } else {
+      const Y3Args<T> a = args_of<T>(s, set);
+      Y3SrcPhase<T> sh, se;
+      Y3MonPhase<T> mh, me;
+      phases_of<T>(s, true, set, &sh, &mh);
+      phases_of<T>(s, false, set, &se, &me);
+      *launches += launch_step<T>(s, a, sh, mh, se, me, k, s->stream);
+    }
+  }
+  k3_step_add<<<1, 1, 0, s->stream>>>(s->d_step, g);
+  *launches += 1;
+  return set;
+}
+
+template <typename T>
 int advance(etg_yee3d* s, int64_t steps) {
-  const Y3Args<T> a = args_of<T>(s);
-  Y3SrcPhase<T> sh, se;
-  Y3MonPhase<T> mh, me;
-  phases_of<T>(s, true, &sh, &mh);
-  phases_of<T>(s, false, &se, &me);
+  Y3FSrc<T> hs, es;
+  const bool fused = use_fused<T>(s, &hs, &es);
+  if (fused) {
+    int r = ensure_two_sets(s);
+    if (r) return r;
+  }
   int64_t launches = 0;
   ETG_TRY_CUDA(cudaEventRecord(s->ev0, s->stream));
-  const int g = Y3_GRAPH_STEPS;
+  const int g = Y3_GRAPH_STEPS;  // even: a graph ends in the set it starts from
   int64_t left = steps;
   if (left >= g) {
-    auto it = s->graphs.find(g);
+    const int key = s->cur + (fused ? 2 : 0);
+    auto it = s->graphs.find(key);
+    int64_t per = 0;
     if (it == s->graphs.end()) {
       cudaGraph_t graph = nullptr;
       ETG_TRY_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-      int per = 0;
-      for (int k = 0; k < g; ++k) per += launch_step<T>(s, a, sh, mh, se, me, k, s->stream);
-      k3_step_add<<<1, 1, 0, s->stream>>>(s->d_step, g);
+      steps_from<T>(s, fused, hs, es, s->cur, g, &per);
       cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
       if (e != cudaSuccess) {
         set_error("etg_yee3d_advance: graph capture failed: %s", cudaGetErrorString(e));
@@ -385,19 +661,15 @@ int advance(etg_yee3d* s, int64_t steps) {
         set_error("etg_yee3d_advance: graph instantiation failed: %s", cudaGetErrorString(e));
         return ETG_ERR_CUDA;
       }
-      it = s->graphs.emplace(g, exec).first;
-      (void)per;
+      it = s->graphs.emplace(key, exec).first;
+      s->graph_launches[key] = per;
     }
     for (; left >= g; left -= g) {
       ETG_TRY_CUDA(cudaGraphLaunch(it->second, s->stream));
-      launches += (int64_t)g * (2 + (sh.n > 0) + (mh.n > 0) + (se.n > 0) + (me.n > 0)) + 1;
+      launches += s->graph_launches[key];
     }
   }
-  for (int k = 0; k < left; ++k) launches += launch_step<T>(s, a, sh, mh, se, me, k, s->stream);
-  if (left) {
-    k3_step_add<<<1, 1, 0, s->stream>>>(s->d_step, (int)left);
-    ++launches;
-  }
+  if (left) s->cur = steps_from<T>(s, fused, hs, es, s->cur, (int)left, &launches);
   ETG_LAUNCH_CHECK();
   ETG_TRY_CUDA(cudaEventRecord(s->ev1, s->stream));
   g_launches += launches;
@@ -463,15 +735,64 @@ int64_t padded(const etg_yee3d* s, int c, int64_t flat) {
 
 int alloc_psi(etg_yee3d* s, int axis) {
   for (int p = 0; p < Y3_NPSI; ++p) {
-    if (kPsiAxis[p] != axis || s->psi[p]) continue;
-    ETG_REQUIRE(cudaMalloc(&s->psi[p], s->elems * esize(s)) == cudaSuccess, ETG_ERR_ALLOC,
-                "etg_yee3d: psi allocation of %zu bytes failed", s->elems * esize(s));
-    ETG_TRY_CUDA(cudaMemsetAsync(s->psi[p], 0, s->elems * esize(s), s->stream));
+    if (kPsiAxis[p] != axis || s->psi[0][p]) continue;
+    for (int set = 0; set < (s->two_sets ? 2 : 1); ++set) {
+      ETG_REQUIRE(cudaMalloc(&s->psi[set][p], s->elems * esize(s)) == cudaSuccess, ETG_ERR_ALLOC,
+                  "etg_yee3d: psi allocation of %zu bytes failed", s->elems * esize(s));
+      ETG_TRY_CUDA(cudaMemsetAsync(s->psi[set][p], 0, s->elems * esize(s), s->stream));
+    }
   }
   return ETG_OK;
 }
 
+// n steps, each stencil launch timed alone (events): the fused step's kernel in ms_h and 0 in
+// ms_e, or the H and E kernels of the two-kernel step
+template <typename T>
+int time_kernels(etg_yee3d* s, int n_steps, double* ms_h, double* ms_e) {
+  Y3FSrc<T> hs, es;
+  const bool fused = use_fused<T>(s, &hs, &es);
+  if (fused) {
+    int r = ensure_two_sets(s);
+    if (r) return r;
+  }
+  cudaEvent_t ev[4];
+  for (auto& e : ev) ETG_TRY_CUDA(cudaEventCreate(&e));
+  double th = 0, te = 0;
+  int rc = ETG_OK;
+  for (int k = 0; k < n_steps; ++k) {
+    if (fused) {
+      launch_fused<T>(s, s->cur, hs, es, 0, s->stream, ev);
+      s->cur ^= 1;
+    } else {
+      const Y3Args<T> a = args_of<T>(s, s->cur);
+      Y3SrcPhase<T> sh, se;
+      Y3MonPhase<T> mh, me;
+      phases_of<T>(s, true, s->cur, &sh, &mh);
+      phases_of<T>(s, false, s->cur, &se, &me);
+      launch_step<T>(s, a, sh, mh, se, me, 0, s->stream, ev);
+    }
+    k3_step_add<<<1, 1, 0, s->stream>>>(s->d_step, 1);
+    if (cudaEventSynchronize(ev[1]) != cudaSuccess || (!fused && cudaEventSynchronize(ev[3]) != cudaSuccess)) {
+      set_error("etg_yee3d_kernel_timing: %s", cudaGetErrorString(cudaGetLastError()));
+      rc = ETG_ERR_CUDA;
+      break;
+    }
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, ev[0], ev[1]);
+    if (!fused) cudaEventElapsedTime(&b, ev[2], ev[3]);
+    th += a, te += b;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (rc) return rc;
+  ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
+  s->h_step += n_steps;
+  *ms_h = th / n_steps;
+  *ms_e = te / n_steps;
+  return ETG_OK;
+}
+
 }  // namespace
+
 
 extern "C" {
 
@@ -505,7 +826,7 @@ int etg_yee3d_create(etg_yee3d** out, int dtype, int nx, int ny, int nz, int per
     return fail(ETG_ERR_CUDA);
   }
   for (int c = 0; c < Y3_NFIELD + Y3_NCB; ++c) {
-    void** p = c < Y3_NFIELD ? &s->f[c] : &s->cb[c - Y3_NFIELD];
+    void** p = c < Y3_NFIELD ? &s->f[0][c] : &s->cb[c - Y3_NFIELD];
     if (cudaMalloc(p, s->elems * z) != cudaSuccess || cudaMemsetAsync(*p, 0, s->elems * z, s->stream) != cudaSuccess) {
       set_error("etg_yee3d_create: allocation of %zu bytes failed", s->elems * z);
       return fail(ETG_ERR_ALLOC);
@@ -541,8 +862,10 @@ int etg_yee3d_destroy(etg_yee3d* s) {
   if (!s) return ETG_OK;
   if (s->stream) cudaStreamSynchronize(s->stream);
   drop_graphs(s);
-  for (void* p : s->f) cudaFree(p);
-  for (void* p : s->psi) cudaFree(p);
+  for (auto& set : s->f)
+    for (void* p : set) cudaFree(p);
+  for (auto& set : s->psi)
+    for (void* p : set) cudaFree(p);
   for (void* p : s->cb) cudaFree(p);
   for (auto& ax : s->prof)
     for (void* p : ax) cudaFree(p);
@@ -598,7 +921,11 @@ int etg_yee3d_set_field(etg_yee3d* s, int id, const void* host) {
   ETG_REQUIRE(s && host && id >= 0 && id < Y3_NFIELD + Y3_NPSI + Y3_NCB, ETG_ERR_ARGUMENT,
               "etg_yee3d_set_field: bad field id %d", id);
   const int c = field_comp(id);
-  void* dst = id < Y3_NFIELD ? s->f[id] : id < Y3_NFIELD + Y3_NPSI ? s->psi[id - Y3_NFIELD] : s->cb[c];
+  // fields and psi go to both sets: positions no update writes then stay equal in both
+  auto array_of = [&](int set) -> void* {
+    return id < Y3_NFIELD ? s->f[set][id] : id < Y3_NFIELD + Y3_NPSI ? s->psi[set][id - Y3_NFIELD] : s->cb[c];
+  };
+  void* dst = array_of(s->cur);
   if (!dst) {  // psi of an axis without CPML: identically zero, not stored
     int64_t e[3];
     extent(s, c, e);
@@ -609,14 +936,18 @@ int etg_yee3d_set_field(etg_yee3d* s, int id, const void* host) {
                   "etg_yee3d_set_field: psi %d belongs to an axis without CPML and must be +0", id);
     return ETG_OK;
   }
-  return copy_in(s, dst, host, c);
+  int r = copy_in(s, dst, host, c);
+  if (r == ETG_OK && s->two_sets && id < Y3_NFIELD + Y3_NPSI) r = copy_in(s, array_of(s->cur ^ 1), host, c);
+  return r;
 }
 
 int etg_yee3d_get_field(etg_yee3d* s, int id, void* host) {
   ETG_REQUIRE(s && host && id >= 0 && id < Y3_NFIELD + Y3_NPSI + Y3_NCB, ETG_ERR_ARGUMENT,
               "etg_yee3d_get_field: bad field id %d", id);
   const int c = field_comp(id);
-  const void* src = id < Y3_NFIELD ? s->f[id] : id < Y3_NFIELD + Y3_NPSI ? s->psi[id - Y3_NFIELD] : s->cb[c];
+  const void* src = id < Y3_NFIELD              ? s->f[s->cur][id]
+                    : id < Y3_NFIELD + Y3_NPSI ? s->psi[s->cur][id - Y3_NFIELD]
+                                               : s->cb[c];
   if (!src) {
     int64_t e[3];
     extent(s, c, e);
@@ -642,7 +973,7 @@ int etg_yee3d_add_source(etg_yee3d* s, int component, int n_nodes, const int64_t
     ETG_REQUIRE(idx[k] >= 0, ETG_ERR_ARGUMENT, "etg_yee3d_add_source: node %lld outside component %d",
                 (long long)flat[k], component);
   }
-  etg_yee3d::Src q{component, n_nodes, nullptr, nullptr, n0, rows};
+  etg_yee3d::Src q{component, n_nodes, nullptr, nullptr, n0, rows, idx};
   const size_t tb = (size_t)rows * n_nodes * esize(s);
   if (cudaMalloc(&q.idx, n_nodes * sizeof(int64_t)) != cudaSuccess || cudaMalloc(&q.table, tb) != cudaSuccess) {
     cudaFree(q.idx);
@@ -747,43 +1078,15 @@ int etg_yee3d_kernel_timing(etg_yee3d* s, int n_steps, double* ms_h, double* ms_
   for (const auto& q : s->mon)
     ETG_REQUIRE(q.n0 <= s->h_step && s->h_step + n_steps <= q.n0 + q.rows, ETG_ERR_STATE,
                 "etg_yee3d_kernel_timing: a phasor table does not cover the steps");
-  cudaEvent_t ev[4];
-  for (auto& e : ev) ETG_TRY_CUDA(cudaEventCreate(&e));
-  double th = 0, te = 0;
-  int rc = ETG_OK;
-  for (int k = 0; k < n_steps && rc == ETG_OK; ++k) {
-    if (s->dtype == ETG_F32) {
-      const Y3Args<float> a = args_of<float>(s);
-      Y3SrcPhase<float> sh, se;
-      Y3MonPhase<float> mh, me;
-      phases_of<float>(s, true, &sh, &mh);
-      phases_of<float>(s, false, &se, &me);
-      launch_step<float>(s, a, sh, mh, se, me, 0, s->stream, ev);
-    } else {
-      const Y3Args<double> a = args_of<double>(s);
-      Y3SrcPhase<double> sh, se;
-      Y3MonPhase<double> mh, me;
-      phases_of<double>(s, true, &sh, &mh);
-      phases_of<double>(s, false, &se, &me);
-      launch_step<double>(s, a, sh, mh, se, me, 0, s->stream, ev);
-    }
-    k3_step_add<<<1, 1, 0, s->stream>>>(s->d_step, 1);
-    if (cudaEventSynchronize(ev[3]) != cudaSuccess) {
-      set_error("etg_yee3d_kernel_timing: %s", cudaGetErrorString(cudaGetLastError()));
-      rc = ETG_ERR_CUDA;
-      break;
-    }
-    float a = 0, b = 0;
-    cudaEventElapsedTime(&a, ev[0], ev[1]);
-    cudaEventElapsedTime(&b, ev[2], ev[3]);
-    th += a, te += b;
-  }
-  for (auto& e : ev) cudaEventDestroy(e);
-  if (rc) return rc;
+  return s->dtype == ETG_F32 ? time_kernels<float>(s, n_steps, ms_h, ms_e) : time_kernels<double>(s, n_steps, ms_h, ms_e);
+}
+
+int etg_yee3d_set_option(etg_yee3d* s, int option, int64_t value) {
+  ETG_REQUIRE(s && option == ETG3_OPT_FUSED && (value == 0 || value == 1), ETG_ERR_ARGUMENT,
+              "etg_yee3d_set_option: bad option %d or value %lld", option, (long long)value);
   ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
-  s->h_step += n_steps;
-  *ms_h = th / n_steps;
-  *ms_e = te / n_steps;
+  s->fused = value == 1;
+  drop_graphs(s);
   return ETG_OK;
 }
 

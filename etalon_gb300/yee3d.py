@@ -336,9 +336,11 @@ def _ptr(a: np.ndarray) -> int:
 
 class Yee3DEngine:
     """One resident 3D run. ``table_steps``: steps the source and phasor tables cover (the
-    problem's n_steps by default). Not thread-safe; one engine per host thread."""
+    problem's n_steps by default). ``fused``: an H and an E kernel per step in place (False,
+    the default and the faster), or one kernel per step over two buffer sets; both give the
+    same bits. Not thread-safe; one engine per host thread."""
 
-    def __init__(self, problem: Yee3DProblem, *, table_steps: int | None = None) -> None:
+    def __init__(self, problem: Yee3DProblem, *, table_steps: int | None = None, fused: bool = False) -> None:
         self.problem = problem
         g = problem.grid
         self.real, self.complex = problem.real, problem.complex
@@ -348,6 +350,7 @@ class Yee3DEngine:
         call("etg_yee3d_create", C.byref(handle), _lib.dtype_code(self.real), g.nx, g.ny, g.nz, mask)
         self._h = handle
         try:
+            call("etg_yee3d_set_option", self._h, 0, int(bool(fused)))
             c = cast_coefficients_3d(problem)
             self._coeffs = c
             scal = np.array([c["db"], c["inv_dx"], c["inv_dy"], c["inv_dz"]], dtype=self.real)
@@ -380,6 +383,10 @@ class Yee3DEngine:
 
     def advance(self, k: int) -> None:
         call("etg_yee3d_advance", self._h, int(k))
+
+    def set_fused(self, fused: bool) -> None:
+        """Switch between the fused step and the two-kernel step (the state carries over)."""
+        call("etg_yee3d_set_option", self._h, 0, int(bool(fused)))
 
     def synchronize(self) -> None:
         call("etg_yee3d_synchronize", self._h)
@@ -414,7 +421,8 @@ class Yee3DEngine:
         return ms.value, launches.value
 
     def kernel_timing(self, steps: int) -> tuple[float, float]:
-        """Run ``steps`` more steps, timing each H and E stencil launch alone: mean ms of each."""
+        """Run ``steps`` more steps, timing each stencil launch alone: mean ms of the fused
+        step's kernel and 0, or of the H and the E kernel."""
         h, e = C.c_double(), C.c_double()
         call("etg_yee3d_kernel_timing", self._h, int(steps), C.byref(h), C.byref(e))
         return h.value, e.value

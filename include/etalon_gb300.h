@@ -318,7 +318,7 @@ int etg_debug_set_wait_tries(int64_t tries);
  * Ey -= cb_ey ((dHz/dx / kx + psi_ey_x) - (dHx/dz / kz + psi_ey_z)),
  * Ez += cb_ez ((dHy/dx / kx + psi_ez_x) - (dHx/dy / ky + psi_ez_y)),
  * psi <- b psi + c d before each use; one IEEE rounding per operation, no fused multiply-add.
- * A step is H, H sources, H monitors, E, E sources, E monitors. */
+ * A step is H, H sources, H monitors, E, E sources, E monitors (etg_yee3d_set_option). */
 #define ETG3_EX 0
 #define ETG3_EY 1
 #define ETG3_EZ 2
@@ -361,8 +361,16 @@ int etg_yee3d_synchronize(etg_yee3d* sim);
 int etg_yee3d_step_index(etg_yee3d* sim, int64_t* n);
 /* device time (CUDA events) of the last etg_yee3d_advance and its kernel launches */
 int etg_yee3d_last_timing(etg_yee3d* sim, double* ms, int64_t* launches);
-/* n_steps more steps, each H and E stencil launch timed alone: mean ms per launch */
+/* n_steps more steps, each stencil launch timed alone: mean ms per launch of the fused step's
+ * kernel (ms_h; ms_e = 0) or of the H and E kernels of the two-kernel step */
 int etg_yee3d_kernel_timing(etg_yee3d* sim, int n_steps, double* ms_h, double* ms_e);
+/* ETG3_OPT_FUSED (default 0): 0 = an H and an E kernel per step, in place, sources by their
+ * own kernels; 1 = one kernel per step, H and E together, from one buffer set into a second
+ * (allocated at the first such step: twice the field and psi memory), point sources applied
+ * inside it (at most 16 per phase, 32 distinct nodes per phase; more run the two-kernel step).
+ * Both give the same bits; the two-kernel step is the faster on GB300. */
+#define ETG3_OPT_FUSED 0
+int etg_yee3d_set_option(etg_yee3d* sim, int option, int64_t value);
 
 #ifdef __cplusplus
 }

@@ -4,8 +4,9 @@ oracle/yee3d_numpy.py is pinned to the 2D TE oracle, and so to Etalon's outputs,
 tests/test_yee3d_oracle.py. Here the CUDA engine (etalon_gb300/csrc/etg_yee3d.cu, through the
 etg_yee3d_* C ABI) must match it on every field, psi and DFT accumulator: CPML on all faces,
 periodic axes, an invariant (2D) run, float32 and float64, step counts that end inside and
-on a 32-step graph. At a size too large for the oracle, a centred dipole must stay exactly
-mirror symmetric.
+on a 32-step graph, the fused step (one kernel over two buffer sets, sources applied inside
+it) and the two-kernel step. At a size too large for the oracle, a centred dipole must stay
+exactly mirror symmetric.
 """
 
 import ctypes as C
@@ -34,14 +35,15 @@ CASES = {
 }
 
 
+@pytest.mark.parametrize("fused", [True, False], ids=["fused", "two-kernel"])
 @pytest.mark.parametrize("precision", ["single", "double"])
 @pytest.mark.parametrize("steps", [70, 32])
 @pytest.mark.parametrize("case", list(CASES))
-def test_engine_matches_oracle(gpu, precision, steps, case):
+def test_engine_matches_oracle(gpu, precision, steps, case, fused):
     p = case3d(precision, n_steps=steps, **CASES[case])
     o = oracle_3d(p)
     o.run(steps)
-    with yee3d.Yee3DEngine(p) as e:
+    with yee3d.Yee3DEngine(p, fused=fused) as e:
         e.advance(steps)
         e.synchronize()
         assert e.n == steps
@@ -52,14 +54,15 @@ def test_engine_matches_oracle(gpu, precision, steps, case):
     assert np.abs(o.ez).max() > 0 and np.abs(o.hy).max() > 0
 
 
+@pytest.mark.parametrize("fused", [True, False], ids=["fused", "two-kernel"])
 @pytest.mark.parametrize("precision", ["single", "double"])
-def test_engine_from_a_random_state(gpu, precision):
+def test_engine_from_a_random_state(gpu, precision, fused):
     """Uploaded fields and psi (inside the strips) continue exactly as in the oracle."""
     p = case3d(precision, n_steps=40)
     o = oracle_3d(p)
     rng = np.random.default_rng(11)
     g = p.grid
-    with yee3d.Yee3DEngine(p) as e:
+    with yee3d.Yee3DEngine(p, fused=fused) as e:
         for c in ("ex", "ey", "ez", "hx", "hy", "hz"):
             v = rng.standard_normal(getattr(o, c).shape).astype(p.real)
             getattr(o, c)[...] = v
@@ -74,8 +77,15 @@ def test_engine_from_a_random_state(gpu, precision):
             getattr(o, name)[...] = v
             e.set_field(name, v)
         # the E arrays on PEC walls stay as uploaded; the oracle keeps them as well
-        o.run(40)
-        e.advance(40)
+        o.run(33)
+        e.advance(33)
+        e.synchronize()
+        for name in Oracle3D.FIELDS:
+            assert np.array_equal(raw(e.field(name)), raw(getattr(o, name))), name
+        # switching the step form mid-run continues the same bits
+        e.set_fused(not fused)
+        o.run(7)
+        e.advance(7)
         e.synchronize()
         for name in Oracle3D.FIELDS:
             assert np.array_equal(raw(e.field(name)), raw(getattr(o, name))), name

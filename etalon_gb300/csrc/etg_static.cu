@@ -76,11 +76,11 @@ int advance_static(int nx, int ny, int64_t pitch, void* const f[7], const void* 
                    const void* cb_ey, const void* const c[12], double db, double inv_dx,
                    double inv_dy, int64_t n_steps) {
   // size check first, before any device access: the tile count of the default shape bounds
-  // the tile list whatever the interior/CPML split
+  // the tile list whatever the interior/CPML split (one column more for a shifted first column)
   int ER, EC, K;
   tb_default_shape((int)sizeof(T), &ER, &EC, &K);
   const int64_t tiles_max = (int64_t)((nx + 1 + ER - 2 * K - 1) / (ER - 2 * K)) *
-                            ((ny + 1 + EC - 2 * K - 1) / (EC - 2 * K));
+                            ((ny + 1 + EC - 2 * K - 1) / (EC - 2 * K) + 1);
   const size_t plane = (size_t)(nx + 2) * pitch * sizeof(T);
   const size_t counters = 7 * plane, tiles_at = counters + 256;
   const size_t need = tiles_at + (size_t)tiles_max * sizeof(int2);

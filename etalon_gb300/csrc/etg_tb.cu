@@ -1019,9 +1019,24 @@ static void split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_
                         int* n_hot = nullptr, int* kind_hot = nullptr) {
   const int OR = ER - 2 * K, OC = EC - 2 * K;
   const int rlo = std::max(ux_lo, 1), rhi = std::min(ux_hi, nx), clo = std::max(uy_lo, 1), chi = std::min(uy_hi, ny);
+  // First output column: shifted left by up to one tile width, in steps of a lane's W columns
+  // (vector loads and TMA boxes stay 16-byte aligned), so that the fewest tile columns reach
+  // the CPML columns. A CPML tile costs about two interior ones; ties keep column 0. At 2024
+  // columns and 112-column tiles a shift of -52 leaves two CPML tile columns instead of three
+  // (the third held the last 8 columns). Rows keep row 0: the tile kind is packed above them.
+  int co = 0;
+  {
+    const int W = EC / 32;
+    int best = 1 << 30;
+    for (int off = 0; off > -OC; off -= W) {
+      int cost = 0;
+      for (int c0 = off; c0 <= ny; c0 += OC) cost += (c0 - K >= clo && c0 + OC + K <= chi) ? 1 : 2;
+      if (cost < best) best = cost, co = off;
+    }
+  }
   std::vector<int2> inner, pml;
   for (int r0 = 0; r0 <= nx; r0 += OR)
-    for (int c0 = 0; c0 <= ny; c0 += OC) {
+    for (int c0 = co; c0 <= ny; c0 += OC) {
       const bool ux = r0 - K >= rlo && r0 + OR + K <= rhi, uy = c0 - K >= clo && c0 + OC + K <= chi;
       if (ux && uy) {
         inner.push_back(make_int2(r0, c0));

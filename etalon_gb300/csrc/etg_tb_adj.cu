@@ -337,8 +337,10 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
         Vw cx;
         cx.ld(sCbx + (lr0 + t) * EC + lj0);
         gx_row(t, cx, gxr);
+        // interior tiles leave lane 31 its own value: the tile's last column is K columns from
+        // the output and a wrong value there moves one column per reverse step
         T gxn = __shfl_down_sync(0xffffffffu, gxr[0], 1);
-        if (lane == 31) gxn = zero<T>();
+        if (PML && lane == 31) gxn = zero<T>();
         if (t < RPT - 1) {
           Vw cy;
           cy.ld(sCby + (lr0 + t + 1) * EC + lj0);
@@ -396,7 +398,7 @@ __device__ __forceinline__ void tb_adj_tile(const TBAdjArgs<T>& a, const int2 ti
           }
         }
         T hxp = __shfl_up_sync(0xffffffffu, hxc[W - 1], 1);
-        if (lane == 0) hxp = zero<T>();
+        if (PML && lane == 0) hxp = zero<T>();  // lane 0 of interior tiles: as lane 31 above
 #pragma unroll
         for (int e = 0; e < W; ++e) {
           const T hxleft = e > 0 ? hxc[e - 1] : hxp;

@@ -87,34 +87,40 @@ struct Y3MonPhase {
 // CPML term of an update along `axis` at position `pos` (W = 0: integer positions, E updates;
 // W = 1: half positions, H updates): psi <- b psi + c d, then d / kappa + psi
 // (numpy_backend.py:41-61 per axis). Outside the strips b = 1, c = 0, 1/kappa = 1 and psi is +0,
-// so the term is d + 0 exactly and nothing is loaded. Inside, psi and the profile are read
-// here, after the field loads: strip cells pay the extra round trip, the others keep few
-// registers (many cells in flight per SM).
+// so the term is d + 0 exactly and nothing is loaded. Inside (`strip`, worked out once per axis
+// and thread), psi and the profile are read here, after the field loads: strip cells pay the
+// extra round trip, the others keep few registers (many cells in flight per SM).
 template <typename T, int W>
-__device__ __forceinline__ T term(const Y3Args<T>& a, int p, int axis, int pos, int64_t idx, T d) {
+__device__ __forceinline__ T term(const Y3Args<T>& a, bool strip, int p, int axis, int pos, int64_t idx, T d) {
+  if (!strip) return add(d, T(0));
   T* const psi = a.psi[p];
-  const int lo = W ? a.lo_h[axis] : a.lo_e[axis], hi = W ? a.hi_h[axis] : a.hi_e[axis];
-  if (psi == nullptr || (pos >= lo && pos < hi)) return add(d, T(0));
   const T* const* pr = a.prof[axis] + 3 * W;
   const T v = add(mul(pr[0][pos], psi[idx]), mul(pr[1][pos], d));
   psi[idx] = v;
   return add(mul(d, pr[2][pos]), v);
 }
 
-// H^(n-1/2) -> H^(n+1/2) from E^n: forward differences (the +1 neighbour wraps to 0 on a
+// whether position `pos` along `axis` lies in a CPML strip of the H (W = 1) or E (W = 0) profile
+template <typename T, int W>
+__device__ __forceinline__ bool in_strip(const Y3Args<T>& a, int axis, int pos) {
+  const int lo = W ? a.lo_h[axis] : a.lo_e[axis], hi = W ? a.hi_h[axis] : a.hi_e[axis];
+  return a.psi[axis == 0 ? 3 : axis == 1 ? 0 : 1] != nullptr && (pos < lo || pos >= hi);
+}
+
+// H^(n-1/2) -> H^(n+1/2) from E^n: forward differences (PER: the +1 neighbour wraps to 0 on a
 // periodic axis). Hx lives at (integer x, half y, half z), Hy at (half, integer, half), Hz at
 // (half, half, integer). One thread per (i, j, k), z across the lanes of a warp; all field
 // loads first, then the three updates.
-template <typename T>
+template <typename T, bool PER>
 __global__ void __launch_bounds__(256) k3_update_h(const Y3Args<T> a) {
   const int k = blockIdx.x * 32 + threadIdx.x;
   const int j = blockIdx.y * 8 + threadIdx.y;
   const int i = blockIdx.z;
   if (k >= a.m2 || j >= a.m1) return;
   const int64_t idx = i * a.si + j * a.sj + k;
-  const int dk = (a.p2 && k + 1 == a.n2) ? -k : 1;
-  const int dj = (a.p1 && j + 1 == a.n1) ? -j * (int)a.sj : (int)a.sj;
-  const int64_t di = (a.p0 && i + 1 == a.n0) ? -(int64_t)i * a.si : a.si;
+  const int dk = (PER && a.p2 && k + 1 == a.n2) ? -k : 1;
+  const int dj = (PER && a.p1 && j + 1 == a.n1) ? -j * (int)a.sj : (int)a.sj;
+  const int64_t di = (PER && a.p0 && i + 1 == a.n0) ? -(int64_t)i * a.si : a.si;
   const bool vx = j < a.n1 && k < a.n2, vy = i < a.n0 && k < a.n2, vz = i < a.n0 && j < a.n1;
   const T* __restrict__ ex = a.ex + idx;
   const T* __restrict__ ey = a.ey + idx;
@@ -124,39 +130,42 @@ __global__ void __launch_bounds__(256) k3_update_h(const Y3Args<T> a) {
   const T ey_k = vx ? ey[dk] : T(0), ez_j = vx ? ez[dj] : T(0);
   const T ez_i = vy ? ez[di] : T(0), ex_k = vy ? ex[dk] : T(0);
   const T ex_j = vz ? ex[dj] : T(0), ey_i = vz ? ey[di] : T(0);
+  // (the strip tests are evaluated where they are used: held across the loads they cost the
+  // fp32 kernel registers and occupancy)
   if (vx) {
-    const T tz = term<T, 1>(a, 1, 2, k, idx, mul(sub(ey_k, ey0), a.inv_dz));
-    const T ty = term<T, 1>(a, 0, 1, j, idx, mul(sub(ez_j, ez0), a.inv_dy));
+    const T tz = term<T, 1>(a, in_strip<T, 1>(a, 2, k), 1, 2, k, idx, mul(sub(ey_k, ey0), a.inv_dz));
+    const T ty = term<T, 1>(a, in_strip<T, 1>(a, 1, j), 0, 1, j, idx, mul(sub(ez_j, ez0), a.inv_dy));
     a.hx[idx] = add(hx0, mul(a.db, sub(tz, ty)));
   }
   if (vy) {
-    const T tx = term<T, 1>(a, 3, 0, i, idx, mul(sub(ez_i, ez0), a.inv_dx));
-    const T tz = term<T, 1>(a, 2, 2, k, idx, mul(sub(ex_k, ex0), a.inv_dz));
+    const T tx = term<T, 1>(a, in_strip<T, 1>(a, 0, i), 3, 0, i, idx, mul(sub(ez_i, ez0), a.inv_dx));
+    const T tz = term<T, 1>(a, in_strip<T, 1>(a, 2, k), 2, 2, k, idx, mul(sub(ex_k, ex0), a.inv_dz));
     a.hy[idx] = add(hy0, mul(a.db, sub(tx, tz)));
   }
   if (vz) {
-    const T ty = term<T, 1>(a, 5, 1, j, idx, mul(sub(ex_j, ex0), a.inv_dy));
-    const T tx = term<T, 1>(a, 4, 0, i, idx, mul(sub(ey_i, ey0), a.inv_dx));
+    const T ty = term<T, 1>(a, in_strip<T, 1>(a, 1, j), 5, 1, j, idx, mul(sub(ex_j, ex0), a.inv_dy));
+    const T tx = term<T, 1>(a, in_strip<T, 1>(a, 0, i), 4, 0, i, idx, mul(sub(ey_i, ey0), a.inv_dx));
     a.hz[idx] = add(hz0, mul(a.db, sub(ty, tx)));
   }
 }
 
 // E^n -> E^(n+1) from H^(n+1/2): backward differences at the integer positions off the PEC
-// walls (1 .. n-1), or at all n on a periodic axis (the -1 neighbour of 0 is n-1). Tangential
-// E on a wall is never written and stays as it is. All loads first, then the three updates.
-template <typename T>
+// walls (1 .. n-1), or at all n on a periodic axis (PER; the -1 neighbour of 0 is n-1).
+// Tangential E on a wall is never written and stays as it is. All loads first, then the
+// three updates.
+template <typename T, bool PER>
 __global__ void __launch_bounds__(256) k3_update_e(const Y3Args<T> a) {
   const int k = blockIdx.x * 32 + threadIdx.x;
   const int j = blockIdx.y * 8 + threadIdx.y;
   const int i = blockIdx.z;
   if (k >= a.m2 || j >= a.m1) return;
   const int64_t idx = i * a.si + j * a.sj + k;
-  const bool in_i = a.p0 ? i < a.n0 : (i >= 1 && i < a.n0);
-  const bool in_j = a.p1 ? j < a.n1 : (j >= 1 && j < a.n1);
-  const bool in_k = a.p2 ? k < a.n2 : (k >= 1 && k < a.n2);
-  const int bk = (k == 0) ? a.n2 - 1 : -1;
-  const int bj = (j == 0) ? (a.n1 - 1) * (int)a.sj : -(int)a.sj;
-  const int64_t bi = (i == 0) ? (int64_t)(a.n0 - 1) * a.si : -a.si;
+  const bool in_i = (PER && a.p0) ? i < a.n0 : (i >= 1 && i < a.n0);
+  const bool in_j = (PER && a.p1) ? j < a.n1 : (j >= 1 && j < a.n1);
+  const bool in_k = (PER && a.p2) ? k < a.n2 : (k >= 1 && k < a.n2);
+  const int bk = (PER && k == 0) ? a.n2 - 1 : -1;
+  const int bj = (PER && j == 0) ? (a.n1 - 1) * (int)a.sj : -(int)a.sj;
+  const int64_t bi = (PER && i == 0) ? (int64_t)(a.n0 - 1) * a.si : -a.si;
   const bool vx = i < a.n0 && in_j && in_k, vy = in_i && j < a.n1 && in_k, vz = in_i && in_j && k < a.n2;
   const T* __restrict__ hx = a.hx + idx;
   const T* __restrict__ hy = a.hy + idx;
@@ -168,19 +177,20 @@ __global__ void __launch_bounds__(256) k3_update_e(const Y3Args<T> a) {
   const T ex0 = vx ? a.ex[idx] : T(0), cx = vx ? a.cb_ex[idx] : T(0);
   const T ey0 = vy ? a.ey[idx] : T(0), cy = vy ? a.cb_ey[idx] : T(0);
   const T ez0 = vz ? a.ez[idx] : T(0), cz = vz ? a.cb_ez[idx] : T(0);
+  const bool sx = in_strip<T, 0>(a, 0, i), sy = in_strip<T, 0>(a, 1, j), sz = in_strip<T, 0>(a, 2, k);
   if (vx) {
-    const T ty = term<T, 0>(a, 6, 1, j, idx, mul(sub(hz0, hz_j), a.inv_dy));
-    const T tz = term<T, 0>(a, 7, 2, k, idx, mul(sub(hy0, hy_k), a.inv_dz));
+    const T ty = term<T, 0>(a, sy, 6, 1, j, idx, mul(sub(hz0, hz_j), a.inv_dy));
+    const T tz = term<T, 0>(a, sz, 7, 2, k, idx, mul(sub(hy0, hy_k), a.inv_dz));
     a.ex[idx] = add(ex0, mul(cx, sub(ty, tz)));
   }
   if (vy) {
-    const T tx = term<T, 0>(a, 9, 0, i, idx, mul(sub(hz0, hz_i), a.inv_dx));
-    const T tz = term<T, 0>(a, 8, 2, k, idx, mul(sub(hx0, hx_k), a.inv_dz));
+    const T tx = term<T, 0>(a, sx, 9, 0, i, idx, mul(sub(hz0, hz_i), a.inv_dx));
+    const T tz = term<T, 0>(a, sz, 8, 2, k, idx, mul(sub(hx0, hx_k), a.inv_dz));
     a.ey[idx] = sub(ey0, mul(cy, sub(tx, tz)));
   }
   if (vz) {
-    const T tx = term<T, 0>(a, 10, 0, i, idx, mul(sub(hy0, hy_i), a.inv_dx));
-    const T ty = term<T, 0>(a, 11, 1, j, idx, mul(sub(hx0, hx_j), a.inv_dy));
+    const T tx = term<T, 0>(a, sx, 10, 0, i, idx, mul(sub(hy0, hy_i), a.inv_dx));
+    const T ty = term<T, 0>(a, sy, 11, 1, j, idx, mul(sub(hx0, hx_j), a.inv_dy));
     a.ez[idx] = add(ez0, mul(cz, sub(tx, ty)));
   }
 }
@@ -589,12 +599,16 @@ int launch_step(const etg_yee3d* s, const Y3Args<T>& a, const Y3SrcPhase<T>& sh,
   const dim3 block(32, 8), grid((s->m[2] + 31) / 32, (s->m[1] + 7) / 8, s->m[0]);
   int launches = 2;
   if (ev) cudaEventRecord(ev[0], st);
-  k3_update_h<T><<<grid, block, 0, st>>>(a);
+  // the H kernel keeps its run-time periodic tests either way: specialised it takes 36 fp32
+  // registers (against 32) and loses more in occupancy than it saves in instructions
+  const bool per = s->per[0] || s->per[1] || s->per[2];
+  k3_update_h<T, true><<<grid, block, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[1], st);
   if (sh.n) k3_inject<T><<<1, 32, 0, st>>>(sh, s->d_step, s_off, s->d_flag), ++launches;
   if (mh.n) k3_dft<T><<<dim3(mon_blocks(s, true), mh.n), 256, 0, st>>>(mh, s->d_step, s_off, s->d_flag), ++launches;
   if (ev) cudaEventRecord(ev[2], st);
-  k3_update_e<T><<<grid, block, 0, st>>>(a);
+  if (per) k3_update_e<T, true><<<grid, block, 0, st>>>(a);
+  else k3_update_e<T, false><<<grid, block, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[3], st);
   if (se.n) k3_inject<T><<<1, 32, 0, st>>>(se, s->d_step, s_off, s->d_flag), ++launches;
   if (me.n) k3_dft<T><<<dim3(mon_blocks(s, false), me.n), 256, 0, st>>>(me, s->d_step, s_off, s->d_flag), ++launches;

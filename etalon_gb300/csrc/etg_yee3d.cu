@@ -457,6 +457,14 @@ namespace {
 
 size_t esize(const etg_yee3d* s) { return s->dtype == ETG_F32 ? 4 : 8; }
 
+// cudaMalloc that leaves *p null when it fails (so a later attempt or destroy sees no array)
+bool dev_alloc(void** p, size_t bytes) {
+  if (cudaMalloc(p, bytes) == cudaSuccess) return true;
+  *p = nullptr;
+  (void)cudaGetLastError();
+  return false;
+}
+
 // extent of field c (0..5) along each axis
 void extent(const etg_yee3d* s, int c, int64_t out[3]) {
   for (int a = 0; a < 3; ++a) out[a] = kHalf[c][a] ? s->n[a] : s->m[a];
@@ -545,20 +553,23 @@ bool fused_sources(const etg_yee3d* s, bool magnetic, Y3FSrc<T>* out) {
   return true;
 }
 
-// The second set: allocated at the first fused step as a copy of the current one.
+// The second set: allocated at the first fused step as a copy of the current one (arrays a
+// failed earlier attempt allocated are kept, not allocated again; destroy frees them).
 int ensure_two_sets(etg_yee3d* s) {
   if (s->two_sets) return ETG_OK;
   const size_t bytes = s->elems * esize(s);
   const int other = s->cur ^ 1;
   for (int c = 0; c < Y3_NFIELD; ++c) {
-    ETG_REQUIRE(cudaMalloc(&s->f[other][c], bytes) == cudaSuccess, ETG_ERR_ALLOC,
-                "etg_yee3d: second field set (%zu bytes per array) could not be allocated", bytes);
+    if (!s->f[other][c])
+      ETG_REQUIRE(dev_alloc(&s->f[other][c], bytes), ETG_ERR_ALLOC,
+                  "etg_yee3d: second field set (%zu bytes per array) could not be allocated", bytes);
     ETG_TRY_CUDA(cudaMemcpyAsync(s->f[other][c], s->f[s->cur][c], bytes, cudaMemcpyDeviceToDevice, s->stream));
   }
   for (int p = 0; p < Y3_NPSI; ++p) {
     if (!s->psi[s->cur][p]) continue;
-    ETG_REQUIRE(cudaMalloc(&s->psi[other][p], bytes) == cudaSuccess, ETG_ERR_ALLOC,
-                "etg_yee3d: second psi set could not be allocated");
+    if (!s->psi[other][p])
+      ETG_REQUIRE(dev_alloc(&s->psi[other][p], bytes), ETG_ERR_ALLOC,
+                  "etg_yee3d: second psi set could not be allocated");
     ETG_TRY_CUDA(cudaMemcpyAsync(s->psi[other][p], s->psi[s->cur][p], bytes, cudaMemcpyDeviceToDevice, s->stream));
   }
   ETG_TRY_CUDA(cudaStreamSynchronize(s->stream));
@@ -749,9 +760,10 @@ int64_t padded(const etg_yee3d* s, int c, int64_t flat) {
 
 int alloc_psi(etg_yee3d* s, int axis) {
   for (int p = 0; p < Y3_NPSI; ++p) {
-    if (kPsiAxis[p] != axis || s->psi[0][p]) continue;
+    if (kPsiAxis[p] != axis) continue;
     for (int set = 0; set < (s->two_sets ? 2 : 1); ++set) {
-      ETG_REQUIRE(cudaMalloc(&s->psi[set][p], s->elems * esize(s)) == cudaSuccess, ETG_ERR_ALLOC,
+      if (s->psi[set][p]) continue;
+      ETG_REQUIRE(dev_alloc(&s->psi[set][p], s->elems * esize(s)), ETG_ERR_ALLOC,
                   "etg_yee3d: psi allocation of %zu bytes failed", s->elems * esize(s));
       ETG_TRY_CUDA(cudaMemsetAsync(s->psi[set][p], 0, s->elems * esize(s), s->stream));
     }
@@ -841,7 +853,7 @@ int etg_yee3d_create(etg_yee3d** out, int dtype, int nx, int ny, int nz, int per
   }
   for (int c = 0; c < Y3_NFIELD + Y3_NCB; ++c) {
     void** p = c < Y3_NFIELD ? &s->f[0][c] : &s->cb[c - Y3_NFIELD];
-    if (cudaMalloc(p, s->elems * z) != cudaSuccess || cudaMemsetAsync(*p, 0, s->elems * z, s->stream) != cudaSuccess) {
+    if (!dev_alloc(p, s->elems * z) || cudaMemsetAsync(*p, 0, s->elems * z, s->stream) != cudaSuccess) {
       set_error("etg_yee3d_create: allocation of %zu bytes failed", s->elems * z);
       return fail(ETG_ERR_ALLOC);
     }
@@ -852,7 +864,7 @@ int etg_yee3d_create(etg_yee3d** out, int dtype, int nx, int ny, int nz, int per
     for (int q = 0; q < 6; ++q) {
       std::vector<double> one(len[q], q % 3 == 1 ? 0.0 : 1.0);
       std::vector<float> onef(one.begin(), one.end());
-      if (cudaMalloc(&s->prof[a][q], len[q] * z) != cudaSuccess ||
+      if (!dev_alloc(&s->prof[a][q], len[q] * z) ||
           cudaMemcpy(s->prof[a][q], dtype == ETG_F32 ? (const void*)onef.data() : (const void*)one.data(), len[q] * z,
                      cudaMemcpyHostToDevice) != cudaSuccess) {
         set_error("etg_yee3d_create: profile allocation failed");
@@ -861,7 +873,7 @@ int etg_yee3d_create(etg_yee3d** out, int dtype, int nx, int ny, int nz, int per
     }
     s->lo_e[a] = 0, s->hi_e[a] = s->m[a], s->lo_h[a] = 0, s->hi_h[a] = s->n[a];
   }
-  if (cudaMalloc(&s->d_step, sizeof(int64_t)) != cudaSuccess || cudaMalloc(&s->d_flag, sizeof(int)) != cudaSuccess ||
+  if (!dev_alloc((void**)&s->d_step, sizeof(int64_t)) || !dev_alloc((void**)&s->d_flag, sizeof(int)) ||
       cudaMemsetAsync(s->d_step, 0, sizeof(int64_t), s->stream) != cudaSuccess ||
       cudaMemsetAsync(s->d_flag, 0, sizeof(int), s->stream) != cudaSuccess ||
       cudaStreamSynchronize(s->stream) != cudaSuccess) {
@@ -989,7 +1001,7 @@ int etg_yee3d_add_source(etg_yee3d* s, int component, int n_nodes, const int64_t
   }
   etg_yee3d::Src q{component, n_nodes, nullptr, nullptr, n0, rows, idx};
   const size_t tb = (size_t)rows * n_nodes * esize(s);
-  if (cudaMalloc(&q.idx, n_nodes * sizeof(int64_t)) != cudaSuccess || cudaMalloc(&q.table, tb) != cudaSuccess) {
+  if (!dev_alloc((void**)&q.idx, n_nodes * sizeof(int64_t)) || !dev_alloc(&q.table, tb)) {
     cudaFree(q.idx);
     set_error("etg_yee3d_add_source: allocation failed");
     return ETG_ERR_ALLOC;
@@ -1018,8 +1030,7 @@ int etg_yee3d_add_monitor(etg_yee3d* s, int component, int n_nodes, const int64_
   }
   etg_yee3d::Mon q{component, n_nodes, n_f, nullptr, nullptr, nullptr, n0, rows};
   const size_t ab = (size_t)2 * n_nodes * n_f * esize(s), tb = (size_t)2 * rows * n_f * esize(s);
-  if (cudaMalloc(&q.idx, n_nodes * sizeof(int64_t)) != cudaSuccess || cudaMalloc(&q.acc, ab) != cudaSuccess ||
-      cudaMalloc(&q.table, tb) != cudaSuccess) {
+  if (!dev_alloc((void**)&q.idx, n_nodes * sizeof(int64_t)) || !dev_alloc(&q.acc, ab) || !dev_alloc(&q.table, tb)) {
     cudaFree(q.idx);
     cudaFree(q.acc);
     set_error("etg_yee3d_add_monitor: allocation failed");

@@ -382,9 +382,10 @@ def kernel_roofline(e, p) -> dict:
     Temporally blocked path: one more run of the workload with every kernel launch timed on
     its own (option TIMING = 2: the kernels one after the other, an event pair around each, no
     graphs). The dominant kernel is the lean interior kernel (interior tiles without a source,
-    monitor or trace node); it advances its output cells K steps per launch, and its algorithmic
-    bytes are those of K single-pass steps over them, 8 values per cell-step (Ex, Ey, Hz read
-    and write, cb_ex and cb_ey read).
+    monitor or trace node; at 2024² with 40-row, K = 8 tiles the segment kernel, which steps them
+    as column segments, a tile and three tiles that take the row above from it); it advances its
+    output cells K steps per launch, and its algorithmic bytes are those of K single-pass steps
+    over them, 8 values per cell-step (Ex, Ey, Hz read and write, cb_ex and cb_ey read).
     One-step path: the run's own time per step against the algorithmic bytes of a step.
     """
     from etalon_gb300 import _lib
@@ -400,9 +401,12 @@ def kernel_roofline(e, p) -> dict:
     kt = e.kernel_timing()
     e.set_option(_lib.OPT_TIMING, 1)
     ms, launches, cells = kt["interior"]
+    segments = get_option(e, _lib.OPT_TB_SEGMENTS_USED)
     if launches:
         dt = "float" if s == 4 else "double"
         name = f"k_tb_step<{dt},{rows // warps},{depth},false,{warps},false>"  # the lean interior kernel
+        if segments:  # the lean interior tiles as column segments (the leftover tiles timed with the rest)
+            name = f"k_tb_seg<{dt},{rows // warps},{depth},{warps}> ({segments} column segments of 5 tile rows)"
         launch_ms = ms / launches
         bytes_launch = 8 * s * cells * depth
         cp_ms, cp_launches, cp_cells = kt["cpml"]
@@ -410,8 +414,8 @@ def kernel_roofline(e, p) -> dict:
                  "output_cells_per_launch": cells, "launch_ms": launch_ms, "launches_timed": launches,
                  "cpml_kernel": {"launch_ms": cp_ms / max(cp_launches, 1), "output_cells_per_launch": cp_cells},
                  "timing": "CUDA events around each launch, one extra run of the workload, kernels serialised"}
-        tag = (f"k_tb_step_interior_{rows}x{128 if s == 4 else 64}" + ("" if warps == 8 else f"_{warps}w")
-               + ("" if depth == (4 if s == 4 else 2) else f"_k{depth}"))
+        tag = (f"k_tb_{'seg' if segments else 'step'}_interior_{rows}x{128 if s == 4 else 64}"
+               + ("" if warps == 8 else f"_{warps}w") + ("" if depth == (4 if s == 4 else 2) else f"_k{depth}"))
     elif kind in (3, 4):  # persistent kernels: the run's device time over its launches
         e.reset()
         e.advance(p.n_steps)

@@ -19,6 +19,7 @@ FIELD_IDS = {"ex": EX, "ey": EY, "hz": HZ, "psi_ex_y": PSI_EX_Y, "psi_ey_x": PSI
              "psi_hz_x": PSI_HZ_X, "psi_hz_y": PSI_HZ_Y}  # fmt: skip
 COMPONENT_IDS = {"Ex": EX, "Ey": EY, "Hz": HZ}
 OPT_KERNEL, OPT_TB_DEPTH, OPT_GRAPH_STEPS, OPT_TILE_ROWS, OPT_TILE_COLS, OPT_CHECK_FINITE, OPT_TIMING, OPT_TB_WARPS = range(8)
+OPT_TB_SEGMENTS, OPT_TB_SEGMENTS_USED = 8, 9
 
 vp, i32, i64, f64, sz = C.c_void_p, C.c_int, C.c_int64, C.c_double, C.c_size_t
 pi64 = C.POINTER(C.c_int64)

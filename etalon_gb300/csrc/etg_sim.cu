@@ -211,7 +211,7 @@ int advance_plain(etg_sim* s, int64_t n_steps) {
 
 template <typename T>
 int advance_dispatch(etg_sim* s, int64_t n_steps) {
-  int64_t opt[8];
+  int64_t opt[10];
   memcpy(opt, s->opt, sizeof opt);
   // per-node db (TM mode): the TMA-fed kernels stage cb themselves and do not take it, so such a
   // simulation runs the plain temporally blocked kernel instead
@@ -698,7 +698,7 @@ int etg_sim_synchronize(etg_sim* s) {
 }
 
 int etg_sim_set_option(etg_sim* s, int option, int64_t value) {
-  ETG_REQUIRE(s && option >= 0 && option < 8, ETG_ERR_ARGUMENT, "etg_sim_set_option: bad option %d", option);
+  ETG_REQUIRE(s && option >= 0 && option < 9, ETG_ERR_ARGUMENT, "etg_sim_set_option: bad option %d", option);
   ETG_REQUIRE(value >= 0, ETG_ERR_ARGUMENT, "etg_sim_set_option: negative value");
   s->opt[option] = value;
   invalidate_graphs(s);
@@ -707,7 +707,11 @@ int etg_sim_set_option(etg_sim* s, int option, int64_t value) {
 }
 
 int etg_sim_get_option(etg_sim* s, int option, int64_t* value) {
-  ETG_REQUIRE(s && value && option >= 0 && option < 8, ETG_ERR_ARGUMENT, "etg_sim_get_option: bad option");
+  ETG_REQUIRE(s && value && option >= 0 && option < 10, ETG_ERR_ARGUMENT, "etg_sim_get_option: bad option");
+  if (option == ETG_OPT_TB_SEGMENTS_USED) {  // read-only: column segments of the current tile list
+    *value = s->tb ? tb_segments(s->tb) : 0;
+    return ETG_OK;
+  }
   *value = s->opt[option];
   if (*value == 0 && option == ETG_OPT_TB_WARPS) *value = 8;
   if (*value == 0 && (option == ETG_OPT_TB_DEPTH || option == ETG_OPT_TILE_ROWS || option == ETG_OPT_TILE_COLS)) {

@@ -209,7 +209,7 @@ struct etg_sim {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0;
   int64_t last_launches = 0;
-  int64_t opt[8] = {0, 0, 32, 0, 0, 0, 0, 0};  // 0 = default (tile shape: per dtype)
+  int64_t opt[10] = {0, 0, 32, 0, 0, 0, 0, 0, 0, 0};  // 0 = default (tile shape: per dtype)
   std::map<int64_t, cudaGraphExec_t> graphs;  // keyed by steps per graph
   TBState* tb = nullptr;                      // temporally blocked kernel state
   // adjoint support: Hz trace window and whether monitors accumulate (off while recomputing)

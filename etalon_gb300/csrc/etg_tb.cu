@@ -622,6 +622,12 @@ struct TBState {
   int n_kind[6] = {};            // CPML tiles of each kind (the CPML list is sorted by kind), then
                                  // how many of each lead their kind with a source, monitor or trace
   unsigned* ctr = nullptr;       // persistent pipelined kernel: claim counters of the two launches
+  // column segments of the lean interior tiles (k_tb_seg; tiles ER = 5K rows high): segs[0 ..
+  // n_segs) = (first output row of the head, first column), then n_left lean tiles (r0, c0)
+  // that no segment takes; the lean tiles of the tile list stay for the launches that cannot
+  // use segments (traces, the TM variants, per-kernel timing)
+  int2* segs = nullptr;
+  int n_segs = 0, n_left = 0, seg_carried = 0;
 };
 
 TBState* tb_create() { return new TBState; }
@@ -636,6 +642,7 @@ void tb_destroy(TBState* tb) {
   tb_drop_graphs(tb);
   for (void* p : tb->alt) cudaFree(p);
   cudaFree(tb->tiles);
+  cudaFree(tb->segs);
   cudaFree(tb->ctr);
   for (cudaEvent_t e : tb->pev)
     if (e) cudaEventDestroy(e);
@@ -648,6 +655,8 @@ void tb_destroy(TBState* tb) {
   if (tb->join) cudaEventDestroy(tb->join);
   delete tb;
 }
+
+int tb_segments(const TBState* tb) { return tb && tb->tiles_valid ? tb->n_segs : 0; }
 
 void tb_invalidate(TBState* tb) {
   if (!tb) return;
@@ -723,9 +732,29 @@ static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<
   const int2* hot = tb->tiles;                 // interior tiles with sources, monitors or traces
   const int2* cold = tb->tiles + tb->n_hot;    // the other interior tiles: the lean kernel
   const int n_cold = tb->n_inner - tb->n_hot;
+  // lean interior tiles as column segments (a head and carried tiles, k_tb_seg) plus the lean
+  // tiles no segment takes; not with a trace (a segment recompute may skip tiles) or TM
+  bool segments = false;
+  if constexpr (!TMM && RPT * NW == 5 * K) segments = tb->n_segs > 0 && ph.trace.buf == nullptr;
+  auto launch_segments = [&](cudaStream_t main) {
+    cudaError_t e2 = cudaSuccess;
+    if constexpr (!TMM && RPT * NW == 5 * K) {
+      k_tb_seg<T, RPT, K, NW><<<tb->n_segs, dim3(32, NW), tb_smem<T, RPT, K, false, NW>(), main>>>(
+          a, d, tb->segs, tb->seg_carried, ph, pe, step_off);
+      g_launches += 1;
+      e2 = cudaGetLastError();
+    }
+    return e2;
+  };
+  auto launch_left = [&](cudaStream_t stream) {  // the lean tiles no segment takes
+    return tb_launch_one<T, RPT, K, false, NW, false, TMM>(a, d, tb->segs + tb->n_segs, tb->n_left, ph, pe,
+                                                           step_off, stream);
+  };
   if (tb->profile) {  // one after the other on s, an event pair around each kernel
     cudaError_t e = cudaEventRecord(tb->pev[0], s);
-    if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW, false, TMM>(a, d, cold, n_cold, ph, pe, step_off, s);
+    if (e == cudaSuccess)  // timed as the interior: the segments alone, or every lean tile
+      e = segments ? launch_segments(s)
+                   : tb_launch_one<T, RPT, K, false, NW, false, TMM>(a, d, cold, n_cold, ph, pe, step_off, s);
     const int2* t = tb->tiles + tb->n_inner;
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
       int only[6] = {0, 0, 0, 0, 0, 0};
@@ -740,6 +769,7 @@ static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<
     }
     if (e == cudaSuccess) e = cudaEventRecord(tb->pev[4], s);
     if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW, true, TMM>(a, d, hot, tb->n_hot, ph, pe, step_off, s);
+    if (e == cudaSuccess && segments) e = launch_left(s);  // with the other tiles
     if (e == cudaSuccess) e = cudaEventRecord(tb->pev[5], s);
     if (e == cudaSuccess) e = cudaEventSynchronize(tb->pev[5]);
     float m[5] = {};
@@ -759,7 +789,11 @@ static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<
     e = tb_launch_kinds<T, RP, K, TMM>(a, d, tb->tiles + tb->n_inner, tb->n_kind, ph, pe, step_off, tb->sides);
   if (e == cudaSuccess)
     e = tb_launch_one<T, RPT, K, false, NW, true, TMM>(a, d, hot, tb->n_hot, ph, pe, step_off, tb->sides[3]);
-  if (e == cudaSuccess) e = tb_launch_one<T, RPT, K, false, NW, false, TMM>(a, d, cold, n_cold, ph, pe, step_off, s);
+  // (segments on the main stream, the lean tiles no segment takes beside the plan tiles)
+  if (e == cudaSuccess && segments) e = launch_left(tb->sides[3]);
+  if (e == cudaSuccess)
+    e = segments ? launch_segments(s)
+                 : tb_launch_one<T, RPT, K, false, NW, false, TMM>(a, d, cold, n_cold, ph, pe, step_off, s);
   for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
     e = cudaEventRecord(tb->joins[k], tb->sides[k]);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, tb->joins[k], 0);
@@ -837,6 +871,11 @@ static cudaError_t tb_attrs() {
   }
 #undef ETG_STEP_ATTR
 #undef ETG_KIND_ATTR
+  if constexpr (RPT * NW == 5 * K) {
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_tb_seg<T, RPT, K, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)tb_smem<T, RPT, K, false, NW>());
+  }
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_tb_step<T, RPT * NW / 8, K, true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)tb_smem<T, RPT * NW / 8, K, true, 8>());
@@ -1192,6 +1231,43 @@ static int tb_prepare(TBState* tb, const SimArgs<T>& a, const int64_t* opt, cons
     tb->tiles = nullptr;
     ETG_TRY_CUDA(cudaMalloc(&tb->tiles, inner.size() * sizeof(int2)));
     ETG_TRY_CUDA(cudaMemcpy(tb->tiles, inner.data(), inner.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    // column segments: runs of lean interior tiles in one column, five ordinary tiles' rows per
+    // segment (a head and three carried tiles), when the tile is ER = 5K rows high
+    cudaFree(tb->segs);
+    tb->segs = nullptr;
+    tb->n_segs = tb->n_left = tb->seg_carried = 0;
+    if (tb->cfg.NW * tb->cfg.RPT == 5 * tb->cfg.K && mode == 0 && opt[ETG_OPT_TB_SEGMENTS] == 0) {
+      if (tb->sms == 0) {
+        int dev = 0;
+        ETG_TRY_CUDA(cudaGetDevice(&dev));
+        ETG_TRY_CUDA(cudaDeviceGetAttribute(&tb->sms, cudaDevAttrMultiProcessorCount, dev));
+      }
+      std::vector<int2> lean(inner.begin() + tb->n_hot, inner.begin() + tb->n_inner);
+      std::sort(lean.begin(), lean.end(), [](int2 p, int2 q) { return p.y != q.y ? p.y < q.y : p.x < q.x; });
+      std::vector<int2> segs, left;
+      for (size_t b = 0; b < lean.size();) {
+        size_t e = b + 1;  // a run: one column, rows OR apart
+        while (e < lean.size() && lean[e].y == lean[b].y && lean[e].x == lean[e - 1].x + OR) ++e;
+        const size_t n = e - b, g = n / 5;
+        for (size_t q = 0; q < g; ++q) segs.push_back(lean[b + 5 * q]);
+        for (size_t q = 5 * g; q < n; ++q) left.push_back(lean[b + q]);
+        b = e;
+      }
+      // a segment holds four tiles' work in one CTA: with fewer segments than SMs the launch
+      // cannot fill the GPU and the ordinary tiles are faster
+      if ((int)segs.size() >= tb->sms && tb->sms > 0) {
+        tb->n_segs = (int)segs.size();
+        tb->n_left = (int)left.size();
+        tb->seg_carried = 3;
+        // per-kernel timing counts the segments as the interior, the leftover tiles with the rest
+        const int64_t per_tile = (int64_t)OR * OC;  // an interior tile's output lies inside the grid
+        tb->owned_cells[0] -= (int64_t)left.size() * per_tile;
+        tb->owned_cells[1] += (int64_t)left.size() * per_tile;
+        segs.insert(segs.end(), left.begin(), left.end());
+        ETG_TRY_CUDA(cudaMalloc(&tb->segs, segs.size() * sizeof(int2)));
+        ETG_TRY_CUDA(cudaMemcpy(tb->segs, segs.data(), segs.size() * sizeof(int2), cudaMemcpyHostToDevice));
+      }
+    }
     tb->nx = a.nx;
     tb->ny = a.ny;
     tb->tiles_valid = true;

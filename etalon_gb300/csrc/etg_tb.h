@@ -53,6 +53,8 @@ void tb_split_tiles(int nx, int ny, int ux_lo, int ux_hi, int uy_lo, int uy_hi, 
                     int* kind_hot = nullptr);
 
 inline int tb_tile_row(int2 t) { return t.x & ((1 << 28) - 1); }
+// Column segments (k_tb_seg) of the current tile list, 0 if it uses none.
+int tb_segments(const TBState* tb);
 inline int tb_tile_kind(int2 t) { return t.x >> 28; }
 
 TBState* tb_create();

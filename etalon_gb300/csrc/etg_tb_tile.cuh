@@ -110,6 +110,18 @@ struct TBNoHook {
   __device__ void operator()() const {}
 };
 
+// Carried tiles (CARRY): consecutive interior tiles of one column, stepped by one CTA. Each
+// tile stores, at every step s, the new Hz of its local row ER - K - 1 in half `par` of a
+// shared carry buffer (the row just above the next tile's first output row); a carried tile
+// has no top halo (its first local row is its first output row) and takes that row's Hz at
+// step s from the other half for the Ey update of its first row, the one value from above a
+// step needs. The values are the ones a top halo would have recomputed, bit for bit.
+template <typename T>
+struct TBCarry {
+  int par = 0;            // the half this tile writes; a carried tile reads the other
+  bool carried = false;   // false: an ordinary tile with its K-row top halo (a segment's head)
+};
+
 // STAGED (interior tiles of the persistent kernel): Ex, Ey, Hz of the extended tile are
 // already in shared memory at `stage` (three planes) and cb at `cb_s` (two planes), placed
 // there by TMA; the exchange rows live at `xch_s`. `after_load` runs on every thread right
@@ -122,17 +134,18 @@ struct TBNoHook {
 // cb_ex and cb_ey both hold dt/mu0, so the cb_ey plane of the tile carries the per-node
 // Hz-position coefficient (SimArgs::db_node) and the Ey update reads the cb_ex plane.
 template <typename T, int RPT, int K, int KIND, bool STAGED = false, typename Hook = TBNoHook, int NW = 8,
-          bool PLAN = true, bool TMM = false>
+          bool PLAN = true, bool TMM = false, bool CARRY = false>
 __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst, const int2 tile,
                                         const PhasePlan<T>& ph, const PhasePlan<T>& pe, int step_off,
                                         const T* stage = nullptr, T* cb_s = nullptr, T* xch_s = nullptr,
-                                        Hook after_load = Hook()) {
+                                        Hook after_load = Hook(), const TBCarry<T>& carry = TBCarry<T>()) {
   using S = TBShape<T, RPT, K, KIND, NW>;
   using Vw = TBVec<T>;
   constexpr int W = S::W, ER = S::ER, EC = S::EC, PL = S::PL;
   constexpr bool PML = KIND != KIND_INNER, PX = (KIND & KIND_X) != 0, PY = (KIND & KIND_Y) != 0;
   static_assert(!STAGED || !PML, "only interior tiles are staged");
   static_assert(!STAGED || NW == 8, "the staged layout is for 8 warps");
+  static_assert(!CARRY || (!PML && !PLAN && !STAGED && !TMM), "carried tiles are lean interior tiles");
   extern __shared__ __align__(16) unsigned char tb_smem[];
   T* const sCbx = STAGED ? cb_s : reinterpret_cast<T*>(tb_smem);
   T* const sCby = sCbx + PL;
@@ -157,7 +170,11 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
     }
   }
   const int lane = threadIdx.x, ty = threadIdx.y;
-  const int R0 = tile.x - K, C0 = tile.y - K;  // global cell of local (0, 0); C0 % W == 0
+  // carried tiles: one carry buffer per CTA, kept from tile to tile (declared here, once for
+  // both forms of the step loop below)
+  __shared__ __align__(16) T carry_s[CARRY ? 2 * K * EC : 1];
+  const int TH = (CARRY && carry.carried) ? 0 : K;  // top halo rows
+  const int R0 = tile.x - TH, C0 = tile.y - K;     // global cell of local (0, 0); C0 % W == 0
   const int nx = a.nx, ny = a.ny;
   const int64_t P = a.P;
   const int lj0 = W * lane, j0 = C0 + lj0;     // this lane's first column, local and global
@@ -313,7 +330,7 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
   const int64_t n_base = *a.step + step_off;
   const T db = a.db, idx = a.inv_dx, idy = a.inv_dy;
   // owned output cells of this thread: rows t in [t_lo, t_hi), columns e in [e_lo, e_hi)
-  const int t_lo = max(0, K - lr0), t_hi = min(RPT, ER - K - lr0);
+  const int t_lo = max(0, TH - lr0), t_hi = min(RPT, ER - K - lr0);
   const int e_lo = lj0 >= K ? 0 : W, e_hi = lj0 + W <= EC - K ? W : 0;
   const bool traced = PLAN && ph.trace.buf && ph.trace.ti0 < tile.x + S::OR && ph.trace.ti0 + ph.trace.tnx > tile.x &&
                       ph.trace.tj0 < tile.y + S::OC && ph.trace.tj0 + ph.trace.tny > tile.y;
@@ -408,6 +425,15 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
         }
       }
       hz[RPT - 1].st(sHzX + (ty + 1) * EC + lj0);
+      if constexpr (CARRY) {
+        constexpr int CR = ER - K - 1;  // the row above the next tile
+        if (ty == CR / RPT) hz[CR % RPT].st(carry_s + (carry.par * K + s) * EC + lj0);
+        if (carry.carried && ty == 0) {  // the row above this tile, from the previous tile
+          Vw c;
+          c.ld(carry_s + ((carry.par ^ 1) * K + s) * EC + lj0);
+          c.st(sHzX + lj0);
+        }
+      }
       __syncthreads();
       // ---------------------------------------------------------------- E half step
       {
@@ -566,6 +592,29 @@ k_tb_step(const __grid_constant__ SimArgs<T> a, const __grid_constant__ TBDst<T>
     case KIND_X: tb_tile_nw<T, RPT, K, KIND_X, NW>(a, dst, u, ph, pe, step_off); break;
     case KIND_Y: tb_tile_nw<T, RPT, K, KIND_Y, NW>(a, dst, u, ph, pe, step_off); break;
     default: tb_tile_nw<T, RPT, K, KIND_XY, NW>(a, dst, u, ph, pe, step_off); break;
+  }
+}
+
+// A column segment of interior tiles in one CTA: an ordinary lean tile (the head, output rows
+// [r, r + ER - 2K)) followed by n_carried carried tiles of ER - K output rows each, every one
+// taking the row above it from its predecessor (TBCarry). With ER = 5K, a head and three
+// carried tiles cover the rows of five ordinary tiles with four tiles' arithmetic.
+template <typename T, int RPT, int K, int NW>
+__global__ void __launch_bounds__(32 * NW, TBShape<T, RPT, K, KIND_INNER, NW>::MIN_BLOCKS)
+k_tb_seg(const __grid_constant__ SimArgs<T> a, const __grid_constant__ TBDst<T> dst,
+         const int2* __restrict__ segs, int n_carried, const __grid_constant__ PhasePlan<T> ph,
+         const __grid_constant__ PhasePlan<T> pe, int step_off) {
+  using S = TBShape<T, RPT, K, KIND_INNER, NW>;
+  const int2 g = segs[blockIdx.x];
+  int r = g.x;
+  for (int u = 0; u <= n_carried; ++u) {
+    TBCarry<T> c;
+    c.par = u & 1;
+    c.carried = u > 0;
+    tb_tile<T, RPT, K, KIND_INNER, false, TBNoHook, NW, false, false, true>(a, dst, make_int2(r, g.y), ph, pe,
+                                                                            step_off, nullptr, nullptr, nullptr,
+                                                                            TBNoHook(), c);
+    r += u == 0 ? S::OR : S::ER - K;
   }
 }
 

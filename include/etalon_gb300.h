@@ -300,6 +300,12 @@ int etg_debug_set_wait_tries(int64_t tries);
                                    tile has TILE_ROWS / TB_WARPS rows per warp */
 #define ETG_OPT_TIMING 6        /* 1 = record CUDA-event timing of each advance,
                                    2 = also time each temporally blocked kernel launch */
+#define ETG_OPT_TB_SEGMENTS 8   /* 0 = lean interior tiles of one column stepped as segments by one
+                                   CTA (a tile with its top halo, then three tiles that take the row
+                                   above from their predecessor: five tiles' rows for four tiles'
+                                   work, same bits) when the tile is 5K rows high and the segments
+                                   at least fill the SMs; 1 = ordinary tiles only */
+#define ETG_OPT_TB_SEGMENTS_USED 9  /* read-only: column segments of the current tile list */
 
 /* ---------------------------------------------------------------- 3D Yee
  * Has no counterpart in Etalon: etalon/fdtd/capabilities.py:7-24 refuses 3D. The engine

@@ -11,6 +11,7 @@ CPML ψ and every DFT accumulator is bitwise identical, in float32 and float64.
 
 from __future__ import annotations
 
+import ctypes as C
 import os
 from concurrent.futures import ThreadPoolExecutor
 from types import SimpleNamespace
@@ -353,6 +354,31 @@ def test_config2_prefix_vs_live_oracle(gpu, precision, depth):
     if depth:
         e.set_option(_lib.OPT_TB_DEPTH, depth)
     e.advance(n)
+    o = _oracle_for(p)
+    workers = min(16, os.cpu_count() or 1)
+    with ThreadPoolExecutor(workers) as pool:
+        o.run(n, pool=pool, bands=workers)
+    for f in FIELDS:
+        assert np.array_equal(_bits(e.field(f)), _bits(getattr(o, f))), f
+    for k, acc in enumerate(o.acc):
+        assert np.array_equal(e.dft(k).view(np.uint8), acc.view(np.uint8))
+
+
+@pytest.mark.parametrize("segments", [0, 1], ids=["column-segments", "ordinary-tiles"])
+def test_column_segments_vs_live_oracle(gpu, segments):
+    """At 2024² with 40-row tiles and K = 8 the lean interior tiles run as column segments (a
+    tile with its top halo, then three that take the row above from it); with segments off,
+    as ordinary tiles. Both against the oracle for 136 steps (8 launch pairs and a remainder),
+    in raw bits."""
+    n = 136
+    p = cases.config2("single", n_steps=n)
+    e = TEEngine(p)
+    e.set_option(_lib.OPT_TB_DEPTH, 8)
+    e.set_option(_lib.OPT_TB_SEGMENTS, segments)
+    e.advance(n)
+    used = C.c_int64()
+    _lib.call("etg_sim_get_option", e._h, _lib.OPT_TB_SEGMENTS_USED, C.byref(used))
+    assert (used.value > 0) == (segments == 0), used.value
     o = _oracle_for(p)
     workers = min(16, os.cpu_count() or 1)
     with ThreadPoolExecutor(workers) as pool:

@@ -399,9 +399,9 @@ def kernel_roofline(e, p) -> dict:
     e.advance(p.n_steps)
     e.synchronize()
     kt = e.kernel_timing()
+    segments = get_option(e, _lib.OPT_TB_SEGMENTS_USED)  # of the tile list this run used
     e.set_option(_lib.OPT_TIMING, 1)
     ms, launches, cells = kt["interior"]
-    segments = get_option(e, _lib.OPT_TB_SEGMENTS_USED)
     if launches:
         dt = "float" if s == 4 else "double"
         name = f"k_tb_step<{dt},{rows // warps},{depth},false,{warps},false>"  # the lean interior kernel

@@ -733,13 +733,13 @@ static cudaError_t tb_launch_pair(TBState* tb, const SimArgs<T>& a, const TBDst<
   const int2* cold = tb->tiles + tb->n_hot;    // the other interior tiles: the lean kernel
   const int n_cold = tb->n_inner - tb->n_hot;
   // lean interior tiles as column segments (a head and carried tiles, k_tb_seg) plus the lean
-  // tiles no segment takes; not with a trace (a segment recompute may skip tiles) or TM
+  // tiles no segment takes; not with a trace (a segment recompute may skip tiles)
   bool segments = false;
-  if constexpr (!TMM && RPT * NW == 5 * K) segments = tb->n_segs > 0 && ph.trace.buf == nullptr;
+  if constexpr (RPT * NW == 5 * K) segments = tb->n_segs > 0 && ph.trace.buf == nullptr;
   auto launch_segments = [&](cudaStream_t main) {
     cudaError_t e2 = cudaSuccess;
-    if constexpr (!TMM && RPT * NW == 5 * K) {
-      k_tb_seg<T, RPT, K, NW><<<tb->n_segs, dim3(32, NW), tb_smem<T, RPT, K, false, NW>(), main>>>(
+    if constexpr (RPT * NW == 5 * K) {
+      k_tb_seg<T, RPT, K, NW, TMM><<<tb->n_segs, dim3(32, NW), tb_smem<T, RPT, K, false, NW>(), main>>>(
           a, d, tb->segs, tb->seg_carried, ph, pe, step_off);
       g_launches += 1;
       e2 = cudaGetLastError();
@@ -873,7 +873,10 @@ static cudaError_t tb_attrs() {
 #undef ETG_KIND_ATTR
   if constexpr (RPT * NW == 5 * K) {
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_tb_seg<T, RPT, K, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      e = cudaFuncSetAttribute(k_tb_seg<T, RPT, K, NW, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)tb_smem<T, RPT, K, false, NW>());
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_tb_seg<T, RPT, K, NW, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)tb_smem<T, RPT, K, false, NW>());
   }
   if (e == cudaSuccess)

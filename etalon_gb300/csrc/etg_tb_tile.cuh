@@ -145,7 +145,7 @@ __device__ __forceinline__ void tb_tile(const SimArgs<T>& a, const TBDst<T>& dst
   constexpr bool PML = KIND != KIND_INNER, PX = (KIND & KIND_X) != 0, PY = (KIND & KIND_Y) != 0;
   static_assert(!STAGED || !PML, "only interior tiles are staged");
   static_assert(!STAGED || NW == 8, "the staged layout is for 8 warps");
-  static_assert(!CARRY || (!PML && !PLAN && !STAGED && !TMM), "carried tiles are lean interior tiles");
+  static_assert(!CARRY || (!PML && !PLAN && !STAGED), "carried tiles are lean interior tiles");
   extern __shared__ __align__(16) unsigned char tb_smem[];
   T* const sCbx = STAGED ? cb_s : reinterpret_cast<T*>(tb_smem);
   T* const sCby = sCbx + PL;
@@ -599,7 +599,7 @@ k_tb_step(const __grid_constant__ SimArgs<T> a, const __grid_constant__ TBDst<T>
 // [r, r + ER - 2K)) followed by n_carried carried tiles of ER - K output rows each, every one
 // taking the row above it from its predecessor (TBCarry). With ER = 5K, a head and three
 // carried tiles cover the rows of five ordinary tiles with four tiles' arithmetic.
-template <typename T, int RPT, int K, int NW>
+template <typename T, int RPT, int K, int NW, bool TMM = false>
 __global__ void __launch_bounds__(32 * NW, TBShape<T, RPT, K, KIND_INNER, NW>::MIN_BLOCKS)
 k_tb_seg(const __grid_constant__ SimArgs<T> a, const __grid_constant__ TBDst<T> dst,
          const int2* __restrict__ segs, int n_carried, const __grid_constant__ PhasePlan<T> ph,
@@ -611,7 +611,7 @@ k_tb_seg(const __grid_constant__ SimArgs<T> a, const __grid_constant__ TBDst<T> 
     TBCarry<T> c;
     c.par = u & 1;
     c.carried = u > 0;
-    tb_tile<T, RPT, K, KIND_INNER, false, TBNoHook, NW, false, false, true>(a, dst, make_int2(r, g.y), ph, pe,
+    tb_tile<T, RPT, K, KIND_INNER, false, TBNoHook, NW, false, TMM, true>(a, dst, make_int2(r, g.y), ph, pe,
                                                                             step_off, nullptr, nullptr, nullptr,
                                                                             TBNoHook(), c);
     r += u == 0 ? S::OR : S::ER - K;

@@ -55,3 +55,33 @@ def test_tm_runs_are_refused_by_batches_and_the_adjoint(gpu):
             _lib.call("etg_batch_create", C.byref(h), 1, (C.c_void_p * 1)(e.te._h.value))
         with pytest.raises(ValueError, match="TM mode"):
             _lib.call("etg_adj_create", C.byref(h), e.te._h, 20, 4, 20, 4)
+
+
+def test_tm_column_segments_vs_tm_oracle(gpu):
+    """The headline grid in TM mode (2024², the strip, an Ez source) with 40-row tiles and K = 8:
+    the lean interior tiles run as column segments of the TM variant. 80 steps against the TM
+    oracle, bit for bit (the wave has reached the segments above and below the source tile)."""
+    import ctypes as C
+
+    from etalon_gb300 import _lib
+    from tests import cases
+
+    p = tm.tm_problem(
+        size=(40.0, 40.0), dl=0.02, background_eps=cases.EPS_OXIDE,
+        boxes=[ph.Box((0.0, 0.0, 0.0), (42.0, 0.5, 0.22), cases.EPS_SILICON)], pml=ph.PMLSpec(layers=12),
+        sources=[tm.TMPointSource((-15.0, 0.0, 0.0), ph.GaussianPulse(1.55, 0.5))],
+        monitors=[ph.DFTMonitor("m", [1.5, 1.6], center=(5.0, 0.0, 0.0))], n_steps=80, precision="single",
+    )  # fmt: skip
+    o = oracle_tm(p)
+    o.run(80)
+    with tm.TMEngine(p) as e:
+        e.te.set_option(_lib.OPT_TB_DEPTH, 8)
+        e.advance(80)
+        e.synchronize()
+        used = C.c_int64()
+        _lib.call("etg_sim_get_option", e.te._h, _lib.OPT_TB_SEGMENTS_USED, C.byref(used))
+        assert used.value > 0
+        for name in o.FIELDS:
+            assert np.array_equal(raw(e.field(name)), raw(getattr(o, name))), name
+        for k in range(len(p.components)):
+            assert np.array_equal(raw(e.dft(k)), raw(o.acc[k])), k

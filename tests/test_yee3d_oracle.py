@@ -125,3 +125,31 @@ def test_layout_and_setup_errors():
     with pytest.raises(ValueError, match="outside the grid"):
         yee3d.yee3d_problem((0.4, 0.3, 0.2), 0.05, layers=0,
                             sources=[ph.PointSource((5.0, 0.0, 0.0), "Ez", ph.GaussianPulse(1.55, 0.5))])  # fmt: skip
+
+
+def test_trilinear_sampling_and_injection_weights():
+    """Point sources and point monitors take the bracketing nodes along each axis with linear
+    weights (etalon/fdtd/dft.py:39-66 per axis): the weights sum to one, a field linear in x, y
+    and z interpolates exactly, and a plane monitor covers the nodes inside its span."""
+    p = yee3d.yee3d_problem((1.0, 0.8, 0.6), 0.05, layers=4, background_eps=2.085,
+                            sources=[ph.PointSource((0.013, -0.021, 0.037), "Ez", ph.GaussianPulse(1.55, 0.5))],
+                            monitors=[ph.DFTMonitor("p", [1.55], center=(0.11, 0.07, -0.03)),
+                                      ph.DFTMonitor("plane", [1.55], center=(0.0, 0.0, 0.0), size=(0.4, 0.3, 0.0),
+                                                    components=("Hz",))])  # fmt: skip
+    g = p.grid
+    inj = p.injections[0]
+    assert inj.flat.size == 8 and abs(inj.weights.sum() - 1.0) < 1e-12
+    for s in p.samplings:
+        x, y, z = g.coords(s.component)
+        ii, jj, kk = np.unravel_index(s.flat_index, g.shape(s.component))
+        if s.monitor == "p":
+            f = 2.0 * x[ii] - 3.0 * y[jj] + 0.5 * z[kk] + 1.0  # linear: the interpolation is exact
+            value = s.interpolate(f[None, :].astype(np.complex128))[0].real
+            assert abs(value - (2.0 * 0.11 - 3.0 * 0.07 + 0.5 * -0.03 + 1.0)) < 1e-12
+        else:
+            assert np.all(np.abs(x[ii]) <= 0.2 + 1e-9) and np.all(np.abs(y[jj]) <= 0.15 + 1e-9)
+            assert s.flat_index.size == np.unique(ii).size * np.unique(jj).size * np.unique(kk).size
+    # the E coefficient of an injection uses the permittivity at each of its nodes
+    i, j, k = np.unravel_index(inj.flat, g.shape("Ez"))
+    expected = g.dt / (yee3d.EPSILON_0 * p.eps["Ez"][i, j, k]) * inj.weights / (g.dx * g.dy * g.dz * 1e-18)
+    np.testing.assert_allclose(inj.coefficient, expected, rtol=1e-12)

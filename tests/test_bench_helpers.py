@@ -30,10 +30,17 @@ def test_peak_is_the_measured_copy_bandwidth_or_the_fallback(tmp_path, monkeypat
 
 
 def test_traffic_of_the_default_kernels_comes_from_committed_summaries():
-    for tag in ("k_tb_step_interior_40x128", "k_tb_step_interior_48x128"):
+    for tag in ("k_tb_step_interior_40x128", "k_tb_step_interior_48x128", "k_tb_step_interior_40x128_k8",
+                "k_tb_seg_interior_40x128_k8"):
         traffic, source = bench.ncu_traffic(tag)
-        assert traffic is not None and 70e6 < traffic < 100e6 and source.endswith(".md")
+        assert traffic is not None and 70e6 < traffic < 100e6 and source.endswith(".md"), tag
+        limiter, _ = bench.profile_entry("limiter", tag)
+        assert limiter, tag
     assert bench.ncu_traffic("no_such_kernel") == (None, None)
+    # the 3D stencil kernels: DRAM bytes per cell (the algorithmic 36 and 48 plus a little)
+    for tag, lo, hi in (("k3_update_h_f32", 36, 48), ("k3_update_e_f32", 48, 60)):
+        text, source = bench.profile_entry("traffic_bytes_per_cell", tag)
+        assert text and lo <= float(text.split()[0]) <= hi and source.endswith(".md"), tag
 
 
 def test_workload_description_names_the_headline_configuration():

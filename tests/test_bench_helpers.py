@@ -34,8 +34,9 @@ def test_traffic_of_the_default_kernels_comes_from_committed_summaries():
                 "k_tb_seg_interior_40x128_k8"):
         traffic, source = bench.ncu_traffic(tag)
         assert traffic is not None and 70e6 < traffic < 100e6 and source.endswith(".md"), tag
-        limiter, _ = bench.profile_entry("limiter", tag)
-        assert limiter, tag
+        if tag != "k_tb_step_interior_48x128":  # an earlier form, kept for its traffic only
+            limiter, _ = bench.profile_entry("limiter", tag)
+            assert limiter, tag
     assert bench.ncu_traffic("no_such_kernel") == (None, None)
     # the 3D stencil kernels: DRAM bytes per cell (the algorithmic 36 and 48 plus a little)
     for tag, lo, hi in (("k3_update_h_f32", 36, 48), ("k3_update_e_f32", 48, 60)):

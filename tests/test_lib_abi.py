@@ -64,6 +64,18 @@ def test_injected_fault_is_reported(monkeypatch):
     assert err.value.code == _lib.ERR_INJECTED
 
 
+def test_injected_fault_in_the_3d_create_is_reported(monkeypatch):
+    import ctypes as C
+
+    from etalon_gb300 import _lib
+
+    monkeypatch.setenv("ETG_FAULT", "etg_yee3d_create")
+    h = C.c_void_p()
+    with pytest.raises(_lib.EtgError, match="fault injected") as err:
+        _lib.call("etg_yee3d_create", C.byref(h), 4, 8, 8, 8, 0)
+    assert err.value.code == _lib.ERR_INJECTED and h.value is None
+
+
 @pytest.mark.parametrize(
     "name,args,words",
     [
@@ -75,6 +87,25 @@ def test_injected_fault_is_reported(monkeypatch):
         ("etg_sim_rasterize_cb", (None, 0.0, 0.0, 0.02, 0.02, 1e-16, 8.85e-12, 1.0, 0, None), "bad arguments"),
         ("etg_sim_get_cb", (None, 0, None), "bad arguments"),
         ("etg_sim_set_cb_window", (None, 0, 0, 1, 0, 1, None), "bad arguments"),
+        ("etg_yee3d_create", ("HANDLE", 3, 8, 8, 8, 0), "bad arguments"),      # dtype must be 4 or 8
+        ("etg_yee3d_create", ("HANDLE", 4, 8, 8, 0, 0), "bad arguments"),      # empty axis
+        ("etg_yee3d_create", ("HANDLE", 4, 8, 8, 8, 8), "bad arguments"),      # periodic mask of 3 bits
+        ("etg_yee3d_create", (None, 4, 8, 8, 8, 0), "bad arguments"),
+        ("etg_yee3d_create", ("HANDLE", 8, 70000, 8, 8, 0), "too large"),
+        ("etg_yee3d_create", ("HANDLE", 4, 60000, 60000, 60000, 0), "too large"),
+        ("etg_yee3d_set_scalars", (None, None), "null argument"),
+        ("etg_yee3d_set_profile", (None, 0, None, None, None, None, None, None), "bad arguments"),
+        ("etg_yee3d_set_field", (None, 0, None), "bad field id"),
+        ("etg_yee3d_get_field", (None, 0, None), "bad field id"),
+        ("etg_yee3d_add_source", (None, 0, 1, None, 0, 1, None), "bad arguments"),
+        ("etg_yee3d_add_monitor", (None, 0, 1, None, 1, 0, 1, None), "bad arguments"),
+        ("etg_yee3d_get_dft", (None, 0, None), "bad monitor"),
+        ("etg_yee3d_advance", (None, 1), "bad arguments"),
+        ("etg_yee3d_synchronize", (None,), "null handle"),
+        ("etg_yee3d_step_index", (None, None), "null argument"),
+        ("etg_yee3d_last_timing", (None, None, None), "null argument"),
+        ("etg_yee3d_kernel_timing", (None, 1, None, None), "bad arguments"),
+        ("etg_yee3d_set_option", (None, 0, 1), "bad option"),
     ],
 )  # fmt: skip
 def test_entry_points_reject_bad_arguments_before_touching_the_gpu(name, args, words):
@@ -83,7 +114,7 @@ def test_entry_points_reject_bad_arguments_before_touching_the_gpu(name, args, w
 
     from etalon_gb300 import _lib
 
-    out = C.c_double()
-    args = tuple(C.byref(out) if a == "OUT" else a for a in args)
+    out, handle = C.c_double(), C.c_void_p()
+    args = tuple(C.byref(out) if a == "OUT" else C.byref(handle) if a == "HANDLE" else a for a in args)
     with pytest.raises(ValueError, match=words):
         _lib.call(name, *args)

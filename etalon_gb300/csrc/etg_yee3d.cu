@@ -826,8 +826,11 @@ int etg_yee3d_create(etg_yee3d** out, int dtype, int nx, int ny, int nz, int per
   ETG_REQUIRE(out && dtype_ok(dtype) && nx > 0 && ny > 0 && nz > 0 && periodic_mask >= 0 && periodic_mask < 8,
               ETG_ERR_ARGUMENT, "etg_yee3d_create: bad arguments (dtype %d, %d x %d x %d, periodic %d)", dtype, nx,
               ny, nz, periodic_mask);
-  ETG_REQUIRE(nx < 65535 && (int64_t)(nx + 1) * (ny + 1) * (nz + 8) < (int64_t(1) << 40), ETG_ERR_ARGUMENT,
-              "etg_yee3d_create: grid %d x %d x %d too large", nx, ny, nz);
+  // grid dimensions: x planes on gridDim.z, rows of 8 (7 in the fused step) on gridDim.y; the
+  // kernels take row offsets (j * Pz, up to (ny + 1) * Pz) in 32 bits
+  ETG_REQUIRE(nx < 65535 && ny < 458738 && (int64_t)(ny + 1) * (((int64_t)nz + 8) / 8 * 8) < (int64_t(1) << 31) &&
+                  (int64_t)(nx + 1) * (ny + 1) * (nz + 8) < (int64_t(1) << 40),
+              ETG_ERR_ARGUMENT, "etg_yee3d_create: grid %d x %d x %d too large", nx, ny, nz);
   if (fault_injected("etg_yee3d_create")) return ETG_ERR_INJECTED;
   auto* s = new etg_yee3d();
   s->dtype = dtype;

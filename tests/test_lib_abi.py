@@ -93,6 +93,8 @@ def test_injected_fault_in_the_3d_create_is_reported(monkeypatch):
         ("etg_yee3d_create", (None, 4, 8, 8, 8, 0), "bad arguments"),
         ("etg_yee3d_create", ("HANDLE", 8, 70000, 8, 8, 0), "too large"),
         ("etg_yee3d_create", ("HANDLE", 4, 60000, 60000, 60000, 0), "too large"),
+        ("etg_yee3d_create", ("HANDLE", 4, 1, 400000, 10000, 0), "too large"),  # row offsets past 32 bits
+        ("etg_yee3d_create", ("HANDLE", 4, 1, 500000, 8, 0), "too large"),      # rows past the launch grid
         ("etg_yee3d_set_scalars", (None, None), "null argument"),
         ("etg_yee3d_set_profile", (None, 0, None, None, None, None, None, None), "bad arguments"),
         ("etg_yee3d_set_field", (None, 0, None), "bad field id"),

@@ -42,6 +42,8 @@ extern "C" {
 int etg_sim_rasterize_cb(etg_sim* s, double x_min, double y_min, double dx, double dy, double dt, double eps0,
                          double background, int n_boxes, const double* boxes) {
   ETG_REQUIRE(s && (n_boxes == 0 || boxes) && n_boxes >= 0, ETG_ERR_ARGUMENT, "etg_sim_rasterize_cb: bad arguments");
+  ETG_REQUIRE(s->nx + 1 <= 65535, ETG_ERR_ARGUMENT,
+              "etg_sim_rasterize_cb: %d x rows, at most 65534 (one launch row per Ey row)", s->nx);
   ETG_REQUIRE(s->have_coeffs, ETG_ERR_STATE, "etg_sim_rasterize_cb: set the coefficients first");
   std::vector<RasterBox> host(n_boxes);
   for (int b = 0; b < n_boxes; ++b)

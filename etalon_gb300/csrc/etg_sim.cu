@@ -305,8 +305,9 @@ extern "C" {
 int etg_sim_create(etg_sim** out, int dtype, int nx, int ny) {
   ETG_REQUIRE(out, ETG_ERR_ARGUMENT, "etg_sim_create: null output pointer");
   ETG_REQUIRE(dtype_ok(dtype), ETG_ERR_ARGUMENT, "etg_sim_create: dtype must be 4 or 8, got %d", dtype);
-  ETG_REQUIRE(nx >= 2 && ny >= 2 && nx < (1 << 28) && ny < (1 << 28), ETG_ERR_ARGUMENT,
-              "etg_sim_create: grid %d x %d out of range", nx, ny);
+  // rows: the one-step and adjoint kernels put 4 x rows per block on gridDim.y (at most 65535)
+  ETG_REQUIRE(nx >= 2 && ny >= 2 && nx <= 262136 && ny < (1 << 28), ETG_ERR_ARGUMENT,
+              "etg_sim_create: grid %d x %d out of range (2 <= nx <= 262136, 2 <= ny < 2^28)", nx, ny);
   if (fault_injected("etg_sim_create")) return ETG_ERR_INJECTED;
   *out = nullptr;
   etg_sim* s = new etg_sim;

@@ -115,6 +115,7 @@ int etg_cast(int from_dtype, int to_dtype, int64_t n, const void* in, void* out)
  * round trip. Replaces FDTDSolver.step/run (solver.py:120-160). */
 typedef struct etg_sim etg_sim;
 
+/* 2 <= nx <= 262136 rows (x), 2 <= ny < 2^28 columns (y); larger grids are refused. */
 int etg_sim_create(etg_sim** out, int dtype, int nx, int ny);
 int etg_sim_destroy(etg_sim* sim);
 /* Coefficients already cast to dtype (etalon/fdtd/state.py:75-97): cb_ex (nx, ny+1),
@@ -141,7 +142,8 @@ int etg_sim_set_db_nodes(etg_sim* sim, const void* host);
  * box b with |x - cx| <= hx and |y - cy| <= hy (float64), else `background`; cb = dt / (eps0 eps)
  * in float64, cast to dtype. boxes: n_boxes rows of (cx, cy, hx, hy, eps), hx = sx/2 + tolerance
  * already added, boxes that miss the simulated plane already left out. Bit-identical to the host
- * rasterisation and cast; set the coefficients once first (the CPML profiles stay). */
+ * rasterisation and cast; set the coefficients once first (the CPML profiles stay). Grids of at
+ * most 65534 rows (nx). */
 int etg_sim_rasterize_cb(etg_sim* sim, double x_min, double y_min, double dx, double dy, double dt,
                          double eps0, double background, int n_boxes, const double* boxes);
 /* Copy cb_ex (which = 0, (nx, ny+1)) or cb_ey (which = 1, (nx+1, ny)) to a host array in dtype. */

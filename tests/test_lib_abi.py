@@ -49,6 +49,8 @@ def test_bad_arguments_fail_before_touching_the_device():
         _lib.call("etg_sim_create", C.byref(C.c_void_p()), 3, 10, 10)
     with pytest.raises(ValueError, match="out of range"):
         _lib.call("etg_sim_create", C.byref(C.c_void_p()), 4, 1, 10)
+    with pytest.raises(ValueError, match="out of range"):  # rows past the one-step kernels' launch grid
+        _lib.call("etg_sim_create", C.byref(C.c_void_p()), 4, 262137, 10)
     with pytest.raises(ValueError):
         _lib.call("etg_update_h_te", 4, 0, 5, *([None] * 11), 1.0, 1.0, 1.0)
 

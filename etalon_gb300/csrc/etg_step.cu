@@ -208,7 +208,7 @@ int etg_update_h_te(int dtype, int nx, int ny, void* hz, const void* ex, const v
                     void* psi_hz_x, void* psi_hz_y, const void* bx_h, const void* cx_h,
                     const void* ikx_h, const void* by_h, const void* cy_h, const void* iky_h,
                     double db, double inv_dx, double inv_dy) {
-  ETG_REQUIRE(dtype_ok(dtype) && nx > 0 && ny > 0, ETG_ERR_ARGUMENT,
+  ETG_REQUIRE(dtype_ok(dtype) && nx > 0 && ny > 0 && nx <= 524272, ETG_ERR_ARGUMENT,  // rows of 8 on gridDim.y
               "etg_update_h_te: bad dtype %d or size %d x %d", dtype, nx, ny);
   if (fault_injected("etg_update_h_te")) return ETG_ERR_INJECTED;
   dim3 block(32, 8), grid((ny + 31) / 32, (nx + 7) / 8);
@@ -232,7 +232,7 @@ int etg_update_e_te(int dtype, int nx, int ny, void* ex, void* ey, const void* h
                     void* psi_ex_y, void* psi_ey_x, const void* cb_ex, const void* cb_ey,
                     const void* bx_e, const void* cx_e, const void* ikx_e, const void* by_e,
                     const void* cy_e, const void* iky_e, double inv_dx, double inv_dy) {
-  ETG_REQUIRE(dtype_ok(dtype) && nx > 0 && ny > 0, ETG_ERR_ARGUMENT,
+  ETG_REQUIRE(dtype_ok(dtype) && nx > 0 && ny > 0 && nx <= 524272, ETG_ERR_ARGUMENT,  // rows of 8 on gridDim.y
               "etg_update_e_te: bad dtype %d or size %d x %d", dtype, nx, ny);
   if (fault_injected("etg_update_e_te")) return ETG_ERR_INJECTED;
   dim3 block(32, 8), grid((ny + 1 + 31) / 32, (nx + 1 + 7) / 8);

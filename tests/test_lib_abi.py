@@ -53,6 +53,8 @@ def test_bad_arguments_fail_before_touching_the_device():
         _lib.call("etg_sim_create", C.byref(C.c_void_p()), 4, 262137, 10)
     with pytest.raises(ValueError):
         _lib.call("etg_update_h_te", 4, 0, 5, *([None] * 11), 1.0, 1.0, 1.0)
+    with pytest.raises(ValueError, match="size"):  # rows past the launch grid
+        _lib.call("etg_update_e_te", 4, 524273, 5, *([None] * 13), 1.0, 1.0)
 
 
 def test_injected_fault_is_reported(monkeypatch):

@@ -96,22 +96,23 @@ def write_back(dst, m, r0, c0, rows, cols):
     """Copy the cells [rows) x [cols) that the small simulation owns into the global state."""
     for name in STATE:
         a = getattr(dst, name)
-        a0, a1 = rows[0], min(rows[1], a.shape[0])
-        b0, b1 = cols[0], min(cols[1], a.shape[1])
+        a0, a1 = max(rows[0], 0), min(rows[1], a.shape[0])
+        b0, b1 = max(cols[0], 0), min(cols[1], a.shape[1])
         if a1 > a0 and b1 > b0:
             a[a0:a1, b0:b1] = getattr(m, name)[a0 - r0 : a1 - r0, b0 - c0 : b1 - c0]
 
 
-def blocked(g, srcs, k, er, ec, segments, halo=None, carry_rows=True):
+def blocked(g, srcs, k, er, ec, segments, halo=None, carry_rows=True, shift=0):
     """K steps of the whole grid as tiles of er x ec extended cells (output er - 2K rows, ec - 2K
     columns). With `segments`, each run of five tile rows of a column is one head tile and three
     carried tiles (er - K output rows, no top halo, the Hz row above taken from the predecessor
-    after every H update), the scheme of the column-segment kernel; er must then be 5K.
+    after every H update), the scheme of the column-segment kernel; er must then be 5K. The
+    first tile column starts at `shift` (<= 0), as the kernels' tile lists may.
     `halo` and `carry_rows` exist to plant mistakes: a shorter halo, carried tiles left alone."""
     h = k if halo is None else halo
     out_r, out_c = er - 2 * k, ec - 2 * k
     new = SimpleNamespace(**{name: getattr(g, name).copy() for name in STATE})
-    for c in range(0, g.ny + 1, out_c):
+    for c in range(shift, g.ny + 1, out_c):
         cols = (c, c + out_c)
         rows = list(range(0, g.nx + 1, out_r))
         q = 0
@@ -156,12 +157,13 @@ def same_bits(a, b) -> bool:
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 @pytest.mark.parametrize("k", [2, 4])
 @pytest.mark.parametrize("segments", [False, True], ids=["tiles", "segments"])
-def test_blocked_tiles_equal_the_whole_grid_run(dtype, k, segments):
+@pytest.mark.parametrize("shift", [0, -5])
+def test_blocked_tiles_equal_the_whole_grid_run(dtype, k, segments, shift):
     nx, ny = 67, 45
     g = random_state(nx, ny, dtype, seed=k)
     srcs = sources(nx, ny, k, dtype, seed=k)
     want = whole_grid(g, srcs, k)
-    got = blocked(g, srcs, k, er=5 * k, ec=8 + 2 * k, segments=segments)
+    got = blocked(g, srcs, k, er=5 * k, ec=8 + 2 * k, segments=segments, shift=shift)
     for name in STATE:
         assert same_bits(getattr(got, name), getattr(want, name)), name
 

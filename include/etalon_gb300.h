@@ -339,7 +339,8 @@ int etg_debug_set_wait_tries(int64_t tries);
 #define ETG3_CB0 18
 typedef struct etg_yee3d etg_yee3d;
 /* periodic_mask: bit a set = axis a (0 x, 1 y, 2 z) periodic. Fields, psi and cb start at 0;
- * profiles start as b = 1, c = 0, 1/kappa = 1 (no CPML). */
+ * profiles start as b = 1, c = 0, 1/kappa = 1 (no CPML). Grids need nx < 65535, ny < 458738
+ * and (ny + 1) * Pz < 2^31 with Pz = nz + 1 rounded up to 8; larger ones are refused. */
 int etg_yee3d_create(etg_yee3d** out, int dtype, int nx, int ny, int nz, int periodic_mask);
 int etg_yee3d_destroy(etg_yee3d* sim);
 /* db, 1/dx, 1/dy, 1/dz (1/m), four values of the run's dtype */

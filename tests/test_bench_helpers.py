@@ -50,3 +50,21 @@ def test_workload_description_names_the_headline_configuration():
     assert d["grid"] == [2024, 2024] and d["time_steps_per_step"] == 10
     assert "2000^2" in d["workload"] and "16 wavelengths" in d["workload"] and "l2" in d
     assert np.dtype(p.real) == np.float32
+
+
+def test_clock_summary_takes_the_median_and_the_active_reasons():
+    """The samples nvidia-smi prints during the timed region (csv, noheader, nounits): the median
+    SM clock, the maximum, and which throttle reasons were ever active; unreadable lines skipped."""
+    c = bench.ClockSampler(0)
+    c.lines = [
+        "0, 2070, 2070, 812.5, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, 1965, 2070, 1390.1, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "0, 2070, 2070, 820.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, [N/A], [N/A], [N/A], [N/A], [N/A], [N/A], [N/A], [N/A]",
+        "",
+    ]
+    assert c.summary() == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    c.lines = ["0, 1200, 2070, 900.0, 0x0000000000000008, Active, Not Active, Active, Not Active"]
+    assert c.summary()["reasons"] == ["hw_slowdown", "sw_thermal_slowdown"]
+    c.lines = []
+    assert c.summary() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}

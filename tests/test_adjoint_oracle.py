@@ -53,3 +53,15 @@ def test_torch_gradient_matches_central_differences():
                 vals.append(float((te.run(x, cby)[1][2] ** 2).sum()))
         fd = (vals[0] - vals[1]) / (2 * h)
         assert float(cbx.grad[i, k]) == pytest.approx(fd, rel=1e-5, abs=1e-12 * abs(float(j.detach())) / abs(h))
+
+
+@pytest.mark.parametrize("n_steps", [1, 15, 16, 255, 256, 2000, 20000, 10**6])
+def test_checkpoint_stride_is_root_n_rounded_up_to_whole_launch_pairs(n_steps):
+    """√N checkpoint segments are whole launch pairs of the 8- and 4-step tiles: multiples of 16,
+    never shorter than √N rounded (144 at the 20 000-step single-design workload)."""
+    from etalon_gb300.adjoint import AdjointRunner
+
+    s = AdjointRunner.sqrt_stride(n_steps)
+    assert s % 16 == 0 and s >= round(np.sqrt(n_steps)) and s - round(np.sqrt(n_steps)) < 16
+    if n_steps == 20000:
+        assert s == 144
